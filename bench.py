@@ -1,0 +1,321 @@
+"""Benchmark of the CUDA renderer level on the 20,000-path 4K scene.
+
+One step = one full frame of the compute rasterization path (bound, flatten,
+bin, backdrop propagation, fill grouping, fill + composite) over the seeded
+synthetic 4K scene (20,000 paths, ~2.1M segments) into an RGBA8 3840x2160
+target.  `value` is input segments per second with the scene resident in HBM
+(L2 flushed between steps); `e2e` is the same metric through the public API
+with host buffers: scene upload from pinned host memory, render, and the
+RGBA8 image read back, every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cuda|reference]
+
+`--impl reference` times the CPU restatement of the reference's Rayon + SIMD
+CPU tiling path (tiling, FP32 coverage, composite) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mseg/s"
+WORKLOAD = "svg_4k_20000_paths"
+W, H = 3840, 2160
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0])); mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def stage_bytes(st, npts: int, nseg: int) -> dict:
+    """Algorithmic bytes per stage from the per-unit figures:
+    8 B per point, 8 B per segment record, 12 B per fill, 16 B per path tile,
+    1 B per mask pixel (256 per alpha tile), 4 B per output pixel."""
+    P, S, F, T, A = npts, nseg, st.fill_count, st.tile_count, st.alpha_tile_count
+    return {
+        "bound": 8 * P,
+        "tile_count": 8 * P + 8 * S,
+        "scans": 4 * S + 8 * T,
+        "tile_emit": 8 * P + 8 * S + 12 * F,
+        "propagate": 16 * T,
+        "visibility": 16 * T,
+        "fill_composite": 12 * F + 256 * A + 4 * W * H,
+        "frame": 8 * P + 8 * S + 12 * F + 16 * T + 256 * A + 4 * W * H,
+    }
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import pathfinder_gb300 as pf
+    import oracle
+    from pathfinder_gb300 import build as pbuild
+    pbuild.build()
+    oracle.build()
+    scene = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=args.seed)
+    nseg = scene.segment_count
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        oracle.cpu_frame(scene, W, H, threads)
+    times = []
+    for _ in range(args.steps):
+        secs, _, counts = oracle.cpu_frame(scene, W, H, threads)
+        times.append(secs)
+    ms = 1e3 * sum(times) / len(times)
+    value = nseg / (ms / 1e3) / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": METRIC,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded, PF_SCENE_SVG_4K)",
+        "config": {"workload": WORKLOAD, "paths": 20000, "segments": nseg, "width": W, "height": H,
+                   "seed": args.seed},
+        "cpu_baseline": {"value": round(value, 4), "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full frames of the 4K scene (tiling + FP32 coverage + composite)"},
+        "e2e": {"value": round(value, 4), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "mpx_per_s": round(W * H / (ms / 1e3) / 1e6, 3),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(scene, nseg: int, budget_s: float = 12.0) -> dict:
+    import oracle
+    threads = os.cpu_count() or 1
+    oracle.cpu_frame(scene, W, H, threads)  # warm
+    times = []
+    t0 = time.time()
+    while time.time() - t0 < budget_s or len(times) < 2:
+        secs, _, _ = oracle.cpu_frame(scene, W, H, threads)
+        times.append(secs)
+        if len(times) >= 50:
+            break
+    ms = 1e3 * sum(times) / len(times)
+    return {"value": round(nseg / (ms / 1e3) / 1e6, 4), "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{len(times)} full frames of the 4K scene, all host threads ({ms:.1f} ms/frame)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="cuda", choices=["cuda", "reference"])
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    from pathfinder_gb300 import build as pbuild
+    pbuild.build()
+    import pathfinder_gb300 as pf
+
+    # replicas only: each rank renders its own scene (seed + rank)
+    scene = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=args.seed + rank)
+    nseg = scene.segment_count
+    npts = len(scene.points)
+    r = pf.Renderer(local)
+    # a dedicated stream: the renderer, the L2 flush and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    r.set_stream(stream.cuda_stream)
+    out = torch.empty((H, W, 4), dtype=torch.uint8, device="cuda")
+    r.render(scene, out=out)  # first frame: sizes the buffers
+    st = r.stats()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        r.render_async(scene, out)
+    code, _ = r.render_status()
+    if code != 0:
+        raise RuntimeError(f"render failed with status {code}")
+
+    r.set_profiling(True)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stage_sum = {}
+    sampler = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    for k in range(args.steps):
+        flush.zero_()  # inputs are below L2 size: flush between steps
+        evs[k][0].record(stream)
+        r.render_async(scene, out)
+        evs[k][1].record(stream)
+        for n, v in r.stage_times().items():
+            stage_sum[n] = stage_sum.get(n, 0.0) + v
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    code, _ = r.render_status()
+    if code != 0:
+        raise RuntimeError(f"render failed with status {code}")
+    st = r.stats()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * nseg / (ms / 1e3) / 1e6
+
+    # roofline of the dominant stage
+    stage_ms = {n: v / args.steps for n, v in stage_sum.items()}
+    sb = stage_bytes(st, npts, nseg)
+    dom = max(stage_ms, key=stage_ms.get)
+    peak, peak_kind = _peaks()
+    achieved = sb[dom] / (stage_ms[dom] / 1e3) / 1e9
+    frame_gbs = sb["frame"] / (ms / 1e3) / 1e9
+
+    # e2e through the public API with host buffers
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    pinned = {}
+    for name in ("points", "flags", "contour_starts"):
+        a = getattr(scene, name)
+        t = torch.from_numpy(a.copy()).pin_memory()
+        pinned[name] = t
+        setattr(scene, name, t.numpy())
+    host_out = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
+    host_np = host_out.numpy()
+    h2d = scene.points.nbytes + scene.flags.nbytes + scene.contour_starts.nbytes
+    d2h = host_np.nbytes
+    r.set_profiling(False)
+    for _ in range(2):
+        r.upload_scene(scene, force=True)
+        r.render(scene, out=host_np)
+    torch.cuda.synchronize()
+    e2e_times = []
+    for _ in range(e2e_steps):
+        t0 = time.perf_counter()
+        r.upload_scene(scene, force=True)
+        r.render(scene, out=host_np)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * sum(e2e_times) / len(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * nseg / (e2e_ms / 1e3) / 1e6
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded PF_SCENE_SVG_4K: 20,000 log-normal star paths, 40/30/30 line/quad/cubic)",
+            "config": {"workload": WORKLOAD, "paths": 20000, "clip_paths": len(scene.clip_paths), "segments": nseg,
+                       "points": npts, "width": W, "height": H, "seed": args.seed,
+                       "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}"},
+            "mpx_per_s": round(world * W * H / (ms / 1e3) / 1e6, 3),
+            "frame": {"fills": st.fill_count, "tiles": st.tile_count, "alpha_tiles": st.alpha_tile_count,
+                      "visible_tiles": st.visible_tile_count, "lines": st.line_count,
+                      "algorithmic_bytes": sb["frame"], "achieved_gbs": round(frame_gbs, 1),
+                      "frac_of_" + peak_kind: round(frame_gbs / peak, 4)},
+            "stages_ms": {n: round(v, 4) for n, v in stage_ms.items()},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": sb[dom], "traffic": None},
+            "e2e": {"value": round(e2e_value, 4), "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
+            "gpu_launches": int(st.kernel_launches * args.steps),
+            "clocks": clocks,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(scene, nseg)
+        print(json.dumps(line), flush=True)
+    r.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,251 @@
+/*
+ * pathfinder_cuda.h — C ABI of the CUDA renderer level (sm_103a, one GPU).
+ *
+ * This is the drop-in boundary for Pathfinder's compute rasterization path
+ * (bound -> flatten -> bin into 16x16 tiles -> backdrop propagate -> group
+ * fills by tile -> trapezoid-area fill -> tile composite).  It plays the role
+ * that `RendererLevel::D3D11` (renderer/src/gpu/options.rs:41-46) plays in the
+ * reference: the scene builder hands over the scene outlines once per scene
+ * epoch (`RenderCommand::UploadSceneD3D11`, renderer/src/gpu_data.rs:75-101,
+ * renderer/src/builder.rs:190-216) and then asks for frames.
+ *
+ * Conventions, in the style of the reference's C bindings (c/src/lib.rs):
+ *   - opaque handles, created by `*Create` and released by `*Destroy`
+ *     (c/src/lib.rs:606-620);
+ *   - unlike the reference, every call returns an int32_t status
+ *     (PF_CUDA_OK == 0); a capacity failure reports the size it needed;
+ *   - pointers are plain; each argument states whether it may point to host
+ *     or device memory;
+ *   - all calls are asynchronous on the renderer's stream unless they say
+ *     that they synchronise.
+ *
+ * Reference interfaces these entry points replace are cited per function.
+ */
+#ifndef PATHFINDER_CUDA_H
+#define PATHFINDER_CUDA_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PF_CUDA_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+#define PF_CUDA_OK                 0
+#define PF_CUDA_ERR_INVALID        1  /* bad argument or malformed scene            */
+#define PF_CUDA_ERR_CAPACITY       2  /* a device buffer was too small (see needed) */
+#define PF_CUDA_ERR_LAUNCH         3  /* a CUDA call failed                          */
+#define PF_CUDA_ERR_NO_DEVICE      4  /* no CUDA device / driver                     */
+#define PF_CUDA_ERR_LIMIT          5  /* a bounded device loop hit its limit         */
+#define PF_CUDA_ERR_NO_SCENE       6  /* render called before a scene was uploaded   */
+
+/* ---- geometry / colour (same layout as c/src/lib.rs:102-170) ------------- */
+typedef struct PFVector2F { float x, y; } PFVector2F;
+typedef struct PFVector2I { int32_t x, y; } PFVector2I;
+typedef struct PFRectF { PFVector2F origin, lower_right; } PFRectF;
+typedef struct PFRectI { PFVector2I origin, lower_right; } PFRectI;
+typedef struct PFColorU { uint8_t r, g, b, a; } PFColorU;
+typedef struct PFColorF { float r, g, b, a; } PFColorF;
+/* Row-major, as PFMatrix2x2F/PFTransform2F in c/src/lib.rs:150-162. */
+typedef struct PFTransform2F { float m00, m01, m10, m11; PFVector2F vector; } PFTransform2F;
+
+/* ---- point flags and fill rules (content/src/outline.rs:32-41,
+ *      content/src/fill.rs) ---------------------------------------------- */
+#define PF_POINT_FLAG_CONTROL_POINT_0 0x01
+#define PF_POINT_FLAG_CONTROL_POINT_1 0x02
+#define PF_FILL_RULE_WINDING  0
+#define PF_FILL_RULE_EVEN_ODD 1
+#define PF_BLEND_MODE_SRC_OVER 0   /* the only blend mode on this path */
+
+#define PF_MEMORY_HOST   0
+#define PF_MEMORY_DEVICE 1
+
+/* One path of the scene: a range of contours of the shared outline buffers.
+ * Mirrors DrawPath / ClipPath (renderer/src/scene.rs:441-472): outline,
+ * paint (a solid colour here), fill rule, optional clip path. */
+typedef struct PFCUDAPath {
+    uint32_t first_contour;
+    uint32_t contour_count;
+    PFColorU paint;          /* draw paths: solid paint; ignored for clip paths  */
+    int32_t  clip_path;      /* draw paths: index into clip paths, or -1         */
+    uint8_t  fill_rule;      /* PF_FILL_RULE_*                                   */
+    uint8_t  blend_mode;     /* PF_BLEND_MODE_SRC_OVER                           */
+    uint16_t reserved;
+} PFCUDAPath;
+
+/* The scene as flat outline buffers.  Every contour is treated as closed
+ * (Outline::close_all_contours, content/src/outline.rs:279-281, applied by
+ * Scene::apply_render_options, renderer/src/scene.rs:228-274).
+ * Contour c owns points [contour_starts[c], contour_starts[c+1]). */
+typedef struct PFCUDASceneDesc {
+    const PFVector2F* points;          /* point_count                        */
+    const uint8_t*    point_flags;     /* point_count PF_POINT_FLAG_* bits    */
+    const uint32_t*   contour_starts;  /* contour_count + 1                   */
+    const PFCUDAPath* clip_paths;      /* host memory always                  */
+    const PFCUDAPath* draw_paths;      /* host memory always                  */
+    uint32_t point_count;
+    uint32_t contour_count;
+    uint32_t clip_path_count;
+    uint32_t draw_path_count;
+    PFRectF  view_box;                 /* Scene::set_view_box                 */
+    int32_t  memory;                   /* PF_MEMORY_* for points/flags/starts */
+} PFCUDASceneDesc;
+
+/* BuildOptions (renderer/src/options.rs:53-61): only the 2-D transform is on
+ * this path (dilation and subpixel AA are front-end preprocessing). */
+typedef struct PFCUDABuildOptions {
+    PFTransform2F transform;
+    int32_t       has_transform;       /* 0: identity (no arithmetic applied) */
+} PFCUDABuildOptions;
+
+/* RendererOptions (renderer/src/gpu/options.rs:19-33). */
+typedef struct PFCUDARendererOptions {
+    PFColorF background_color;         /* premultiplied clear colour           */
+    int32_t  has_background_color;     /* 0: transparent                       */
+    int32_t  flags;                    /* reserved, 0                          */
+} PFCUDARendererOptions;
+
+/* RenderStats (renderer/src/gpu/perf.rs:21-44) + the device counters of the
+ * last frame. */
+typedef struct PFCUDARenderStats {
+    uint64_t path_count;
+    uint64_t segment_count;     /* input segments (lines+quads+cubics, with close) */
+    uint64_t line_count;        /* flattened lines                                 */
+    uint64_t fill_count;        /* fills (Fill records)                            */
+    uint64_t tile_count;        /* path tiles (TileObjectPrimitive records)        */
+    uint64_t alpha_tile_count;  /* tiles with a mask                               */
+    uint64_t visible_tile_count;/* tiles composited after occlusion culling        */
+    uint64_t screen_tile_count;
+    uint64_t status;            /* device status bits of the last frame            */
+    double   gpu_time_ms;       /* CUDA-event time of the last frame               */
+    uint64_t kernel_launches;   /* kernels this library launched for the frame     */
+} PFCUDARenderStats;
+
+/* Record layouts read back for parity checks. */
+/* Fill (renderer/src/gpu_data.rs:354-363): LineSegmentU16 in 8.8 fixed point
+ * relative to the tile; `link` here is the fill's emission index in the CPU
+ * tiler's order (path, segment, flattened line, DDA step, auxiliary). */
+typedef struct PFCUDAFill {
+    uint16_t from_x, from_y, to_x, to_y;
+    uint32_t emission_index;
+} PFCUDAFill;
+/* TileObjectPrimitive (renderer/src/gpu_data.rs:264-275). */
+typedef struct PFCUDATile {
+    int16_t  tile_x, tile_y;
+    uint32_t alpha_tile_id;     /* 0xffffffff: solid tile */
+    uint32_t path_id;           /* index within clip paths or within draw paths */
+    uint16_t color;
+    uint8_t  ctrl;
+    int8_t   backdrop;
+} PFCUDATile;
+/* Clip (renderer/src/gpu_data.rs:436-442). */
+typedef struct PFCUDAClip {
+    uint32_t dest_tile_id;
+    int32_t  dest_backdrop;
+    uint32_t src_tile_id;
+    int32_t  src_backdrop;
+} PFCUDAClip;
+
+typedef struct PFCUDARenderer* PFCUDARendererRef;
+
+/* ---- renderer lifetime ---------------------------------------------------
+ * Replaces PFGLRendererCreate / PFMetalRendererCreate (c/src/lib.rs:606-615,
+ * 646-657) and Renderer::new (renderer/src/gpu/renderer.rs:181-341). */
+int32_t PFCUDARendererCreate(int32_t device_ordinal,
+                             const PFCUDARendererOptions* options,
+                             PFCUDARendererRef* out_renderer);
+/* Replaces PFGLRendererDestroy (c/src/lib.rs:618-620). */
+int32_t PFCUDARendererDestroy(PFCUDARendererRef renderer);
+/* Runs subsequent work on `stream` (a cudaStream_t; NULL = the renderer's own). */
+int32_t PFCUDARendererSetStream(PFCUDARendererRef renderer, void* stream);
+/* Renderer::set_options background colour (gpu/options.rs:27-30). */
+int32_t PFCUDARendererSetOptions(PFCUDARendererRef renderer,
+                                 const PFCUDARendererOptions* options);
+
+/* ---- scene upload ----------------------------------------------------------
+ * Replaces RenderCommand::UploadSceneD3D11 + RendererD3D11::upload_scene
+ * (renderer/src/gpu/d3d11/renderer.rs:236-241) and the segment packing of
+ * SegmentsD3D11::add_path (renderer/src/builder.rs:804-841), which here runs
+ * on the GPU.  Copies the outline buffers to device memory (host or device
+ * source per desc->memory).  The scene stays resident until the next upload
+ * (scene-epoch caching, renderer/src/builder.rs:190-216). */
+int32_t PFCUDASceneUpload(PFCUDARendererRef renderer, const PFCUDASceneDesc* scene);
+
+/* ---- frames ----------------------------------------------------------------
+ * Scene::build_and_render (renderer/src/scene.rs:369-381) for the CUDA level:
+ * Renderer::begin_scene / render_command / end_scene
+ * (renderer/src/gpu/renderer.rs:350-460) with the seven D3D11 dispatches
+ * (renderer/src/gpu/d3d11/renderer.rs:427-782) replaced by this library's
+ * kernels.  Writes premultiplied RGBA8, row 0 = top, into `out_rgba8`
+ * (width*height*4 bytes; host or device memory per out_memory).
+ * Synchronises the stream before returning. */
+int32_t PFCUDARenderScene(PFCUDARendererRef renderer,
+                          const PFCUDABuildOptions* options,
+                          int32_t width, int32_t height,
+                          uint8_t* out_rgba8, int32_t out_memory);
+
+/* Same frame, but only enqueued: no synchronisation and no status readback.
+ * `out_rgba8_device` must be device memory.  Capacity overflow is reported
+ * by the next PFCUDARenderStatus call.  Used for CUDA-graph capture. */
+int32_t PFCUDARenderSceneAsync(PFCUDARendererRef renderer,
+                               const PFCUDABuildOptions* options,
+                               int32_t width, int32_t height,
+                               uint8_t* out_rgba8_device);
+/* Synchronises and returns the status of the frames enqueued since the last
+ * call (PF_CUDA_OK or the first error), with the needed capacity on overflow. */
+int32_t PFCUDARenderStatus(PFCUDARendererRef renderer, uint64_t* out_needed);
+
+/* Single-channel FP32 render: per pixel, SrcOver of (paint alpha x coverage)
+ * over the draw paths in order; used by the differentiable form.  Row 0 = top.
+ * Synchronises. */
+int32_t PFCUDARenderCoverage(PFCUDARendererRef renderer,
+                             const PFCUDABuildOptions* options,
+                             int32_t width, int32_t height,
+                             float* out, int32_t out_memory);
+
+/* Raw mask of every alpha tile (the D3D9 mask texture contents, fill.fs.glsl:
+ * sum of trapezoid areas, no backdrop) as FP32 [alpha_tile_count][16][16],
+ * and the resolved coverage of every path tile (sampleMask,
+ * shaders/tile_fragment.inc.glsl:539-556) as FP32 [tile_count][16][16].
+ * Either pointer may be NULL.  Host memory.  Valid after a render call. */
+int32_t PFCUDAReadMasks(PFCUDARendererRef renderer,
+                        float* out_alpha_masks, uint64_t alpha_capacity,
+                        float* out_tile_coverage, uint64_t tile_capacity);
+
+/* Read back the records of the last frame for parity checks (host memory).
+ * fills: grouped by tile; within a tile in any order (emission_index gives
+ * the canonical order).  fill_tile: the global tile index of each fill.
+ * tiles: one record per path tile, clip paths first, each path row-major
+ * over its tile rect.  path_tile_offsets: clip_count+draw_count+1 entries.
+ * clips: one record per draw tile of a clipped draw path (gpu_data Clip).
+ * z_buffer: one i32 per screen tile.  Any pointer may be NULL. */
+int32_t PFCUDAReadRecords(PFCUDARendererRef renderer,
+                          PFCUDAFill* fills, uint32_t* fill_tile, uint64_t fill_capacity,
+                          PFCUDATile* tiles, uint64_t tile_capacity,
+                          uint32_t* path_tile_offsets, PFRectI* path_tile_rects,
+                          uint64_t path_capacity,
+                          PFCUDAClip* clips, int32_t* z_buffer, uint64_t z_capacity);
+
+/* Renderer::stats (renderer/src/gpu/renderer.rs:626) + last_rendering_time
+ * (:537). */
+int32_t PFCUDAGetStats(PFCUDARendererRef renderer, PFCUDARenderStats* out_stats);
+
+/* Per-stage CUDA-event timing of subsequent frames (Renderer timer queries,
+ * renderer/src/gpu/perf.rs:96-186, bucketed like RenderTime :223-240).
+ * Stages: 0 bound, 1 tile count, 2 scans, 3 tile emit, 4 propagate,
+ * 5 visibility, 6 fill+composite. */
+#define PF_CUDA_STAGE_COUNT 7
+int32_t PFCUDASetProfiling(PFCUDARendererRef renderer, int32_t enable);
+/* Milliseconds per stage of the last profiled frame; synchronises. */
+int32_t PFCUDAGetStageTimes(PFCUDARendererRef renderer, float* out_ms, int32_t capacity);
+
+/* Human-readable text for a status code (static storage). */
+const char* PFCUDAStatusString(int32_t status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PATHFINDER_CUDA_H */

@@ -1,0 +1,184 @@
+"""The parity oracle — TEST INFRASTRUCTURE, NOT PART OF THE PRODUCT.
+
+A CPU restatement (pf_oracle.cpp) of the reference's CPU tiler plus an FP64
+evaluation of its coverage formula, mask resolve and composite.  Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg use it, and only as
+the checker or the timed CPU baseline.
+
+Parity status: the tiler is pinned by hand-derived known-answer cases only
+(the reference has no tiler tests and its Rust cannot be built here); the
+coverage formula is pinned by the reference's own area LUT
+(tests/golden/area_lut.*).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+SRC = os.path.join(HERE, "pf_oracle.cpp")
+LIB_PATH = os.path.join(HERE, "libpforacle.so")
+
+CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-Wall"]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (no FMA contraction: SSE op order)."""
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC):
+        return LIB_PATH
+    cmd = ["g++"] + CXXFLAGS + ["-o", LIB_PATH, SRC, "-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        l = C.CDLL(LIB_PATH)
+        l.pfo_build.restype = C.c_void_p
+        l.pfo_build.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64]
+        l.pfo_free.argtypes = [C.c_void_p]
+        l.pfo_counts.argtypes = [C.c_void_p, C.c_void_p]
+        l.pfo_fills.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        l.pfo_tiles.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        l.pfo_zbuffer.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        l.pfo_masks.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        l.pfo_render.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                 C.c_int]
+        l.pfo_cpu_frame.restype = C.c_double
+        l.pfo_cpu_frame.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        l.pfo_area.restype = C.c_double
+        l.pfo_area.argtypes = [C.c_double, C.c_double]
+        l.pfo_fill_coverage.argtypes = [C.c_void_p, C.c_void_p]
+        l.pfo_area_lut_value.restype = C.c_uint8
+        l.pfo_area_lut_value.argtypes = [C.c_int, C.c_int, C.c_int]
+        l.pfo_sse_cvt.restype = C.c_int32
+        l.pfo_sse_cvt.argtypes = [C.c_float]
+        _lib = l
+    return _lib
+
+
+def _dtypes():
+    from pathfinder_gb300 import _abi
+    return _abi.record_dtypes()
+
+
+def _opts(build_options):
+    if build_options is None:
+        return None
+    o = build_options.to_c()
+    return o
+
+
+class OracleFrame:
+    """One build of a scene by the CPU tiler restatement."""
+
+    def __init__(self, scene, build_options=None, threads: int = 0, dda_limit: int = 0):
+        L = lib()
+        self._scene = scene
+        self._desc = scene.desc()
+        self._bo = _opts(build_options)
+        threads = threads or (os.cpu_count() or 1)
+        self.threads = threads
+        h = L.pfo_build(C.byref(self._desc), C.byref(self._bo) if self._bo is not None else None, threads,
+                        dda_limit)
+        if not h:
+            raise ValueError("oracle rejected the scene")
+        self._h = h
+        c = np.zeros((8,), np.uint64)
+        L.pfo_counts(h, c.ctypes.data)
+        (self.path_count, self.tile_count, self.fill_count, self.alpha_tile_count, self.line_count,
+         self.screen_tile_count, limit, self.clip_path_count) = [int(v) for v in c]
+        self.limit_hit = bool(limit)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().pfo_free(self._h)
+            self._h = None
+
+    def fills(self):
+        fill, *_ = _dtypes()
+        f = np.zeros((self.fill_count,), fill)
+        t = np.zeros((self.fill_count,), np.uint32)
+        lib().pfo_fills(self._h, f.ctypes.data, t.ctypes.data)
+        return f, t
+
+    def tiles(self):
+        _, tile, clip, _, rect = _dtypes()
+        tiles = np.zeros((self.tile_count,), tile)
+        clips = np.zeros((self.tile_count,), clip)
+        offs = np.zeros((self.path_count + 1,), np.uint32)
+        rects = np.zeros((self.path_count,), rect)
+        lib().pfo_tiles(self._h, tiles.ctypes.data, clips.ctypes.data, offs.ctypes.data, rects.ctypes.data, None)
+        return tiles, clips, offs, rects
+
+    def zbuffer(self):
+        z = np.zeros((self.screen_tile_count,), np.int32)
+        lib().pfo_zbuffer(self._h, z.ctypes.data, None)
+        return z
+
+    def masks(self):
+        """(raw alpha masks [A,16,16] FP64, resolved coverage per path tile [T,16,16] FP64)."""
+        a = np.zeros((self.alpha_tile_count, 16, 16), np.float64)
+        t = np.zeros((self.tile_count, 16, 16), np.float64)
+        lib().pfo_masks(self._h, a.ctypes.data, t.ctypes.data, self.threads)
+        return a, t
+
+    def render(self, width: int, height: int, background=None, channels: int = 4):
+        from pathfinder_gb300 import _abi
+        bg = None
+        if background is not None:
+            bg = _abi.PFColorF(*background)
+        if channels == 4:
+            out = np.zeros((height, width, 4), np.uint8)
+            f64 = np.zeros((height, width, 4), np.float64)
+        else:
+            out = np.zeros((height, width), np.uint8)
+            f64 = np.zeros((height, width), np.float64)
+        lib().pfo_render(self._h, width, height, C.byref(bg) if bg is not None else None, channels,
+                         out.ctypes.data, f64.ctypes.data, self.threads)
+        return out, f64
+
+
+def cpu_frame(scene, width: int, height: int, threads: int = 0, build_options=None, want_image: bool = False):
+    """Time one CPU-baseline frame (tiling + FP32 coverage + composite).
+    Returns (seconds, image or None, counts)."""
+    L = lib()
+    d = scene.desc()
+    bo = _opts(build_options)
+    out = np.zeros((height, width, 4), np.uint8) if want_image else None
+    counts = np.zeros((8,), np.uint64)
+    secs = L.pfo_cpu_frame(C.byref(d), C.byref(bo) if bo is not None else None, width, height,
+                           threads or (os.cpu_count() or 1), out.ctypes.data if out is not None else None,
+                           counts.ctypes.data)
+    return secs, out, counts
+
+
+def area(y: float, dydx: float) -> float:
+    return lib().pfo_area(y, dydx)
+
+
+def fill_coverage(seg) -> np.ndarray:
+    m = np.zeros((16, 16), np.float64)
+    s = (C.c_uint16 * 4)(*[int(v) for v in seg])
+    lib().pfo_fill_coverage(s, m.ctypes.data)
+    return m
+
+
+def area_lut_value(u: int, v: int, k: int) -> int:
+    """The reference LUT texel (u, v) channel k, computed in f32 by the oracle."""
+    return int(lib().pfo_area_lut_value(u, v, k))
+
+
+def sse_cvt(x: float) -> int:
+    return int(lib().pfo_sse_cvt(x))

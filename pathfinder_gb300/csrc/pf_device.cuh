@@ -1,0 +1,360 @@
+// pf_device.cuh — device-side records and building blocks of the CUDA level.
+//
+// Bit-exactness: the tiler functions below reproduce the reference CPU
+// tiler's single-precision arithmetic (renderer/src/tiler.rs,
+// content/src/segment.rs, content/src/clip.rs, renderer/src/builder.rs) with
+// explicit round-to-nearest intrinsics, so no multiply-add is ever contracted
+// (the reference runs SSE mulps/addps; simd/src/x86/mod.rs).  Their
+// translation unit is also compiled with -fmad=false.
+#pragma once
+
+#include <cstdint>
+#include <climits>
+#include <cuda_runtime.h>
+
+namespace pf {
+
+// ---------------------------------------------------------------------------
+// Constants
+// ---------------------------------------------------------------------------
+constexpr uint32_t kInvalid = 0xffffffffu;
+constexpr int kTileSize = 16;             // renderer/src/tiles.rs:19-20
+constexpr int kMaxFlattenDepth = 32;      // explicit-stack bound (see DESIGN)
+constexpr uint32_t kSegLine = 1, kSegQuad = 2, kSegCubic = 3;
+
+// status bits (device word, OR-ed)
+constexpr uint32_t kStatusFillCapacity   = 1u << 0;
+constexpr uint32_t kStatusTileCapacity   = 1u << 1;
+constexpr uint32_t kStatusVisibleCapacity= 1u << 2;
+constexpr uint32_t kStatusDdaLimit       = 1u << 3;
+constexpr uint32_t kStatusDepthLimit     = 1u << 4;
+constexpr uint32_t kStatusMalformed      = 1u << 5;
+constexpr uint32_t kStatusColumnCapacity = 1u << 6;
+constexpr uint32_t kStatusAlphaCapacity  = 1u << 7;
+
+// ---------------------------------------------------------------------------
+// Records in HBM
+// ---------------------------------------------------------------------------
+// One input segment (the role of SegmentIndicesD3D11, renderer/src/gpu_data.rs):
+// x = index of its first point, y = index of its end point (the contour start
+// for the closing line), z = kind, w = global path index.
+using SegRec = int4;
+
+// Per-path data, one struct-of-arrays per field (PathDev).
+struct PathDev {
+    uint32_t* first_ord_contour;   // [P+1] range into the ordered contour list
+    uint32_t* paint;               // [P] RGBA8 (r in the low byte)
+    int32_t*  clip_gpath;          // [P] global index of the clip path, or -1
+    uint8_t*  rule;                // [P] PF_FILL_RULE_*
+    uint8_t*  is_clip;             // [P]
+    uint32_t* local_index;         // [P] index within clip paths / draw paths
+    uint32_t* scene;               // [P] scene of the path (batched frames)
+    int4*     tile_rect;           // [P] tile rect (min x, min y, max x, max y)
+    uint32_t* tile_offset;         // [P+1] global tile index of the path's first tile
+    uint32_t* col_offset;          // [P+1] offset of its above-rect column backdrops
+};
+
+// Per-scene data.
+struct SceneDev {
+    float4 view_box;               // min x, min y, max x, max y
+    int4   screen;                 // screen tile rect = round_out(view_box / 16)
+    uint32_t screen_offset;        // first global screen tile
+    uint32_t first_path;           // global index of the first path
+    uint32_t clip_count, draw_count;
+    int32_t width, height;         // output size in pixels
+    uint64_t out_offset;           // element offset of the scene's output image
+};
+
+// Device counters written by the pipeline (one struct, zeroed per frame).
+struct Counters {
+    uint32_t status;
+    uint32_t pad0;
+    uint64_t tiles;        // T
+    uint64_t columns;      // sum of tile rect widths
+    uint64_t fills;        // F
+    uint64_t alpha_tiles;  // A
+    uint64_t lines;        // flattened lines
+    uint64_t visible;      // composited tiles
+    uint64_t needed_fills, needed_tiles, needed_visible;
+};
+
+// ---------------------------------------------------------------------------
+// Exact single-precision helpers (SSE lane semantics, simd/src/x86/mod.rs)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+// _mm_min_ps / _mm_max_ps: the second operand wins when either is NaN.
+__device__ __forceinline__ float smin(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ float smax(float a, float b) { return a > b ? a : b; }
+// _mm_cvtps_epi32: nearest even, 0x80000000 out of range or NaN.
+__device__ __forceinline__ int32_t cvt_rne(float x) {
+    if (!(x >= -2147483648.0f && x < 2147483648.0f)) return INT_MIN;
+    return __float2int_rn(x);
+}
+__device__ __forceinline__ float i2f(int32_t v) { return __int2float_rn(v); }
+
+struct Line { float fx, fy, tx, ty; };
+struct Cubic { Line base; Line ctrl; };
+
+// Segment::to_cubic (content/src/segment.rs:171-182).
+__device__ __forceinline__ Cubic quad_to_cubic(float p0x, float p0y, float cx, float cy, float p3x, float p3y) {
+    const float third = 1.0f / 3.0f;
+    float p12x = fadd(cx, cx), p12y = fadd(cy, cy);
+    Cubic c;
+    c.base = Line{p0x, p0y, p3x, p3y};
+    c.ctrl = Line{fmul(fadd(p0x, p12x), third), fmul(fadd(p0y, p12y), third),
+                  fmul(fadd(p12x, p3x), third), fmul(fadd(p12y, p3y), third)};
+    return c;
+}
+
+// CubicSegment::is_flat(0.25) (content/src/segment.rs:292-300).
+__device__ __forceinline__ bool cubic_is_flat(const Cubic& s) {
+    float u0 = fmul(3.0f, s.ctrl.fx), u1 = fmul(3.0f, s.ctrl.fy);
+    float u2 = fmul(3.0f, s.ctrl.tx), u3 = fmul(3.0f, s.ctrl.ty);
+    u0 = fsub(fsub(fsub(u0, s.base.fx), s.base.fx), s.base.tx);
+    u1 = fsub(fsub(fsub(u1, s.base.fy), s.base.fy), s.base.ty);
+    u2 = fsub(fsub(fsub(u2, s.base.tx), s.base.tx), s.base.fx);
+    u3 = fsub(fsub(fsub(u3, s.base.ty), s.base.ty), s.base.fy);
+    u0 = fmul(u0, u0); u1 = fmul(u1, u1); u2 = fmul(u2, u2); u3 = fmul(u3, u3);
+    return fadd(smax(u0, u2), smax(u1, u3)) <= 1.0f;  // 16 * 0.25 * 0.25
+}
+
+// CubicSegment::split at t = 0.5 (content/src/segment.rs:307-359).
+__device__ __forceinline__ void cubic_split_half(const Cubic& s, Cubic& a, Cubic& b) {
+    const float t = 0.5f;
+    float p0x = s.base.fx, p0y = s.base.fy, p3x = s.base.tx, p3y = s.base.ty;
+    float p1x = s.ctrl.fx, p1y = s.ctrl.fy, p2x = s.ctrl.tx, p2y = s.ctrl.ty;
+    float p01x = fadd(p0x, fmul(t, fsub(p1x, p0x))), p01y = fadd(p0y, fmul(t, fsub(p1y, p0y)));
+    float p12x = fadd(p1x, fmul(t, fsub(p2x, p1x))), p12y = fadd(p1y, fmul(t, fsub(p2y, p1y)));
+    float p23x = fadd(p2x, fmul(t, fsub(p3x, p2x))), p23y = fadd(p2y, fmul(t, fsub(p3y, p2y)));
+    float p012x = fadd(p01x, fmul(t, fsub(p12x, p01x))), p012y = fadd(p01y, fmul(t, fsub(p12y, p01y)));
+    float p123x = fadd(p12x, fmul(t, fsub(p23x, p12x))), p123y = fadd(p12y, fmul(t, fsub(p23y, p12y)));
+    float mx = fadd(p012x, fmul(t, fsub(p123x, p012x))), my = fadd(p012y, fmul(t, fsub(p123y, p012y)));
+    a.base = Line{p0x, p0y, mx, my};  a.ctrl = Line{p01x, p01y, p012x, p012y};
+    b.base = Line{mx, my, p3x, p3y};  b.ctrl = Line{p123x, p123y, p23x, p23y};
+}
+
+// Per-path context for the DDA.
+struct PathCtx {
+    int32_t minx, miny, maxx, maxy;  // tile rect
+    uint32_t tile_base;              // global tile index of (minx, miny)
+    uint32_t col_base;               // first above-rect column backdrop
+    float vminx, vmaxx, vmaxy;       // clip box x range and max y (view box)
+};
+
+__device__ __forceinline__ uint32_t outcode(float x, float y, float minx, float maxx, float maxy) {
+    uint32_t o = 0;
+    if (x < minx) o |= 1u;
+    // y < -inf never holds (TOP)
+    if (x > maxx) o |= 2u;
+    if (y > maxy) o |= 8u;
+    return o;
+}
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return fadd(a, fmul(fsub(b, a), t)); }
+
+// clip_line_segment_to_rect (content/src/clip.rs:494-560) against
+// (view min x, -inf) .. (view max x, view max y) (renderer/src/tiler.rs:194-200).
+__device__ __forceinline__ bool clip_to_view(Line& s, float minx, float maxx, float maxy) {
+    uint32_t of = outcode(s.fx, s.fy, minx, maxx, maxy), ot = outcode(s.tx, s.ty, minx, maxx, maxy);
+    for (int it = 0; it < 8; it++) {
+        if ((of | ot) == 0) return true;
+        if ((of & ot) != 0) return false;
+        bool clip_from = of > ot;
+        uint32_t oc = clip_from ? of : ot;
+        float px = clip_from ? s.fx : s.tx, py = clip_from ? s.fy : s.ty;
+        if (oc & 1u) {
+            px = minx; py = lerpf(s.fy, s.ty, fdiv(fsub(minx, s.fx), fsub(s.tx, s.fx)));
+        } else if (oc & 2u) {
+            px = maxx; py = lerpf(s.fy, s.ty, fdiv(fsub(maxx, s.fx), fsub(s.tx, s.fx)));
+        } else if (oc & 8u) {
+            px = lerpf(s.fx, s.tx, fdiv(fsub(maxy, s.fy), fsub(s.ty, s.fy))); py = maxy;
+        }
+        if (clip_from) { s.fx = px; s.fy = py; of = outcode(px, py, minx, maxx, maxy); }
+        else { s.tx = px; s.ty = py; ot = outcode(px, py, minx, maxx, maxy); }
+    }
+    return false;
+}
+
+// ObjectBuilder::add_fill (renderer/src/builder.rs:509-553) without the push:
+// returns false when the fill is culled, else the packed LineSegmentU16 and the
+// global tile index.
+__device__ __forceinline__ bool make_fill(const PathCtx& pc, Line s, int32_t tx, int32_t ty,
+                                          uint2& rec, uint32_t& g) {
+    if (!(pc.minx <= tx && pc.miny <= ty && tx <= pc.maxx - 1 && ty <= pc.maxy - 1)) return false;
+    float ulx = fmul(i2f(tx), 16.0f), uly = fmul(i2f(ty), 16.0f);
+    const float hi = 4095.0f;
+    int32_t i0 = cvt_rne(smin(smax(fmul(fsub(s.fx, ulx), 256.0f), 0.0f), hi));
+    int32_t i1 = cvt_rne(smin(smax(fmul(fsub(s.fy, uly), 256.0f), 0.0f), hi));
+    int32_t i2 = cvt_rne(smin(smax(fmul(fsub(s.tx, ulx), 256.0f), 0.0f), hi));
+    int32_t i3 = cvt_rne(smin(smax(fmul(fsub(s.ty, uly), 256.0f), 0.0f), hi));
+    if (i0 == i2) return false;
+    rec.x = (uint32_t)i0 | ((uint32_t)i1 << 16);
+    rec.y = (uint32_t)i2 | ((uint32_t)i3 << 16);
+    g = pc.tile_base + (uint32_t)(tx - pc.minx) + (uint32_t)(pc.maxx - pc.minx) * (uint32_t)(ty - pc.miny);
+    return true;
+}
+
+// process_line_segment (renderer/src/tiler.rs:191-308).  `sink` receives
+// sink.fill(rec, g) for every kept fill in emission order and
+// sink.backdrop(tx, ty, delta) for every backdrop adjustment.
+template <class Sink>
+__device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink, uint32_t dda_limit,
+                                         uint32_t* status) {
+    if (!clip_to_view(seg, pc.vminx, pc.vmaxx, pc.vmaxy)) return;
+    const float r = 1.0f / 16.0f;
+    int32_t ftx = cvt_rne(floorf(fmul(seg.fx, r))), fty = cvt_rne(floorf(fmul(seg.fy, r)));
+    int32_t ttx = cvt_rne(floorf(fmul(seg.tx, r))), tty = cvt_rne(floorf(fmul(seg.ty, r)));
+    float vx = fsub(seg.tx, seg.fx), vy = fsub(seg.ty, seg.fy);
+    bool negx = vx < 0.0f, negy = vy < 0.0f;
+    int32_t stepx = negx ? -1 : 1, stepy = negy ? -1 : 1;
+    float fcx = fmul(i2f(ftx + (negx ? 0 : 1)), 16.0f), fcy = fmul(i2f(fty + (negy ? 0 : 1)), 16.0f);
+    float tmx = fdiv(fsub(fcx, seg.fx), vx), tmy = fdiv(fsub(fcy, seg.fy), vy);
+    float tdx = fabsf(fdiv(16.0f, vx)), tdy = fabsf(fdiv(16.0f, vy));
+    float cx = seg.fx, cy = seg.fy;
+    int32_t tcx = ftx, tcy = fty;
+    int last = 0;  // 0 none, 1 X, 2 Y
+    for (uint32_t it = 0;; it++) {
+        if (it >= dda_limit) { atomicOr(status, kStatusDdaLimit); return; }
+        int dir;
+        if (tmx < tmy) dir = 1;
+        else if (tmx > tmy) dir = 2;
+        else dir = stepx > 0 ? 1 : 2;
+        float next_t = fminf(dir == 1 ? tmx : tmy, 1.0f);
+        if (tcx == ttx && tcy == tty) dir = 0;
+        float npx = fadd(seg.fx, fmul(vx, next_t)), npy = fadd(seg.fy, fmul(vy, next_t));
+        uint2 rec; uint32_t g;
+        if (make_fill(pc, Line{cx, cy, npx, npy}, tcx, tcy, rec, g)) sink.fill(rec, g);
+        if (stepy < 0 && dir == 2) {
+            if (make_fill(pc, Line{npx, npy, fmul(i2f(tcx), 16.0f), fmul(i2f(tcy), 16.0f)}, tcx, tcy, rec, g))
+                sink.fill(rec, g);
+        } else if (stepy > 0 && last == 2) {
+            if (make_fill(pc, Line{fmul(i2f(tcx), 16.0f), fmul(i2f(tcy), 16.0f), cx, cy}, tcx, tcy, rec, g))
+                sink.fill(rec, g);
+        }
+        if (stepx < 0 && last == 1) sink.backdrop(tcx, tcy, 1);
+        else if (stepx > 0 && dir == 1) sink.backdrop(tcx, tcy, -1);
+        if (dir == 0) break;
+        if (dir == 1) {
+            if (tcx == ttx) break;
+            tmx = fadd(tmx, tdx); tmy = fadd(tmy, 0.0f);
+            tcx += stepx;
+        } else {
+            if (tcy == tty) break;
+            tmx = fadd(tmx, 0.0f); tmy = fadd(tmy, tdy);
+            tcy += stepy;
+        }
+        cx = npx; cy = npy;
+        last = dir;
+    }
+}
+
+// process_segment (renderer/src/tiler.rs:166-184) with an explicit stack in
+// place of recursion; lines come out in the same depth-first order.
+template <class Sink>
+__device__ __forceinline__ void tile_segment(const PathCtx& pc, const float2* pts, SegRec sr, Sink& sink,
+                                             uint32_t dda_limit, uint32_t* status, uint32_t& lines) {
+    float2 p0 = pts[sr.x];
+    float2 pe = pts[sr.y];
+    if (sr.z == (int)kSegLine) {
+        lines++;
+        dda_line(pc, Line{p0.x, p0.y, pe.x, pe.y}, sink, dda_limit, status);
+        return;
+    }
+    Cubic c;
+    if (sr.z == (int)kSegQuad) {
+        float2 q = pts[sr.x + 1];
+        c = quad_to_cubic(p0.x, p0.y, q.x, q.y, pe.x, pe.y);
+    } else {
+        float2 c0 = pts[sr.x + 1], c1 = pts[sr.x + 2];
+        c.base = Line{p0.x, p0.y, pe.x, pe.y};
+        c.ctrl = Line{c0.x, c0.y, c1.x, c1.y};
+    }
+    Cubic stack[kMaxFlattenDepth + 2];
+    uint8_t depth[kMaxFlattenDepth + 2];
+    int sp = 0;
+    stack[0] = c; depth[0] = 0; sp = 1;
+    while (sp > 0) {
+        --sp;
+        Cubic cur = stack[sp];
+        int d = depth[sp];
+        bool flat = cubic_is_flat(cur);
+        if (flat || d >= kMaxFlattenDepth) {
+            if (!flat) atomicOr(status, kStatusDepthLimit);
+            lines++;
+            dda_line(pc, cur.base, sink, dda_limit, status);
+        } else {
+            Cubic a, b;
+            cubic_split_half(cur, a, b);
+            stack[sp] = b; depth[sp] = (uint8_t)(d + 1); sp++;
+            stack[sp] = a; depth[sp] = (uint8_t)(d + 1); sp++;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Coverage: exact signed area below each fill inside each pixel.
+//
+// The reference evaluates, per fill and per pixel, dX * area(y, -|d dX|)
+// (shaders/fill_area.inc.glsl:11-27 with utils/area-lut/src/main.rs:29-65):
+// the area of the pixel lying below the fill inside the fill's x-window,
+// signed by direction.  The same quantity is accumulated here cell by cell:
+// the fill is cut at pixel columns and rows; each piece adds its trapezoid
+// area to its own cell and its x-extent to every cell below it in the column
+// (a carry resolved by a prefix down the column).  Sums are kept in 2^-22
+// fixed point so the result does not depend on summation order.
+// ---------------------------------------------------------------------------
+constexpr float kCovScale = 4194304.0f;      // 2^22
+constexpr float kCovInvScale = 1.0f / 4194304.0f;
+
+// Accumulate one fill (8.8 fixed point, tile-local) into acc[row][col] and
+// carry[row][col] (int, 256 each, shared memory).
+__device__ __forceinline__ void accumulate_fill_cells(uint2 rec, int* acc, int* carry) {
+    float x0 = (float)(rec.x & 0xffffu) * (1.0f / 256.0f), y0 = (float)(rec.x >> 16) * (1.0f / 256.0f);
+    float x1 = (float)(rec.y & 0xffffu) * (1.0f / 256.0f), y1 = (float)(rec.y >> 16) * (1.0f / 256.0f);
+    if (x0 == x1) return;
+    float slope = (y1 - y0) / (x1 - x0);
+    float xmin = fminf(x0, x1), xmax = fmaxf(x0, x1);
+    int c0 = (int)floorf(xmin), c1 = (int)ceilf(xmax) - 1;
+    c0 = max(c0, 0); c1 = min(c1, 15);
+    for (int px = c0; px <= c1; px++) {
+        float lo = (float)px, hi = (float)(px + 1);
+        float xa = fminf(fmaxf(x0, lo), hi), xb = fminf(fmaxf(x1, lo), hi);
+        float w = xa - xb;  // oriented x-extent (window.x - window.y)
+        if (w == 0.0f) continue;
+        float ya = y0 + (xa - x0) * slope, yb = y0 + (xb - x0) * slope;
+        float ylo = fminf(ya, yb), yhi = fmaxf(ya, yb);
+        ylo = fminf(fmaxf(ylo, 0.0f), 16.0f); yhi = fminf(fmaxf(yhi, 0.0f), 16.0f);
+        if (yhi - ylo <= 0.0f) {
+            int r = (int)floorf(ylo);
+            if (r > 15) continue;
+            atomicAdd(&acc[r * 16 + px], __float2int_rn(w * ((float)(r + 1) - ylo) * kCovScale));
+            if (r + 1 < 16) atomicAdd(&carry[(r + 1) * 16 + px], __float2int_rn(w * kCovScale));
+            continue;
+        }
+        float inv_h = 1.0f / (yhi - ylo);
+        int r0 = (int)floorf(ylo), r1 = min((int)floorf(yhi), 15);
+        for (int r = r0; r <= r1; r++) {
+            float yt = fmaxf(ylo, (float)r), yb2 = fminf(yhi, (float)(r + 1));
+            float h = yb2 - yt;
+            if (h <= 0.0f) continue;
+            float wr = w * (h * inv_h);
+            float a = wr * ((float)(r + 1) - 0.5f * (yt + yb2));
+            atomicAdd(&acc[r * 16 + px], __float2int_rn(a * kCovScale));
+            if (r + 1 < 16) atomicAdd(&carry[(r + 1) * 16 + px], __float2int_rn(wr * kCovScale));
+        }
+    }
+}
+
+// sampleMask resolve (shaders/tile_fragment.inc.glsl:539-556).
+__device__ __forceinline__ float resolve_coverage(float c, bool even_odd) {
+    if (!even_odd) c = fabsf(c);
+    else {
+        float m = c - 2.0f * floorf(c * 0.5f);
+        c = 1.0f - fabsf(1.0f - m);
+    }
+    return fminf(1.0f, c);
+}
+
+}  // namespace pf

@@ -1,0 +1,69 @@
+// pf_kernels.cuh — launch wrappers of the CUDA level's kernels (host side).
+#pragma once
+
+#include "pf_device.cuh"
+
+namespace pf {
+
+struct FrameDev {
+    // scene
+    const float2* pts;           // points used by the tiler (transformed copy when needed)
+    const SegRec* segs;
+    uint32_t seg_count;
+    PathDev path;
+    const SceneDev* scenes;
+    uint32_t path_count;
+    uint32_t scene_count;
+    // tile arrays (capacity tile_cap; +1 for scan totals)
+    uint32_t tile_cap, col_cap, fill_cap, vis_cap, screen_count;
+    uint32_t* tile_fill_count;   // [tile_cap+1]
+    uint32_t* tile_fill_base;    // [tile_cap+1]
+    uint32_t* tile_alpha;        // [tile_cap+1] exclusive scan of has-fill flags
+    int32_t*  tile_delta;        // [tile_cap] backdrop deltas
+    int32_t*  col_backdrop;      // [col_cap] above-rect column sums
+    uint32_t* seg_fill_count;    // [seg_count+1]
+    uint32_t* seg_fill_base;     // [seg_count+1]
+    uint2*    fills;             // [fill_cap] LineSegmentU16
+    uint32_t* fill_e;            // [fill_cap] emission index
+    int4*     tiles;             // [tile_cap] PFCUDATile records
+    int4*     clips;             // [tile_cap] PFCUDAClip records
+    uint32_t* alpha_owner;       // [tile_cap] alpha id -> owning global tile
+    int32_t*  zbuf;              // [screen_count]
+    uint32_t* screen_cnt;        // [screen_count+1]
+    uint32_t* screen_base;       // [screen_count+1]
+    uint32_t* vis;               // [vis_cap] global tile indices
+    Counters* counters;
+    uint32_t dda_limit;
+};
+
+// Number of kernels this library has launched (host counter).
+uint64_t launch_counter();
+void count_launch(uint32_t n = 1);
+
+// scan scratch
+struct ScanTemp { uint32_t* partials; uint32_t cap; };
+
+void launch_transform(const float2* in, float2* out, uint32_t n, const float* m6, cudaStream_t s);
+void launch_contour_segcount(const uint32_t* ord_contour, uint32_t nord, const uint32_t* contour_starts,
+                             const uint8_t* flags, uint32_t* seg_count, uint32_t* status, cudaStream_t s);
+void launch_contour_segemit(const uint32_t* ord_contour, const uint32_t* ord_path, uint32_t nord,
+                            const uint32_t* contour_starts, const uint8_t* flags, const uint32_t* seg_base,
+                            SegRec* segs, cudaStream_t s);
+void launch_bound(const FrameDev& f, const uint32_t* ord_contour, const uint32_t* contour_starts, cudaStream_t s);
+void launch_path_scan(const FrameDev& f, cudaStream_t s);
+void launch_tile_count(const FrameDev& f, cudaStream_t s);
+void launch_tile_emit(const FrameDev& f, cudaStream_t s);
+// Exclusive scan of n (device-resident count at d_n, capacity n_cap) u32
+// values; mode 0: values, mode 1: (value != 0).  Writes out[0..n] (out[n] = total)
+// and, when total_out != NULL, the total as u64.
+void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_t n_host, uint32_t n_cap,
+                 int mode, uint64_t* total_out, ScanTemp& tmp, cudaStream_t s);
+
+void launch_propagate(const FrameDev& f, bool clip_pass, uint32_t first_path, uint32_t path_count,
+                      uint32_t max_width, cudaStream_t s);
+void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s);
+// mode 0: RGBA8, 1: R8 single channel, 2: FP32 single channel
+void launch_composite(const FrameDev& f, int mode, void* out, const float4& background, cudaStream_t s);
+void launch_masks(const FrameDev& f, float* alpha_masks, float* tile_cov, cudaStream_t s);
+
+}  // namespace pf

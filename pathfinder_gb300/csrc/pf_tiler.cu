@@ -1,0 +1,443 @@
+// pf_tiler.cu — scene packing, bound, and the two tiling passes of the CUDA
+// level.  Built with -fmad=false: the tiling arithmetic must match the
+// reference CPU tiler bit for bit (see pf_device.cuh).
+//
+// Stage map (reference -> here):
+//   SegmentsD3D11::add_path (renderer/src/builder.rs:804-841) and
+//   ContourIter::next (content/src/outline.rs:1024-1065)  -> k_contour_seg*
+//   Tiler::new bounds / BuiltPath::new tile rect
+//   (renderer/src/tiler.rs:40-66, builder.rs:415-485)     -> k_bound, k_path_scan
+//   generate_fills: process_segment/process_line_segment/add_fill/
+//   adjust_alpha_tile_backdrop (tiler.rs:83-308,
+//   builder.rs:509-616)                                    -> k_tile_count, k_tile_emit
+#include "pf_kernels.cuh"
+
+#include <atomic>
+
+namespace pf {
+
+static std::atomic<uint64_t> g_launches{0};
+uint64_t launch_counter() { return g_launches.load(); }
+void count_launch(uint32_t n) { g_launches += n; }
+
+// ---------------------------------------------------------------------------
+// warp / block scan helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t warp_inclusive_scan(uint32_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Exclusive block scan for blockDim.x == NT (multiple of 32); returns the
+// block total in *total.
+template <int NT>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t warp_sums[NT / 32];
+    __shared__ uint32_t block_total;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t inc = warp_inclusive_scan(v);
+    if (lane == 31) warp_sums[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t s = lane < NT / 32 ? warp_sums[lane] : 0;
+        uint32_t si = warp_inclusive_scan(s);
+        if (lane < NT / 32) warp_sums[lane] = si - s;
+        if (lane == NT / 32 - 1) block_total = si;
+    }
+    __syncthreads();
+    uint32_t r = inc - v + warp_sums[wid];
+    *total = block_total;
+    __syncthreads();
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// generic exclusive scan (reduce, scan partials, down-sweep)
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 256, kScanItems = 8, kScanChunk = kScanThreads * kScanItems;
+
+// Element count: the device-side total clamped to the buffer capacity (an
+// overflowing frame is flagged elsewhere and re-run), or the host count.
+__device__ __forceinline__ uint32_t scan_count(const uint64_t* d_n, uint32_t n_host) {
+    if (!d_n) return n_host;
+    uint64_t n = *d_n;
+    return n < (uint64_t)n_host ? (uint32_t)n : n_host;
+}
+
+__device__ __forceinline__ uint32_t scan_in(const uint32_t* in, uint32_t i, uint32_t n, int mode) {
+    if (i >= n) return 0;
+    uint32_t v = in[i];
+    return mode == 1 ? (v != 0u ? 1u : 0u) : v;
+}
+
+__global__ void k_scan_reduce(const uint32_t* __restrict__ in, const uint64_t* d_n, uint32_t n_host, int mode,
+                              uint32_t* __restrict__ partials) {
+    uint32_t n = scan_count(d_n, n_host);
+    uint32_t base = blockIdx.x * kScanChunk;
+    if (base >= n) return;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) s += scan_in(in, base + k * kScanThreads + threadIdx.x, n, mode);
+    uint32_t total;
+    block_exclusive_scan<kScanThreads>(s, &total);
+    if (threadIdx.x == 0) partials[blockIdx.x] = total;
+}
+
+__global__ void k_scan_partials(uint32_t* partials, const uint64_t* d_n, uint32_t n_host, uint32_t* out,
+                                uint64_t* total_out) {
+    uint32_t n = scan_count(d_n, n_host);
+    uint32_t nb = (n + kScanChunk - 1) / kScanChunk;
+    uint32_t carry = 0;
+    for (uint32_t b0 = 0; b0 < nb; b0 += 1024) {
+        uint32_t i = b0 + threadIdx.x;
+        uint32_t v = i < nb ? partials[i] : 0;
+        uint32_t total;
+        uint32_t ex = block_exclusive_scan<1024>(v, &total);
+        if (i < nb) partials[i] = ex + carry;
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        out[n] = carry;
+        if (total_out) *total_out = carry;
+    }
+}
+
+__global__ void k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, const uint64_t* d_n,
+                            uint32_t n_host, int mode, const uint32_t* __restrict__ partials) {
+    uint32_t n = scan_count(d_n, n_host);
+    uint32_t base = blockIdx.x * kScanChunk;
+    if (base >= n) return;
+    // each thread owns kScanItems consecutive items
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+    uint32_t first = base + threadIdx.x * kScanItems;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) { v[k] = scan_in(in, first + k, n, mode); s += v[k]; }
+    uint32_t total;
+    uint32_t ex = block_exclusive_scan<kScanThreads>(s, &total) + partials[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (first + k < n) out[first + k] = ex;
+        ex += v[k];
+    }
+}
+
+void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_t n_host, uint32_t n_cap, int mode,
+                 uint64_t* total_out, ScanTemp& tmp, cudaStream_t s) {
+    uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
+    if (nb == 0) nb = 1;
+    if (d_n) n_host = n_cap;  // device count is clamped to the capacity
+    { count_launch(); k_scan_reduce<<<nb, kScanThreads, 0, s>>>(in, d_n, n_host, mode, tmp.partials); }
+    { count_launch(); k_scan_partials<<<1, 1024, 0, s>>>(tmp.partials, d_n, n_host, out, total_out); }
+    { count_launch(); k_scan_down<<<nb, kScanThreads, 0, s>>>(in, out, d_n, n_host, mode, tmp.partials); }
+}
+
+// ---------------------------------------------------------------------------
+// transform (Contour::transform, content/src/outline.rs:884-893;
+// Transform2F * Vector2F, geometry/src/transform2d.rs:123-129, :312-318)
+// ---------------------------------------------------------------------------
+__global__ void k_transform(const float2* __restrict__ in, float2* __restrict__ out, uint32_t n, float m00,
+                            float m01, float m10, float m11, float vx, float vy) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float2 p = in[i];
+        float hx = fmul(m00, p.x), hy = fmul(m10, p.x), hz = fmul(m01, p.y), hw = fmul(m11, p.y);
+        out[i] = make_float2(fadd(fadd(hx, hz), vx), fadd(fadd(hy, hw), vy));
+    }
+}
+
+void launch_transform(const float2* in, float2* out, uint32_t n, const float* m6, cudaStream_t s) {
+    if (n == 0) return;
+    uint32_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    { count_launch(); k_transform<<<blocks, 256, 0, s>>>(in, out, n, m6[0], m6[1], m6[2], m6[3], m6[4], m6[5]); }
+}
+
+// ---------------------------------------------------------------------------
+// segment packing: one warp per contour (in global path order)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool is_endpoint(const uint8_t* flags, uint32_t i) {
+    return (flags[i] & 3u) == 0;
+}
+
+__global__ void k_contour_segcount(const uint32_t* __restrict__ ord_contour, uint32_t nord,
+                                   const uint32_t* __restrict__ starts, const uint8_t* __restrict__ flags,
+                                   uint32_t* __restrict__ seg_count, uint32_t* status) {
+    uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (k >= nord) return;
+    uint32_t c = ord_contour[k];
+    uint32_t a = starts[c], b = starts[c + 1];
+    uint32_t n = b > a ? b - a : 0;
+    uint32_t count = 0;
+    bool bad = false;
+    for (uint32_t i0 = 0; i0 < n; i0 += 32) {
+        uint32_t i = i0 + lane;
+        bool start = i < n && (i == 0 || is_endpoint(flags, a + i));
+        if (start && i + 1 < n && !is_endpoint(flags, a + i + 1)) {
+            // curve: needs its end point inside the contour
+            if (i + 2 >= n) bad = true;
+            else if (!is_endpoint(flags, a + i + 2) && i + 3 >= n) bad = true;
+        }
+        count += __popc(__ballot_sync(0xffffffffu, start));
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(status, kStatusMalformed);
+    if (lane == 0) seg_count[k] = count;
+}
+
+__global__ void k_contour_segemit(const uint32_t* __restrict__ ord_contour, const uint32_t* __restrict__ ord_path,
+                                  uint32_t nord, const uint32_t* __restrict__ starts,
+                                  const uint8_t* __restrict__ flags, const uint32_t* __restrict__ seg_base,
+                                  SegRec* __restrict__ segs) {
+    uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (k >= nord) return;
+    uint32_t c = ord_contour[k], gp = ord_path[k];
+    uint32_t a = starts[c], b = starts[c + 1];
+    uint32_t n = b > a ? b - a : 0;
+    uint32_t out = seg_base[k];
+    for (uint32_t i0 = 0; i0 < n; i0 += 32) {
+        uint32_t i = i0 + lane;
+        bool start = i < n && (i == 0 || is_endpoint(flags, a + i));
+        uint32_t m = __ballot_sync(0xffffffffu, start);
+        if (start) {
+            SegRec r;
+            r.x = (int)(a + i);
+            r.w = (int)gp;
+            if (i + 1 >= n) { r.y = (int)a; r.z = (int)kSegLine; }
+            else if (is_endpoint(flags, a + i + 1)) { r.y = (int)(a + i + 1); r.z = (int)kSegLine; }
+            else if (i + 2 < n && is_endpoint(flags, a + i + 2)) { r.y = (int)(a + i + 2); r.z = (int)kSegQuad; }
+            else if (i + 3 < n) { r.y = (int)(a + i + 3); r.z = (int)kSegCubic; }
+            else { r.y = (int)a; r.z = (int)kSegLine; }  // malformed (flagged by k_contour_segcount)
+            segs[out + __popc(m & ((1u << lane) - 1u))] = r;
+        }
+        out += __popc(m);
+    }
+}
+
+void launch_contour_segcount(const uint32_t* ord_contour, uint32_t nord, const uint32_t* starts, const uint8_t* flags,
+                             uint32_t* seg_count, uint32_t* status, cudaStream_t s) {
+    if (nord == 0) return;
+    uint32_t blocks = (nord * 32 + 255) / 256;
+    { count_launch(); k_contour_segcount<<<blocks, 256, 0, s>>>(ord_contour, nord, starts, flags, seg_count, status); }
+}
+
+void launch_contour_segemit(const uint32_t* ord_contour, const uint32_t* ord_path, uint32_t nord,
+                            const uint32_t* starts, const uint8_t* flags, const uint32_t* seg_base, SegRec* segs,
+                            cudaStream_t s) {
+    if (nord == 0) return;
+    uint32_t blocks = (nord * 32 + 255) / 256;
+    { count_launch(); k_contour_segemit<<<blocks, 256, 0, s>>>(ord_contour, ord_path, nord, starts, flags, seg_base, segs); }
+}
+
+// ---------------------------------------------------------------------------
+// bound: one warp per path
+// ---------------------------------------------------------------------------
+__global__ void k_bound(FrameDev f, const uint32_t* __restrict__ ord_contour, const uint32_t* __restrict__ starts) {
+    uint32_t gp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gp >= f.path_count) return;
+    float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+    bool any = false;
+    uint32_t k0 = f.path.first_ord_contour[gp], k1 = f.path.first_ord_contour[gp + 1];
+    for (uint32_t k = k0; k < k1; k++) {
+        uint32_t c = ord_contour[k];
+        uint32_t a = starts[c], b = starts[c + 1];
+        if (b > a) any = true;
+        for (uint32_t i = a + lane; i < b; i += 32) {
+            float2 p = f.pts[i];
+            mnx = smin(mnx, p.x); mny = smin(mny, p.y);
+            mxx = smax(mxx, p.x); mxy = smax(mxy, p.y);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = smin(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mny = smin(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxx = smax(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxy = smax(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    if (lane != 0) return;
+    const SceneDev& sc = f.scenes[f.path.scene[gp]];
+    float bx0 = 0.0f, by0 = 0.0f, bx1 = 0.0f, by1 = 0.0f;
+    if (any) {
+        // RectF::intersection (geometry/src/rect.rs:116-139); default rect when disjoint
+        float4 v = sc.view_box;
+        if (mnx < v.z && mny < v.w && v.x < mxx && v.y < mxy) {
+            bx0 = smax(mnx, v.x); by0 = smax(mny, v.y);
+            bx1 = smin(mxx, v.z); by1 = smin(mxy, v.w);
+        }
+    }
+    // round_rect_out_to_tile_bounds (renderer/src/tiles.rs:64-66)
+    const float q = 1.0f / 16.0f;
+    int4 r;
+    r.x = cvt_rne(floorf(fmul(bx0, q))); r.y = cvt_rne(floorf(fmul(by0, q)));
+    r.z = cvt_rne(ceilf(fmul(bx1, q)));  r.w = cvt_rne(ceilf(fmul(by1, q)));
+    f.path.tile_rect[gp] = r;
+}
+
+void launch_bound(const FrameDev& f, const uint32_t* ord_contour, const uint32_t* starts, cudaStream_t s) {
+    if (f.path_count == 0) return;
+    uint32_t blocks = (f.path_count * 32 + 255) / 256;
+    { count_launch(); k_bound<<<blocks, 256, 0, s>>>(f, ord_contour, starts); }
+}
+
+// single block: tile and column offsets of every path
+__global__ void k_path_scan(FrameDev f) {
+    uint64_t tcarry = 0, ccarry = 0;
+    for (uint32_t b0 = 0; b0 < f.path_count; b0 += 1024) {
+        uint32_t gp = b0 + threadIdx.x;
+        uint32_t tiles = 0, cols = 0;
+        if (gp < f.path_count) {
+            int4 r = f.path.tile_rect[gp];
+            int w = r.z - r.x, h = r.w - r.y;
+            if (w > 0 && h > 0) { tiles = (uint32_t)w * (uint32_t)h; }
+            cols = w > 0 ? (uint32_t)w : 0u;
+        }
+        uint32_t tt, ct;
+        uint32_t te = block_exclusive_scan<1024>(tiles, &tt);
+        uint32_t ce = block_exclusive_scan<1024>(cols, &ct);
+        if (gp < f.path_count) {
+            f.path.tile_offset[gp] = (uint32_t)(tcarry + te);
+            f.path.col_offset[gp] = (uint32_t)(ccarry + ce);
+        }
+        tcarry += tt;
+        ccarry += ct;
+    }
+    if (threadIdx.x == 0) {
+        f.path.tile_offset[f.path_count] = (uint32_t)tcarry;
+        f.path.col_offset[f.path_count] = (uint32_t)ccarry;
+        f.counters->tiles = tcarry;
+        f.counters->columns = ccarry;
+        if (tcarry > f.tile_cap) {
+            atomicOr(&f.counters->status, kStatusTileCapacity);
+            f.counters->needed_tiles = tcarry;
+        }
+        if (ccarry > f.col_cap) {
+            atomicOr(&f.counters->status, kStatusColumnCapacity);
+            f.counters->needed_tiles = tcarry > f.counters->needed_tiles ? tcarry : f.counters->needed_tiles;
+        }
+    }
+}
+
+// zero the per-tile accumulators of this frame
+__global__ void k_zero_tiles(FrameDev f) {
+    uint64_t T = f.counters->tiles, C = f.counters->columns;
+    if (T > f.tile_cap || C > f.col_cap) return;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < T || i < C;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if (i < T) { f.tile_fill_count[i] = 0; f.tile_delta[i] = 0; }
+        if (i < C) f.col_backdrop[i] = 0;
+    }
+}
+
+void launch_path_scan(const FrameDev& f, cudaStream_t s) {
+    { count_launch(); k_path_scan<<<1, 1024, 0, s>>>(f); }
+    { count_launch(); k_zero_tiles<<<152 * 8, 256, 0, s>>>(f); }
+}
+
+// ---------------------------------------------------------------------------
+// tiling passes: one thread per input segment
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ PathCtx path_ctx(const FrameDev& f, uint32_t gp) {
+    PathCtx pc;
+    int4 r = f.path.tile_rect[gp];
+    pc.minx = r.x; pc.miny = r.y; pc.maxx = r.z; pc.maxy = r.w;
+    pc.tile_base = f.path.tile_offset[gp];
+    pc.col_base = f.path.col_offset[gp];
+    float4 v = f.scenes[f.path.scene[gp]].view_box;
+    pc.vminx = v.x; pc.vmaxx = v.z; pc.vmaxy = v.w;
+    return pc;
+}
+
+struct CountSink {
+    const PathCtx* pc;
+    uint32_t* tile_fill_count;
+    int32_t* tile_delta;
+    int32_t* col_backdrop;
+    uint32_t n;
+    __device__ __forceinline__ void fill(uint2, uint32_t g) {
+        n++;
+        atomicAdd(&tile_fill_count[g], 1u);
+    }
+    __device__ __forceinline__ void backdrop(int32_t tx, int32_t ty, int32_t d) {
+        // ObjectBuilder::adjust_alpha_tile_backdrop (renderer/src/builder.rs:595-616)
+        int32_t w = pc->maxx - pc->minx, h = pc->maxy - pc->miny;
+        int32_t ox = tx - pc->minx, oy = ty - pc->miny;
+        if (ox < 0 || ox >= w || oy >= h) return;
+        if (oy < 0) atomicAdd(&col_backdrop[pc->col_base + (uint32_t)ox], d);
+        else atomicAdd(&tile_delta[pc->tile_base + (uint32_t)(oy * w + ox)], d);
+    }
+};
+
+__global__ void __launch_bounds__(128) k_tile_count(FrameDev f) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    bool ok = f.counters->tiles <= f.tile_cap && f.counters->columns <= f.col_cap;
+    uint32_t lines = 0;
+    if (s < f.seg_count && ok) {
+        SegRec sr = f.segs[s];
+        PathCtx pc = path_ctx(f, (uint32_t)sr.w);
+        CountSink sink{&pc, f.tile_fill_count, f.tile_delta, f.col_backdrop, 0};
+        tile_segment(pc, f.pts, sr, sink, f.dda_limit, &f.counters->status, lines);
+        f.seg_fill_count[s] = sink.n;
+    } else if (s < f.seg_count) {
+        f.seg_fill_count[s] = 0;
+    }
+    // line count for RenderStats
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lines += __shfl_xor_sync(0xffffffffu, lines, o);
+    if ((threadIdx.x & 31) == 0 && lines) atomicAdd((unsigned long long*)&f.counters->lines, (unsigned long long)lines);
+}
+
+struct EmitSink {
+    uint2* fills;
+    uint32_t* fill_e;
+    const uint32_t* tile_fill_base;
+    uint32_t* cursor;
+    uint32_t fill_cap;
+    uint32_t e;
+    __device__ __forceinline__ void fill(uint2 rec, uint32_t g) {
+        uint32_t slot = tile_fill_base[g] + atomicSub(&cursor[g], 1u) - 1u;
+        if (slot < fill_cap) { fills[slot] = rec; fill_e[slot] = e; }
+        e++;
+    }
+    __device__ __forceinline__ void backdrop(int32_t, int32_t, int32_t) {}
+};
+
+__global__ void __launch_bounds__(128) k_tile_emit(FrameDev f) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= f.seg_count) return;
+    if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
+    if (f.counters->fills > f.fill_cap) return;
+    if (f.seg_fill_count[s] == 0) return;
+    SegRec sr = f.segs[s];
+    PathCtx pc = path_ctx(f, (uint32_t)sr.w);
+    EmitSink sink{f.fills, f.fill_e, f.tile_fill_base, f.tile_fill_count, f.fill_cap, f.seg_fill_base[s]};
+    uint32_t lines = 0;
+    tile_segment(pc, f.pts, sr, sink, f.dda_limit, &f.counters->status, lines);
+}
+
+void launch_tile_count(const FrameDev& f, cudaStream_t s) {
+    if (f.seg_count == 0) return;
+    { count_launch(); k_tile_count<<<(f.seg_count + 127) / 128, 128, 0, s>>>(f); }
+}
+
+__global__ void k_check_fills(FrameDev f) {
+    if (f.counters->fills > f.fill_cap) {
+        atomicOr(&f.counters->status, kStatusFillCapacity);
+        f.counters->needed_fills = f.counters->fills;
+    }
+    if (f.counters->alpha_tiles > f.tile_cap) atomicOr(&f.counters->status, kStatusAlphaCapacity);
+}
+
+void launch_tile_emit(const FrameDev& f, cudaStream_t s) {
+    { count_launch(); k_check_fills<<<1, 1, 0, s>>>(f); }
+    if (f.seg_count == 0) return;
+    { count_launch(); k_tile_emit<<<(f.seg_count + 127) / 128, 128, 0, s>>>(f); }
+}
+
+}  // namespace pf

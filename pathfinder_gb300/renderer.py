@@ -1,0 +1,239 @@
+"""The CUDA renderer level behind the reference's Renderer API shape
+(renderer/src/gpu/renderer.rs:76-460, renderer/src/gpu/options.rs:19-46,
+renderer/src/options.rs:53-61), over the C ABI in include/pathfinder_cuda.h.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from enum import IntEnum
+
+import numpy as np
+
+from . import _abi
+from .scene import ColorF, Scene
+
+_FILL, _TILE, _CLIP, _PATH, _RECT = _abi.record_dtypes()
+
+
+class RendererLevel(IntEnum):
+    """renderer/src/gpu/options.rs:41-46, extended with the CUDA level."""
+    D3D9 = 0
+    D3D11 = 1
+    CUDA = 2
+
+
+@dataclass
+class Transform2F:
+    """Row-major 2x3 affine transform (geometry/src/transform2d.rs:187-192)."""
+    m00: float = 1.0
+    m01: float = 0.0
+    m10: float = 0.0
+    m11: float = 1.0
+    tx: float = 0.0
+    ty: float = 0.0
+
+
+@dataclass
+class BuildOptions:
+    """renderer/src/options.rs:53-61 (transform only on this path)."""
+    transform: Transform2F | None = None
+
+    def to_c(self) -> _abi.PFCUDABuildOptions:
+        o = _abi.PFCUDABuildOptions()
+        if self.transform is not None:
+            t = self.transform
+            o.transform = _abi.PFTransform2F(t.m00, t.m01, t.m10, t.m11, _abi.PFVector2F(t.tx, t.ty))
+            o.has_transform = 1
+        return o
+
+
+@dataclass
+class RendererOptions:
+    """renderer/src/gpu/options.rs:19-33."""
+    background_color: ColorF | None = None
+
+    def to_c(self) -> _abi.PFCUDARendererOptions:
+        o = _abi.PFCUDARendererOptions()
+        if self.background_color is not None:
+            c = self.background_color
+            o.background_color = _abi.PFColorF(c.r, c.g, c.b, c.a)
+            o.has_background_color = 1
+        return o
+
+
+@dataclass
+class RenderStats:
+    """renderer/src/gpu/perf.rs:21-44 plus the device counters of the frame."""
+    path_count: int = 0
+    segment_count: int = 0
+    line_count: int = 0
+    fill_count: int = 0
+    tile_count: int = 0
+    alpha_tile_count: int = 0
+    visible_tile_count: int = 0
+    screen_tile_count: int = 0
+    status: int = 0
+    gpu_time_ms: float = 0.0
+    kernel_launches: int = 0
+
+
+def _ptr(x):
+    """(address, memory kind) of a numpy array or a torch tensor."""
+    if isinstance(x, np.ndarray):
+        if not x.flags["C_CONTIGUOUS"]:
+            raise ValueError("output array must be C-contiguous")
+        return x.ctypes.data, _abi.PF_MEMORY_HOST
+    try:
+        import torch
+        if isinstance(x, torch.Tensor):
+            if not x.is_contiguous():
+                raise ValueError("output tensor must be contiguous")
+            return x.data_ptr(), (_abi.PF_MEMORY_DEVICE if x.is_cuda else _abi.PF_MEMORY_HOST)
+    except ImportError:
+        pass
+    raise TypeError(f"unsupported output buffer {type(x)}")
+
+
+class Renderer:
+    """Renderer::new / render_command / end_scene for RendererLevel::CUDA.
+
+    One renderer per stream; not thread-safe (as the reference's &mut self).
+    """
+
+    level = RendererLevel.CUDA
+
+    def __init__(self, device: int = 0, options: RendererOptions | None = None):
+        self._lib = _abi.lib()
+        self._h = C.c_void_p()
+        self.options = options or RendererOptions()
+        o = self.options.to_c()
+        _abi.check(self._lib.PFCUDARendererCreate(device, C.byref(o), C.byref(self._h)), "PFCUDARendererCreate")
+        self._uploaded = None  # (scene id, epoch)
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.PFCUDARendererDestroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def set_stream(self, stream) -> None:
+        """Run on a cudaStream_t (int handle or torch.cuda.Stream)."""
+        h = getattr(stream, "cuda_stream", stream)
+        _abi.check(self._lib.PFCUDARendererSetStream(self._h, C.c_void_p(h)), "PFCUDARendererSetStream")
+
+    def set_options(self, options: RendererOptions) -> None:
+        self.options = options
+        o = options.to_c()
+        _abi.check(self._lib.PFCUDARendererSetOptions(self._h, C.byref(o)), "PFCUDARendererSetOptions")
+
+    def upload_scene(self, scene: Scene, force: bool = False) -> None:
+        """UploadSceneD3D11: only when the scene id or epoch changed."""
+        key = (scene.id, scene.epoch)
+        if not force and self._uploaded == key:
+            return
+        d = scene.desc()
+        _abi.check(self._lib.PFCUDASceneUpload(self._h, C.byref(d)), "PFCUDASceneUpload")
+        self._uploaded = key
+
+    def render(self, scene: Scene, options: BuildOptions | None = None, out=None,
+               width: int | None = None, height: int | None = None):
+        """Scene::build_and_render for the CUDA level: premultiplied RGBA8,
+        row 0 at the top.  ``out`` may be a host numpy array or a CUDA tensor."""
+        self.upload_scene(scene)
+        w, h = width or scene.width, height or scene.height
+        if out is None:
+            out = np.zeros((h, w, 4), np.uint8)
+        p, mem = _ptr(out)
+        bo = (options or BuildOptions()).to_c()
+        _abi.check(self._lib.PFCUDARenderScene(self._h, C.byref(bo), w, h, C.c_void_p(p), mem), "PFCUDARenderScene")
+        return out
+
+    def render_coverage(self, scene: Scene, options: BuildOptions | None = None, out=None,
+                        width: int | None = None, height: int | None = None):
+        """Single-channel FP32 render (SrcOver of paint alpha x coverage)."""
+        self.upload_scene(scene)
+        w, h = width or scene.width, height or scene.height
+        if out is None:
+            out = np.zeros((h, w), np.float32)
+        p, mem = _ptr(out)
+        bo = (options or BuildOptions()).to_c()
+        _abi.check(self._lib.PFCUDARenderCoverage(self._h, C.byref(bo), w, h, C.c_void_p(p), mem),
+                   "PFCUDARenderCoverage")
+        return out
+
+    def render_async(self, scene: Scene, out, options: BuildOptions | None = None,
+                     width: int | None = None, height: int | None = None):
+        """Enqueue a frame into a CUDA uint8 tensor without synchronising
+        (capacity overflows surface in render_status())."""
+        self.upload_scene(scene)
+        w, h = width or scene.width, height or scene.height
+        p, mem = _ptr(out)
+        if mem != _abi.PF_MEMORY_DEVICE:
+            raise ValueError("render_async needs a device output buffer")
+        bo = (options or BuildOptions()).to_c()
+        _abi.check(self._lib.PFCUDARenderSceneAsync(self._h, C.byref(bo), w, h, C.c_void_p(p)),
+                   "PFCUDARenderSceneAsync")
+        return out
+
+    def render_status(self) -> tuple[int, int]:
+        """(status code, needed capacity) of the frames enqueued since the last call."""
+        n = C.c_uint64()
+        code = self._lib.PFCUDARenderStatus(self._h, C.byref(n))
+        return code, n.value
+
+    def set_profiling(self, enable: bool) -> None:
+        _abi.check(self._lib.PFCUDASetProfiling(self._h, 1 if enable else 0), "PFCUDASetProfiling")
+
+    def stage_times(self) -> dict:
+        """Per-stage milliseconds of the last profiled frame (synchronises)."""
+        a = (C.c_float * _abi.PF_CUDA_STAGE_COUNT)()
+        _abi.check(self._lib.PFCUDAGetStageTimes(self._h, a, _abi.PF_CUDA_STAGE_COUNT), "PFCUDAGetStageTimes")
+        return {n: float(a[i]) for i, n in enumerate(_abi.STAGE_NAMES)}
+
+    def stats(self) -> RenderStats:
+        s = _abi.PFCUDARenderStats()
+        _abi.check(self._lib.PFCUDAGetStats(self._h, C.byref(s)), "PFCUDAGetStats")
+        return RenderStats(**{k: getattr(s, k) for k, _ in s._fields_})
+
+    def read_records(self, scene: Scene) -> dict:
+        """Fill / tile / clip records and the z-buffer of the last frame."""
+        st = self.stats()
+        F, T = st.fill_count, st.tile_count
+        P = len(scene.clip_paths) + len(scene.draw_paths)
+        fills = np.zeros((F,), _FILL)
+        fill_tile = np.zeros((F,), np.uint32)
+        tiles = np.zeros((T,), _TILE)
+        clips = np.zeros((T,), _CLIP)
+        offs = np.zeros((P + 1,), np.uint32)
+        rects = np.zeros((P + 1,), _RECT)
+        z = np.zeros((max(st.screen_tile_count, 1),), np.int32)
+        _abi.check(self._lib.PFCUDAReadRecords(self._h, fills.ctypes.data, fill_tile.ctypes.data, F,
+                                               tiles.ctypes.data, T, offs.ctypes.data, rects.ctypes.data, P + 1,
+                                               clips.ctypes.data, z.ctypes.data, len(z)), "PFCUDAReadRecords")
+        return dict(fills=fills, fill_tile=fill_tile, tiles=tiles, clips=clips, path_tile_offsets=offs,
+                    path_tile_rects=rects[:P], z_buffer=z[:st.screen_tile_count])
+
+    def read_masks(self):
+        """(raw alpha masks [A,16,16], resolved coverage per path tile [T,16,16]) of the last frame."""
+        st = self.stats()
+        a = np.zeros((max(st.alpha_tile_count, 1), 16, 16), np.float32)
+        t = np.zeros((max(st.tile_count, 1), 16, 16), np.float32)
+        _abi.check(self._lib.PFCUDAReadMasks(self._h, a.ctypes.data, st.alpha_tile_count, t.ctypes.data,
+                                             st.tile_count), "PFCUDAReadMasks")
+        return a[:st.alpha_tile_count], t[:st.tile_count]

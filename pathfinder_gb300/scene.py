@@ -1,0 +1,243 @@
+"""Host-side scene model: the shape of the reference's Scene / DrawPath /
+ClipPath / Outline / Contour API (renderer/src/scene.rs:39-472,
+content/src/outline.rs:17-41, :531-557), stored as flat numpy buffers that the
+C ABI consumes without conversion.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import itertools
+from dataclasses import dataclass, field
+from enum import IntEnum
+
+import numpy as np
+
+from . import _abi
+
+_NEXT_SCENE_ID = itertools.count()
+
+CONTROL_POINT_0 = 0x01
+CONTROL_POINT_1 = 0x02
+
+
+class FillRule(IntEnum):
+    """content/src/fill.rs: FillRule::{Winding, EvenOdd}."""
+    WINDING = 0
+    EVEN_ODD = 1
+
+
+@dataclass(frozen=True)
+class ColorU:
+    r: int
+    g: int
+    b: int
+    a: int = 255
+
+    def is_opaque(self) -> bool:  # color/src/lib.rs:76-78
+        return self.a == 255
+
+
+@dataclass(frozen=True)
+class ColorF:
+    r: float
+    g: float
+    b: float
+    a: float
+
+
+@dataclass
+class RectF:
+    x0: float
+    y0: float
+    x1: float
+    y1: float
+
+
+class Contour:
+    """A contour of on-curve points and control points (content/src/outline.rs:23-28)."""
+
+    def __init__(self):
+        self.points: list[tuple[float, float]] = []
+        self.flags: list[int] = []
+
+    def push_endpoint(self, x: float, y: float) -> "Contour":
+        self.points.append((x, y)); self.flags.append(0)
+        return self
+
+    def push_quadratic(self, cx: float, cy: float, x: float, y: float) -> "Contour":
+        self.points += [(cx, cy), (x, y)]; self.flags += [CONTROL_POINT_0, 0]
+        return self
+
+    def push_cubic(self, c0x, c0y, c1x, c1y, x, y) -> "Contour":
+        self.points += [(c0x, c0y), (c1x, c1y), (x, y)]
+        self.flags += [CONTROL_POINT_0, CONTROL_POINT_1, 0]
+        return self
+
+    def close(self) -> "Contour":
+        """Contours are always closed on this path (Outline::close_all_contours)."""
+        return self
+
+
+class Outline:
+    def __init__(self, contours: list[Contour] | None = None):
+        self.contours = list(contours or [])
+
+    def push_contour(self, contour: Contour) -> None:
+        if contour.points:  # Outline::push_contour skips empty contours
+            self.contours.append(contour)
+
+
+@dataclass
+class DrawPath:
+    outline: Outline
+    paint: ColorU = ColorU(0, 0, 0, 255)
+    fill_rule: FillRule = FillRule.WINDING
+    clip_path: int | None = None
+
+
+@dataclass
+class ClipPath:
+    outline: Outline
+    fill_rule: FillRule = FillRule.WINDING
+
+
+_FILL, _TILE, _CLIP, _PATH, _RECT = _abi.record_dtypes()
+
+
+class Scene:
+    """The vector scene (renderer/src/scene.rs:39-48) as flat buffers.
+
+    ``points`` (N, 2) float32, ``flags`` (N,) uint8, ``contour_starts``
+    (C + 1,) uint32, ``clip_paths`` / ``draw_paths`` structured arrays with the
+    layout of PFCUDAPath, and the view box.  ``id``/``epoch`` drive the
+    renderer's scene-upload cache (renderer/src/builder.rs:190-216).
+    """
+
+    def __init__(self):
+        self.id = next(_NEXT_SCENE_ID)
+        self.epoch = 0
+        self.points = np.zeros((0, 2), np.float32)
+        self.flags = np.zeros((0,), np.uint8)
+        self.contour_starts = np.zeros((1,), np.uint32)
+        self.clip_paths = np.zeros((0,), _PATH)
+        self.draw_paths = np.zeros((0,), _PATH)
+        self.view_box = RectF(0.0, 0.0, 0.0, 0.0)
+        self.width = 0
+        self.height = 0
+        self.cells = None  # glyph atlas cells, when generated
+        self._pending: list = []
+
+    # --- the reference's mutators -----------------------------------------
+    def set_view_box(self, rect: RectF) -> None:
+        self.view_box = rect
+        self.width = int(np.ceil(rect.x1))
+        self.height = int(np.ceil(rect.y1))
+        self.epoch += 1
+
+    def _append_outline(self, outline: Outline) -> tuple[int, int]:
+        first = len(self.contour_starts) - 1
+        pts, fl, starts = [self.points], [self.flags], [self.contour_starts]
+        n = len(self.points)
+        new_starts = []
+        for c in outline.contours:
+            pts.append(np.asarray(c.points, np.float32).reshape(-1, 2))
+            fl.append(np.asarray(c.flags, np.uint8))
+            n += len(c.points)
+            new_starts.append(n)
+        self.points = np.concatenate(pts)
+        self.flags = np.concatenate(fl)
+        self.contour_starts = np.concatenate([self.contour_starts, np.asarray(new_starts, np.uint32)])
+        return first, len(outline.contours)
+
+    def push_clip_path(self, clip: ClipPath) -> int:
+        first, count = self._append_outline(clip.outline)
+        rec = np.zeros((1,), _PATH)
+        rec["first_contour"], rec["contour_count"] = first, count
+        rec["clip_path"], rec["fill_rule"] = -1, int(clip.fill_rule)
+        self.clip_paths = np.concatenate([self.clip_paths, rec])
+        self.epoch += 1
+        return len(self.clip_paths) - 1
+
+    def push_draw_path(self, path: DrawPath) -> int:
+        first, count = self._append_outline(path.outline)
+        rec = np.zeros((1,), _PATH)
+        rec["first_contour"], rec["contour_count"] = first, count
+        rec["paint"] = (path.paint.r, path.paint.g, path.paint.b, path.paint.a)
+        rec["clip_path"] = -1 if path.clip_path is None else path.clip_path
+        rec["fill_rule"] = int(path.fill_rule)
+        self.draw_paths = np.concatenate([self.draw_paths, rec])
+        self.epoch += 1
+        return len(self.draw_paths) - 1
+
+    # --- C ABI view -----------------------------------------------------------
+    def desc(self) -> _abi.PFCUDASceneDesc:
+        """PFCUDASceneDesc pointing at this scene's host buffers."""
+        for name in ("points", "flags", "contour_starts", "clip_paths", "draw_paths"):
+            a = getattr(self, name)
+            if not a.flags["C_CONTIGUOUS"]:
+                setattr(self, name, np.ascontiguousarray(a))
+        d = _abi.PFCUDASceneDesc()
+        d.points = self.points.ctypes.data
+        d.point_flags = self.flags.ctypes.data
+        d.contour_starts = self.contour_starts.ctypes.data
+        d.clip_paths = self.clip_paths.ctypes.data if len(self.clip_paths) else None
+        d.draw_paths = self.draw_paths.ctypes.data if len(self.draw_paths) else None
+        d.point_count = len(self.points)
+        d.contour_count = len(self.contour_starts) - 1
+        d.clip_path_count = len(self.clip_paths)
+        d.draw_path_count = len(self.draw_paths)
+        vb = self.view_box
+        d.view_box = _abi.PFRectF(_abi.PFVector2F(vb.x0, vb.y0), _abi.PFVector2F(vb.x1, vb.y1))
+        d.memory = _abi.PF_MEMORY_HOST
+        return d
+
+    @property
+    def segment_count(self) -> int:
+        """Input segments as ContourIter yields them (closing lines included)."""
+        f = self.flags
+        n = 0
+        for c in range(len(self.contour_starts) - 1):
+            a, b = int(self.contour_starts[c]), int(self.contour_starts[c + 1])
+            if b > a:
+                n += 1 + int(np.count_nonzero((f[a + 1:b] & 3) == 0))
+        return n
+
+
+def generate_scene(workload: int, seed: int = 1, scale: float = 1.0, jitter_sigma: float = 0.0,
+                   jitter_seed: int = 0, width: int = 0, height: int = 0) -> Scene:
+    """A seeded synthetic scene (include/pathfinder_cuda_scenes.h)."""
+    L = _abi.lib()
+    p = _abi.PFCUDASceneParams(workload, seed, scale, jitter_sigma, jitter_seed, width, height)
+    h = C.c_void_p()
+    _abi.check(L.PFCUDASceneGenerate(C.byref(p), C.byref(h)), "PFCUDASceneGenerate")
+    try:
+        d = _abi.PFCUDASceneDesc()
+        w, hh = C.c_int32(), C.c_int32()
+        _abi.check(L.PFCUDASceneGetDesc(h, C.byref(d), C.byref(w), C.byref(hh)), "PFCUDASceneGetDesc")
+        s = Scene()
+        npt, nc = d.point_count, d.contour_count
+
+        def arr(ptr, ctype, count, dtype):
+            if count == 0:
+                return np.zeros((0,), dtype)
+            buf = (ctype * count).from_address(ptr)
+            return np.frombuffer(buf, dtype=dtype, count=count).copy()
+
+        s.points = arr(d.points, C.c_float, 2 * npt, np.float32).reshape(-1, 2)
+        s.flags = arr(d.point_flags, C.c_uint8, npt, np.uint8)
+        s.contour_starts = arr(d.contour_starts, C.c_uint32, nc + 1, np.uint32)
+        s.clip_paths = arr(d.clip_paths, C.c_uint8, d.clip_path_count * _PATH.itemsize, np.uint8).view(_PATH) \
+            if d.clip_path_count else np.zeros((0,), _PATH)
+        s.draw_paths = arr(d.draw_paths, C.c_uint8, d.draw_path_count * _PATH.itemsize, np.uint8).view(_PATH) \
+            if d.draw_path_count else np.zeros((0,), _PATH)
+        s.view_box = RectF(d.view_box.origin.x, d.view_box.origin.y, d.view_box.lower_right.x,
+                           d.view_box.lower_right.y)
+        s.width, s.height = w.value, hh.value
+        if workload == _abi.PF_SCENE_GLYPH_ATLAS:
+            n = d.draw_path_count
+            cells = np.zeros((n,), _RECT)
+            L.PFCUDASceneGetCells(h, cells.ctypes.data, n)
+            s.cells = cells
+        return s
+    finally:
+        L.PFCUDASceneDestroy(h)
