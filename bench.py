@@ -175,6 +175,8 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0)
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="fraction of the 20,000 paths (small cases for profiling only)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -198,7 +200,7 @@ def main():
     import pathfinder_gb300 as pf
 
     # replicas only: each rank renders its own scene (seed + rank)
-    scene = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=args.seed + rank)
+    scene = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=args.seed + rank, scale=args.scale)
     nseg = scene.segment_count
     npts = len(scene.points)
     r = pf.Renderer(local)
@@ -292,7 +294,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded PF_SCENE_SVG_4K: 20,000 log-normal star paths, 40/30/30 line/quad/cubic)",
-            "config": {"workload": WORKLOAD, "paths": 20000, "clip_paths": len(scene.clip_paths), "segments": nseg,
+            "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}_scale{args.scale}",
+                       "paths": len(scene.draw_paths), "clip_paths": len(scene.clip_paths), "segments": nseg,
                        "points": npts, "width": W, "height": H, "seed": args.seed,
                        "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}"},
             "mpx_per_s": round(world * W * H / (ms / 1e3) / 1e6, 3),

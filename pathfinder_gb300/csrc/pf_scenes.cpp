@@ -191,18 +191,20 @@ void gen_glyph_atlas(Builder& b, Rng& r, double scale, int W, int H) {
     std::vector<G> gs(n);
     for (int i = 0; i < n; i++) {
         double em = r.uniform(8.0, 128.0);
-        // ink box of 0.38 em per side so that 16,384 glyphs fit one 4096^2 atlas
-        int side = std::max(3, (int)std::ceil(0.38 * em)) + 2;  // + 1 px padding each side
+        // ink box of 0.34 em per side so that 16,384 glyphs fit one 4096^2 atlas
+        int side = std::max(3, (int)std::ceil(0.34 * em)) + 2;  // + 1 px padding each side
         gs[i] = G{em, side, side};
     }
-    // Shelf packing in generation order.
+    // Shelf packing, tallest first (glyph order itself is unchanged).
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return gs[a].h > gs[c].h; });
     int x = 0, y = 0, shelf_h = 0;
     b.cells.resize(n);
-    for (int i = 0; i < n; i++) {
+    for (int oi = 0; oi < n; oi++) {
+        int i = order[oi];
         if (x + gs[i].w > W) { x = 0; y += shelf_h; shelf_h = 0; }
-        if (y + gs[i].h > H) {  // atlas full: wrap (only for scale > 1)
-            y = 0;
-        }
+        if (y + gs[i].h > H) y = 0;  // atlas full: only reachable for scales above 1
         b.cells[i] = PFRectI{{x, y}, {x + gs[i].w, y + gs[i].h}};
         x += gs[i].w;
         shelf_h = std::max(shelf_h, gs[i].h);

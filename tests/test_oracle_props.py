@@ -1,0 +1,52 @@
+"""Size-independent properties of the oracle restatement."""
+import numpy as np
+
+import oracle
+import pathfinder_gb300 as pf
+from tests.kat import rect_scene
+
+
+def test_thread_count_does_not_change_the_build(built):
+    s = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=2, scale=0.02)
+    a, b = oracle.OracleFrame(s, threads=1), oracle.OracleFrame(s, threads=8)
+    fa, ta = a.fills()
+    fb, tb = b.fills()
+    assert np.array_equal(fa, fb) and np.array_equal(ta, tb)
+    assert np.array_equal(a.tiles()[0], b.tiles()[0])
+    assert np.array_equal(a.zbuffer(), b.zbuffer())
+
+
+def test_single_fill_integrates_to_its_signed_area(built):
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        seg = rng.integers(0, 4096, 4)
+        if seg[0] == seg[2]:
+            continue
+        m = oracle.fill_coverage(seg)
+        x0, y0, x1, y1 = seg / 256.0
+        # signed area of the tile below the segment: integral from x1 to x0 of (16 - y)
+        expect = (x0 - x1) * (16.0 - 0.5 * (y0 + y1))
+        assert abs(m.sum() - expect) < 1e-9
+
+
+def test_rect_interior_is_fully_covered(built):
+    fr = oracle.OracleFrame(rect_scene(5.25, 7.5, 60.75, 58.0, w=64, h=64))
+    img, f64 = fr.render(64, 64)
+    a = f64[..., 3]
+    # interior pixels are covered; a fill that runs to a tile's right edge is
+    # clamped to x = 4095/256 (builder.rs:527-529), which leaves the last
+    # 1/256 px column of such a tile uncovered
+    assert np.all(np.abs(a[8:58, 6:60] - 1.0) <= 1.0 / 256 + 1e-12)
+    assert np.allclose(a[24:58, 6:60], 1.0)
+    # outside: zero, up to the same 1/256 residue in a tile's last column
+    # below an edge whose fill was clamped
+    assert np.all(a[59:, :] <= 1.0 / 256 + 1e-12) and np.allclose(a[:, 61:], 0.0)
+    # partially covered boundary pixels carry the exact area fraction
+    assert abs(a[7, 30] - 0.5) < 1e-9 and abs(a[30, 5] - 0.75) < 1e-9
+    assert abs(a[7, 31] - 0.5 * 255 / 256) < 1e-9
+
+
+def test_resolved_coverage_is_a_fraction(built):
+    fr = oracle.OracleFrame(pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=4, scale=0.01))
+    _, cov = fr.masks()
+    assert cov.min() >= 0.0 and cov.max() <= 1.0
