@@ -58,7 +58,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
             return
@@ -99,15 +99,18 @@ class ClockSampler:
 
 
 def stage_bytes(st, npts: int, nseg: int) -> dict:
-    """Algorithmic bytes per stage from the per-unit figures:
-    8 B per point, 8 B per segment record, 12 B per fill, 16 B per path tile,
-    1 B per mask pixel (256 per alpha tile), 4 B per output pixel."""
-    P, S, F, T, A = npts, nseg, st.fill_count, st.tile_count, st.alpha_tile_count
+    """Algorithmic bytes per stage from the per-unit figures: 8 B per point,
+    8 B per segment record, 12 B per fill, 16 B per path tile, 1 B per mask
+    pixel (256 per alpha tile), 4 B per output pixel; the flattened lines are
+    an intermediate of this design (16 B + 4 B path index, written once and
+    read by both binning passes)."""
+    P, S, F, T, A, L = npts, nseg, st.fill_count, st.tile_count, st.alpha_tile_count, st.line_count
     return {
         "bound": 8 * P,
-        "tile_count": 8 * P + 8 * S,
-        "scans": 4 * S + 8 * T,
-        "tile_emit": 8 * P + 8 * S + 12 * F,
+        "flatten": 8 * P + 8 * S + 20 * L,
+        "bin_count": 20 * L + 4 * L,
+        "scans": 4 * L + 8 * T,
+        "bin_emit": 20 * L + 12 * F,
         "propagate": 16 * T,
         "visibility": 16 * T,
         "fill_composite": 12 * F + 256 * A + 4 * W * H,
@@ -169,7 +172,7 @@ def cpu_baseline(scene, nseg: int, budget_s: float = 12.0) -> dict:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cuda", choices=["cuda", "reference"])
     ap.add_argument("--seed", type=int, default=1)
@@ -259,7 +262,7 @@ def main():
     frame_gbs = sb["frame"] / (ms / 1e3) / 1e9
 
     # e2e through the public API with host buffers
-    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 20))
     pinned = {}
     for name in ("points", "flags", "contour_starts"):
         a = getattr(scene, name)

@@ -235,9 +235,9 @@ int32_t PFCUDAGetStats(PFCUDARendererRef renderer, PFCUDARenderStats* out_stats)
 
 /* Per-stage CUDA-event timing of subsequent frames (Renderer timer queries,
  * renderer/src/gpu/perf.rs:96-186, bucketed like RenderTime :223-240).
- * Stages: 0 bound, 1 tile count, 2 scans, 3 tile emit, 4 propagate,
- * 5 visibility, 6 fill+composite. */
-#define PF_CUDA_STAGE_COUNT 7
+ * Stages: 0 bound, 1 flatten, 2 bin count, 3 scans, 4 bin emit,
+ * 5 propagate, 6 visibility, 7 fill+composite. */
+#define PF_CUDA_STAGE_COUNT 8
 int32_t PFCUDASetProfiling(PFCUDARendererRef renderer, int32_t enable);
 /* Milliseconds per stage of the last profiled frame; synchronises. */
 int32_t PFCUDAGetStageTimes(PFCUDARendererRef renderer, float* out_ms, int32_t capacity);

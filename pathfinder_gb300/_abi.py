@@ -30,8 +30,8 @@ PF_SCENE_GLYPH_ATLAS = 3
 PF_SCENE_CUBIC_1K = 4
 PF_SCENE_EDGE_CASES = 5
 
-PF_CUDA_STAGE_COUNT = 7
-STAGE_NAMES = ["bound", "tile_count", "scans", "tile_emit", "propagate", "visibility", "fill_composite"]
+PF_CUDA_STAGE_COUNT = 8
+STAGE_NAMES = ["bound", "flatten", "bin_count", "scans", "bin_emit", "propagate", "visibility", "fill_composite"]
 
 
 class PFVector2F(C.Structure):

@@ -31,6 +31,7 @@ constexpr uint32_t kStatusDepthLimit     = 1u << 4;
 constexpr uint32_t kStatusMalformed      = 1u << 5;
 constexpr uint32_t kStatusColumnCapacity = 1u << 6;
 constexpr uint32_t kStatusAlphaCapacity  = 1u << 7;
+constexpr uint32_t kStatusLineCapacity   = 1u << 8;
 
 // ---------------------------------------------------------------------------
 // Records in HBM
@@ -75,7 +76,7 @@ struct Counters {
     uint64_t alpha_tiles;  // A
     uint64_t lines;        // flattened lines
     uint64_t visible;      // composited tiles
-    uint64_t needed_fills, needed_tiles, needed_visible;
+    uint64_t needed_fills, needed_tiles, needed_visible, needed_lines;
 };
 
 // ---------------------------------------------------------------------------
@@ -251,15 +252,14 @@ __device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink
 }
 
 // process_segment (renderer/src/tiler.rs:166-184) with an explicit stack in
-// place of recursion; lines come out in the same depth-first order.
-template <class Sink>
-__device__ __forceinline__ void tile_segment(const PathCtx& pc, const float2* pts, SegRec sr, Sink& sink,
-                                             uint32_t dda_limit, uint32_t* status, uint32_t& lines) {
+// place of recursion: calls emit(Line) for every flattened line in the same
+// depth-first order as the reference's recursion.
+template <class Emit>
+__device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Emit&& emit, uint32_t* status) {
     float2 p0 = pts[sr.x];
     float2 pe = pts[sr.y];
     if (sr.z == (int)kSegLine) {
-        lines++;
-        dda_line(pc, Line{p0.x, p0.y, pe.x, pe.y}, sink, dda_limit, status);
+        emit(Line{p0.x, p0.y, pe.x, pe.y});
         return;
     }
     Cubic c;
@@ -282,8 +282,7 @@ __device__ __forceinline__ void tile_segment(const PathCtx& pc, const float2* pt
         bool flat = cubic_is_flat(cur);
         if (flat || d >= kMaxFlattenDepth) {
             if (!flat) atomicOr(status, kStatusDepthLimit);
-            lines++;
-            dda_line(pc, cur.base, sink, dda_limit, status);
+            emit(cur.base);
         } else {
             Cubic a, b;
             cubic_split_half(cur, a, b);
@@ -307,6 +306,39 @@ __device__ __forceinline__ void tile_segment(const PathCtx& pc, const float2* pt
 // ---------------------------------------------------------------------------
 constexpr float kCovScale = 4194304.0f;      // 2^22
 constexpr float kCovInvScale = 1.0f / 4194304.0f;
+
+// Accumulate the part of a fill (x0,y0)->(x1,y1) (tile pixels, x0 != x1)
+// that lies in pixel column px into acc[row][col] and carry[row][col].
+__device__ __forceinline__ void accumulate_fill_column(float x0, float y0, float x1, float y1, int px, int* acc,
+                                                       int* carry) {
+    const float slope = (y1 - y0) / (x1 - x0);
+    const float lo = (float)px, hi = (float)(px + 1);
+    const float xa = fminf(fmaxf(x0, lo), hi), xb = fminf(fmaxf(x1, lo), hi);
+    const float w = xa - xb;  // oriented x-extent (window.x - window.y)
+    if (w == 0.0f) return;
+    const float ya = y0 + (xa - x0) * slope, yb = y0 + (xb - x0) * slope;
+    float ylo = fminf(ya, yb), yhi = fmaxf(ya, yb);
+    ylo = fminf(fmaxf(ylo, 0.0f), 16.0f);
+    yhi = fminf(fmaxf(yhi, 0.0f), 16.0f);
+    if (yhi - ylo <= 0.0f) {
+        const int r = (int)floorf(ylo);
+        if (r > 15) return;
+        atomicAdd(&acc[r * 16 + px], __float2int_rn(w * ((float)(r + 1) - ylo) * kCovScale));
+        if (r + 1 < 16) atomicAdd(&carry[(r + 1) * 16 + px], __float2int_rn(w * kCovScale));
+        return;
+    }
+    const float inv_h = 1.0f / (yhi - ylo);
+    const int r0 = (int)floorf(ylo), r1 = min((int)floorf(yhi), 15);
+    for (int r = r0; r <= r1; r++) {
+        const float yt = fmaxf(ylo, (float)r), yb2 = fminf(yhi, (float)(r + 1));
+        const float h = yb2 - yt;
+        if (h <= 0.0f) continue;
+        const float wr = w * (h * inv_h);
+        const float a = wr * ((float)(r + 1) - 0.5f * (yt + yb2));
+        atomicAdd(&acc[r * 16 + px], __float2int_rn(a * kCovScale));
+        if (r + 1 < 16) atomicAdd(&carry[(r + 1) * 16 + px], __float2int_rn(wr * kCovScale));
+    }
+}
 
 // Accumulate one fill (8.8 fixed point, tile-local) into acc[row][col] and
 // carry[row][col] (int, 256 each, shared memory).

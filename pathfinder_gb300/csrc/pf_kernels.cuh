@@ -19,10 +19,18 @@ struct FrameDev {
     uint32_t* tile_fill_count;   // [tile_cap+1]
     uint32_t* tile_fill_base;    // [tile_cap+1]
     uint32_t* tile_alpha;        // [tile_cap+1] exclusive scan of has-fill flags
-    int32_t*  tile_delta;        // [tile_cap] backdrop deltas
+    int32_t*  tile_delta;        // [tile_cap+1] backdrop deltas, column-major within a path
+    uint32_t* tile_delta_scan;   // [tile_cap+1] exclusive scan of tile_delta
+    uint32_t* path_tiles;        // [P+1] tiles per path (scan input)
+    uint32_t* path_cols;         // [P+1] tile columns per path (scan input)
     int32_t*  col_backdrop;      // [col_cap] above-rect column sums
-    uint32_t* seg_fill_count;    // [seg_count+1]
-    uint32_t* seg_fill_base;     // [seg_count+1]
+    uint32_t* seg_line_count;    // [seg_count+1] flattened lines per input segment
+    uint32_t* seg_line_base;     // [seg_count+1] exclusive scan
+    float4*   lines;             // [line_cap] flattened lines in emission order
+    uint32_t* line_path;         // [line_cap] global path of each line
+    uint32_t* line_fill_count;   // [line_cap+1] kept fills per line
+    uint32_t* line_fill_base;    // [line_cap+1] exclusive scan = emission index of the first fill
+    uint32_t  line_cap;
     uint2*    fills;             // [fill_cap] LineSegmentU16
     uint32_t* fill_e;            // [fill_cap] emission index
     int4*     tiles;             // [tile_cap] PFCUDATile records
@@ -36,12 +44,13 @@ struct FrameDev {
     uint32_t dda_limit;
 };
 
+// scan scratch
+struct ScanTemp { uint32_t* partials; uint32_t cap; };
+
 // Number of kernels this library has launched (host counter).
 uint64_t launch_counter();
 void count_launch(uint32_t n = 1);
 
-// scan scratch
-struct ScanTemp { uint32_t* partials; uint32_t cap; };
 
 void launch_transform(const float2* in, float2* out, uint32_t n, const float* m6, cudaStream_t s);
 void launch_contour_segcount(const uint32_t* ord_contour, uint32_t nord, const uint32_t* contour_starts,
@@ -50,9 +59,10 @@ void launch_contour_segemit(const uint32_t* ord_contour, const uint32_t* ord_pat
                             const uint32_t* contour_starts, const uint8_t* flags, const uint32_t* seg_base,
                             SegRec* segs, cudaStream_t s);
 void launch_bound(const FrameDev& f, const uint32_t* ord_contour, const uint32_t* contour_starts, cudaStream_t s);
-void launch_path_scan(const FrameDev& f, cudaStream_t s);
-void launch_tile_count(const FrameDev& f, cudaStream_t s);
-void launch_tile_emit(const FrameDev& f, cudaStream_t s);
+void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s);
+void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s);
+void launch_bin_count(const FrameDev& f, cudaStream_t s);
+void launch_bin_emit(const FrameDev& f, cudaStream_t s);
 // Exclusive scan of n (device-resident count at d_n, capacity n_cap) u32
 // values; mode 0: values, mode 1: (value != 0).  Writes out[0..n] (out[n] = total)
 // and, when total_out != NULL, the total as u64.

@@ -67,9 +67,12 @@ struct PFCUDARenderer {
     // per-frame buffers
     DevBuf<int4> tile_rect;
     DevBuf<uint32_t> tile_offset, col_offset;
-    DevBuf<uint32_t> seg_fill_count, seg_fill_base;
+    DevBuf<uint32_t> seg_line_count, seg_line_base;
+    DevBuf<float4> lines;
+    DevBuf<uint32_t> line_path, line_fill_count, line_fill_base;
     DevBuf<uint32_t> tile_fill_count, tile_fill_base, tile_alpha, alpha_owner;
     DevBuf<int32_t> tile_delta, col_backdrop, zbuf;
+    DevBuf<uint32_t> tile_delta_scan, path_tiles, path_cols;
     DevBuf<uint2> fills;
     DevBuf<uint32_t> fill_e;
     DevBuf<int4> tiles, clips;
@@ -79,7 +82,7 @@ struct PFCUDARenderer {
     DevBuf<uint8_t> out_tmp;
     Counters* h_counters = nullptr;  // pinned
 
-    uint32_t tile_cap = 0, col_cap = 0, fill_cap = 0, vis_cap = 0;
+    uint32_t tile_cap = 0, col_cap = 0, fill_cap = 0, vis_cap = 0, line_cap = 0;
     uint32_t screen_count = 0;
     int4 screen_rect{0, 0, 0, 0};
     int32_t last_w = 0, last_h = 0;
@@ -139,9 +142,17 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed) {
     f.tile_fill_base = r->tile_fill_base.p;
     f.tile_alpha = r->tile_alpha.p;
     f.tile_delta = r->tile_delta.p;
+    f.tile_delta_scan = r->tile_delta_scan.p;
+    f.path_tiles = r->path_tiles.p;
+    f.path_cols = r->path_cols.p;
     f.col_backdrop = r->col_backdrop.p;
-    f.seg_fill_count = r->seg_fill_count.p;
-    f.seg_fill_base = r->seg_fill_base.p;
+    f.seg_line_count = r->seg_line_count.p;
+    f.seg_line_base = r->seg_line_base.p;
+    f.lines = r->lines.p;
+    f.line_path = r->line_path.p;
+    f.line_fill_count = r->line_fill_count.p;
+    f.line_fill_base = r->line_fill_base.p;
+    f.line_cap = r->line_cap;
     f.fills = r->fills.p;
     f.fill_e = r->fill_e.p;
     f.tiles = r->tiles.p;
@@ -163,16 +174,24 @@ cudaError_t ensure_frame_buffers(PFCUDARenderer* r) {
     if ((e = r->tile_alpha.ensure((size_t)r->tile_cap + 1))) return e;
     if ((e = r->alpha_owner.ensure((size_t)r->tile_cap + 1))) return e;
     if ((e = r->tile_delta.ensure((size_t)r->tile_cap + 1))) return e;
+    if ((e = r->tile_delta_scan.ensure((size_t)r->tile_cap + 1))) return e;
+    if ((e = r->path_tiles.ensure((size_t)r->P + 1))) return e;
+    if ((e = r->path_cols.ensure((size_t)r->P + 1))) return e;
     if ((e = r->tiles.ensure((size_t)r->tile_cap + 1))) return e;
     if ((e = r->clips.ensure((size_t)r->tile_cap + 1))) return e;
     if ((e = r->col_backdrop.ensure((size_t)r->col_cap + 1))) return e;
     if ((e = r->fills.ensure((size_t)r->fill_cap + 1))) return e;
     if ((e = r->fill_e.ensure((size_t)r->fill_cap + 1))) return e;
+    if ((e = r->lines.ensure((size_t)r->line_cap + 1))) return e;
+    if ((e = r->line_path.ensure((size_t)r->line_cap + 1))) return e;
+    if ((e = r->line_fill_count.ensure((size_t)r->line_cap + 1))) return e;
+    if ((e = r->line_fill_base.ensure((size_t)r->line_cap + 1))) return e;
     if ((e = r->vis.ensure((size_t)r->vis_cap + 1))) return e;
     if ((e = r->zbuf.ensure((size_t)r->screen_count + 1))) return e;
     if ((e = r->screen_cnt.ensure((size_t)r->screen_count + 1))) return e;
     if ((e = r->screen_base.ensure((size_t)r->screen_count + 1))) return e;
-    size_t nmax = std::max<size_t>({(size_t)r->tile_cap, (size_t)r->S, (size_t)r->screen_count, (size_t)r->nord}) + 1;
+    size_t nmax = std::max<size_t>({(size_t)r->tile_cap, (size_t)r->S, (size_t)r->screen_count, (size_t)r->nord,
+                                    (size_t)r->line_cap, (size_t)r->P}) + 1;
     if ((e = r->scan_partials.ensure(nmax / 2048 + 2))) return e;
     return cudaSuccess;
 }
@@ -205,25 +224,29 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     if ((e = cudaMemsetAsync(c, 0, sizeof(Counters), s))) return e;
     mark(0);
     launch_bound(f, r->ord_contour.p, r->starts.p, s);
-    launch_path_scan(f, s);
+    launch_path_scan(f, tmp, s);
     mark(1);
-    launch_tile_count(f, s);
+    launch_flatten(f, tmp, s);
     mark(2);
-    launch_scan(r->seg_fill_count.p, r->seg_fill_base.p, nullptr, r->S, r->S, 0, &c->fills, tmp, s);
+    launch_bin_count(f, s);
+    mark(3);
+    launch_scan((const uint32_t*)r->tile_delta.p, r->tile_delta_scan.p, &c->tiles, 0, r->tile_cap, 0, nullptr, tmp, s);
+    launch_scan(r->line_fill_count.p, r->line_fill_base.p, &c->lines, 0, r->line_cap, 0, &c->fills, tmp, s);
     launch_scan(r->tile_fill_count.p, r->tile_fill_base.p, &c->tiles, 0, r->tile_cap, 0, nullptr, tmp, s);
     launch_scan(r->tile_fill_count.p, r->tile_alpha.p, &c->tiles, 0, r->tile_cap, 1, &c->alpha_tiles, tmp, s);
-    mark(3);
-    launch_tile_emit(f, s);
     mark(4);
-    if ((e = cudaMemsetAsync(r->zbuf.p, 0, sizeof(int32_t) * (r->screen_count + 1), s))) return e;
-    launch_propagate(f, true, 0, 0, 0, s);
-    launch_propagate(f, false, 0, 0, 0, s);
+    launch_bin_emit(f, s);
     mark(5);
+    if ((e = cudaMemsetAsync(r->zbuf.p, 0, sizeof(int32_t) * (r->screen_count + 1), s))) return e;
+    // clip paths first: draw paths read their finished tiles
+    launch_propagate(f, true, 0, r->nclip, 0, s);
+    launch_propagate(f, false, r->nclip, r->ndraw, 0, s);
+    mark(6);
     if ((e = cudaMemsetAsync(r->screen_cnt.p, 0, sizeof(uint32_t) * (r->screen_count + 1), s))) return e;
     launch_visible(f, false, s);
     launch_scan(r->screen_cnt.p, r->screen_base.p, nullptr, r->screen_count, r->screen_count, 0, &c->visible, tmp, s);
     launch_visible(f, true, s);
-    mark(6);
+    mark(7);
     if (mode >= 0) {
         float4 bg = make_float4(0, 0, 0, 0);
         if (r->options.has_background_color)
@@ -231,7 +254,7 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
                              r->options.background_color.b, r->options.background_color.a);
         launch_composite(f, mode, out_dev, bg, s);
     }
-    mark(7);
+    mark(8);
     r->launches = launch_counter() - before;
     return cudaGetLastError();
 }
@@ -245,11 +268,12 @@ void grow(PFCUDARenderer* r, const Counters& h) {
         r->vis_cap = std::max(r->vis_cap, r->tile_cap);
     }
     if (h.status & kStatusFillCapacity) r->fill_cap = std::max(r->fill_cap, up(h.fills));
+    if (h.status & kStatusLineCapacity) r->line_cap = std::max(r->line_cap, up(h.lines));
     if (h.status & kStatusVisibleCapacity) r->vis_cap = std::max(r->vis_cap, up(h.visible));
 }
 
 const uint32_t kCapacityBits = kStatusTileCapacity | kStatusColumnCapacity | kStatusFillCapacity |
-                               kStatusVisibleCapacity | kStatusAlphaCapacity;
+                               kStatusVisibleCapacity | kStatusAlphaCapacity | kStatusLineCapacity;
 
 int32_t status_to_code(uint32_t st) {
     if (st & kCapacityBits) return PF_CUDA_ERR_CAPACITY;
@@ -356,8 +380,10 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->segs.release(); r->first_ord.release(); r->paint.release(); r->local_index.release();
     r->scene_of.release(); r->clip_gpath.release(); r->rule.release(); r->is_clip.release();
     r->scenes.release(); r->tile_rect.release(); r->tile_offset.release(); r->col_offset.release();
-    r->seg_fill_count.release(); r->seg_fill_base.release(); r->tile_fill_count.release();
+    r->seg_line_count.release(); r->seg_line_base.release(); r->lines.release(); r->line_path.release();
+    r->line_fill_count.release(); r->line_fill_base.release(); r->tile_fill_count.release();
     r->tile_fill_base.release(); r->tile_alpha.release(); r->alpha_owner.release(); r->tile_delta.release();
+    r->tile_delta_scan.release(); r->path_tiles.release(); r->path_cols.release();
     r->col_backdrop.release(); r->zbuf.release(); r->fills.release(); r->fill_e.release(); r->tiles.release();
     r->clips.release(); r->screen_cnt.release(); r->screen_base.release(); r->vis.release();
     r->scan_partials.release(); r->counters.release(); r->out_tmp.release();
@@ -474,7 +500,7 @@ int32_t PFCUDASceneUpload(PFCUDARendererRef r, const PFCUDASceneDesc* sc) {
     PF_TRY(cudaStreamSynchronize(s));
     if (r->h_counters->status & kStatusMalformed) return PF_CUDA_ERR_INVALID;
     uint32_t S = (uint32_t)r->h_counters->lines;
-    if ((e = r->segs.ensure(S + 1)) || (e = r->seg_fill_count.ensure(S + 1)) || (e = r->seg_fill_base.ensure(S + 1)))
+    if ((e = r->segs.ensure(S + 1)) || (e = r->seg_line_count.ensure(S + 1)) || (e = r->seg_line_base.ensure(S + 1)))
         return cuda_status(e);
     launch_contour_segemit(r->ord_contour.p, r->ord_path.p, nord, r->starts.p, r->flags.p, r->contour_seg_base.p,
                            r->segs.p, s);
@@ -495,6 +521,7 @@ int32_t PFCUDASceneUpload(PFCUDARendererRef r, const PFCUDASceneDesc* sc) {
     r->tile_cap = std::max<uint32_t>(r->tile_cap, std::max<uint32_t>(1u << 16, 4 * r->screen_count));
     r->col_cap = std::max<uint32_t>(r->col_cap, std::max<uint32_t>(1u << 16, 16 * P));
     r->fill_cap = std::max<uint32_t>(r->fill_cap, std::max<uint32_t>(1u << 18, 4 * S));
+    r->line_cap = std::max<uint32_t>(r->line_cap, std::max<uint32_t>(1u << 16, 2 * S));
     r->vis_cap = std::max<uint32_t>(r->vis_cap, r->tile_cap);
     r->has_scene = true;
     PF_TRY(cudaStreamSynchronize(s));
@@ -617,7 +644,14 @@ int32_t PFCUDAReadRecords(PFCUDARendererRef r, PFCUDAFill* fills, uint32_t* fill
             fill_tile[i] = (uint32_t)g;
         }
     }
-    if (tiles && T) PF_TRY(cudaMemcpyAsync(tiles, r->tiles.p, T * sizeof(PFCUDATile), cudaMemcpyDeviceToHost, s));
+    if (tiles && T) {
+        PF_TRY(cudaMemcpyAsync(tiles, r->tiles.p, T * sizeof(PFCUDATile), cudaMemcpyDeviceToHost, s));
+        PF_TRY(cudaStreamSynchronize(s));
+        // device records carry the global path index; report the index within
+        // the clip paths or the draw paths, as TileObjectPrimitive::path_id
+        for (uint64_t i = 0; i < T; i++)
+            if (tiles[i].path_id >= r->nclip) tiles[i].path_id -= r->nclip;
+    }
     if (clips && T) {
         PF_TRY(cudaMemcpyAsync(clips, r->clips.p, T * sizeof(PFCUDAClip), cudaMemcpyDeviceToHost, s));
         PF_TRY(cudaStreamSynchronize(s));

@@ -278,6 +278,11 @@ __global__ void k_bound(FrameDev f, const uint32_t* __restrict__ ord_contour, co
     r.x = cvt_rne(floorf(fmul(bx0, q))); r.y = cvt_rne(floorf(fmul(by0, q)));
     r.z = cvt_rne(ceilf(fmul(bx1, q)));  r.w = cvt_rne(ceilf(fmul(by1, q)));
     f.path.tile_rect[gp] = r;
+    // scan inputs: tiles and above-rect columns of the path (DenseTileMap
+    // and backdrops vector of BuiltPath::new, renderer/src/builder.rs:441-456)
+    int w = r.z - r.x, h = r.w - r.y;
+    f.path_tiles[gp] = (w > 0 && h > 0) ? (uint32_t)w * (uint32_t)h : 0u;
+    f.path_cols[gp] = w > 0 ? (uint32_t)w : 0u;
 }
 
 void launch_bound(const FrameDev& f, const uint32_t* ord_contour, const uint32_t* starts, cudaStream_t s) {
@@ -286,42 +291,14 @@ void launch_bound(const FrameDev& f, const uint32_t* ord_contour, const uint32_t
     { count_launch(); k_bound<<<blocks, 256, 0, s>>>(f, ord_contour, starts); }
 }
 
-// single block: tile and column offsets of every path
-__global__ void k_path_scan(FrameDev f) {
-    uint64_t tcarry = 0, ccarry = 0;
-    for (uint32_t b0 = 0; b0 < f.path_count; b0 += 1024) {
-        uint32_t gp = b0 + threadIdx.x;
-        uint32_t tiles = 0, cols = 0;
-        if (gp < f.path_count) {
-            int4 r = f.path.tile_rect[gp];
-            int w = r.z - r.x, h = r.w - r.y;
-            if (w > 0 && h > 0) { tiles = (uint32_t)w * (uint32_t)h; }
-            cols = w > 0 ? (uint32_t)w : 0u;
-        }
-        uint32_t tt, ct;
-        uint32_t te = block_exclusive_scan<1024>(tiles, &tt);
-        uint32_t ce = block_exclusive_scan<1024>(cols, &ct);
-        if (gp < f.path_count) {
-            f.path.tile_offset[gp] = (uint32_t)(tcarry + te);
-            f.path.col_offset[gp] = (uint32_t)(ccarry + ce);
-        }
-        tcarry += tt;
-        ccarry += ct;
+// capacity checks after the path scans
+__global__ void k_check_tiles(FrameDev f) {
+    uint64_t T = f.counters->tiles, C = f.counters->columns;
+    if (T > f.tile_cap) {
+        atomicOr(&f.counters->status, kStatusTileCapacity);
+        f.counters->needed_tiles = T;
     }
-    if (threadIdx.x == 0) {
-        f.path.tile_offset[f.path_count] = (uint32_t)tcarry;
-        f.path.col_offset[f.path_count] = (uint32_t)ccarry;
-        f.counters->tiles = tcarry;
-        f.counters->columns = ccarry;
-        if (tcarry > f.tile_cap) {
-            atomicOr(&f.counters->status, kStatusTileCapacity);
-            f.counters->needed_tiles = tcarry;
-        }
-        if (ccarry > f.col_cap) {
-            atomicOr(&f.counters->status, kStatusColumnCapacity);
-            f.counters->needed_tiles = tcarry > f.counters->needed_tiles ? tcarry : f.counters->needed_tiles;
-        }
-    }
+    if (C > f.col_cap) atomicOr(&f.counters->status, kStatusColumnCapacity);
 }
 
 // zero the per-tile accumulators of this frame
@@ -335,13 +312,57 @@ __global__ void k_zero_tiles(FrameDev f) {
     }
 }
 
-void launch_path_scan(const FrameDev& f, cudaStream_t s) {
-    { count_launch(); k_path_scan<<<1, 1024, 0, s>>>(f); }
+void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
+    launch_scan(f.path_tiles, f.path.tile_offset, nullptr, f.path_count, f.path_count, 0, &f.counters->tiles, tmp, s);
+    launch_scan(f.path_cols, f.path.col_offset, nullptr, f.path_count, f.path_count, 0, &f.counters->columns, tmp, s);
+    { count_launch(); k_check_tiles<<<1, 1, 0, s>>>(f); }
     { count_launch(); k_zero_tiles<<<152 * 8, 256, 0, s>>>(f); }
 }
 
 // ---------------------------------------------------------------------------
-// tiling passes: one thread per input segment
+// flattening: one thread per input segment (process_segment's recursion,
+// renderer/src/tiler.rs:166-184).  Lines are written in emission order: input
+// segments in path order, each segment's lines depth first.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_flatten_count(FrameDev f) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= f.seg_count) return;
+    uint32_t n = 0;
+    flatten_segment(f.pts, f.segs[s], [&](const Line&) { n++; }, &f.counters->status);
+    f.seg_line_count[s] = n;
+}
+
+__global__ void k_check_lines(FrameDev f) {
+    if (f.counters->lines > f.line_cap) {
+        atomicOr(&f.counters->status, kStatusLineCapacity);
+        f.counters->needed_lines = f.counters->lines;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_flatten_emit(FrameDev f) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= f.seg_count || f.counters->lines > f.line_cap) return;
+    const SegRec sr = f.segs[s];
+    uint32_t l = f.seg_line_base[s];
+    flatten_segment(f.pts, sr, [&](const Line& ln) {
+        f.lines[l] = make_float4(ln.fx, ln.fy, ln.tx, ln.ty);
+        f.line_path[l] = (uint32_t)sr.w;
+        l++;
+    }, &f.counters->status);
+}
+
+void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
+    if (f.seg_count == 0) return;
+    { count_launch(); k_flatten_count<<<(f.seg_count + 127) / 128, 128, 0, s>>>(f); }
+    launch_scan(f.seg_line_count, f.seg_line_base, nullptr, f.seg_count, f.seg_count, 0, &f.counters->lines, tmp, s);
+    { count_launch(); k_check_lines<<<1, 1, 0, s>>>(f); }
+    { count_launch(); k_flatten_emit<<<(f.seg_count + 127) / 128, 128, 0, s>>>(f); }
+}
+
+// ---------------------------------------------------------------------------
+// binning: one thread per flattened line (process_line_segment, add_fill,
+// adjust_alpha_tile_backdrop: renderer/src/tiler.rs:191-308,
+// renderer/src/builder.rs:509-616)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ PathCtx path_ctx(const FrameDev& f, uint32_t gp) {
     PathCtx pc;
@@ -352,6 +373,11 @@ __device__ __forceinline__ PathCtx path_ctx(const FrameDev& f, uint32_t gp) {
     float4 v = f.scenes[f.path.scene[gp]].view_box;
     pc.vminx = v.x; pc.vmaxx = v.z; pc.vmaxy = v.w;
     return pc;
+}
+
+__device__ __forceinline__ uint32_t line_total(const FrameDev& f) {
+    uint64_t L = f.counters->lines;
+    return L <= f.line_cap ? (uint32_t)L : 0u;
 }
 
 struct CountSink {
@@ -370,27 +396,20 @@ struct CountSink {
         int32_t ox = tx - pc->minx, oy = ty - pc->miny;
         if (ox < 0 || ox >= w || oy >= h) return;
         if (oy < 0) atomicAdd(&col_backdrop[pc->col_base + (uint32_t)ox], d);
-        else atomicAdd(&tile_delta[pc->tile_base + (uint32_t)(oy * w + ox)], d);
+        else atomicAdd(&tile_delta[pc->tile_base + (uint32_t)(ox * h + oy)], d);  // column-major
     }
 };
 
-__global__ void __launch_bounds__(128) k_tile_count(FrameDev f) {
-    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    bool ok = f.counters->tiles <= f.tile_cap && f.counters->columns <= f.col_cap;
-    uint32_t lines = 0;
-    if (s < f.seg_count && ok) {
-        SegRec sr = f.segs[s];
-        PathCtx pc = path_ctx(f, (uint32_t)sr.w);
+__global__ void __launch_bounds__(256) k_bin_count(FrameDev f) {
+    if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
+    const uint32_t L = line_total(f);
+    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
+        const float4 ln = f.lines[l];
+        const PathCtx pc = path_ctx(f, f.line_path[l]);
         CountSink sink{&pc, f.tile_fill_count, f.tile_delta, f.col_backdrop, 0};
-        tile_segment(pc, f.pts, sr, sink, f.dda_limit, &f.counters->status, lines);
-        f.seg_fill_count[s] = sink.n;
-    } else if (s < f.seg_count) {
-        f.seg_fill_count[s] = 0;
+        dda_line(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+        f.line_fill_count[l] = sink.n;
     }
-    // line count for RenderStats
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) lines += __shfl_xor_sync(0xffffffffu, lines, o);
-    if ((threadIdx.x & 31) == 0 && lines) atomicAdd((unsigned long long*)&f.counters->lines, (unsigned long long)lines);
 }
 
 struct EmitSink {
@@ -408,22 +427,21 @@ struct EmitSink {
     __device__ __forceinline__ void backdrop(int32_t, int32_t, int32_t) {}
 };
 
-__global__ void __launch_bounds__(128) k_tile_emit(FrameDev f) {
-    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= f.seg_count) return;
+__global__ void __launch_bounds__(256) k_bin_emit(FrameDev f) {
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     if (f.counters->fills > f.fill_cap) return;
-    if (f.seg_fill_count[s] == 0) return;
-    SegRec sr = f.segs[s];
-    PathCtx pc = path_ctx(f, (uint32_t)sr.w);
-    EmitSink sink{f.fills, f.fill_e, f.tile_fill_base, f.tile_fill_count, f.fill_cap, f.seg_fill_base[s]};
-    uint32_t lines = 0;
-    tile_segment(pc, f.pts, sr, sink, f.dda_limit, &f.counters->status, lines);
+    const uint32_t L = line_total(f);
+    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
+        if (f.line_fill_count[l] == 0) continue;
+        const float4 ln = f.lines[l];
+        const PathCtx pc = path_ctx(f, f.line_path[l]);
+        EmitSink sink{f.fills, f.fill_e, f.tile_fill_base, f.tile_fill_count, f.fill_cap, f.line_fill_base[l]};
+        dda_line(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+    }
 }
 
-void launch_tile_count(const FrameDev& f, cudaStream_t s) {
-    if (f.seg_count == 0) return;
-    { count_launch(); k_tile_count<<<(f.seg_count + 127) / 128, 128, 0, s>>>(f); }
+void launch_bin_count(const FrameDev& f, cudaStream_t s) {
+    { count_launch(); k_bin_count<<<152 * 16, 256, 0, s>>>(f); }
 }
 
 __global__ void k_check_fills(FrameDev f) {
@@ -434,10 +452,9 @@ __global__ void k_check_fills(FrameDev f) {
     if (f.counters->alpha_tiles > f.tile_cap) atomicOr(&f.counters->status, kStatusAlphaCapacity);
 }
 
-void launch_tile_emit(const FrameDev& f, cudaStream_t s) {
+void launch_bin_emit(const FrameDev& f, cudaStream_t s) {
     { count_launch(); k_check_fills<<<1, 1, 0, s>>>(f); }
-    if (f.seg_count == 0) return;
-    { count_launch(); k_tile_emit<<<(f.seg_count + 127) / 128, 128, 0, s>>>(f); }
+    { count_launch(); k_bin_emit<<<152 * 16, 256, 0, s>>>(f); }
 }
 
 }  // namespace pf
