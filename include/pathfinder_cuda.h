@@ -242,6 +242,16 @@ int32_t PFCUDASetProfiling(PFCUDARendererRef renderer, int32_t enable);
 /* Milliseconds per stage of the last profiled frame; synchronises. */
 int32_t PFCUDAGetStageTimes(PFCUDARendererRef renderer, float* out_ms, int32_t capacity);
 
+/* Device-wide exclusive prefix sum of `n` uint32 values, the primitive that
+ * turns per-tile fill counts into fill offsets and tile-has-fill flags into
+ * alpha-tile ids (it replaces the D3D11 level's counter readbacks,
+ * renderer/src/gpu/d3d11/renderer.rs:218-229, :634-648).  `in` and `out`
+ * are device pointers (`in` may be NULL when n == 0); out[0..n] is written,
+ * out[n] = total.  Scratch comes
+ * from the renderer (grown with cudaMalloc when needed).  Runs on the
+ * renderer's stream and synchronises. */
+int32_t PFCUDAExclusiveScan(PFCUDARendererRef renderer, const uint32_t* in, uint32_t* out, uint32_t n);
+
 /* Human-readable text for a status code (static storage). */
 const char* PFCUDAStatusString(int32_t status);
 

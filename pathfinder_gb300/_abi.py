@@ -147,6 +147,7 @@ _SIGS = {
     "PFCUDAGetStats": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDARenderStats)]),
     "PFCUDASetProfiling": (C.c_int32, [C.c_void_p, C.c_int32]),
     "PFCUDAGetStageTimes": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32]),
+    "PFCUDAExclusiveScan": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]),
     "PFCUDAStatusString": (C.c_char_p, [C.c_int32]),
     "PFCUDASceneGenerate": (C.c_int32, [C.POINTER(PFCUDASceneParams), C.POINTER(C.c_void_p)]),
     "PFCUDASceneGetDesc": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDASceneDesc), C.POINTER(C.c_int32),

@@ -693,6 +693,17 @@ int32_t PFCUDAGetStageTimes(PFCUDARendererRef r, float* out_ms, int32_t capacity
     return PF_CUDA_OK;
 }
 
+int32_t PFCUDAExclusiveScan(PFCUDARendererRef r, const uint32_t* in, uint32_t* out, uint32_t n) {
+    if (!r || !out || (!in && n) || n >= 0x80000000u) return PF_CUDA_ERR_INVALID;
+    PF_TRY(cudaSetDevice(r->device));
+    PF_TRY(r->scan_partials.ensure((size_t)n / 2048 + 2));
+    ScanTemp tmp{r->scan_partials.p, (uint32_t)r->scan_partials.cap};
+    launch_scan(in, out, nullptr, n, n, 0, nullptr, tmp, r->stream);
+    PF_TRY(cudaGetLastError());
+    PF_TRY(cudaStreamSynchronize(r->stream));
+    return PF_CUDA_OK;
+}
+
 int32_t PFCUDAGetStats(PFCUDARendererRef r, PFCUDARenderStats* out) {
     if (!r || !out) return PF_CUDA_ERR_INVALID;
     *out = r->stats;
