@@ -252,6 +252,21 @@ int32_t PFCUDAGetStageTimes(PFCUDARendererRef renderer, float* out_ms, int32_t c
  * renderer's stream and synchronises. */
 int32_t PFCUDAExclusiveScan(PFCUDARendererRef renderer, const uint32_t* in, uint32_t* out, uint32_t n);
 
+/* The same scan for callers that cannot allocate device memory while they
+ * work (a frame loop that must not stall on cudaMalloc's implicit device
+ * synchronisation, a host whose device memory belongs to its own pool, code
+ * running while another module captures a CUDA graph).  This entry point has
+ * no counterpart in the reference.  It allocates nothing: its scratch is a
+ * fixed 32 KiB device array that every GPU loading the library holds until
+ * the process exits.  At most 16,777,216 values per call; larger n returns
+ * PF_CUDA_ERR_CAPACITY without launching.  `in`/`out` are device pointers
+ * (`in` may be NULL when n == 0), out[0..n] is written, out[n] = total.
+ * Asynchronous on `stream` (a cudaStream_t, NULL = legacy default stream).
+ * The first call on a device looks up the array's device address, so make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race, so serialise them. */
+int32_t PFCUDAExclusiveScanNoAlloc(const uint32_t* in, uint32_t* out, uint32_t n, void* stream);
+
 /* Human-readable text for a status code (static storage). */
 const char* PFCUDAStatusString(int32_t status);
 

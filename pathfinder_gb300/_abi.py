@@ -148,6 +148,7 @@ _SIGS = {
     "PFCUDASetProfiling": (C.c_int32, [C.c_void_p, C.c_int32]),
     "PFCUDAGetStageTimes": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32]),
     "PFCUDAExclusiveScan": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]),
+    "PFCUDAExclusiveScanNoAlloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "PFCUDAStatusString": (C.c_char_p, [C.c_int32]),
     "PFCUDASceneGenerate": (C.c_int32, [C.POINTER(PFCUDASceneParams), C.POINTER(C.c_void_p)]),
     "PFCUDASceneGetDesc": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDASceneDesc), C.POINTER(C.c_int32),

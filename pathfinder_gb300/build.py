@@ -28,6 +28,7 @@ UNITS = [
     ("pf_tiler.cu", ["-fmad=false"]),
     ("pf_raster.cu", []),
     ("pf_renderer.cu", []),
+    ("pf_noalloc.cu", []),
     ("pf_scenes.cpp", []),
 ]
 
