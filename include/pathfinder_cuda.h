@@ -233,6 +233,66 @@ int32_t PFCUDAReadRecords(PFCUDARendererRef renderer,
  * (:537). */
 int32_t PFCUDAGetStats(PFCUDARendererRef renderer, PFCUDARenderStats* out_stats);
 
+/* ---- batched frames --------------------------------------------------------
+ * Many independent scenes (glyph sets, tiles of an atlas, a batch of
+ * differentiable scenes) rendered by one set of launches: the batch is
+ * uploaded once and any contiguous range of its scenes is one frame.  The
+ * reference renders one scene per Renderer call; this has no direct
+ * counterpart there. */
+#define PF_CUDA_FORMAT_RGBA8 0   /* premultiplied RGBA8, 4 bytes per pixel */
+#define PF_CUDA_FORMAT_R8    1   /* single channel, SrcOver of paint alpha x coverage, 1 byte */
+#define PF_CUDA_FORMAT_F32   2   /* the same single channel as float */
+
+/* Where a scene's pixels go: scene pixel (x, y) inside `clip` is written to
+ * element out_offset + (y - origin_y) * pitch + (x - origin_x) of the output
+ * buffer (elements of the format's size).  Pixels outside `clip` are not
+ * written, so scenes may share one output (e.g. glyph cells of an atlas). */
+typedef struct PFCUDASceneTarget {
+    uint64_t out_offset;
+    int32_t  pitch;
+    int32_t  origin_x, origin_y;
+    PFRectI  clip;
+} PFCUDASceneTarget;
+
+/* Upload `scene_count` scenes (each as in PFCUDASceneUpload) with their
+ * targets.  Replaces the resident scene(s). */
+int32_t PFCUDASceneUploadBatch(PFCUDARendererRef renderer, const PFCUDASceneDesc* scenes,
+                               const PFCUDASceneTarget* targets, uint32_t scene_count);
+/* Render scenes [first_scene, first_scene + scene_count) of the uploaded batch
+ * into device memory `out_device` in `format`; synchronises, regrows buffers
+ * and re-runs once on overflow. */
+int32_t PFCUDARenderBatch(PFCUDARendererRef renderer, const PFCUDABuildOptions* options,
+                          uint32_t first_scene, uint32_t scene_count, int32_t format, void* out_device);
+/* The same frame, only enqueued (check PFCUDARenderStatus afterwards). */
+int32_t PFCUDARenderBatchAsync(PFCUDARendererRef renderer, const PFCUDABuildOptions* options,
+                               uint32_t first_scene, uint32_t scene_count, int32_t format, void* out_device);
+
+/* CUDA graph of a whole frame: runs the frame once synchronously (sizing the
+ * buffers), then captures its launches into a graph bound to these
+ * arguments.  PFCUDAGraphLaunch replays it asynchronously on the renderer's
+ * stream (status via PFCUDARenderStatus; an overflow there means the scene
+ * changed: capture again).  Uploading a scene releases the graph. */
+int32_t PFCUDAGraphCapture(PFCUDARendererRef renderer, const PFCUDABuildOptions* options,
+                           uint32_t first_scene, uint32_t scene_count, int32_t format, void* out_device);
+int32_t PFCUDAGraphLaunch(PFCUDARendererRef renderer);
+int32_t PFCUDAGraphRelease(PFCUDARendererRef renderer);
+
+/* Launch shapes of the kernels (outputs never depend on them). */
+typedef struct PFCUDATuning {
+    int32_t flatten_threads;     /* 64, 128 or 256 */
+    int32_t bin_threads;         /* 128, 256 or 512 */
+    int32_t bin_blocks_per_sm;   /* 4 .. 64 */
+    int32_t composite_warps;     /* 2, 4 or 8 */
+} PFCUDATuning;
+int32_t PFCUDASetTuning(PFCUDARendererRef renderer, const PFCUDATuning* tuning);
+int32_t PFCUDAGetTuning(PFCUDARendererRef renderer, PFCUDATuning* out_tuning);
+/* Autotuner: times `repeats` frames of the given range per candidate shape
+ * (coordinate descent over the four parameters), keeps the fastest and
+ * returns it.  Synchronises. */
+int32_t PFCUDAAutotune(PFCUDARendererRef renderer, const PFCUDABuildOptions* options,
+                       uint32_t first_scene, uint32_t scene_count, int32_t format, void* out_device,
+                       int32_t repeats, PFCUDATuning* out_best);
+
 /* Per-stage CUDA-event timing of subsequent frames (Renderer timer queries,
  * renderer/src/gpu/perf.rs:96-186, bucketed like RenderTime :223-240).
  * Stages: 0 bound, 1 flatten, 2 bin count, 3 scans, 4 bin emit,

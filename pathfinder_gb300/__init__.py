@@ -9,6 +9,11 @@ from .scene import (ClipPath, ColorF, ColorU, Contour, DrawPath, FillRule, Outli
                     generate_scene)
 from .renderer import (BuildOptions, Renderer, RendererLevel, RendererOptions, RenderStats, Transform2F)
 from . import _abi
+from .batch import SceneBatch, target
+
+PF_CUDA_FORMAT_RGBA8 = _abi.PF_CUDA_FORMAT_RGBA8
+PF_CUDA_FORMAT_R8 = _abi.PF_CUDA_FORMAT_R8
+PF_CUDA_FORMAT_F32 = _abi.PF_CUDA_FORMAT_F32
 
 PF_SCENE_STARS_512 = _abi.PF_SCENE_STARS_512
 PF_SCENE_SVG_4K = _abi.PF_SCENE_SVG_4K

@@ -107,6 +107,21 @@ class PFCUDAClip(C.Structure):
                 ("src_backdrop", C.c_int32)]
 
 
+class PFCUDASceneTarget(C.Structure):
+    _fields_ = [("out_offset", C.c_uint64), ("pitch", C.c_int32), ("origin_x", C.c_int32), ("origin_y", C.c_int32),
+                ("clip", PFRectI)]
+
+
+class PFCUDATuning(C.Structure):
+    _fields_ = [("flatten_threads", C.c_int32), ("bin_threads", C.c_int32), ("bin_blocks_per_sm", C.c_int32),
+                ("composite_warps", C.c_int32)]
+
+
+PF_CUDA_FORMAT_RGBA8 = 0
+PF_CUDA_FORMAT_R8 = 1
+PF_CUDA_FORMAT_F32 = 2
+
+
 class PFCUDASceneParams(C.Structure):
     _fields_ = [("workload", C.c_int32), ("seed", C.c_uint64), ("scale", C.c_double),
                 ("jitter_sigma", C.c_double), ("jitter_seed", C.c_uint64), ("width", C.c_int32),
@@ -145,6 +160,19 @@ _SIGS = {
     "PFCUDAReadRecords": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,
                                       C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64]),
     "PFCUDAGetStats": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDARenderStats)]),
+    "PFCUDASceneUploadBatch": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]),
+    "PFCUDARenderBatch": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDABuildOptions), C.c_uint32, C.c_uint32, C.c_int32,
+                                      C.c_void_p]),
+    "PFCUDARenderBatchAsync": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDABuildOptions), C.c_uint32, C.c_uint32,
+                                           C.c_int32, C.c_void_p]),
+    "PFCUDAGraphCapture": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDABuildOptions), C.c_uint32, C.c_uint32, C.c_int32,
+                                       C.c_void_p]),
+    "PFCUDAGraphLaunch": (C.c_int32, [C.c_void_p]),
+    "PFCUDAGraphRelease": (C.c_int32, [C.c_void_p]),
+    "PFCUDASetTuning": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDATuning)]),
+    "PFCUDAGetTuning": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDATuning)]),
+    "PFCUDAAutotune": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDABuildOptions), C.c_uint32, C.c_uint32, C.c_int32,
+                                   C.c_void_p, C.c_int32, C.POINTER(PFCUDATuning)]),
     "PFCUDASetProfiling": (C.c_int32, [C.c_void_p, C.c_int32]),
     "PFCUDAGetStageTimes": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32]),
     "PFCUDAExclusiveScan": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]),

@@ -62,8 +62,13 @@ struct SceneDev {
     uint32_t screen_offset;        // first global screen tile
     uint32_t first_path;           // global index of the first path
     uint32_t clip_count, draw_count;
-    int32_t width, height;         // output size in pixels
-    uint64_t out_offset;           // element offset of the scene's output image
+    // output placement: scene pixel (x, y) inside `clip` goes to element
+    // out_offset + (y - origin_y) * pitch + (x - origin_x)
+    int4   clip;                   // x0, y0, x1, y1 (exclusive)
+    int32_t origin_x, origin_y;
+    int32_t pitch;
+    int32_t pad;
+    uint64_t out_offset;
 };
 
 // Device counters written by the pipeline (one struct, zeroed per frame).

@@ -5,15 +5,29 @@
 
 namespace pf {
 
+// Launch shapes chosen by the autotuner (outputs do not depend on them).
+struct TuneParams {
+    int flatten_threads;   // threads per block of the flattening passes
+    int bin_threads;       // threads per block of the binning passes
+    int bin_blocks_per_sm; // grid of the binning passes = SMs x this
+    int comp_warps;        // warps per block of the composite (2, 4 or 8)
+};
+
+// One frame covers a contiguous range of the uploaded scenes; paths,
+// segments and screen tiles of that range are contiguous too.  Path and
+// segment arrays are indexed globally; per-frame arrays (tiles, lines, fills,
+// screen tiles) are indexed from the start of the range.
 struct FrameDev {
     // scene
     const float2* pts;           // points used by the tiler (transformed copy when needed)
     const SegRec* segs;
-    uint32_t seg_count;
+    uint32_t seg_begin, seg_count;
     PathDev path;
     const SceneDev* scenes;
-    uint32_t path_count;
-    uint32_t scene_count;
+    uint32_t path_begin, path_count;
+    uint32_t scene_begin, scene_count;
+    uint32_t screen_begin;       // global index of the range's first screen tile
+    TuneParams tune;
     // tile arrays (capacity tile_cap; +1 for scan totals)
     uint32_t tile_cap, col_cap, fill_cap, vis_cap, screen_count;
     uint32_t* tile_fill_count;   // [tile_cap+1]
@@ -69,8 +83,7 @@ void launch_bin_emit(const FrameDev& f, cudaStream_t s);
 void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_t n_host, uint32_t n_cap,
                  int mode, uint64_t* total_out, ScanTemp& tmp, cudaStream_t s);
 
-void launch_propagate(const FrameDev& f, bool clip_pass, uint32_t first_path, uint32_t path_count,
-                      uint32_t max_width, cudaStream_t s);
+void launch_propagate(const FrameDev& f, bool clip_pass, cudaStream_t s);
 void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s);
 // mode 0: RGBA8, 1: R8 single channel, 2: FP32 single channel
 void launch_composite(const FrameDev& f, int mode, void* out, const float4& background, cudaStream_t s);

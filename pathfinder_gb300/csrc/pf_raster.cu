@@ -14,7 +14,8 @@
 //
 // Device tile records use the PFCUDATile layout with one difference: the
 // path field holds the global path index (the readback converts it to the
-// index within the clip or draw paths).
+// index within the clip or draw paths).  Screen-tile arrays (z-buffer, list
+// counts) are indexed from the first screen tile of the frame's scene range.
 #include "pf_kernels.cuh"
 
 namespace pf {
@@ -45,12 +46,6 @@ __device__ __forceinline__ bool frame_ok(const FrameDev& f) {
     return f.counters->tiles <= f.tile_cap && f.counters->columns <= f.col_cap;
 }
 
-// ---------------------------------------------------------------------------
-// propagate: one warp per path, lanes over all of its tiles.  The backdrop of
-// tile (ox, oy) is the above-rect column sum plus the deltas of the tiles
-// above it in its column: with the deltas stored column-major and scanned,
-// that is above[ox] + S[ox*h + oy] - S[ox*h] (wrapping int32 sums).
-// ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t upper_bound_u32(const uint32_t* a, uint32_t n, uint32_t v) {
     // first index i in [0, n) with a[i] > v
     uint32_t lo = 0, hi = n;
@@ -61,28 +56,40 @@ __device__ __forceinline__ uint32_t upper_bound_u32(const uint32_t* a, uint32_t 
     return lo;
 }
 
-// One thread per tile of the paths [first_path, first_path + path_count):
-// path sizes are log-normal, so per-path work items would leave a long tail.
-__global__ void k_propagate(FrameDev f, uint32_t first_path, uint32_t path_count) {
-    if (!frame_ok(f) || path_count == 0) return;
-    const uint32_t t0 = f.path.tile_offset[first_path], t1 = f.path.tile_offset[first_path + path_count];
-    for (uint32_t g = t0 + blockIdx.x * blockDim.x + threadIdx.x; g < t1; g += gridDim.x * blockDim.x) {
-    const uint32_t gp = first_path + upper_bound_u32(f.path.tile_offset + first_path, path_count + 1, g) - 1;
-    const int4 r = f.path.tile_rect[gp];
-    const int32_t w = r.z - r.x, h = r.w - r.y;
-    const uint32_t tbase = f.path.tile_offset[gp], cbase_col = f.path.col_offset[gp];
-    const bool is_clip = f.path.is_clip[gp] != 0;
-    const bool even_odd = f.path.rule[gp] == 1;
-    const uint8_t ctrl = is_clip ? 0 : (even_odd ? 0x2 : 0x1);
-    const uint32_t local = f.path.local_index[gp];
-    const uint16_t color = is_clip ? 0 : (uint16_t)(local & 0xffffu);
-    const int32_t clip_gp = is_clip ? -1 : f.path.clip_gpath[gp];
-    int4 cr = make_int4(0, 0, 0, 0);
-    uint32_t cbase = 0;
-    if (clip_gp >= 0) { cr = f.path.tile_rect[clip_gp]; cbase = f.path.tile_offset[clip_gp]; }
-    const SceneDev& sc = f.scenes[f.path.scene[gp]];
-    const bool occluder_path = !is_clip && ((f.path.paint[gp] >> 24) == 255u);
-    {
+// Screen tile of (tx, ty) in its scene, relative to the frame; false outside.
+__device__ __forceinline__ bool frame_screen_tile(const FrameDev& f, const SceneDev& sc, int32_t tx, int32_t ty,
+                                                  uint32_t* st) {
+    const int4 s = sc.screen;
+    if (!(s.x <= tx && s.y <= ty && tx <= s.z - 1 && ty <= s.w - 1)) return false;
+    *st = sc.screen_offset - f.screen_begin + (uint32_t)((ty - s.y) * (s.z - s.x) + (tx - s.x));
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// propagate: one thread per tile; clip tiles in the first launch, draw tiles
+// in the second (draw tiles of clipped paths read their clip's final tiles).
+// The backdrop of tile (ox, oy) is the above-rect column sum plus the deltas of
+// the tiles above it in its column: with the deltas stored column-major and
+// scanned, that is above[ox] + S[ox*h + oy] - S[ox*h] (wrapping int32 sums).
+// Path sizes are log-normal, so per-path work items would leave a long tail.
+// ---------------------------------------------------------------------------
+__global__ void k_propagate(FrameDev f, int clip_pass) {
+    if (!frame_ok(f) || f.path_count == 0) return;
+    const uint32_t T = (uint32_t)f.counters->tiles;
+    const uint32_t* offs = f.path.tile_offset + f.path_begin;
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < T; g += gridDim.x * blockDim.x) {
+        const uint32_t gp = f.path_begin + upper_bound_u32(offs, f.path_count + 1, g) - 1;
+        const bool is_clip = f.path.is_clip[gp] != 0;
+        if (is_clip != (clip_pass != 0)) continue;
+        const int4 r = f.path.tile_rect[gp];
+        const int32_t w = r.z - r.x, h = r.w - r.y;
+        const uint32_t tbase = f.path.tile_offset[gp], cbase_col = f.path.col_offset[gp];
+        const bool even_odd = f.path.rule[gp] == 1;
+        const uint8_t ctrl = is_clip ? 0 : (even_odd ? 0x2 : 0x1);
+        const uint32_t local = f.path.local_index[gp];
+        const uint16_t color = is_clip ? 0 : (uint16_t)(local & 0xffffu);
+        const int32_t clip_gp = is_clip ? -1 : f.path.clip_gpath[gp];
+
         const uint32_t i = g - tbase;
         const int32_t ox = (int32_t)(i % (uint32_t)w), oy = (int32_t)(i / (uint32_t)w);
         const uint32_t cm = tbase + (uint32_t)(ox * h);
@@ -95,11 +102,13 @@ __global__ void k_propagate(FrameDev f, uint32_t first_path, uint32_t path_count
         int8_t backdrop = (int8_t)acc;
         const int32_t tx = r.x + ox, ty = r.y + oy;
         if (clip_gp >= 0) {
+            const int4 cr = f.path.tile_rect[clip_gp];
             int4 clip_rec = make_int4((int)kInvalid, 0, (int)kInvalid, 0);
             if (cr.x <= tx && cr.y <= ty && tx <= cr.z - 1 && ty <= cr.w - 1) {
-                int4 ct = f.tiles[cbase + (uint32_t)((ty - cr.y) * (cr.z - cr.x) + (tx - cr.x))];
-                uint32_t calpha = (uint32_t)ct.y;
-                int8_t cb = tile_backdrop(ct);
+                const uint32_t cg = f.path.tile_offset[clip_gp] + (uint32_t)((ty - cr.y) * (cr.z - cr.x) + (tx - cr.x));
+                const int4 ct = f.tiles[cg];
+                const uint32_t calpha = (uint32_t)ct.y;
+                const int8_t cb = tile_backdrop(ct);
                 if (calpha != kInvalid && alpha != kInvalid) {
                     clip_rec = make_int4((int)alpha, (int)backdrop, (int)calpha, (int)cb);
                     backdrop = 0;
@@ -119,20 +128,16 @@ __global__ void k_propagate(FrameDev f, uint32_t first_path, uint32_t path_count
             f.clips[g] = make_int4((int)kInvalid, 0, (int)kInvalid, 0);
         }
         f.tiles[g] = pack_tile(tx, ty, alpha, gp, color, ctrl, backdrop);
-        if (occluder_path && alpha == kInvalid && solid_occludes(backdrop, even_odd)) {
-            int4 s = sc.screen;
-            if (s.x <= tx && s.y <= ty && tx <= s.z - 1 && ty <= s.w - 1) {
-                uint32_t st = sc.screen_offset + (uint32_t)((ty - s.y) * (s.z - s.x) + (tx - s.x));
-                atomicMax(&f.zbuf[st], (int32_t)local);
-            }
+        if (!is_clip && (f.path.paint[gp] >> 24) == 255u && alpha == kInvalid && solid_occludes(backdrop, even_odd)) {
+            uint32_t st;
+            if (frame_screen_tile(f, f.scenes[f.path.scene[gp]], tx, ty, &st)) atomicMax(&f.zbuf[st], (int32_t)local);
         }
-    }
     }
 }
 
-void launch_propagate(const FrameDev& f, bool, uint32_t first_path, uint32_t path_count, uint32_t, cudaStream_t s) {
-    if (path_count == 0) return;
-    { count_launch(); k_propagate<<<152 * 16, 256, 0, s>>>(f, first_path, path_count); }
+void launch_propagate(const FrameDev& f, bool clip_pass, cudaStream_t s) {
+    if (f.path_count == 0) return;
+    { count_launch(); k_propagate<<<152 * 16, 256, 0, s>>>(f, clip_pass ? 1 : 0); }
 }
 
 // ---------------------------------------------------------------------------
@@ -147,12 +152,9 @@ __global__ void k_visible(FrameDev f, int scatter) {
         int4 rec = f.tiles[g];
         if (tile_ctrl(rec) == 0) continue;                                  // clip path tile
         if ((uint32_t)rec.y == kInvalid && tile_backdrop(rec) == 0) continue;  // empty (builder.rs:1016-1018)
-        uint32_t gp = (uint32_t)rec.z;
-        const SceneDev& sc = f.scenes[f.path.scene[gp]];
-        int32_t tx = tile_x(rec), ty = tile_y(rec);
-        int4 s = sc.screen;
-        if (!(s.x <= tx && s.y <= ty && tx <= s.z - 1 && ty <= s.w - 1)) continue;
-        uint32_t st = sc.screen_offset + (uint32_t)((ty - s.y) * (s.z - s.x) + (tx - s.x));
+        const uint32_t gp = (uint32_t)rec.z;
+        uint32_t st;
+        if (!frame_screen_tile(f, f.scenes[f.path.scene[gp]], tile_x(rec), tile_y(rec), &st)) continue;
         if ((int32_t)f.path.local_index[gp] < f.zbuf[st]) continue;  // occluded (tile.vs.glsl:51-55)
         if (!scatter) {
             atomicAdd(&f.screen_cnt[st], 1u);
@@ -271,9 +273,9 @@ __device__ __forceinline__ void warp_column_values(const CovBuf& buf, int out[8]
     }
 }
 
-// Per-pixel coverage of one visible tile for this lane's 8 pixels.
 struct WarpScratch { uint32_t keys[128]; CovBuf b0, b1; };
 
+// Per-pixel coverage of one path tile for this lane's 8 pixels.
 __device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint32_t g, WarpScratch& ws,
                                                float cov[8]) {
     const uint32_t gp = (uint32_t)rec.z;
@@ -315,23 +317,29 @@ __device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint
 // ---------------------------------------------------------------------------
 // fused fill + composite: one warp per screen tile, no block barriers
 // ---------------------------------------------------------------------------
-constexpr int kCompWarps = 4;
 constexpr uint32_t kWarpListCap = 128;
 
-template <int MODE>
-__global__ void __launch_bounds__(kCompWarps * 32) k_composite(FrameDev f, void* out, float4 bg) {
-    __shared__ WarpScratch scratch[kCompWarps];
+__device__ __forceinline__ uint32_t scene_of_screen_tile(const FrameDev& f, uint32_t st_global) {
+    uint32_t lo = f.scene_begin, hi = f.scene_begin + f.scene_count;  // last scene with offset <= st
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (f.scenes[mid].screen_offset <= st_global) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+template <int MODE, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out, float4 bg) {
+    __shared__ WarpScratch scratch[WARPS];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t st = blockIdx.x * kCompWarps + wid;
+    const uint32_t st = blockIdx.x * WARPS + wid;  // frame screen tile
     if (st >= f.screen_count) return;
     WarpScratch& ws = scratch[wid];
 
-    uint32_t si = 0;
-    while (si + 1 < f.scene_count && f.scenes[si + 1].screen_offset <= st) si++;
-    const SceneDev& sc = f.scenes[si];
+    const SceneDev& sc = f.scenes[scene_of_screen_tile(f, f.screen_begin + st)];
     const int4 s = sc.screen;
     const int32_t sw = s.z - s.x;
-    const uint32_t lst = st - sc.screen_offset;
+    const uint32_t lst = f.screen_begin + st - sc.screen_offset;
     const int32_t tx = s.x + (int32_t)(lst % (uint32_t)sw), ty = s.y + (int32_t)(lst / (uint32_t)sw);
     const int col = lane & 15, half = lane >> 4;
 
@@ -380,12 +388,13 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(FrameDev f, void*
         }
     }
     const int X = tx * 16 + col;
-    if (X < 0 || X >= sc.width) return;
+    if (X < sc.clip.x || X >= sc.clip.z) return;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         const int Y = ty * 16 + half * 8 + k;
-        if (Y < 0 || Y >= sc.height) continue;
-        uint64_t o = sc.out_offset + (uint64_t)Y * (uint64_t)sc.width + (uint64_t)X;
+        if (Y < sc.clip.y || Y >= sc.clip.w) continue;
+        const uint64_t o = sc.out_offset + (uint64_t)(int64_t)(Y - sc.origin_y) * (uint64_t)(int64_t)sc.pitch +
+                           (uint64_t)(int64_t)(X - sc.origin_x);
         if (MODE == 0) {
             auto q = [](float v) { return (uint32_t)__float2uint_rn(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f); };
             ((uint32_t*)out)[o] = q(d0[k]) | (q(d1[k]) << 8) | (q(d2[k]) << 16) | (q(d3[k]) << 24);
@@ -397,21 +406,31 @@ __global__ void __launch_bounds__(kCompWarps * 32) k_composite(FrameDev f, void*
     }
 }
 
+template <int MODE>
+void launch_composite_mode(const FrameDev& f, void* out, const float4& bg, cudaStream_t s) {
+    const int w = f.tune.comp_warps;
+    const uint32_t blocks = (f.screen_count + w - 1) / w;
+    if (w == 2) { count_launch(); k_composite<MODE, 2><<<blocks, 64, 0, s>>>(f, out, bg); }
+    else if (w == 8) { count_launch(); k_composite<MODE, 8><<<blocks, 256, 0, s>>>(f, out, bg); }
+    else { count_launch(); k_composite<MODE, 4><<<(f.screen_count + 3) / 4, 128, 0, s>>>(f, out, bg); }
+}
+
 void launch_composite(const FrameDev& f, int mode, void* out, const float4& bg, cudaStream_t s) {
     if (f.screen_count == 0) return;
-    uint32_t blocks = (f.screen_count + kCompWarps - 1) / kCompWarps;
-    if (mode == 0) { count_launch(); k_composite<0><<<blocks, kCompWarps * 32, 0, s>>>(f, out, bg); }
-    else if (mode == 1) { count_launch(); k_composite<1><<<blocks, kCompWarps * 32, 0, s>>>(f, out, bg); }
-    else { count_launch(); k_composite<2><<<blocks, kCompWarps * 32, 0, s>>>(f, out, bg); }
+    if (mode == 0) launch_composite_mode<0>(f, out, bg, s);
+    else if (mode == 1) launch_composite_mode<1>(f, out, bg, s);
+    else launch_composite_mode<2>(f, out, bg, s);
 }
 
 // ---------------------------------------------------------------------------
 // readback of raw alpha masks and resolved tile coverage (parity checks)
 // ---------------------------------------------------------------------------
+constexpr int kMaskWarps = 4;
+
 __global__ void k_alpha_masks(FrameDev f, float* out) {
-    __shared__ WarpScratch scratch[kCompWarps];
+    __shared__ WarpScratch scratch[kMaskWarps];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t a = blockIdx.x * kCompWarps + wid;
+    const uint32_t a = blockIdx.x * kMaskWarps + wid;
     if (a >= f.counters->alpha_tiles) return;
     warp_accumulate_tile(f, a, scratch[wid].b0);
     int v[8];
@@ -422,9 +441,9 @@ __global__ void k_alpha_masks(FrameDev f, float* out) {
 }
 
 __global__ void k_tile_cov(FrameDev f, float* out) {
-    __shared__ WarpScratch scratch[kCompWarps];
+    __shared__ WarpScratch scratch[kMaskWarps];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t g = blockIdx.x * kCompWarps + wid;
+    const uint32_t g = blockIdx.x * kMaskWarps + wid;
     if (g >= f.counters->tiles) return;
     float cov[8];
     tile_coverage8(f, f.tiles[g], g, scratch[wid], cov);
@@ -434,9 +453,9 @@ __global__ void k_tile_cov(FrameDev f, float* out) {
 }
 
 void launch_masks(const FrameDev& f, float* alpha_masks, float* tile_cov, cudaStream_t s) {
-    uint32_t blocks = (f.tile_cap + kCompWarps - 1) / kCompWarps + 1;
-    if (alpha_masks) { count_launch(); k_alpha_masks<<<blocks, kCompWarps * 32, 0, s>>>(f, alpha_masks); }
-    if (tile_cov) { count_launch(); k_tile_cov<<<blocks, kCompWarps * 32, 0, s>>>(f, tile_cov); }
+    uint32_t blocks = (f.tile_cap + kMaskWarps - 1) / kMaskWarps + 1;
+    if (alpha_masks) { count_launch(); k_alpha_masks<<<blocks, kMaskWarps * 32, 0, s>>>(f, alpha_masks); }
+    if (tile_cov) { count_launch(); k_tile_cov<<<blocks, kMaskWarps * 32, 0, s>>>(f, tile_cov); }
 }
 
 }  // namespace pf

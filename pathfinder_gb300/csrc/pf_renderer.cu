@@ -1,6 +1,6 @@
 // pf_renderer.cu — host side of the CUDA renderer level and its C ABI.
 //
-// The frame replaces RendererD3D11::prepare_tiles / draw_tiles
+// A frame replaces RendererD3D11::prepare_tiles / draw_tiles
 // (renderer/src/gpu/d3d11/renderer.rs:414-782).  The reference sizes its
 // buffers with three blocking readbacks and a regrow-and-retry loop
 // (:218-229, :338-353, :463-499, :634-648).  Here every kernel checks the
@@ -8,6 +8,11 @@
 // without any mid-frame synchronisation, and the single status readback at
 // the end triggers a regrow and one re-run only when a capacity was exceeded
 // (in steady state: never).
+//
+// The renderer holds a batch of scenes (one for the plain API).  Global path
+// order is scene-major, each scene's clip paths before its draw paths, so the
+// paths, segments and screen tiles of any contiguous range of scenes are
+// contiguous and one frame covers such a range.
 #include "pf_kernels.cuh"
 #include "../../include/pathfinder_cuda.h"
 
@@ -41,6 +46,26 @@ inline int32_t cvt_rne_host(float x) {
     return (int32_t)std::nearbyint(x);
 }
 
+struct SceneInfo {
+    uint32_t first_path = 0, nclip = 0, ndraw = 0;
+    uint32_t seg_begin = 0, seg_end = 0;
+    uint32_t screen_offset = 0, screen_count = 0;
+    PFRectF view_box{};
+    int4 screen{0, 0, 0, 0};
+    bool has_target = false;
+    bool explicit_target = false;  // given at upload: plain renders keep it
+    PFCUDASceneTarget target{};
+};
+
+struct Range {
+    uint32_t s0 = 0, s1 = 0;     // scenes
+    uint32_t p0 = 0, p1 = 0;     // paths
+    uint32_t g0 = 0, g1 = 0;     // segments
+    uint32_t st0 = 0, st1 = 0;   // screen tiles
+};
+
+const TuneParams kDefaultTune{128, 256, 16, 4};
+
 }  // namespace
 
 struct PFCUDARenderer {
@@ -50,10 +75,12 @@ struct PFCUDARenderer {
     PFCUDARendererOptions options{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
-    // scene (resident)
+    // scenes (resident)
     bool has_scene = false;
-    uint32_t P = 0, nclip = 0, ndraw = 0, NP = 0, NC = 0, nord = 0, S = 0;
-    PFRectF view_box{};
+    uint32_t P = 0, NP = 0, NC = 0, nord = 0, S = 0, screen_total = 0;
+    std::vector<SceneInfo> scenes;
+    std::vector<uint32_t> path_local;  // host copy: index within clip / draw paths
+    std::vector<uint8_t> path_is_clip;
     DevBuf<float2> pts, pts_t;
     DevBuf<uint8_t> flags;
     DevBuf<uint32_t> starts, ord_contour, ord_path, contour_segs, contour_seg_base;
@@ -61,8 +88,8 @@ struct PFCUDARenderer {
     DevBuf<uint32_t> first_ord, paint, local_index, scene_of;
     DevBuf<int32_t> clip_gpath;
     DevBuf<uint8_t> rule, is_clip;
-    DevBuf<SceneDev> scenes;
-    std::vector<PFCUDAPath> host_paths;  // clip paths then draw paths
+    DevBuf<SceneDev> scenes_dev;
+    std::vector<SceneDev> scenes_host;
 
     // per-frame buffers
     DevBuf<int4> tile_rect;
@@ -83,15 +110,16 @@ struct PFCUDARenderer {
     Counters* h_counters = nullptr;  // pinned
 
     uint32_t tile_cap = 0, col_cap = 0, fill_cap = 0, vis_cap = 0, line_cap = 0;
-    uint32_t screen_count = 0;
-    int4 screen_rect{0, 0, 0, 0};
-    int32_t last_w = 0, last_h = 0;
+    Range last;
     PFCUDARenderStats stats{};
-    uint64_t last_needed = 0;
-    uint32_t pending_status = 0;
     bool profiling = false;
     cudaEvent_t stage_ev[PF_CUDA_STAGE_COUNT + 1] = {};
     uint64_t launches = 0;
+    TuneParams tune = kDefaultTune;
+
+    // captured frame
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
 };
 
 namespace {
@@ -115,11 +143,27 @@ int4 screen_rect_of(PFRectF v) {
                      cvt_rne_host(std::ceil(v.lower_right.x * q)), cvt_rne_host(std::ceil(v.lower_right.y * q)));
 }
 
-FrameDev frame_dev(PFCUDARenderer* r, bool transformed) {
+Range make_range(const PFCUDARenderer* r, uint32_t s0, uint32_t count) {
+    Range g;
+    g.s0 = s0;
+    g.s1 = s0 + count;
+    const SceneInfo& a = r->scenes[s0];
+    const SceneInfo& b = r->scenes[g.s1 - 1];
+    g.p0 = a.first_path;
+    g.p1 = b.first_path + b.nclip + b.ndraw;
+    g.g0 = a.seg_begin;
+    g.g1 = b.seg_end;
+    g.st0 = a.screen_offset;
+    g.st1 = b.screen_offset + b.screen_count;
+    return g;
+}
+
+FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g) {
     FrameDev f{};
     f.pts = transformed ? r->pts_t.p : r->pts.p;
     f.segs = r->segs.p;
-    f.seg_count = r->S;
+    f.seg_begin = g.g0;
+    f.seg_count = g.g1 - g.g0;
     f.path.first_ord_contour = r->first_ord.p;
     f.path.paint = r->paint.p;
     f.path.clip_gpath = r->clip_gpath.p;
@@ -130,14 +174,18 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed) {
     f.path.tile_rect = r->tile_rect.p;
     f.path.tile_offset = r->tile_offset.p;
     f.path.col_offset = r->col_offset.p;
-    f.scenes = r->scenes.p;
-    f.path_count = r->P;
-    f.scene_count = 1;
+    f.scenes = r->scenes_dev.p;
+    f.path_begin = g.p0;
+    f.path_count = g.p1 - g.p0;
+    f.scene_begin = g.s0;
+    f.scene_count = g.s1 - g.s0;
+    f.screen_begin = g.st0;
+    f.tune = r->tune;
     f.tile_cap = r->tile_cap;
     f.col_cap = r->col_cap;
     f.fill_cap = r->fill_cap;
     f.vis_cap = r->vis_cap;
-    f.screen_count = r->screen_count;
+    f.screen_count = g.st1 - g.st0;
     f.tile_fill_count = r->tile_fill_count.p;
     f.tile_fill_base = r->tile_fill_base.p;
     f.tile_alpha = r->tile_alpha.p;
@@ -169,31 +217,19 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed) {
 
 cudaError_t ensure_frame_buffers(PFCUDARenderer* r) {
     cudaError_t e;
-    if ((e = r->tile_fill_count.ensure((size_t)r->tile_cap + 1))) return e;
-    if ((e = r->tile_fill_base.ensure((size_t)r->tile_cap + 1))) return e;
-    if ((e = r->tile_alpha.ensure((size_t)r->tile_cap + 1))) return e;
-    if ((e = r->alpha_owner.ensure((size_t)r->tile_cap + 1))) return e;
-    if ((e = r->tile_delta.ensure((size_t)r->tile_cap + 1))) return e;
-    if ((e = r->tile_delta_scan.ensure((size_t)r->tile_cap + 1))) return e;
-    if ((e = r->path_tiles.ensure((size_t)r->P + 1))) return e;
-    if ((e = r->path_cols.ensure((size_t)r->P + 1))) return e;
-    if ((e = r->tiles.ensure((size_t)r->tile_cap + 1))) return e;
-    if ((e = r->clips.ensure((size_t)r->tile_cap + 1))) return e;
-    if ((e = r->col_backdrop.ensure((size_t)r->col_cap + 1))) return e;
-    if ((e = r->fills.ensure((size_t)r->fill_cap + 1))) return e;
-    if ((e = r->fill_e.ensure((size_t)r->fill_cap + 1))) return e;
-    if ((e = r->lines.ensure((size_t)r->line_cap + 1))) return e;
-    if ((e = r->line_path.ensure((size_t)r->line_cap + 1))) return e;
-    if ((e = r->line_fill_count.ensure((size_t)r->line_cap + 1))) return e;
-    if ((e = r->line_fill_base.ensure((size_t)r->line_cap + 1))) return e;
-    if ((e = r->vis.ensure((size_t)r->vis_cap + 1))) return e;
-    if ((e = r->zbuf.ensure((size_t)r->screen_count + 1))) return e;
-    if ((e = r->screen_cnt.ensure((size_t)r->screen_count + 1))) return e;
-    if ((e = r->screen_base.ensure((size_t)r->screen_count + 1))) return e;
-    size_t nmax = std::max<size_t>({(size_t)r->tile_cap, (size_t)r->S, (size_t)r->screen_count, (size_t)r->nord,
+    const size_t T = (size_t)r->tile_cap + 1, L = (size_t)r->line_cap + 1, F = (size_t)r->fill_cap + 1;
+    const size_t ST = (size_t)r->screen_total + 1, P = (size_t)r->P + 1;
+    if ((e = r->tile_fill_count.ensure(T)) || (e = r->tile_fill_base.ensure(T)) || (e = r->tile_alpha.ensure(T)) ||
+        (e = r->alpha_owner.ensure(T)) || (e = r->tile_delta.ensure(T)) || (e = r->tile_delta_scan.ensure(T)) ||
+        (e = r->tiles.ensure(T)) || (e = r->clips.ensure(T)) || (e = r->col_backdrop.ensure((size_t)r->col_cap + 1)) ||
+        (e = r->fills.ensure(F)) || (e = r->fill_e.ensure(F)) || (e = r->lines.ensure(L)) ||
+        (e = r->line_path.ensure(L)) || (e = r->line_fill_count.ensure(L)) || (e = r->line_fill_base.ensure(L)) ||
+        (e = r->vis.ensure((size_t)r->vis_cap + 1)) || (e = r->zbuf.ensure(ST)) || (e = r->screen_cnt.ensure(ST)) ||
+        (e = r->screen_base.ensure(ST)) || (e = r->path_tiles.ensure(P)) || (e = r->path_cols.ensure(P)))
+        return e;
+    size_t nmax = std::max<size_t>({(size_t)r->tile_cap, (size_t)r->S, (size_t)r->screen_total, (size_t)r->nord,
                                     (size_t)r->line_cap, (size_t)r->P}) + 1;
-    if ((e = r->scan_partials.ensure(nmax / 2048 + 2))) return e;
-    return cudaSuccess;
+    return r->scan_partials.ensure(nmax / 2048 + 2);
 }
 
 bool is_identity(const PFCUDABuildOptions* o) {
@@ -203,8 +239,8 @@ bool is_identity(const PFCUDABuildOptions* o) {
            t.vector.y == 0.0f;
 }
 
-// Enqueue one frame.  mode: 0 RGBA8, 1 R8, 2 FP32 single channel, -1 no composite.
-cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev) {
+// Enqueue one frame over range g.  mode: PF_CUDA_FORMAT_*, or -1 for no composite.
+cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev, const Range& g) {
     cudaStream_t s = r->stream;
     bool transformed = !is_identity(opts);
     cudaError_t e;
@@ -214,12 +250,13 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
                        opts->transform.vector.x, opts->transform.vector.y};
         launch_transform(r->pts.p, r->pts_t.p, r->NP, m6, s);
     }
-    FrameDev f = frame_dev(r, transformed);
+    FrameDev f = frame_dev(r, transformed, g);
     ScanTemp tmp{r->scan_partials.p, (uint32_t)r->scan_partials.cap};
     Counters* c = r->counters.p;
     auto mark = [&](int stage) {
         if (r->profiling) cudaEventRecord(r->stage_ev[stage], s);
     };
+    const size_t nst = (size_t)(g.st1 - g.st0) + 1;
     uint64_t before = launch_counter();
     if ((e = cudaMemsetAsync(c, 0, sizeof(Counters), s))) return e;
     mark(0);
@@ -237,14 +274,15 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     mark(4);
     launch_bin_emit(f, s);
     mark(5);
-    if ((e = cudaMemsetAsync(r->zbuf.p, 0, sizeof(int32_t) * (r->screen_count + 1), s))) return e;
-    // clip paths first: draw paths read their finished tiles
-    launch_propagate(f, true, 0, r->nclip, 0, s);
-    launch_propagate(f, false, r->nclip, r->ndraw, 0, s);
+    if ((e = cudaMemsetAsync(r->zbuf.p, 0, sizeof(int32_t) * nst, s))) return e;
+    // clip paths first: draw tiles of clipped paths read their clip's finished tiles
+    launch_propagate(f, true, s);
+    launch_propagate(f, false, s);
     mark(6);
-    if ((e = cudaMemsetAsync(r->screen_cnt.p, 0, sizeof(uint32_t) * (r->screen_count + 1), s))) return e;
+    if ((e = cudaMemsetAsync(r->screen_cnt.p, 0, sizeof(uint32_t) * nst, s))) return e;
     launch_visible(f, false, s);
-    launch_scan(r->screen_cnt.p, r->screen_base.p, nullptr, r->screen_count, r->screen_count, 0, &c->visible, tmp, s);
+    launch_scan(r->screen_cnt.p, r->screen_base.p, nullptr, (uint32_t)(nst - 1), (uint32_t)(nst - 1), 0, &c->visible,
+                tmp, s);
     launch_visible(f, true, s);
     mark(7);
     if (mode >= 0) {
@@ -283,47 +321,47 @@ int32_t status_to_code(uint32_t st) {
 }
 
 void record_stats(PFCUDARenderer* r, const Counters& h, float ms) {
-    r->stats.path_count = r->P;
-    r->stats.segment_count = r->S;
+    r->stats.path_count = r->last.p1 - r->last.p0;
+    r->stats.segment_count = r->last.g1 - r->last.g0;
     r->stats.line_count = h.lines;
     r->stats.fill_count = h.fills;
     r->stats.tile_count = h.tiles;
     r->stats.alpha_tile_count = h.alpha_tiles;
     r->stats.visible_tile_count = h.visible;
-    r->stats.screen_tile_count = r->screen_count;
+    r->stats.screen_tile_count = r->last.st1 - r->last.st0;
     r->stats.status = h.status;
     r->stats.gpu_time_ms = ms;
     r->stats.kernel_launches = r->launches;
 }
 
-int32_t prepare_size(PFCUDARenderer* r, int32_t width, int32_t height) {
-    if (width <= 0 || height <= 0) return PF_CUDA_ERR_INVALID;
-    SceneDev sd{};
-    sd.view_box = make_float4(r->view_box.origin.x, r->view_box.origin.y, r->view_box.lower_right.x,
-                              r->view_box.lower_right.y);
-    sd.screen = r->screen_rect;
-    sd.screen_offset = 0;
-    sd.first_path = 0;
-    sd.clip_count = r->nclip;
-    sd.draw_count = r->ndraw;
-    sd.width = width;
-    sd.height = height;
-    sd.out_offset = 0;
-    PF_TRY(cudaMemcpyAsync(r->scenes.p, &sd, sizeof(SceneDev), cudaMemcpyHostToDevice, r->stream));
-    r->last_w = width;
-    r->last_h = height;
-    return PF_CUDA_OK;
+cudaError_t upload_scene_records(PFCUDARenderer* r) {
+    return cudaMemcpyAsync(r->scenes_dev.p, r->scenes_host.data(), sizeof(SceneDev) * r->scenes_host.size(),
+                           cudaMemcpyHostToDevice, r->stream);
+}
+
+void set_target(PFCUDARenderer* r, uint32_t k, const PFCUDASceneTarget& t) {
+    r->scenes[k].target = t;
+    r->scenes[k].has_target = true;
+    SceneDev& d = r->scenes_host[k];
+    d.clip = make_int4(t.clip.origin.x, t.clip.origin.y, t.clip.lower_right.x, t.clip.lower_right.y);
+    d.origin_x = t.origin_x;
+    d.origin_y = t.origin_y;
+    d.pitch = t.pitch;
+    d.out_offset = t.out_offset;
+}
+
+bool valid_range(const PFCUDARenderer* r, uint32_t first, uint32_t count) {
+    return r->has_scene && count > 0 && first < r->scenes.size() && count <= r->scenes.size() - first;
 }
 
 // Run one frame synchronously with regrow-and-retry.
-int32_t run_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev, int32_t w, int32_t h) {
+int32_t run_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev, const Range& g) {
     if (!r->has_scene) return PF_CUDA_ERR_NO_SCENE;
-    int32_t rc = prepare_size(r, w, h);
-    if (rc) return rc;
+    r->last = g;
     for (int attempt = 0; attempt < 4; attempt++) {
         PF_TRY(ensure_frame_buffers(r));
         PF_TRY(cudaEventRecord(r->ev0, r->stream));
-        PF_TRY(enqueue_frame(r, opts, mode, out_dev));
+        PF_TRY(enqueue_frame(r, opts, mode, out_dev, g));
         PF_TRY(cudaEventRecord(r->ev1, r->stream));
         PF_TRY(cudaMemcpyAsync(r->h_counters, r->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, r->stream));
         PF_TRY(cudaStreamSynchronize(r->stream));
@@ -338,6 +376,36 @@ int32_t run_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, v
         return status_to_code(h.status);
     }
     return PF_CUDA_ERR_CAPACITY;
+}
+
+void release_graph(PFCUDARenderer* r) {
+    if (r->graph_exec) cudaGraphExecDestroy(r->graph_exec);
+    if (r->graph) cudaGraphDestroy(r->graph);
+    r->graph_exec = nullptr;
+    r->graph = nullptr;
+}
+
+// Single-image rendering: scenes uploaded without targets draw into the
+// width x height image (row 0 = top of the view box's pixel grid).
+int32_t prepare_plain_targets(PFCUDARenderer* r, int32_t width, int32_t height, bool* changed) {
+    if (width <= 0 || height <= 0) return PF_CUDA_ERR_INVALID;
+    *changed = false;
+    for (uint32_t k = 0; k < r->scenes.size(); k++) {
+        if (r->scenes[k].explicit_target) continue;
+        if (r->scenes[k].has_target) {
+            const PFCUDASceneTarget& t = r->scenes[k].target;
+            if (t.out_offset == 0 && t.origin_x == 0 && t.origin_y == 0 && t.pitch == width &&
+                t.clip.lower_right.x == width && t.clip.lower_right.y == height && t.clip.origin.x == 0 &&
+                t.clip.origin.y == 0)
+                continue;
+        }
+        PFCUDASceneTarget t{};
+        t.pitch = width;
+        t.clip = PFRectI{{0, 0}, {width, height}};
+        set_target(r, k, t);
+        *changed = true;
+    }
+    return PF_CUDA_OK;
 }
 
 }  // namespace
@@ -361,8 +429,7 @@ int32_t PFCUDARendererCreate(int32_t device_ordinal, const PFCUDARendererOptions
     if (options) r->options = *options;
     if ((e = cudaStreamCreateWithFlags(&r->own_stream, cudaStreamNonBlocking)) ||
         (e = cudaEventCreate(&r->ev0)) || (e = cudaEventCreate(&r->ev1)) ||
-        (e = cudaMallocHost((void**)&r->h_counters, sizeof(Counters))) || (e = r->counters.ensure(1)) ||
-        (e = r->scenes.ensure(1))) {
+        (e = cudaMallocHost((void**)&r->h_counters, sizeof(Counters))) || (e = r->counters.ensure(1))) {
         PFCUDARendererDestroy(r);
         return cuda_status(e);
     }
@@ -375,11 +442,12 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     if (!r) return PF_CUDA_OK;
     cudaSetDevice(r->device);
     if (r->stream) cudaStreamSynchronize(r->stream);
+    release_graph(r);
     r->pts.release(); r->pts_t.release(); r->flags.release(); r->starts.release();
     r->ord_contour.release(); r->ord_path.release(); r->contour_segs.release(); r->contour_seg_base.release();
     r->segs.release(); r->first_ord.release(); r->paint.release(); r->local_index.release();
     r->scene_of.release(); r->clip_gpath.release(); r->rule.release(); r->is_clip.release();
-    r->scenes.release(); r->tile_rect.release(); r->tile_offset.release(); r->col_offset.release();
+    r->scenes_dev.release(); r->tile_rect.release(); r->tile_offset.release(); r->col_offset.release();
     r->seg_line_count.release(); r->seg_line_base.release(); r->lines.release(); r->line_path.release();
     r->line_fill_count.release(); r->line_fill_base.release(); r->tile_fill_count.release();
     r->tile_fill_base.release(); r->tile_alpha.release(); r->alpha_owner.release(); r->tile_delta.release();
@@ -400,126 +468,181 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
 int32_t PFCUDARendererSetStream(PFCUDARendererRef r, void* stream) {
     if (!r) return PF_CUDA_ERR_INVALID;
     r->stream = stream ? (cudaStream_t)stream : r->own_stream;
+    release_graph(r);
     return PF_CUDA_OK;
 }
 
 int32_t PFCUDARendererSetOptions(PFCUDARendererRef r, const PFCUDARendererOptions* options) {
     if (!r || !options) return PF_CUDA_ERR_INVALID;
     r->options = *options;
+    release_graph(r);
     return PF_CUDA_OK;
 }
 
-int32_t PFCUDASceneUpload(PFCUDARendererRef r, const PFCUDASceneDesc* sc) {
-    if (!r || !sc) return PF_CUDA_ERR_INVALID;
-    if (sc->memory != PF_MEMORY_HOST && sc->memory != PF_MEMORY_DEVICE) return PF_CUDA_ERR_INVALID;
-    if ((sc->clip_path_count && !sc->clip_paths) || (sc->draw_path_count && !sc->draw_paths))
-        return PF_CUDA_ERR_INVALID;
-    if (sc->contour_count && !sc->contour_starts) return PF_CUDA_ERR_INVALID;
-    if (sc->point_count && (!sc->points || !sc->point_flags)) return PF_CUDA_ERR_INVALID;
+int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scenes, const PFCUDASceneTarget* targets,
+                               uint32_t scene_count) {
+    if (!r || !scenes || scene_count == 0) return PF_CUDA_ERR_INVALID;
     PF_TRY(cudaSetDevice(r->device));
     cudaStream_t s = r->stream;
+    release_graph(r);
     r->has_scene = false;
-    const cudaMemcpyKind kind = sc->memory == PF_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
 
-    // contour starts are needed on the host for validation and ordering
-    std::vector<uint32_t> hstarts(sc->contour_count + 1, 0);
-    if (sc->contour_count) {
-        if (sc->memory == PF_MEMORY_HOST)
-            std::memcpy(hstarts.data(), sc->contour_starts, sizeof(uint32_t) * (sc->contour_count + 1));
-        else
-            PF_TRY(cudaMemcpy(hstarts.data(), sc->contour_starts, sizeof(uint32_t) * (sc->contour_count + 1),
-                              cudaMemcpyDeviceToHost));
+    // ---- validate and lay out the batch on the host --------------------------
+    uint64_t np_total = 0, nc_total = 0, P = 0;
+    for (uint32_t k = 0; k < scene_count; k++) {
+        const PFCUDASceneDesc& sc = scenes[k];
+        if (sc.memory != PF_MEMORY_HOST && sc.memory != PF_MEMORY_DEVICE) return PF_CUDA_ERR_INVALID;
+        if ((sc.clip_path_count && !sc.clip_paths) || (sc.draw_path_count && !sc.draw_paths)) return PF_CUDA_ERR_INVALID;
+        if (sc.contour_count && !sc.contour_starts) return PF_CUDA_ERR_INVALID;
+        if (sc.point_count && (!sc.points || !sc.point_flags)) return PF_CUDA_ERR_INVALID;
+        np_total += sc.point_count;
+        nc_total += (uint64_t)sc.contour_count + 1;  // each scene keeps its own end boundary
+        P += (uint64_t)sc.clip_path_count + sc.draw_path_count;
     }
-    for (uint32_t c = 0; c < sc->contour_count; c++)
-        if (hstarts[c] > hstarts[c + 1] || hstarts[c + 1] > sc->point_count) return PF_CUDA_ERR_INVALID;
+    if (np_total >= 0x7fffffffull || nc_total >= 0x7fffffffull || P >= 0x7fffffffull) return PF_CUDA_ERR_INVALID;
 
-    uint32_t P = sc->clip_path_count + sc->draw_path_count;
-    r->host_paths.assign(P, PFCUDAPath{});
-    std::vector<uint32_t> first_ord(P + 1, 0), ord_contour, ord_path, paint(P), local(P), scene(P, 0);
-    std::vector<int32_t> clip(P);
-    std::vector<uint8_t> rule(P), isclip(P);
-    for (uint32_t gp = 0; gp < P; gp++) {
-        bool c = gp < sc->clip_path_count;
-        const PFCUDAPath& p = c ? sc->clip_paths[gp] : sc->draw_paths[gp - sc->clip_path_count];
-        r->host_paths[gp] = p;
-        if ((uint64_t)p.first_contour + p.contour_count > sc->contour_count) return PF_CUDA_ERR_INVALID;
-        if (p.fill_rule > 1 || p.blend_mode != PF_BLEND_MODE_SRC_OVER) return PF_CUDA_ERR_INVALID;
-        if (!c && p.clip_path >= (int32_t)sc->clip_path_count) return PF_CUDA_ERR_INVALID;
-        if (c && p.clip_path >= 0) return PF_CUDA_ERR_INVALID;  // nested clips: not on this path
-        first_ord[gp] = (uint32_t)ord_contour.size();
-        for (uint32_t k = 0; k < p.contour_count; k++) {
-            ord_contour.push_back(p.first_contour + k);
-            ord_path.push_back(gp);
+    std::vector<uint32_t> hstarts((size_t)nc_total + 1, 0);
+    std::vector<uint32_t> first_ord((size_t)P + 1, 0), ord_contour, ord_path, paint((size_t)P), local((size_t)P),
+        scene_of((size_t)P);
+    std::vector<int32_t> clip((size_t)P);
+    std::vector<uint8_t> rule((size_t)P), isclip((size_t)P);
+    r->scenes.assign(scene_count, SceneInfo());
+    r->scenes_host.assign(scene_count, SceneDev{});
+    uint32_t point_base = 0, contour_base = 0, gp = 0, screen_total = 0;
+    for (uint32_t k = 0; k < scene_count; k++) {
+        const PFCUDASceneDesc& sc = scenes[k];
+        std::vector<uint32_t> st(sc.contour_count + 1, 0);
+        if (sc.contour_count) {
+            if (sc.memory == PF_MEMORY_HOST)
+                std::memcpy(st.data(), sc.contour_starts, sizeof(uint32_t) * (sc.contour_count + 1));
+            else
+                PF_TRY(cudaMemcpy(st.data(), sc.contour_starts, sizeof(uint32_t) * (sc.contour_count + 1),
+                                  cudaMemcpyDeviceToHost));
         }
-        paint[gp] = (uint32_t)p.paint.r | ((uint32_t)p.paint.g << 8) | ((uint32_t)p.paint.b << 16) |
-                    ((uint32_t)p.paint.a << 24);
-        local[gp] = c ? gp : gp - sc->clip_path_count;
-        clip[gp] = (!c && p.clip_path >= 0) ? p.clip_path : -1;  // clip paths come first: gp == clip index
-        rule[gp] = p.fill_rule;
-        isclip[gp] = c ? 1 : 0;
+        for (uint32_t c = 0; c < sc.contour_count; c++)
+            if (st[c] > st[c + 1] || st[c + 1] > sc.point_count) return PF_CUDA_ERR_INVALID;
+        // contour c of the scene is global contour contour_base + c; its end is
+        // the next boundary, so the scene's boundaries (count + 1) are copied whole
+        for (uint32_t c = 0; c <= sc.contour_count; c++) hstarts[contour_base + c] = point_base + st[c];
+        SceneInfo& si = r->scenes[k];
+        si.first_path = gp;
+        si.nclip = sc.clip_path_count;
+        si.ndraw = sc.draw_path_count;
+        si.view_box = sc.view_box;
+        si.screen = screen_rect_of(sc.view_box);
+        int32_t sw = std::max(0, si.screen.z - si.screen.x), sh = std::max(0, si.screen.w - si.screen.y);
+        si.screen_offset = screen_total;
+        si.screen_count = (uint32_t)sw * (uint32_t)sh;
+        screen_total += si.screen_count;
+        for (uint32_t i = 0; i < sc.clip_path_count + sc.draw_path_count; i++, gp++) {
+            const bool c = i < sc.clip_path_count;
+            const PFCUDAPath& p = c ? sc.clip_paths[i] : sc.draw_paths[i - sc.clip_path_count];
+            if ((uint64_t)p.first_contour + p.contour_count > sc.contour_count) return PF_CUDA_ERR_INVALID;
+            if (p.fill_rule > 1 || p.blend_mode != PF_BLEND_MODE_SRC_OVER) return PF_CUDA_ERR_INVALID;
+            if (!c && p.clip_path >= (int32_t)sc.clip_path_count) return PF_CUDA_ERR_INVALID;
+            if (c && p.clip_path >= 0) return PF_CUDA_ERR_INVALID;  // nested clips: not on this path
+            first_ord[gp] = (uint32_t)ord_contour.size();
+            for (uint32_t q = 0; q < p.contour_count; q++) {
+                ord_contour.push_back(contour_base + p.first_contour + q);
+                ord_path.push_back(gp);
+            }
+            paint[gp] = (uint32_t)p.paint.r | ((uint32_t)p.paint.g << 8) | ((uint32_t)p.paint.b << 16) |
+                        ((uint32_t)p.paint.a << 24);
+            local[gp] = c ? i : i - sc.clip_path_count;
+            clip[gp] = (!c && p.clip_path >= 0) ? (int32_t)(si.first_path + (uint32_t)p.clip_path) : -1;
+            rule[gp] = p.fill_rule;
+            isclip[gp] = c ? 1 : 0;
+            scene_of[gp] = k;
+        }
+        SceneDev& d = r->scenes_host[k];
+        d.view_box = make_float4(sc.view_box.origin.x, sc.view_box.origin.y, sc.view_box.lower_right.x,
+                                 sc.view_box.lower_right.y);
+        d.screen = si.screen;
+        d.screen_offset = si.screen_offset;
+        d.first_path = si.first_path;
+        d.clip_count = si.nclip;
+        d.draw_count = si.ndraw;
+        if (targets) {
+            set_target(r, k, targets[k]);
+            si.explicit_target = true;
+        }
+        point_base += sc.point_count;
+        contour_base += sc.contour_count + 1;
     }
+    hstarts[nc_total] = point_base;
     first_ord[P] = (uint32_t)ord_contour.size();
-    uint32_t nord = (uint32_t)ord_contour.size();
+    const uint32_t nord = (uint32_t)ord_contour.size();
+    r->path_local.assign(local.begin(), local.end());
+    r->path_is_clip.assign(isclip.begin(), isclip.end());
 
+    // ---- device copies ---------------------------------------------------------
     cudaError_t e;
-    if ((e = r->pts.ensure(sc->point_count)) || (e = r->flags.ensure(sc->point_count)) ||
-        (e = r->starts.ensure(sc->contour_count + 1)) || (e = r->ord_contour.ensure(nord)) ||
-        (e = r->ord_path.ensure(nord)) || (e = r->contour_segs.ensure(nord + 1)) ||
-        (e = r->contour_seg_base.ensure(nord + 1)) || (e = r->first_ord.ensure(P + 1)) ||
-        (e = r->paint.ensure(P)) || (e = r->local_index.ensure(P)) || (e = r->scene_of.ensure(P)) ||
-        (e = r->clip_gpath.ensure(P)) || (e = r->rule.ensure(P)) || (e = r->is_clip.ensure(P)) ||
-        (e = r->tile_rect.ensure(P)) || (e = r->tile_offset.ensure(P + 1)) || (e = r->col_offset.ensure(P + 1)) ||
-        (e = r->scan_partials.ensure(nord / 2048 + 2)))
+    const size_t Pz = (size_t)P;
+    if ((e = r->pts.ensure(np_total)) || (e = r->flags.ensure(np_total)) || (e = r->starts.ensure(nc_total + 1)) ||
+        (e = r->ord_contour.ensure(nord)) || (e = r->ord_path.ensure(nord)) || (e = r->contour_segs.ensure(nord + 1)) ||
+        (e = r->contour_seg_base.ensure(nord + 1)) || (e = r->first_ord.ensure(Pz + 1)) || (e = r->paint.ensure(Pz)) ||
+        (e = r->local_index.ensure(Pz)) || (e = r->scene_of.ensure(Pz)) || (e = r->clip_gpath.ensure(Pz)) ||
+        (e = r->rule.ensure(Pz)) || (e = r->is_clip.ensure(Pz)) || (e = r->tile_rect.ensure(Pz)) ||
+        (e = r->tile_offset.ensure(Pz + 1)) || (e = r->col_offset.ensure(Pz + 1)) ||
+        (e = r->scenes_dev.ensure(scene_count)) || (e = r->scan_partials.ensure(nord / 2048 + 2)))
         return cuda_status(e);
-    if (sc->point_count) {
-        PF_TRY(cudaMemcpyAsync(r->pts.p, sc->points, sizeof(float2) * sc->point_count, kind, s));
-        PF_TRY(cudaMemcpyAsync(r->flags.p, sc->point_flags, sc->point_count, kind, s));
+    point_base = 0;
+    for (uint32_t k = 0; k < scene_count; k++) {
+        const PFCUDASceneDesc& sc = scenes[k];
+        const cudaMemcpyKind kind = sc.memory == PF_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+        if (sc.point_count) {
+            PF_TRY(cudaMemcpyAsync(r->pts.p + point_base, sc.points, sizeof(float2) * sc.point_count, kind, s));
+            PF_TRY(cudaMemcpyAsync(r->flags.p + point_base, sc.point_flags, sc.point_count, kind, s));
+        }
+        point_base += sc.point_count;
     }
-    PF_TRY(cudaMemcpyAsync(r->starts.p, hstarts.data(), sizeof(uint32_t) * (sc->contour_count + 1),
-                           cudaMemcpyHostToDevice, s));
+    PF_TRY(cudaMemcpyAsync(r->starts.p, hstarts.data(), sizeof(uint32_t) * (nc_total + 1), cudaMemcpyHostToDevice, s));
     if (nord) {
         PF_TRY(cudaMemcpyAsync(r->ord_contour.p, ord_contour.data(), sizeof(uint32_t) * nord, cudaMemcpyHostToDevice, s));
         PF_TRY(cudaMemcpyAsync(r->ord_path.p, ord_path.data(), sizeof(uint32_t) * nord, cudaMemcpyHostToDevice, s));
     }
     if (P) {
-        PF_TRY(cudaMemcpyAsync(r->first_ord.p, first_ord.data(), sizeof(uint32_t) * (P + 1), cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->paint.p, paint.data(), sizeof(uint32_t) * P, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->local_index.p, local.data(), sizeof(uint32_t) * P, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->scene_of.p, scene.data(), sizeof(uint32_t) * P, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->clip_gpath.p, clip.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->rule.p, rule.data(), P, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->is_clip.p, isclip.data(), P, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->first_ord.p, first_ord.data(), sizeof(uint32_t) * (Pz + 1), cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->paint.p, paint.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->local_index.p, local.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->scene_of.p, scene_of.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->clip_gpath.p, clip.data(), sizeof(int32_t) * Pz, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->rule.p, rule.data(), Pz, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->is_clip.p, isclip.data(), Pz, cudaMemcpyHostToDevice, s));
     }
     // Segment packing on the GPU (SegmentsD3D11::add_path): count, scan, emit.
     PF_TRY(cudaMemsetAsync(r->counters.p, 0, sizeof(Counters), s));
-    launch_contour_segcount(r->ord_contour.p, nord, r->starts.p, r->flags.p, r->contour_segs.p,
-                            &r->counters.p->status, s);
+    launch_contour_segcount(r->ord_contour.p, nord, r->starts.p, r->flags.p, r->contour_segs.p, &r->counters.p->status, s);
     ScanTemp tmp{r->scan_partials.p, (uint32_t)r->scan_partials.cap};
     launch_scan(r->contour_segs.p, r->contour_seg_base.p, nullptr, nord, nord, 0, &r->counters.p->lines, tmp, s);
+    std::vector<uint32_t> seg_base(nord + 1, 0);
     PF_TRY(cudaMemcpyAsync(r->h_counters, r->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    PF_TRY(cudaMemcpyAsync(seg_base.data(), r->contour_seg_base.p, sizeof(uint32_t) * (nord + 1), cudaMemcpyDeviceToHost, s));
     PF_TRY(cudaStreamSynchronize(s));
     if (r->h_counters->status & kStatusMalformed) return PF_CUDA_ERR_INVALID;
-    uint32_t S = (uint32_t)r->h_counters->lines;
+    const uint32_t S = (uint32_t)r->h_counters->lines;
     if ((e = r->segs.ensure(S + 1)) || (e = r->seg_line_count.ensure(S + 1)) || (e = r->seg_line_base.ensure(S + 1)))
         return cuda_status(e);
     launch_contour_segemit(r->ord_contour.p, r->ord_path.p, nord, r->starts.p, r->flags.p, r->contour_seg_base.p,
                            r->segs.p, s);
     PF_TRY(cudaGetLastError());
+    for (uint32_t k = 0; k < scene_count; k++) {
+        SceneInfo& si = r->scenes[k];
+        const uint32_t pend = si.first_path + si.nclip + si.ndraw;
+        si.seg_begin = seg_base[first_ord[si.first_path]];
+        si.seg_end = seg_base[first_ord[pend]];
+    }
+    PF_TRY(upload_scene_records(r));
 
-    r->P = P;
-    r->nclip = sc->clip_path_count;
-    r->ndraw = sc->draw_path_count;
-    r->NP = sc->point_count;
-    r->NC = sc->contour_count;
+    r->P = (uint32_t)P;
+    r->NP = (uint32_t)np_total;
+    r->NC = (uint32_t)nc_total;
     r->nord = nord;
     r->S = S;
-    r->view_box = sc->view_box;
-    r->screen_rect = screen_rect_of(sc->view_box);
-    int32_t sw = std::max(0, r->screen_rect.z - r->screen_rect.x), sh = std::max(0, r->screen_rect.w - r->screen_rect.y);
-    r->screen_count = (uint32_t)sw * (uint32_t)sh;
+    r->screen_total = screen_total;
     // first-frame capacity guesses; grown on overflow and kept across frames
-    r->tile_cap = std::max<uint32_t>(r->tile_cap, std::max<uint32_t>(1u << 16, 4 * r->screen_count));
-    r->col_cap = std::max<uint32_t>(r->col_cap, std::max<uint32_t>(1u << 16, 16 * P));
+    r->tile_cap = std::max<uint32_t>(r->tile_cap, std::max<uint32_t>(1u << 16, 4 * screen_total));
+    r->col_cap = std::max<uint32_t>(r->col_cap, std::max<uint32_t>(1u << 16, 16 * r->P));
     r->fill_cap = std::max<uint32_t>(r->fill_cap, std::max<uint32_t>(1u << 18, 4 * S));
     r->line_cap = std::max<uint32_t>(r->line_cap, std::max<uint32_t>(1u << 16, 2 * S));
     r->vis_cap = std::max<uint32_t>(r->vis_cap, r->tile_cap);
@@ -528,19 +651,30 @@ int32_t PFCUDASceneUpload(PFCUDARendererRef r, const PFCUDASceneDesc* sc) {
     return PF_CUDA_OK;
 }
 
-int32_t PFCUDARenderScene(PFCUDARendererRef r, const PFCUDABuildOptions* options, int32_t width, int32_t height,
-                          uint8_t* out, int32_t out_memory) {
+int32_t PFCUDASceneUpload(PFCUDARendererRef r, const PFCUDASceneDesc* sc) {
+    if (!r || !sc) return PF_CUDA_ERR_INVALID;
+    return PFCUDASceneUploadBatch(r, sc, nullptr, 1);
+}
+
+static int32_t render_plain(PFCUDARendererRef r, const PFCUDABuildOptions* options, int32_t width, int32_t height,
+                            void* out, int32_t out_memory, int32_t format) {
     if (!r || !out) return PF_CUDA_ERR_INVALID;
+    if (!r->has_scene) return PF_CUDA_ERR_NO_SCENE;
     PF_TRY(cudaSetDevice(r->device));
+    bool changed = false;
+    int32_t rc = prepare_plain_targets(r, width, height, &changed);
+    if (rc) return rc;
+    if (changed) PF_TRY(upload_scene_records(r));
+    const size_t elem = format == PF_CUDA_FORMAT_RGBA8 ? 4 : (format == PF_CUDA_FORMAT_R8 ? 1 : 4);
+    const size_t bytes = (size_t)width * (size_t)height * elem;
     void* dst = out;
-    size_t bytes = (size_t)width * (size_t)height * 4;
     if (out_memory == PF_MEMORY_HOST) {
         PF_TRY(r->out_tmp.ensure(bytes));
         dst = r->out_tmp.p;
     } else if (out_memory != PF_MEMORY_DEVICE) {
         return PF_CUDA_ERR_INVALID;
     }
-    int32_t rc = run_frame(r, options, 0, dst, width, height);
+    rc = run_frame(r, options, format, dst, make_range(r, 0, (uint32_t)r->scenes.size()));
     if (rc == PF_CUDA_OK && out_memory == PF_MEMORY_HOST) {
         PF_TRY(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, r->stream));
         PF_TRY(cudaStreamSynchronize(r->stream));
@@ -548,16 +682,45 @@ int32_t PFCUDARenderScene(PFCUDARendererRef r, const PFCUDABuildOptions* options
     return rc;
 }
 
+int32_t PFCUDARenderScene(PFCUDARendererRef r, const PFCUDABuildOptions* options, int32_t width, int32_t height,
+                          uint8_t* out, int32_t out_memory) {
+    return render_plain(r, options, width, height, out, out_memory, PF_CUDA_FORMAT_RGBA8);
+}
+
+int32_t PFCUDARenderCoverage(PFCUDARendererRef r, const PFCUDABuildOptions* options, int32_t width, int32_t height,
+                             float* out, int32_t out_memory) {
+    return render_plain(r, options, width, height, out, out_memory, PF_CUDA_FORMAT_F32);
+}
+
 int32_t PFCUDARenderSceneAsync(PFCUDARendererRef r, const PFCUDABuildOptions* options, int32_t width,
                                int32_t height, uint8_t* out_rgba8_device) {
     if (!r || !out_rgba8_device) return PF_CUDA_ERR_INVALID;
     if (!r->has_scene) return PF_CUDA_ERR_NO_SCENE;
-    if (width != r->last_w || height != r->last_h) {
-        int32_t rc = prepare_size(r, width, height);
-        if (rc) return rc;
-    }
+    bool changed = false;
+    int32_t rc = prepare_plain_targets(r, width, height, &changed);
+    if (rc) return rc;
+    if (changed) PF_TRY(upload_scene_records(r));
+    r->last = make_range(r, 0, (uint32_t)r->scenes.size());
     PF_TRY(ensure_frame_buffers(r));
-    PF_TRY(enqueue_frame(r, options, 0, out_rgba8_device));
+    PF_TRY(enqueue_frame(r, options, PF_CUDA_FORMAT_RGBA8, out_rgba8_device, r->last));
+    return PF_CUDA_OK;
+}
+
+int32_t PFCUDARenderBatch(PFCUDARendererRef r, const PFCUDABuildOptions* options, uint32_t first, uint32_t count,
+                          int32_t format, void* out_device) {
+    if (!r || !out_device || format < 0 || format > 2) return PF_CUDA_ERR_INVALID;
+    if (!valid_range(r, first, count)) return r->has_scene ? PF_CUDA_ERR_INVALID : PF_CUDA_ERR_NO_SCENE;
+    PF_TRY(cudaSetDevice(r->device));
+    return run_frame(r, options, format, out_device, make_range(r, first, count));
+}
+
+int32_t PFCUDARenderBatchAsync(PFCUDARendererRef r, const PFCUDABuildOptions* options, uint32_t first,
+                               uint32_t count, int32_t format, void* out_device) {
+    if (!r || !out_device || format < 0 || format > 2) return PF_CUDA_ERR_INVALID;
+    if (!valid_range(r, first, count)) return r->has_scene ? PF_CUDA_ERR_INVALID : PF_CUDA_ERR_NO_SCENE;
+    r->last = make_range(r, first, count);
+    PF_TRY(ensure_frame_buffers(r));
+    PF_TRY(enqueue_frame(r, options, format, out_device, r->last));
     return PF_CUDA_OK;
 }
 
@@ -567,29 +730,107 @@ int32_t PFCUDARenderStatus(PFCUDARendererRef r, uint64_t* out_needed) {
     PF_TRY(cudaStreamSynchronize(r->stream));
     Counters h = *r->h_counters;
     record_stats(r, h, 0.0f);
-    if (out_needed) *out_needed = std::max({h.needed_fills, h.needed_tiles, h.needed_visible});
+    if (out_needed) *out_needed = std::max({h.needed_fills, h.needed_tiles, h.needed_visible, h.needed_lines});
     if (h.status & kCapacityBits) grow(r, h);
     return status_to_code(h.status);
 }
 
-int32_t PFCUDARenderCoverage(PFCUDARendererRef r, const PFCUDABuildOptions* options, int32_t width, int32_t height,
-                             float* out, int32_t out_memory) {
-    if (!r || !out) return PF_CUDA_ERR_INVALID;
-    PF_TRY(cudaSetDevice(r->device));
-    void* dst = out;
-    size_t bytes = (size_t)width * (size_t)height * sizeof(float);
-    if (out_memory == PF_MEMORY_HOST) {
-        PF_TRY(r->out_tmp.ensure(bytes));
-        dst = r->out_tmp.p;
-    } else if (out_memory != PF_MEMORY_DEVICE) {
+int32_t PFCUDAGraphCapture(PFCUDARendererRef r, const PFCUDABuildOptions* options, uint32_t first, uint32_t count,
+                           int32_t format, void* out_device) {
+    int32_t rc = PFCUDARenderBatch(r, options, first, count, format, out_device);
+    if (rc != PF_CUDA_OK) return rc;
+    release_graph(r);
+    const bool prof = r->profiling;
+    r->profiling = false;
+    PF_TRY(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue_frame(r, options, format, out_device, r->last);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(r->stream, &g);
+    r->profiling = prof;
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return PF_CUDA_ERR_LAUNCH;
+    }
+    r->graph = g;
+    PF_TRY(cudaGraphInstantiate(&r->graph_exec, g, 0));
+    return PF_CUDA_OK;
+}
+
+int32_t PFCUDAGraphLaunch(PFCUDARendererRef r) {
+    if (!r || !r->graph_exec) return PF_CUDA_ERR_INVALID;
+    PF_TRY(cudaGraphLaunch(r->graph_exec, r->stream));
+    return PF_CUDA_OK;
+}
+
+int32_t PFCUDAGraphRelease(PFCUDARendererRef r) {
+    if (!r) return PF_CUDA_ERR_INVALID;
+    release_graph(r);
+    return PF_CUDA_OK;
+}
+
+int32_t PFCUDASetTuning(PFCUDARendererRef r, const PFCUDATuning* t) {
+    if (!r || !t) return PF_CUDA_ERR_INVALID;
+    auto in = [](int v, std::initializer_list<int> ok) { return std::find(ok.begin(), ok.end(), v) != ok.end(); };
+    if (!in(t->flatten_threads, {64, 128, 256}) || !in(t->bin_threads, {128, 256, 512}) ||
+        t->bin_blocks_per_sm < 4 || t->bin_blocks_per_sm > 64 || !in(t->composite_warps, {2, 4, 8}))
         return PF_CUDA_ERR_INVALID;
+    r->tune = TuneParams{t->flatten_threads, t->bin_threads, t->bin_blocks_per_sm, t->composite_warps};
+    release_graph(r);
+    return PF_CUDA_OK;
+}
+
+int32_t PFCUDAGetTuning(PFCUDARendererRef r, PFCUDATuning* t) {
+    if (!r || !t) return PF_CUDA_ERR_INVALID;
+    *t = PFCUDATuning{r->tune.flatten_threads, r->tune.bin_threads, r->tune.bin_blocks_per_sm, r->tune.comp_warps};
+    return PF_CUDA_OK;
+}
+
+int32_t PFCUDAAutotune(PFCUDARendererRef r, const PFCUDABuildOptions* options, uint32_t first, uint32_t count,
+                       int32_t format, void* out_device, int32_t repeats, PFCUDATuning* out_best) {
+    if (!r || repeats <= 0) return PF_CUDA_ERR_INVALID;
+    int32_t rc = PFCUDARenderBatch(r, options, first, count, format, out_device);  // sizes the buffers
+    if (rc != PF_CUDA_OK) return rc;
+    const Range g = r->last;
+    auto time_it = [&](const TuneParams& tp, float* ms_out) -> int32_t {
+        r->tune = tp;
+        std::vector<float> v;
+        for (int i = 0; i < repeats + 1; i++) {
+            PF_TRY(cudaEventRecord(r->ev0, r->stream));
+            PF_TRY(enqueue_frame(r, options, format, out_device, g));
+            PF_TRY(cudaEventRecord(r->ev1, r->stream));
+            PF_TRY(cudaEventSynchronize(r->ev1));
+            float ms = 0;
+            PF_TRY(cudaEventElapsedTime(&ms, r->ev0, r->ev1));
+            if (i > 0) v.push_back(ms);  // the first run warms the shape
+        }
+        std::sort(v.begin(), v.end());
+        *ms_out = v[v.size() / 2];
+        return PF_CUDA_OK;
+    };
+    TuneParams best = r->tune;
+    float best_ms = 0;
+    if ((rc = time_it(best, &best_ms))) return rc;
+    const int flat[] = {64, 128, 256}, bin[] = {128, 256, 512}, bps[] = {4, 8, 16, 32}, cw[] = {2, 4, 8};
+    for (int dim = 0; dim < 4; dim++) {
+        const int* cand = dim == 0 ? flat : dim == 1 ? bin : dim == 2 ? bps : cw;
+        const int nc = dim == 2 ? 4 : 3;
+        for (int i = 0; i < nc; i++) {
+            TuneParams tp = best;
+            if (dim == 0) tp.flatten_threads = cand[i];
+            if (dim == 1) tp.bin_threads = cand[i];
+            if (dim == 2) tp.bin_blocks_per_sm = cand[i];
+            if (dim == 3) tp.comp_warps = cand[i];
+            float ms = 0;
+            if ((rc = time_it(tp, &ms))) return rc;
+            if (ms < best_ms) { best_ms = ms; best = tp; }
+        }
     }
-    int32_t rc = run_frame(r, options, 2, dst, width, height);
-    if (rc == PF_CUDA_OK && out_memory == PF_MEMORY_HOST) {
-        PF_TRY(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, r->stream));
-        PF_TRY(cudaStreamSynchronize(r->stream));
-    }
-    return rc;
+    r->tune = best;
+    release_graph(r);
+    // the final frame with the chosen shape leaves valid counters behind
+    if ((rc = PFCUDARenderBatch(r, options, first, count, format, out_device))) return rc;
+    if (out_best) PFCUDAGetTuning(r, out_best);
+    return PF_CUDA_OK;
 }
 
 int32_t PFCUDAReadMasks(PFCUDARendererRef r, float* out_alpha, uint64_t alpha_cap, float* out_tile,
@@ -598,7 +839,7 @@ int32_t PFCUDAReadMasks(PFCUDARendererRef r, float* out_alpha, uint64_t alpha_ca
     PF_TRY(cudaSetDevice(r->device));
     uint64_t A = r->stats.alpha_tile_count, T = r->stats.tile_count;
     if ((out_alpha && alpha_cap < A) || (out_tile && tile_cap < T)) return PF_CUDA_ERR_CAPACITY;
-    FrameDev f = frame_dev(r, false);
+    FrameDev f = frame_dev(r, false, r->last);
     DevBuf<float> a, t;
     if (out_alpha) PF_TRY(a.ensure(A * 256 + 1));
     if (out_tile) PF_TRY(t.ensure(T * 256 + 1));
@@ -619,11 +860,12 @@ int32_t PFCUDAReadRecords(PFCUDARendererRef r, PFCUDAFill* fills, uint32_t* fill
     if (!r || !r->has_scene) return PF_CUDA_ERR_NO_SCENE;
     PF_TRY(cudaSetDevice(r->device));
     cudaStream_t s = r->stream;
-    uint64_t F = r->stats.fill_count, T = r->stats.tile_count;
+    const Range& g = r->last;
+    const uint64_t F = r->stats.fill_count, T = r->stats.tile_count, NPth = g.p1 - g.p0, NST = g.st1 - g.st0;
     if ((fills || fill_tile) && fill_capacity < F) return PF_CUDA_ERR_CAPACITY;
     if ((tiles || clips) && tile_capacity < T) return PF_CUDA_ERR_CAPACITY;
-    if ((path_tile_offsets || path_tile_rects) && path_capacity < (uint64_t)r->P + 1) return PF_CUDA_ERR_CAPACITY;
-    if (z_buffer && z_capacity < r->screen_count) return PF_CUDA_ERR_CAPACITY;
+    if ((path_tile_offsets || path_tile_rects) && path_capacity < NPth + 1) return PF_CUDA_ERR_CAPACITY;
+    if (z_buffer && z_capacity < NST) return PF_CUDA_ERR_CAPACITY;
     if (fills && F) {
         std::vector<uint2> seg(F);
         std::vector<uint32_t> e(F);
@@ -638,36 +880,35 @@ int32_t PFCUDAReadRecords(PFCUDARendererRef r, PFCUDAFill* fills, uint32_t* fill
         std::vector<uint32_t> base(T + 1);
         PF_TRY(cudaMemcpyAsync(base.data(), r->tile_fill_base.p, (T + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         PF_TRY(cudaStreamSynchronize(s));
-        uint64_t g = 0;
+        uint64_t t = 0;
         for (uint64_t i = 0; i < F; i++) {
-            while (g + 1 <= T && base[g + 1] <= i) g++;
-            fill_tile[i] = (uint32_t)g;
+            while (t + 1 <= T && base[t + 1] <= i) t++;
+            fill_tile[i] = (uint32_t)t;
         }
     }
+    std::vector<uint32_t> off(NPth + 1);
+    PF_TRY(cudaMemcpyAsync(off.data(), r->tile_offset.p + g.p0, (NPth + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    PF_TRY(cudaStreamSynchronize(s));
     if (tiles && T) {
         PF_TRY(cudaMemcpyAsync(tiles, r->tiles.p, T * sizeof(PFCUDATile), cudaMemcpyDeviceToHost, s));
         PF_TRY(cudaStreamSynchronize(s));
         // device records carry the global path index; report the index within
         // the clip paths or the draw paths, as TileObjectPrimitive::path_id
-        for (uint64_t i = 0; i < T; i++)
-            if (tiles[i].path_id >= r->nclip) tiles[i].path_id -= r->nclip;
+        for (uint64_t i = 0; i < T; i++) tiles[i].path_id = r->path_local[tiles[i].path_id];
     }
     if (clips && T) {
         PF_TRY(cudaMemcpyAsync(clips, r->clips.p, T * sizeof(PFCUDAClip), cudaMemcpyDeviceToHost, s));
         PF_TRY(cudaStreamSynchronize(s));
         // tiles of clip paths carry no clip record
-        std::vector<uint32_t> off(r->P + 1);
-        PF_TRY(cudaMemcpy(off.data(), r->tile_offset.p, (r->P + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-        for (uint32_t gp = 0; gp < r->nclip; gp++)
-            for (uint32_t g = off[gp]; g < off[gp + 1]; g++) clips[g] = PFCUDAClip{0xffffffffu, 0, 0xffffffffu, 0};
+        for (uint64_t q = 0; q < NPth; q++)
+            if (r->path_is_clip[g.p0 + q])
+                for (uint32_t t = off[q]; t < off[q + 1]; t++) clips[t] = PFCUDAClip{0xffffffffu, 0, 0xffffffffu, 0};
     }
-    if (path_tile_offsets)
-        PF_TRY(cudaMemcpyAsync(path_tile_offsets, r->tile_offset.p, (r->P + 1) * sizeof(uint32_t),
-                               cudaMemcpyDeviceToHost, s));
-    if (path_tile_rects && r->P)
-        PF_TRY(cudaMemcpyAsync(path_tile_rects, r->tile_rect.p, r->P * sizeof(PFRectI), cudaMemcpyDeviceToHost, s));
-    if (z_buffer && r->screen_count)
-        PF_TRY(cudaMemcpyAsync(z_buffer, r->zbuf.p, r->screen_count * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    if (path_tile_offsets) std::memcpy(path_tile_offsets, off.data(), (NPth + 1) * sizeof(uint32_t));
+    if (path_tile_rects && NPth)
+        PF_TRY(cudaMemcpyAsync(path_tile_rects, r->tile_rect.p + g.p0, NPth * sizeof(PFRectI), cudaMemcpyDeviceToHost, s));
+    if (z_buffer && NST)
+        PF_TRY(cudaMemcpyAsync(z_buffer, r->zbuf.p, NST * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     PF_TRY(cudaStreamSynchronize(s));
     return PF_CUDA_OK;
 }

@@ -238,9 +238,10 @@ void launch_contour_segemit(const uint32_t* ord_contour, const uint32_t* ord_pat
 // bound: one warp per path
 // ---------------------------------------------------------------------------
 __global__ void k_bound(FrameDev f, const uint32_t* __restrict__ ord_contour, const uint32_t* __restrict__ starts) {
-    uint32_t gp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (gp >= f.path_count) return;
+    if (wi >= f.path_count) return;
+    const uint32_t gp = f.path_begin + wi;
     float mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
     bool any = false;
     uint32_t k0 = f.path.first_ord_contour[gp], k1 = f.path.first_ord_contour[gp + 1];
@@ -313,8 +314,10 @@ __global__ void k_zero_tiles(FrameDev f) {
 }
 
 void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
-    launch_scan(f.path_tiles, f.path.tile_offset, nullptr, f.path_count, f.path_count, 0, &f.counters->tiles, tmp, s);
-    launch_scan(f.path_cols, f.path.col_offset, nullptr, f.path_count, f.path_count, 0, &f.counters->columns, tmp, s);
+    launch_scan(f.path_tiles + f.path_begin, f.path.tile_offset + f.path_begin, nullptr, f.path_count, f.path_count, 0,
+                &f.counters->tiles, tmp, s);
+    launch_scan(f.path_cols + f.path_begin, f.path.col_offset + f.path_begin, nullptr, f.path_count, f.path_count, 0,
+                &f.counters->columns, tmp, s);
     { count_launch(); k_check_tiles<<<1, 1, 0, s>>>(f); }
     { count_launch(); k_zero_tiles<<<152 * 8, 256, 0, s>>>(f); }
 }
@@ -324,11 +327,11 @@ void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
 // renderer/src/tiler.rs:166-184).  Lines are written in emission order: input
 // segments in path order, each segment's lines depth first.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_flatten_count(FrameDev f) {
+__global__ void __launch_bounds__(256) k_flatten_count(FrameDev f) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= f.seg_count) return;
     uint32_t n = 0;
-    flatten_segment(f.pts, f.segs[s], [&](const Line&) { n++; }, &f.counters->status);
+    flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&) { n++; }, &f.counters->status);
     f.seg_line_count[s] = n;
 }
 
@@ -339,10 +342,10 @@ __global__ void k_check_lines(FrameDev f) {
     }
 }
 
-__global__ void __launch_bounds__(128) k_flatten_emit(FrameDev f) {
+__global__ void __launch_bounds__(256) k_flatten_emit(FrameDev f) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= f.seg_count || f.counters->lines > f.line_cap) return;
-    const SegRec sr = f.segs[s];
+    const SegRec sr = f.segs[f.seg_begin + s];
     uint32_t l = f.seg_line_base[s];
     flatten_segment(f.pts, sr, [&](const Line& ln) {
         f.lines[l] = make_float4(ln.fx, ln.fy, ln.tx, ln.ty);
@@ -353,10 +356,11 @@ __global__ void __launch_bounds__(128) k_flatten_emit(FrameDev f) {
 
 void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     if (f.seg_count == 0) return;
-    { count_launch(); k_flatten_count<<<(f.seg_count + 127) / 128, 128, 0, s>>>(f); }
+    const int ft = f.tune.flatten_threads;
+    { count_launch(); k_flatten_count<<<(f.seg_count + ft - 1) / ft, ft, 0, s>>>(f); }
     launch_scan(f.seg_line_count, f.seg_line_base, nullptr, f.seg_count, f.seg_count, 0, &f.counters->lines, tmp, s);
     { count_launch(); k_check_lines<<<1, 1, 0, s>>>(f); }
-    { count_launch(); k_flatten_emit<<<(f.seg_count + 127) / 128, 128, 0, s>>>(f); }
+    { count_launch(); k_flatten_emit<<<(f.seg_count + ft - 1) / ft, ft, 0, s>>>(f); }
 }
 
 // ---------------------------------------------------------------------------
@@ -400,7 +404,7 @@ struct CountSink {
     }
 };
 
-__global__ void __launch_bounds__(256) k_bin_count(FrameDev f) {
+__global__ void __launch_bounds__(512) k_bin_count(FrameDev f) {
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     const uint32_t L = line_total(f);
     for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
@@ -427,7 +431,7 @@ struct EmitSink {
     __device__ __forceinline__ void backdrop(int32_t, int32_t, int32_t) {}
 };
 
-__global__ void __launch_bounds__(256) k_bin_emit(FrameDev f) {
+__global__ void __launch_bounds__(512) k_bin_emit(FrameDev f) {
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     if (f.counters->fills > f.fill_cap) return;
     const uint32_t L = line_total(f);
@@ -441,7 +445,7 @@ __global__ void __launch_bounds__(256) k_bin_emit(FrameDev f) {
 }
 
 void launch_bin_count(const FrameDev& f, cudaStream_t s) {
-    { count_launch(); k_bin_count<<<152 * 16, 256, 0, s>>>(f); }
+    { count_launch(); k_bin_count<<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f); }
 }
 
 __global__ void k_check_fills(FrameDev f) {
@@ -454,7 +458,7 @@ __global__ void k_check_fills(FrameDev f) {
 
 void launch_bin_emit(const FrameDev& f, cudaStream_t s) {
     { count_launch(); k_check_fills<<<1, 1, 0, s>>>(f); }
-    { count_launch(); k_bin_emit<<<152 * 16, 256, 0, s>>>(f); }
+    { count_launch(); k_bin_emit<<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f); }
 }
 
 }  // namespace pf

@@ -206,6 +206,67 @@ class Renderer:
         _abi.check(self._lib.PFCUDAGetStageTimes(self._h, a, _abi.PF_CUDA_STAGE_COUNT), "PFCUDAGetStageTimes")
         return {n: float(a[i]) for i, n in enumerate(_abi.STAGE_NAMES)}
 
+    # --- batches -------------------------------------------------------------
+    def upload_batch(self, batch, force: bool = False) -> None:
+        """PFCUDASceneUploadBatch: many independent scenes at once."""
+        key = ("batch", batch.key)
+        if not force and self._uploaded == key:
+            return
+        _abi.check(self._lib.PFCUDASceneUploadBatch(self._h, *batch.upload_args()), "PFCUDASceneUploadBatch")
+        self._uploaded = key
+
+    def render_batch(self, batch, out, fmt: int = _abi.PF_CUDA_FORMAT_RGBA8, first: int = 0,
+                     count: int | None = None, options: BuildOptions | None = None, sync: bool = True):
+        """Render scenes [first, first+count) of `batch` into device tensor `out`."""
+        self.upload_batch(batch)
+        count = len(batch) - first if count is None else count
+        p, mem = _ptr(out)
+        if mem != _abi.PF_MEMORY_DEVICE:
+            raise ValueError("batched frames render into device memory")
+        bo = (options or BuildOptions()).to_c()
+        fn = self._lib.PFCUDARenderBatch if sync else self._lib.PFCUDARenderBatchAsync
+        _abi.check(fn(self._h, C.byref(bo), first, count, fmt, C.c_void_p(p)), "PFCUDARenderBatch")
+        return out
+
+    def graph_capture(self, batch, out, fmt: int = _abi.PF_CUDA_FORMAT_RGBA8, first: int = 0,
+                      count: int | None = None, options: BuildOptions | None = None) -> None:
+        """Capture one frame of the batch range into a CUDA graph."""
+        self.upload_batch(batch)
+        count = len(batch) - first if count is None else count
+        p, _ = _ptr(out)
+        bo = (options or BuildOptions()).to_c()
+        _abi.check(self._lib.PFCUDAGraphCapture(self._h, C.byref(bo), first, count, fmt, C.c_void_p(p)),
+                   "PFCUDAGraphCapture")
+
+    def graph_launch(self) -> None:
+        _abi.check(self._lib.PFCUDAGraphLaunch(self._h), "PFCUDAGraphLaunch")
+
+    def graph_release(self) -> None:
+        _abi.check(self._lib.PFCUDAGraphRelease(self._h), "PFCUDAGraphRelease")
+
+    def get_tuning(self) -> dict:
+        t = _abi.PFCUDATuning()
+        _abi.check(self._lib.PFCUDAGetTuning(self._h, C.byref(t)), "PFCUDAGetTuning")
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
+    def set_tuning(self, **kw) -> None:
+        cur = self.get_tuning()
+        cur.update(kw)
+        t = _abi.PFCUDATuning(**cur)
+        _abi.check(self._lib.PFCUDASetTuning(self._h, C.byref(t)), "PFCUDASetTuning")
+
+    def autotune(self, batch, out, fmt: int = _abi.PF_CUDA_FORMAT_RGBA8, first: int = 0,
+                 count: int | None = None, repeats: int = 3, options: BuildOptions | None = None) -> dict:
+        """Time candidate launch shapes on this batch range; keep the fastest."""
+        self.upload_batch(batch)
+        count = len(batch) - first if count is None else count
+        p, _ = _ptr(out)
+        bo = (options or BuildOptions()).to_c()
+        t = _abi.PFCUDATuning()
+        _abi.check(self._lib.PFCUDAAutotune(self._h, C.byref(bo), first, count, fmt, C.c_void_p(p), repeats,
+                                            C.byref(t)), "PFCUDAAutotune")
+        return {k: getattr(t, k) for k, _ in t._fields_}
+
     def stats(self) -> RenderStats:
         s = _abi.PFCUDARenderStats()
         _abi.check(self._lib.PFCUDAGetStats(self._h, C.byref(s)), "PFCUDAGetStats")

@@ -1,0 +1,84 @@
+"""Batched frames: many scenes in one set of launches give exactly the pixels
+of one frame per scene; graph replay and autotuned launch shapes give exactly
+the pixels of a plain frame."""
+import numpy as np
+import pytest
+
+import pathfinder_gb300 as pf
+
+pytestmark = pytest.mark.gpu
+
+
+def test_glyph_batch_equals_per_glyph_frames_and_oracle(renderer):
+    torch = pytest.importorskip("torch")
+    import oracle
+    atlas = pf.generate_scene(pf.PF_SCENE_GLYPH_ATLAS, seed=3, scale=0.02)
+    batch = pf.SceneBatch.glyphs_of(atlas)
+    W, H = atlas.width, atlas.height
+    batched = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+    renderer.render_batch(batch, batched, pf.PF_CUDA_FORMAT_R8)
+    assert renderer.stats().path_count == len(batch)
+    per_glyph = torch.zeros((H, W), dtype=torch.uint8, device="cuda")
+    for g in range(len(batch)):
+        renderer.render_batch(batch, per_glyph, pf.PF_CUDA_FORMAT_R8, first=g, count=1, sync=False)
+    code, _ = renderer.render_status()
+    assert code == 0
+    assert torch.equal(batched, per_glyph), "batched atlas differs from per-glyph frames"
+    got = batched.cpu().numpy()
+    ymax = int(atlas.cells["y1"].max())
+    for g in range(0, len(batch), max(1, len(batch) // 24)):
+        c = atlas.cells[g]
+        img, f64 = oracle.OracleFrame(batch.scenes[g]).render(W, ymax, channels=1)
+        cell = (slice(int(c["y0"]), int(c["y1"])), slice(int(c["x0"]), int(c["x1"])))
+        d = np.abs(got[cell].astype(int) - img[cell].astype(int))
+        assert d.max() <= 1, f"glyph {g}: max diff {d.max()}"
+
+
+def test_packed_multi_scene_batch_equals_single_frames(renderer):
+    torch = pytest.importorskip("torch")
+    scenes = [pf.generate_scene(pf.PF_SCENE_STARS_512, seed=s) for s in (1, 2)]
+    scenes.append(pf.generate_scene(pf.PF_SCENE_EDGE_CASES))
+    scenes.append(pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=9, scale=0.01))
+    batch = pf.SceneBatch.packed(scenes)
+    out = torch.zeros((batch.total_pixels,), dtype=torch.int32, device="cuda")
+    renderer.render_batch(batch, out, pf.PF_CUDA_FORMAT_RGBA8)
+    packed = out.cpu().numpy().view(np.uint8)
+    for s, off in zip(scenes, batch.offsets):
+        single = renderer.render(s)
+        part = packed[4 * off:4 * (off + s.width * s.height)].reshape(s.height, s.width, 4)
+        assert np.array_equal(part, single)
+
+
+def test_graph_replay_equals_plain_frame(renderer):
+    torch = pytest.importorskip("torch")
+    s = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=5, scale=0.02)
+    batch = pf.SceneBatch.packed([s])
+    ref = torch.zeros((s.height, s.width), dtype=torch.int32, device="cuda")
+    renderer.render_batch(batch, ref, pf.PF_CUDA_FORMAT_RGBA8)
+    out = torch.zeros_like(ref)
+    renderer.graph_capture(batch, out, pf.PF_CUDA_FORMAT_RGBA8)
+    out.zero_()
+    torch.cuda.synchronize()
+    for _ in range(3):
+        renderer.graph_launch()
+    code, _ = renderer.render_status()
+    assert code == 0
+    assert torch.equal(out, ref)
+    renderer.graph_release()
+
+
+def test_autotune_changes_speed_not_pixels(renderer):
+    torch = pytest.importorskip("torch")
+    s = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=6, scale=0.02)
+    batch = pf.SceneBatch.packed([s])
+    ref = torch.zeros((s.height, s.width), dtype=torch.int32, device="cuda")
+    renderer.render_batch(batch, ref, pf.PF_CUDA_FORMAT_RGBA8)
+    out = torch.zeros_like(ref)
+    best = renderer.autotune(batch, out, pf.PF_CUDA_FORMAT_RGBA8, repeats=2)
+    assert best["composite_warps"] in (2, 4, 8) and best["bin_threads"] in (128, 256, 512)
+    for warps in (2, 8):
+        renderer.set_tuning(composite_warps=warps, flatten_threads=64, bin_threads=512, bin_blocks_per_sm=4)
+        out.zero_()
+        renderer.render_batch(batch, out, pf.PF_CUDA_FORMAT_RGBA8)
+        assert torch.equal(out, ref)
+    renderer.set_tuning(**best)
