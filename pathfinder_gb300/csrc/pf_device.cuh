@@ -264,7 +264,7 @@ __device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Em
     float2 p0 = pts[sr.x];
     float2 pe = pts[sr.y];
     if (sr.z == (int)kSegLine) {
-        emit(Line{p0.x, p0.y, pe.x, pe.y});
+        emit(Line{p0.x, p0.y, pe.x, pe.y}, 0u, 0);
         return;
     }
     Cubic c;
@@ -276,23 +276,35 @@ __device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Em
         c.base = Line{p0.x, p0.y, pe.x, pe.y};
         c.ctrl = Line{c0.x, c0.y, c1.x, c1.y};
     }
-    Cubic stack[kMaxFlattenDepth + 2];
-    uint8_t depth[kMaxFlattenDepth + 2];
-    int sp = 0;
-    stack[0] = c; depth[0] = 0; sp = 1;
-    while (sp > 0) {
-        --sp;
-        Cubic cur = stack[sp];
-        int d = depth[sp];
-        bool flat = cubic_is_flat(cur);
-        if (flat || d >= kMaxFlattenDepth) {
-            if (!flat) atomicOr(status, kStatusDepthLimit);
-            emit(cur.base);
-        } else {
+    // Depth-first without a stack: the current node is named by its split
+    // path `addr` (d bits, first split most significant; the leaf covers
+    // [addr, addr + 1) / 2^d of the curve parameter).  Descending left splits
+    // the current node; moving to a right sibling recomputes it from the root
+    // along its path, i.e. with exactly the splits the recursion performs, so
+    // every node, flatness decision and line is bit-identical to it.
+    const Cubic root = c;
+    uint32_t addr = 0;
+    int d = 0;
+    for (;;) {
+        const bool flat = cubic_is_flat(c);
+        if (!flat && d < kMaxFlattenDepth) {
             Cubic a, b;
-            cubic_split_half(cur, a, b);
-            stack[sp] = b; depth[sp] = (uint8_t)(d + 1); sp++;
-            stack[sp] = a; depth[sp] = (uint8_t)(d + 1); sp++;
+            cubic_split_half(c, a, b);
+            c = a;
+            addr <<= 1;
+            d++;
+            continue;
+        }
+        if (!flat) atomicOr(status, kStatusDepthLimit);
+        emit(c.base, addr, d);
+        while (d > 0 && (addr & 1u)) { addr >>= 1; d--; }  // climb past right children
+        if (d == 0) break;
+        addr |= 1u;  // the right sibling
+        c = root;
+        for (int i = d - 1; i >= 0; i--) {
+            Cubic a, b;
+            cubic_split_half(c, a, b);
+            c = ((addr >> i) & 1u) ? b : a;
         }
     }
 }

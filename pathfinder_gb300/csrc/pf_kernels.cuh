@@ -82,6 +82,17 @@ void launch_bin_emit(const FrameDev& f, cudaStream_t s);
 // and, when total_out != NULL, the total as u64.
 void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_t n_host, uint32_t n_cap,
                  int mode, uint64_t* total_out, ScanTemp& tmp, cudaStream_t s);
+// Several exclusive scans over arrays of one length (device count at d_n,
+// clamped to n_cap); scratch needs count * (n_cap / 2048 + 1) partials.
+constexpr int kMaxScanLanes = 3;
+struct ScanLanes {
+    const uint32_t* in[kMaxScanLanes];
+    uint32_t* out[kMaxScanLanes];
+    uint64_t* total[kMaxScanLanes];
+    int mode[kMaxScanLanes];
+    int count;
+};
+void launch_scan_multi(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp, cudaStream_t s);
 
 void launch_propagate(const FrameDev& f, bool clip_pass, cudaStream_t s);
 void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s);

@@ -229,7 +229,7 @@ cudaError_t ensure_frame_buffers(PFCUDARenderer* r) {
         return e;
     size_t nmax = std::max<size_t>({(size_t)r->tile_cap, (size_t)r->S, (size_t)r->screen_total, (size_t)r->nord,
                                     (size_t)r->line_cap, (size_t)r->P}) + 1;
-    return r->scan_partials.ensure(nmax / 2048 + 2);
+    return r->scan_partials.ensure(kMaxScanLanes * (nmax / 2048 + 2));
 }
 
 bool is_identity(const PFCUDABuildOptions* o) {
@@ -267,10 +267,17 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     mark(2);
     launch_bin_count(f, s);
     mark(3);
-    launch_scan((const uint32_t*)r->tile_delta.p, r->tile_delta_scan.p, &c->tiles, 0, r->tile_cap, 0, nullptr, tmp, s);
     launch_scan(r->line_fill_count.p, r->line_fill_base.p, &c->lines, 0, r->line_cap, 0, &c->fills, tmp, s);
-    launch_scan(r->tile_fill_count.p, r->tile_fill_base.p, &c->tiles, 0, r->tile_cap, 0, nullptr, tmp, s);
-    launch_scan(r->tile_fill_count.p, r->tile_alpha.p, &c->tiles, 0, r->tile_cap, 1, &c->alpha_tiles, tmp, s);
+    {
+        // per tile: fill offsets, alpha-tile ids, column backdrop prefixes
+        ScanLanes lanes{};
+        lanes.count = 3;
+        lanes.in[0] = r->tile_fill_count.p; lanes.out[0] = r->tile_fill_base.p; lanes.mode[0] = 0;
+        lanes.in[1] = r->tile_fill_count.p; lanes.out[1] = r->tile_alpha.p; lanes.mode[1] = 1;
+        lanes.total[1] = &c->alpha_tiles;
+        lanes.in[2] = (const uint32_t*)r->tile_delta.p; lanes.out[2] = r->tile_delta_scan.p; lanes.mode[2] = 0;
+        launch_scan_multi(lanes, &c->tiles, r->tile_cap, tmp, s);
+    }
     mark(4);
     launch_bin_emit(f, s);
     mark(5);

@@ -138,6 +138,76 @@ void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_
 }
 
 // ---------------------------------------------------------------------------
+// fused scans: up to kMaxScanLanes arrays of the same length in one
+// reduce / partials / down-sweep set (the per-tile fill offsets, alpha ids and
+// column backdrop prefixes share their length)
+// ---------------------------------------------------------------------------
+__global__ void k_scanm_reduce(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, uint32_t* __restrict__ partials) {
+    const uint32_t n = scan_count(d_n, n_cap);
+    const uint32_t base = blockIdx.x * kScanChunk;
+    if (base >= n) return;
+    const uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
+    for (int l = 0; l < L.count; l++) {
+        uint32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) s += scan_in(L.in[l], base + k * kScanThreads + threadIdx.x, n, L.mode[l]);
+        uint32_t total;
+        block_exclusive_scan<kScanThreads>(s, &total);
+        if (threadIdx.x == 0) partials[l * nb + blockIdx.x] = total;
+    }
+}
+
+__global__ void k_scanm_partials(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, uint32_t* partials) {
+    const uint32_t n = scan_count(d_n, n_cap);
+    const uint32_t nb = (n + kScanChunk - 1) / kScanChunk, nbc = (n_cap + kScanChunk - 1) / kScanChunk;
+    for (int l = 0; l < L.count; l++) {
+        uint32_t carry = 0;
+        uint32_t* p = partials + l * nbc;
+        for (uint32_t b0 = 0; b0 < nb; b0 += 1024) {
+            uint32_t i = b0 + threadIdx.x;
+            uint32_t v = i < nb ? p[i] : 0;
+            uint32_t total;
+            uint32_t ex = block_exclusive_scan<1024>(v, &total);
+            if (i < nb) p[i] = ex + carry;
+            carry += total;
+        }
+        if (threadIdx.x == 0) {
+            L.out[l][n] = carry;
+            if (L.total[l]) *L.total[l] = carry;
+        }
+    }
+}
+
+__global__ void k_scanm_down(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, const uint32_t* __restrict__ partials) {
+    const uint32_t n = scan_count(d_n, n_cap);
+    const uint32_t base = blockIdx.x * kScanChunk;
+    if (base >= n) return;
+    const uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
+    const uint32_t first = base + threadIdx.x * kScanItems;
+    for (int l = 0; l < L.count; l++) {
+        uint32_t v[kScanItems];
+        uint32_t s = 0;
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) { v[k] = scan_in(L.in[l], first + k, n, L.mode[l]); s += v[k]; }
+        uint32_t total;
+        uint32_t ex = block_exclusive_scan<kScanThreads>(s, &total) + partials[l * nb + blockIdx.x];
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            if (first + k < n) L.out[l][first + k] = ex;
+            ex += v[k];
+        }
+    }
+}
+
+void launch_scan_multi(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp, cudaStream_t s) {
+    uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
+    if (nb == 0) nb = 1;
+    { count_launch(); k_scanm_reduce<<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+    { count_launch(); k_scanm_partials<<<1, 1024, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+    { count_launch(); k_scanm_down<<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+}
+
+// ---------------------------------------------------------------------------
 // transform (Contour::transform, content/src/outline.rs:884-893;
 // Transform2F * Vector2F, geometry/src/transform2d.rs:123-129, :312-318)
 // ---------------------------------------------------------------------------
@@ -314,10 +384,13 @@ __global__ void k_zero_tiles(FrameDev f) {
 }
 
 void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
-    launch_scan(f.path_tiles + f.path_begin, f.path.tile_offset + f.path_begin, nullptr, f.path_count, f.path_count, 0,
-                &f.counters->tiles, tmp, s);
-    launch_scan(f.path_cols + f.path_begin, f.path.col_offset + f.path_begin, nullptr, f.path_count, f.path_count, 0,
-                &f.counters->columns, tmp, s);
+    ScanLanes lanes{};
+    lanes.count = 2;
+    lanes.in[0] = f.path_tiles + f.path_begin; lanes.out[0] = f.path.tile_offset + f.path_begin;
+    lanes.total[0] = &f.counters->tiles;
+    lanes.in[1] = f.path_cols + f.path_begin; lanes.out[1] = f.path.col_offset + f.path_begin;
+    lanes.total[1] = &f.counters->columns;
+    launch_scan_multi(lanes, nullptr, f.path_count, tmp, s);
     { count_launch(); k_check_tiles<<<1, 1, 0, s>>>(f); }
     { count_launch(); k_zero_tiles<<<152 * 8, 256, 0, s>>>(f); }
 }
@@ -331,7 +404,7 @@ __global__ void __launch_bounds__(256) k_flatten_count(FrameDev f) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= f.seg_count) return;
     uint32_t n = 0;
-    flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&) { n++; }, &f.counters->status);
+    flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&, uint32_t, int) { n++; }, &f.counters->status);
     f.seg_line_count[s] = n;
 }
 
@@ -347,7 +420,7 @@ __global__ void __launch_bounds__(256) k_flatten_emit(FrameDev f) {
     if (s >= f.seg_count || f.counters->lines > f.line_cap) return;
     const SegRec sr = f.segs[f.seg_begin + s];
     uint32_t l = f.seg_line_base[s];
-    flatten_segment(f.pts, sr, [&](const Line& ln) {
+    flatten_segment(f.pts, sr, [&](const Line& ln, uint32_t, int) {
         f.lines[l] = make_float4(ln.fx, ln.fy, ln.tx, ln.ty);
         f.line_path[l] = (uint32_t)sr.w;
         l++;
@@ -392,7 +465,7 @@ struct CountSink {
     uint32_t n;
     __device__ __forceinline__ void fill(uint2, uint32_t g) {
         n++;
-        atomicAdd(&tile_fill_count[g], 1u);
+        atomicAdd(&tile_fill_count[g], 1u);  // lanes rarely share a tile: aggregation costs more
     }
     __device__ __forceinline__ void backdrop(int32_t tx, int32_t ty, int32_t d) {
         // ObjectBuilder::adjust_alpha_tile_backdrop (renderer/src/builder.rs:595-616)
@@ -424,7 +497,8 @@ struct EmitSink {
     uint32_t fill_cap;
     uint32_t e;
     __device__ __forceinline__ void fill(uint2 rec, uint32_t g) {
-        uint32_t slot = tile_fill_base[g] + atomicSub(&cursor[g], 1u) - 1u;
+        // the order of fills within a tile does not change any output
+        const uint32_t slot = tile_fill_base[g] + atomicSub(&cursor[g], 1u) - 1u;
         if (slot < fill_cap) { fills[slot] = rec; fill_e[slot] = e; }
         e++;
     }
