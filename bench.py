@@ -244,10 +244,167 @@ def run_atlas(args) -> None:
     r.close()
 
 
+def _diff_common(args):
+    import torch
+    from pathfinder_gb300 import build as pbuild
+    pbuild.build()
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed(fn, reps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize()
+        t = sorted(a.elapsed_time(b) for a, b in evs)
+        return sum(t) / reps
+
+    return torch, stream, timed
+
+
+def run_diff(args) -> None:
+    """256 closed cubic paths (4,096 control points), 1024^2 single-channel
+    FP32 coverage, L2 loss against the render of the points + N(0, 2 px):
+    forward + adjoint (dL/dpoints, dL/dalpha) per step against the plain
+    (non-differentiable) FP32 coverage frame of the same scene."""
+    torch, stream, timed = _diff_common(args)
+    import pathfinder_gb300 as pf
+    from pathfinder_gb300.diff import DiffRenderer
+    scene = pf.generate_scene(pf.PF_SCENE_CUBIC_1K, seed=args.seed)
+    tscene = pf.generate_scene(pf.PF_SCENE_CUBIC_1K, seed=args.seed, jitter_sigma=2.0, jitter_seed=args.seed + 1)
+    Wd, Hd = scene.width, scene.height
+    tdr = DiffRenderer(tscene)
+    target = tdr.forward(tdr.points0, tdr.alpha0).clone()
+    dr = DiffRenderer(scene, sync=False)
+    dr.renderer.set_stream(stream.cuda_stream)
+    pts, alpha = dr.points0.clone(), dr.alpha0.clone()
+    plain = pf.Renderer(0)
+    plain.set_stream(stream.cuda_stream)
+    pbatch = pf.SceneBatch.packed([scene])
+    pout = torch.zeros((Hd, Wd), dtype=torch.float32, device="cuda")
+    plain.render_batch(pbatch, pout, pf.PF_CUDA_FORMAT_F32)
+    grads = {}
+
+    def fwd():
+        img = dr.forward(pts, alpha)
+        grads["img"] = img
+
+    def fwd_bwd():
+        img = dr.forward(pts, alpha)
+        gp, ga = dr.backward(2.0 * (img - target))
+        grads["gp"], grads["ga"] = gp, ga
+
+    for _ in range(args.warmup):
+        fwd_bwd()
+        plain.render_batch(pbatch, pout, pf.PF_CUDA_FORMAT_F32, sync=False)
+    ms_plain = timed(lambda: plain.render_batch(pbatch, pout, pf.PF_CUDA_FORMAT_F32, sync=False), args.steps)
+    ms_fwd = timed(fwd, args.steps)
+    ms_fb = timed(fwd_bwd, args.steps)
+    code, _ = dr.renderer.render_status()
+    assert code == 0, code
+    st = dr.renderer.stats()
+    loss = float(((grads["img"] - target) ** 2).sum()) if "img" in grads else None
+    line = {
+        "metric": "fwd_bwd_ms", "value": round(ms_fb, 4), "unit": "ms", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_fb, 4), "higher_is_better": False, "dtype": "f32",
+        "data": "synthetic (seeded PF_SCENE_CUBIC_1K: 256 closed cubic paths; target = points + N(0, 2 px))",
+        "config": {"workload": "diff_cubic_256_paths_1024", "paths": len(scene.draw_paths),
+                   "control_points": len(scene.points), "width": Wd, "height": Hd, "seed": args.seed,
+                   "l2": "flushed between steps (512 MiB write)"},
+        "plain_forward_ms": round(ms_plain, 4), "diff_forward_ms": round(ms_fwd, 4),
+        "fwd_bwd_over_plain_forward": round(ms_fb / ms_plain, 3),
+        "frame": {"lines": st.line_count, "fills": st.fill_count, "alpha_tiles": st.alpha_tile_count,
+                  "visible_tiles": st.visible_tile_count},
+        "loss": loss, "grad_points_abs_max": float(grads["gp"].abs().max()),
+        "grad_alpha_abs_max": float(grads["ga"].abs().max()),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_fit(args) -> None:
+    """64 independent scenes of uneven size (32-512 cubic paths, canvases
+    256^2-1024^2, drawn from the seed) fitted jointly toward perturbed targets
+    (points + N(0, 2 px)) with Adam (lr 0.5 px) on the control points: one
+    batched differentiable frame and one batched adjoint per step."""
+    torch, stream, timed = _diff_common(args)
+    import numpy as np
+    import pathfinder_gb300 as pf
+    from pathfinder_gb300.diff import DiffRenderer
+    rng = np.random.default_rng(args.seed)
+    n_scenes = 64
+    scenes, targets = [], []
+    for i in range(n_scenes):
+        n_paths = int(rng.integers(32, 513))
+        side = int(rng.integers(256, 1025))
+        sd = args.seed * 1000 + i
+        scenes.append(pf.generate_scene(pf.PF_SCENE_CUBIC_1K, seed=sd, scale=n_paths / 256, width=side, height=side))
+        targets.append(pf.generate_scene(pf.PF_SCENE_CUBIC_1K, seed=sd, scale=n_paths / 256, width=side, height=side,
+                                         jitter_sigma=2.0, jitter_seed=sd + 7))
+    batch, tbatch = pf.SceneBatch.packed(scenes), pf.SceneBatch.packed(targets)
+    tdr = DiffRenderer(tbatch)
+    target = tdr.forward(tdr.points0, tdr.alpha0).clone()
+    goal = tdr.points0.clone()
+    dr = DiffRenderer(batch, sync=False)
+    dr.renderer.set_stream(stream.cuda_stream)
+    plain = pf.Renderer(0)
+    plain.set_stream(stream.cuda_stream)
+    pout = torch.zeros((batch.total_pixels,), dtype=torch.float32, device="cuda")
+    plain.render_batch(batch, pout, pf.PF_CUDA_FORMAT_F32)
+    for _ in range(args.warmup):
+        plain.render_batch(batch, pout, pf.PF_CUDA_FORMAT_F32, sync=False)
+    ms_plain = timed(lambda: plain.render_batch(batch, pout, pf.PF_CUDA_FORMAT_F32, sync=False), 20)
+
+    pts = dr.points0.clone().requires_grad_(True)
+    opt = torch.optim.Adam([pts], lr=0.5)
+    losses = []
+    dist0 = float((dr.points0 - goal).norm(dim=1).mean())
+
+    def step():
+        opt.zero_grad(set_to_none=False)
+        loss = ((dr(pts) - target) ** 2).sum()
+        loss.backward()
+        opt.step()
+        losses.append(loss.detach())
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.fit_steps)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for a, b in evs:
+        a.record(stream)
+        step()
+        b.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    code, _ = dr.renderer.render_status()
+    assert code == 0, code
+    ms = sorted(a.elapsed_time(b) for a, b in evs)
+    ms_step = sum(ms[3:]) / max(1, len(ms) - 3)  # the first steps size the buffers
+    dist1 = float((pts.detach() - goal).norm(dim=1).mean())
+    line = {
+        "metric": "fit_ms_per_step", "value": round(ms_step, 4), "unit": "ms", "n_gpus": 1,
+        "steps": args.fit_steps, "warmup": 3, "ms_per_step": round(ms_step, 4), "higher_is_better": False,
+        "dtype": "f32", "data": "synthetic (seeded PF_SCENE_CUBIC_1K scenes of uneven size; targets = points + N(0, 2 px))",
+        "config": {"workload": "fit_64_scenes_adam", "scenes": n_scenes, "paths": sum(len(s.draw_paths) for s in scenes),
+                   "control_points": int(dr.n_points), "pixels": int(batch.total_pixels), "lr_px": 0.5,
+                   "seed": args.seed},
+        "plain_forward_ms": round(ms_plain, 4), "fwd_bwd_adam_over_plain_forward": round(ms_step / ms_plain, 3),
+        "wall_s": round(wall, 3), "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
+        "mean_point_distance_px": {"start": round(dist0, 4), "end": round(dist1, 4)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="svg4k", choices=["svg4k", "atlas"],
-                    help="svg4k: the 20,000-path 4K frame (default); atlas: the batched glyph atlas")
+    ap.add_argument("--workload", default="svg4k", choices=["svg4k", "atlas", "diff", "fit"],
+                    help="svg4k: the 20,000-path 4K frame (default); atlas: the batched glyph atlas; "
+                         "diff: forward + adjoint of 256 cubic paths at 1024^2; fit: 64-scene Adam fit")
+    ap.add_argument("--fit-steps", type=int, default=200)
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=400)
@@ -266,6 +423,12 @@ def main():
         return
     if args.workload == "atlas":
         run_atlas(args)
+        return
+    if args.workload == "diff":
+        run_diff(args)
+        return
+    if args.workload == "fit":
+        run_fit(args)
         return
 
     import torch

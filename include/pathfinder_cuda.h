@@ -159,7 +159,8 @@ int32_t PFCUDARendererCreate(int32_t device_ordinal,
                              PFCUDARendererRef* out_renderer);
 /* Replaces PFGLRendererDestroy (c/src/lib.rs:618-620). */
 int32_t PFCUDARendererDestroy(PFCUDARendererRef renderer);
-/* Runs subsequent work on `stream` (a cudaStream_t; NULL = the renderer's own). */
+/* Runs subsequent work on `stream` (a cudaStream_t; NULL = the renderer's own;
+ * (void*)1 = cudaStreamLegacy, the legacy default stream). */
 int32_t PFCUDARendererSetStream(PFCUDARendererRef renderer, void* stream);
 /* Renderer::set_options background colour (gpu/options.rs:27-30). */
 int32_t PFCUDARendererSetOptions(PFCUDARendererRef renderer,
@@ -326,6 +327,49 @@ int32_t PFCUDAExclusiveScan(PFCUDARendererRef renderer, const uint32_t* in, uint
  * that first call before any stream capture.  All calls share the array:
  * calls that overlap on the GPU race, so serialise them. */
 int32_t PFCUDAExclusiveScanNoAlloc(const uint32_t* in, uint32_t* out, uint32_t n, void* stream);
+
+/* ---- differentiable rendering ----------------------------------------------
+ * No counterpart in the reference (it has no backward pass); the entry points
+ * follow PFCUDARenderCoverage.  A differentiable frame renders single-channel
+ * FP32 coverage (SrcOver of alpha x coverage) from FP32 fills, without the
+ * 8.8 rounding of the parity path, so the image is piecewise smooth in the
+ * control points, and keeps a per-pixel tape for PFCUDABackward.  Gradients
+ * are exact for pixels wholly inside the scene's view box (use pixel-aligned
+ * view boxes), hold the flattening (the subdivision of each curve) fixed, and
+ * are one-sided at coverage kinks (|winding| = 1 for nonzero, the even-odd
+ * fold, the clip combine's min). */
+
+/* Replaces every point of the uploaded scene or batch (batch order, `count`
+ * = all points) without re-uploading the structure; `memory` says where
+ * `points` lives.  Contours, flags and paths stay as uploaded. */
+int32_t PFCUDASetPoints(PFCUDARendererRef renderer, const PFVector2F* points, uint64_t count,
+                        int32_t memory);
+
+/* Differentiable frame over scenes [first, first + count).  Scenes uploaded
+ * without a target draw into a width x height FP32 image, as in
+ * PFCUDARenderCoverage; pass width = height = 0 to keep the targets of
+ * PFCUDASceneUploadBatch.  `draw_alpha` (device, one float per draw path of
+ * the whole batch in batch order; NULL = paint alpha / 255) is the paint
+ * alpha; it is copied.  Synchronous (sizes its buffers like
+ * PFCUDARenderBatch). */
+int32_t PFCUDARenderDiff(PFCUDARendererRef renderer, const PFCUDABuildOptions* options, uint32_t first,
+                         uint32_t count, int32_t width, int32_t height, const float* draw_alpha,
+                         float* out_device);
+/* The same frame enqueued without synchronising (buffers as sized by earlier
+ * frames; an overflow surfaces in PFCUDARenderStatus, and the frame and its
+ * adjoint must then be re-run). */
+int32_t PFCUDARenderDiffAsync(PFCUDARendererRef renderer, const PFCUDABuildOptions* options, uint32_t first,
+                              uint32_t count, int32_t width, int32_t height, const float* draw_alpha,
+                              float* out_device);
+
+/* Adjoint of the last PFCUDARenderDiff (PF_CUDA_ERR_INVALID if another frame,
+ * upload or PFCUDASetPoints came in between).  d_image: dL/d(image), device,
+ * laid out as that frame's output.  Overwrites d_points (device, one PFVector2F
+ * per uploaded point: dL/d(point), zero for points outside the range) and
+ * d_alpha (device, one float per draw path, may be NULL).  Enqueued on the
+ * renderer's stream without synchronising. */
+int32_t PFCUDABackward(PFCUDARendererRef renderer, const float* d_image, PFVector2F* d_points,
+                       float* d_alpha);
 
 /* Human-readable text for a status code (static storage). */
 const char* PFCUDAStatusString(int32_t status);

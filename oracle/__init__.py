@@ -64,6 +64,13 @@ def lib() -> C.CDLL:
         l.pfo_area_lut_value.argtypes = [C.c_int, C.c_int, C.c_int]
         l.pfo_sse_cvt.restype = C.c_int32
         l.pfo_sse_cvt.argtypes = [C.c_float]
+        l.pfo_diff_build.restype = C.c_void_p
+        l.pfo_diff_build.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        l.pfo_diff_free.argtypes = [C.c_void_p]
+        l.pfo_diff_info.argtypes = [C.c_void_p, C.c_void_p]
+        l.pfo_diff_render.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_void_p]
+        l.pfo_diff_grad.restype = C.c_int32
+        l.pfo_diff_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib = l
     return _lib
 
@@ -148,6 +155,55 @@ class OracleFrame:
         lib().pfo_render(self._h, width, height, C.byref(bg) if bg is not None else None, channels,
                          out.ctypes.data, f64.ctypes.data, self.threads)
         return out, f64
+
+
+class DiffOracle:
+    """FP64 differentiable frame of a scene and its adjoint, with each curve's
+    subdivision fixed by the FP32 flattening of the scene's own points (the
+    checker of the CUDA level's PFCUDARenderDiff / PFCUDABackward)."""
+
+    def __init__(self, scene, width: int, height: int, build_options=None):
+        L = lib()
+        self._scene = scene
+        self._desc = scene.desc()
+        self._bo = _opts(build_options)
+        h = L.pfo_diff_build(C.byref(self._desc), C.byref(self._bo) if self._bo is not None else None, width,
+                             height)
+        if not h:
+            raise ValueError("oracle rejected the scene")
+        self._h = h
+        self.width, self.height = width, height
+        info = np.zeros((5,), np.uint64)
+        L.pfo_diff_info(h, info.ctypes.data)
+        self.point_count, self.clip_path_count, self.draw_path_count, self.line_count, limit = [int(v) for v in info]
+        self.limit_hit = bool(limit)
+        self.points = np.asarray(scene.points, np.float64).reshape(-1, 2).copy()
+        self.alpha = scene.draw_paths["paint"][:, 3].astype(np.float64) / 255.0
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().pfo_diff_free(self._h)
+            self._h = None
+
+    def render(self, points=None, alpha=None, background: float = 0.0) -> np.ndarray:
+        p = np.ascontiguousarray(self.points if points is None else points, np.float64).reshape(-1, 2)
+        a = np.ascontiguousarray(self.alpha if alpha is None else alpha, np.float64)
+        if p.shape[0] != self.point_count or a.shape[0] != self.draw_path_count:
+            raise ValueError("points / alpha do not match the scene")
+        img = np.zeros((self.height, self.width), np.float64)
+        lib().pfo_diff_render(self._h, p.ctypes.data, a.ctypes.data, float(background), img.ctypes.data)
+        return img
+
+    def grad(self, d_image) -> tuple[np.ndarray, np.ndarray]:
+        """(dL/dpoints [N,2], dL/dalpha [draw paths]) of the last render."""
+        g = np.ascontiguousarray(d_image, np.float64)
+        if g.shape != (self.height, self.width):
+            raise ValueError("d_image has the wrong shape")
+        dp = np.zeros((self.point_count, 2), np.float64)
+        da = np.zeros((self.draw_path_count,), np.float64)
+        if lib().pfo_diff_grad(self._h, g.ctypes.data, dp.ctypes.data, da.ctypes.data) != 0:
+            raise RuntimeError("render before grad")
+        return dp, da
 
 
 def cpu_frame(scene, width: int, height: int, threads: int = 0, build_options=None, want_image: bool = False):

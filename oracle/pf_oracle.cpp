@@ -755,6 +755,375 @@ bool make_frame(const PFCUDASceneDesc* sc, const PFCUDABuildOptions* opts, Frame
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// FP64 differentiable frame and its adjoint (checker of the CUDA adjoint)
+// ---------------------------------------------------------------------------
+// With each curve's subdivision held fixed, the CUDA level's differentiable
+// frame is a function of the control points and the paint alphas: every
+// flattened line runs between the curve points at the dyadic parameters
+// [addr, addr + 1) / 2^depth that process_segment's recursion
+// (renderer/src/tiler.rs:166-184) picks for the uploaded FP32 points.  Here it
+// is evaluated in FP64: per path the integral of the winding number over each
+// pixel (the trapezoid areas below each line, fill_area.inc.glsl:11-27, plus
+// the backdrop carried down the column, taken over whole pixel columns rather
+// than 16x16 tiles), the sampleMask resolve, the clip combine min(|d|, |s|)
+// (tile_clip_combine.fs.glsl:27-30), SrcOver of alpha x coverage, and the
+// adjoint of all of it from the first variation of the winding integral: a
+// line A -> B moved by dP(u) = (1-u) dA + u dB changes a pixel's integral by
+// the integral of dP . n over the part of the line inside the pixel,
+// n = (-(B-A).y, (B-A).x).  The pixels a line crosses come from exact lists of
+// its grid crossings.  Derivatives at the resolve's kinks are one-sided like
+// the CUDA level's: nonzero d|c|/dc = +1 at c = 0 and 0 at |c| >= 1; even-odd
+// +1 below the fold at 1 and -1 from it on; ties of the clip min go to the
+// draw path.
+struct DSeg {
+    int kind;
+    uint32_t idx[4];  // first, first + 1, first + 2, end (unused slots repeat)
+    std::vector<std::pair<double, double>> leaves;
+};
+struct DPath {
+    std::vector<DSeg> segs;
+    bool even_odd = false, is_clip = false;
+    int32_t clip = -1;                   // global index of the clip path
+    int bx0 = 0, by0 = 0, bx1 = 0, by1 = 0;  // pixel box of the last render
+    std::vector<double> w;               // winding integral over the box
+    std::vector<double> lines;           // 4 per line (last render)
+    std::vector<uint32_t> line_seg, line_leaf;
+};
+struct DiffFrame {
+    int W = 0, H = 0, X0 = 0, Y0 = 0, X1 = 0, Y1 = 0;  // pixels inside the image and the view box
+    bool transform = false;
+    double m[6] = {1, 0, 0, 1, 0, 0};
+    uint32_t np = 0, nclip = 0, ndraw = 0;
+    uint64_t line_count = 0;
+    bool limit_hit = false;
+    std::vector<DPath> paths;            // clip paths, then draw paths
+    std::vector<double> alpha;           // last render
+    std::vector<std::vector<double>> cov, dprev, dd, dc;  // per draw path over its box
+    bool rendered = false;
+};
+
+void flatten_leaves(const Segment& s, int depth, uint64_t addr, std::vector<std::pair<double, double>>& out,
+                    bool* limit) {
+    if (s.kind == kQuad) { flatten_leaves(to_cubic(s), depth, addr, out, limit); return; }
+    if (s.kind == kLine || is_flat(s) || depth >= 32) {
+        if (depth >= 32 && !is_flat(s)) *limit = true;
+        out.push_back({std::ldexp((double)addr, -depth), std::ldexp((double)(addr + 1), -depth)});
+        return;
+    }
+    Segment a, b;
+    split_half(s, &a, &b);
+    flatten_leaves(a, depth + 1, addr * 2, out, limit);
+    flatten_leaves(b, depth + 1, addr * 2 + 1, out, limit);
+}
+
+bool make_diff_frame(const PFCUDASceneDesc* sc, const PFCUDABuildOptions* opts, int W, int H, DiffFrame& d) {
+    if (!sc || sc->memory != PF_MEMORY_HOST || W <= 0 || H <= 0) return false;
+    d.W = W; d.H = H;
+    d.X0 = std::max(0, (int)std::ceil(sc->view_box.origin.x));
+    d.Y0 = std::max(0, (int)std::ceil(sc->view_box.origin.y));
+    d.X1 = std::min(W, (int)std::floor(sc->view_box.lower_right.x));
+    d.Y1 = std::min(H, (int)std::floor(sc->view_box.lower_right.y));
+    d.np = sc->point_count;
+    d.nclip = sc->clip_path_count;
+    d.ndraw = sc->draw_path_count;
+    PFTransform2F tf{};
+    if (opts && opts->has_transform) {
+        tf = opts->transform;
+        d.transform = !(tf.m00 == 1.0f && tf.m01 == 0.0f && tf.m10 == 0.0f && tf.m11 == 1.0f &&
+                        tf.vector.x == 0.0f && tf.vector.y == 0.0f);
+    }
+    if (d.transform) {
+        d.m[0] = tf.m00; d.m[1] = tf.m01; d.m[2] = tf.m10; d.m[3] = tf.m11; d.m[4] = tf.vector.x; d.m[5] = tf.vector.y;
+    }
+    // FP32 points as the tiler sees them (Transform2F * Vector2F in FP32)
+    std::vector<PFVector2F> p32(sc->points, sc->points + d.np);
+    if (d.transform)
+        for (PFVector2F& v : p32) {
+            float hx = tf.m00 * v.x, hy = tf.m10 * v.x, hz = tf.m01 * v.y, hw = tf.m11 * v.y;
+            v = PFVector2F{(hx + hz) + tf.vector.x, (hy + hw) + tf.vector.y};
+        }
+    auto is_end = [&](uint32_t i) {
+        return (sc->point_flags[i] & (PF_POINT_FLAG_CONTROL_POINT_0 | PF_POINT_FLAG_CONTROL_POINT_1)) == 0;
+    };
+    const uint32_t n = d.nclip + d.ndraw;
+    d.paths.assign(n, DPath());
+    for (uint32_t p = 0; p < n; p++) {
+        const PFCUDAPath& src = p < d.nclip ? sc->clip_paths[p] : sc->draw_paths[p - d.nclip];
+        DPath& dp = d.paths[p];
+        dp.is_clip = p < d.nclip;
+        dp.even_odd = src.fill_rule == PF_FILL_RULE_EVEN_ODD;
+        if (!dp.is_clip && src.clip_path >= (int32_t)d.nclip) return false;
+        dp.clip = (!dp.is_clip && src.clip_path >= 0) ? src.clip_path : -1;
+        for (uint32_t c = 0; c < src.contour_count; c++) {
+            const uint32_t s0 = sc->contour_starts[src.first_contour + c];
+            const uint32_t len = sc->contour_starts[src.first_contour + c + 1] - s0;
+            if (len == 0) continue;
+            // ContourIter::next (content/src/outline.rs:1024-1065) by point index
+            uint32_t index = 1;
+            for (;;) {
+                if (index == len + 1) break;
+                DSeg sg{};
+                const uint32_t i0 = s0 + index - 1;
+                if (index == len) {
+                    sg.kind = kLine; sg.idx[0] = i0; sg.idx[1] = sg.idx[2] = i0; sg.idx[3] = s0;
+                    index++;
+                } else {
+                    const uint32_t i1 = s0 + index++;
+                    if (is_end(i1)) {
+                        sg.kind = kLine; sg.idx[0] = i0; sg.idx[1] = sg.idx[2] = i0; sg.idx[3] = i1;
+                    } else {
+                        const uint32_t i2 = s0 + index++;
+                        if (is_end(i2)) {
+                            sg.kind = kQuad; sg.idx[0] = i0; sg.idx[1] = i1; sg.idx[2] = i0; sg.idx[3] = i2;
+                        } else {
+                            const uint32_t i3 = s0 + index++;
+                            sg.kind = kCubic; sg.idx[0] = i0; sg.idx[1] = i1; sg.idx[2] = i2; sg.idx[3] = i3;
+                        }
+                    }
+                }
+                const PFVector2F a = p32[sg.idx[0]], e = p32[sg.idx[3]];
+                Segment s32{Line{a.x, a.y, e.x, e.y}, Line{0, 0, 0, 0}, sg.kind};
+                if (sg.kind == kQuad) s32.ctrl = Line{p32[sg.idx[1]].x, p32[sg.idx[1]].y, 0, 0};
+                if (sg.kind == kCubic)
+                    s32.ctrl = Line{p32[sg.idx[1]].x, p32[sg.idx[1]].y, p32[sg.idx[2]].x, p32[sg.idx[2]].y};
+                flatten_leaves(s32, 0, 0, sg.leaves, &d.limit_hit);
+                d.line_count += sg.leaves.size();
+                dp.segs.push_back(std::move(sg));
+            }
+        }
+    }
+    return true;
+}
+
+// Bernstein weights of the slots (first, first + 1, first + 2, end) at t.
+void diff_weights(int kind, double t, double w[4]) {
+    const double s = 1.0 - t;
+    if (kind == kCubic) { w[0] = s * s * s; w[1] = 3 * t * s * s; w[2] = 3 * t * t * s; w[3] = t * t * t; }
+    else if (kind == kQuad) { w[0] = s * s; w[1] = 2 * t * s; w[2] = 0; w[3] = t * t; }
+    else { w[0] = s; w[1] = 0; w[2] = 0; w[3] = t; }
+}
+
+// Winding integral of one path over its pixel box (rows clamp: what lies
+// above the box is carried down the column, what lies below is dropped).
+void diff_winding(DiffFrame& d, DPath& dp, const std::vector<double>& q) {
+    dp.lines.clear(); dp.line_seg.clear(); dp.line_leaf.clear();
+    double mnx = INFINITY, mny = INFINITY, mxx = -INFINITY, mxy = -INFINITY;
+    for (uint32_t si = 0; si < dp.segs.size(); si++) {
+        const DSeg& sg = dp.segs[si];
+        for (uint32_t li = 0; li < sg.leaves.size(); li++) {
+            double e[4];
+            for (int end = 0; end < 2; end++) {
+                double w[4], x = 0, y = 0;
+                diff_weights(sg.kind, end ? sg.leaves[li].second : sg.leaves[li].first, w);
+                for (int k = 0; k < 4; k++) { x += w[k] * q[2 * sg.idx[k]]; y += w[k] * q[2 * sg.idx[k] + 1]; }
+                e[2 * end] = x; e[2 * end + 1] = y;
+            }
+            for (double v : e) dp.lines.push_back(v);
+            dp.line_seg.push_back(si);
+            dp.line_leaf.push_back(li);
+            mnx = std::min({mnx, e[0], e[2]}); mxx = std::max({mxx, e[0], e[2]});
+            mny = std::min({mny, e[1], e[3]}); mxy = std::max({mxy, e[1], e[3]});
+        }
+    }
+    dp.bx0 = std::max(d.X0, (int)std::floor(mnx)); dp.bx1 = std::min(d.X1, (int)std::ceil(mxx));
+    dp.by0 = std::max(d.Y0, (int)std::floor(mny)); dp.by1 = std::min(d.Y1, (int)std::ceil(mxy));
+    if (dp.lines.empty() || dp.bx1 <= dp.bx0 || dp.by1 <= dp.by0) { dp.bx1 = dp.bx0; dp.by1 = dp.by0; dp.w.clear(); return; }
+    const int bw = dp.bx1 - dp.bx0, bh = dp.by1 - dp.by0;
+    std::vector<double> acc((size_t)bw * bh, 0.0), carry((size_t)bw * bh, 0.0);
+    const double Y0 = dp.by0, Y1 = dp.by1;
+    for (size_t l = 0; l < dp.lines.size(); l += 4) {
+        const double x0 = dp.lines[l], y0 = dp.lines[l + 1], x1 = dp.lines[l + 2], y1 = dp.lines[l + 3];
+        if (x0 == x1) continue;
+        const double slope = (y1 - y0) / (x1 - x0);
+        const int c0 = std::max(dp.bx0, (int)std::floor(std::min(x0, x1)));
+        const int c1 = std::min(dp.bx1 - 1, (int)std::ceil(std::max(x0, x1)) - 1);
+        for (int px = c0; px <= c1; px++) {
+            const double xa = std::min(std::max(x0, (double)px), (double)px + 1);
+            const double xb = std::min(std::max(x1, (double)px), (double)px + 1);
+            const double wdt = xa - xb;  // signed: right-to-left lines add area below them
+            if (wdt == 0) continue;
+            const double ya = y0 + (xa - x0) * slope, yb = y0 + (xb - x0) * slope;
+            const double ylo = std::min(ya, yb), yhi = std::max(ya, yb);
+            const int col = px - dp.bx0;
+            auto add = [&](int r, double a, double cr) {
+                acc[(size_t)(r - dp.by0) * bw + col] += a;
+                if (r + 1 < dp.by1) carry[(size_t)(r + 1 - dp.by0) * bw + col] += cr;
+            };
+            // the part above the box covers every row of the column; the part
+            // below it covers none
+            if (yhi - ylo <= 0) {
+                if (ylo < Y0) { carry[col] += wdt; continue; }
+                const int r = (int)std::floor(ylo);
+                if (r >= dp.by1) continue;
+                add(r, wdt * ((double)(r + 1) - ylo), wdt);
+                continue;
+            }
+            if (ylo < Y0) carry[col] += wdt * ((std::min(yhi, Y0) - ylo) / (yhi - ylo));
+            const double ys = std::max(ylo, Y0), ye = std::min(yhi, Y1);
+            if (!(ye > ys)) continue;
+            const int r0 = (int)std::floor(ys), r1 = std::min((int)std::floor(ye), dp.by1 - 1);
+            for (int r = r0; r <= r1; r++) {
+                const double yt = std::max(ys, (double)r), yb2 = std::min(ye, (double)(r + 1));
+                const double h = yb2 - yt;
+                if (h <= 0) continue;
+                const double wr = wdt * (h / (yhi - ylo));
+                add(r, wr * ((double)(r + 1) - 0.5 * (yt + yb2)), wr);
+            }
+        }
+    }
+    dp.w.assign((size_t)bw * bh, 0.0);
+    for (int x = 0; x < bw; x++) {
+        double run = 0;
+        for (int y = 0; y < bh; y++) {
+            run += carry[(size_t)y * bw + x];
+            dp.w[(size_t)y * bw + x] = acc[(size_t)y * bw + x] + run;
+        }
+    }
+}
+
+double diff_w_at(const DPath& dp, int X, int Y) {
+    if (X < dp.bx0 || X >= dp.bx1 || Y < dp.by0 || Y >= dp.by1) return 0.0;
+    return dp.w[(size_t)(Y - dp.by0) * (dp.bx1 - dp.bx0) + (X - dp.bx0)];
+}
+
+double diff_resolve(double c, bool even_odd, double* dcdw) {
+    if (!even_odd) {
+        const double a = std::fabs(c);
+        *dcdw = a < 1.0 ? (c >= 0.0 ? 1.0 : -1.0) : 0.0;
+        return std::min(1.0, a);
+    }
+    const double m = c - 2.0 * std::floor(c * 0.5);
+    *dcdw = m < 1.0 ? 1.0 : -1.0;
+    return std::min(1.0, 1.0 - std::fabs(1.0 - m));
+}
+
+void diff_transform(const DiffFrame& d, const double* pts, std::vector<double>& q) {
+    q.assign((size_t)d.np * 2, 0.0);
+    for (uint32_t i = 0; i < d.np; i++) {
+        const double x = pts[2 * i], y = pts[2 * i + 1];
+        q[2 * i] = d.transform ? d.m[0] * x + d.m[1] * y + d.m[4] : x;
+        q[2 * i + 1] = d.transform ? d.m[2] * x + d.m[3] * y + d.m[5] : y;
+    }
+}
+
+void diff_render(DiffFrame& d, const double* pts, const double* alpha, double bg, double* img) {
+    std::vector<double> q;
+    diff_transform(d, pts, q);
+    for (DPath& dp : d.paths) diff_winding(d, dp, q);
+    d.alpha.assign(alpha, alpha + d.ndraw);
+    d.cov.assign(d.ndraw, {}); d.dprev.assign(d.ndraw, {}); d.dd.assign(d.ndraw, {}); d.dc.assign(d.ndraw, {});
+    for (size_t k = 0; k < (size_t)d.W * d.H; k++) img[k] = bg;
+    for (uint32_t k = 0; k < d.ndraw; k++) {
+        const DPath& dp = d.paths[d.nclip + k];
+        const int bw = dp.bx1 - dp.bx0, bh = dp.by1 - dp.by0;
+        const size_t nb = (size_t)std::max(bw, 0) * std::max(bh, 0);
+        d.cov[k].assign(nb, 0); d.dprev[k].assign(nb, 0); d.dd[k].assign(nb, 0); d.dc[k].assign(nb, 0);
+        for (int y = 0; y < bh; y++)
+            for (int x = 0; x < bw; x++) {
+                const int X = dp.bx0 + x, Y = dp.by0 + y;
+                const size_t i = (size_t)y * bw + x;
+                const double wd = dp.w[i];
+                double c, dcdm, ddv = 0, dcv = 0;
+                if (dp.clip >= 0) {
+                    const double wc = diff_w_at(d.paths[dp.clip], X, Y);
+                    const bool own = std::fabs(wd) <= std::fabs(wc);
+                    c = diff_resolve(std::min(std::fabs(wd), std::fabs(wc)), dp.even_odd, &dcdm);
+                    const double s = ((own ? wd : wc) >= 0.0) ? 1.0 : -1.0;
+                    (own ? ddv : dcv) = dcdm * s;
+                } else {
+                    c = diff_resolve(wd, dp.even_odd, &dcdm);
+                    ddv = dcdm;
+                }
+                double& dst = img[(size_t)Y * d.W + X];
+                d.cov[k][i] = c; d.dprev[k][i] = dst; d.dd[k][i] = ddv; d.dc[k][i] = dcv;
+                const double a = d.alpha[k] * c;
+                dst = a + dst * (1.0 - a);
+            }
+    }
+    d.rendered = true;
+}
+
+void diff_grad(DiffFrame& d, const double* dimg, double* dpts, double* dalpha) {
+    std::vector<double> G(dimg, dimg + (size_t)d.W * d.H);
+    std::vector<std::vector<double>> gw(d.paths.size());
+    for (size_t p = 0; p < d.paths.size(); p++) gw[p].assign(d.paths[p].w.size(), 0.0);
+    for (uint32_t k = 0; k < d.ndraw; k++) dalpha[k] = 0;
+    for (uint32_t k = d.ndraw; k-- > 0;) {
+        const uint32_t p = d.nclip + k;
+        const DPath& dp = d.paths[p];
+        const int bw = dp.bx1 - dp.bx0, bh = dp.by1 - dp.by0;
+        for (int y = 0; y < bh; y++)
+            for (int x = 0; x < bw; x++) {
+                const int X = dp.bx0 + x, Y = dp.by0 + y;
+                const size_t i = (size_t)y * bw + x;
+                double& g = G[(size_t)Y * d.W + X];
+                const double c = d.cov[k][i], dlda = g * (1.0 - d.dprev[k][i]);
+                dalpha[k] += dlda * c;
+                const double dm = dlda * d.alpha[k];
+                gw[p][i] += dm * d.dd[k][i];
+                if (dp.clip >= 0 && d.dc[k][i] != 0) {
+                    const DPath& cp = d.paths[dp.clip];
+                    if (X >= cp.bx0 && X < cp.bx1 && Y >= cp.by0 && Y < cp.by1)
+                        gw[dp.clip][(size_t)(Y - cp.by0) * (cp.bx1 - cp.bx0) + (X - cp.bx0)] += dm * d.dc[k][i];
+                }
+                g *= 1.0 - d.alpha[k] * c;
+            }
+    }
+    std::vector<double> dq((size_t)d.np * 2, 0.0);
+    std::vector<double> us;
+    for (size_t p = 0; p < d.paths.size(); p++) {
+        const DPath& dp = d.paths[p];
+        if (dp.w.empty()) continue;
+        const int bw = dp.bx1 - dp.bx0;
+        for (size_t l = 0; l < dp.line_seg.size(); l++) {
+            const double x0 = dp.lines[4 * l], y0 = dp.lines[4 * l + 1];
+            const double dx = dp.lines[4 * l + 2] - x0, dy = dp.lines[4 * l + 3] - y0;
+            if (dx == 0 && dy == 0) continue;
+            us.assign({0.0, 1.0});
+            if (dx != 0)
+                for (double k = std::floor(std::min(x0, x0 + dx)) + 1; k < std::max(x0, x0 + dx); k += 1) {
+                    const double u = (k - x0) / dx;
+                    if (u > 0 && u < 1) us.push_back(u);
+                }
+            if (dy != 0)
+                for (double k = std::floor(std::min(y0, y0 + dy)) + 1; k < std::max(y0, y0 + dy); k += 1) {
+                    const double u = (k - y0) / dy;
+                    if (u > 0 && u < 1) us.push_back(u);
+                }
+            std::sort(us.begin(), us.end());
+            double GA = 0, GB = 0;
+            for (size_t j = 0; j + 1 < us.size(); j++) {
+                const double u0 = us[j], u1 = us[j + 1];
+                if (!(u1 > u0)) continue;
+                const double um = 0.5 * (u0 + u1);
+                const int X = (int)std::floor(x0 + um * dx), Y = (int)std::floor(y0 + um * dy);
+                if (X < dp.bx0 || X >= dp.bx1 || Y < dp.by0 || Y >= dp.by1) continue;
+                const double g = gw[p][(size_t)(Y - dp.by0) * bw + (X - dp.bx0)];
+                GA += g * (u1 - u0) * (1.0 - um);
+                GB += g * (u1 - u0) * um;
+            }
+            const DSeg& sg = dp.segs[dp.line_seg[l]];
+            const auto& lf = sg.leaves[dp.line_leaf[l]];
+            double wa[4], wb[4];
+            diff_weights(sg.kind, lf.first, wa);
+            diff_weights(sg.kind, lf.second, wb);
+            const int used[4] = {1, sg.kind != kLine, sg.kind == kCubic, 1};
+            for (int k = 0; k < 4; k++) {
+                if (!used[k]) continue;
+                const double c = wa[k] * GA + wb[k] * GB;
+                dq[2 * sg.idx[k]] += c * -dy;
+                dq[2 * sg.idx[k] + 1] += c * dx;
+            }
+        }
+    }
+    for (uint32_t i = 0; i < d.np; i++) {
+        const double gx = dq[2 * i], gy = dq[2 * i + 1];
+        dpts[2 * i] = d.transform ? d.m[0] * gx + d.m[2] * gy : gx;
+        dpts[2 * i + 1] = d.transform ? d.m[1] * gx + d.m[3] * gy : gy;
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -917,5 +1286,34 @@ void pfo_fill_coverage(const uint16_t seg[4], double* mask) {
     accumulate_fill<double>(f, mask);
 }
 int32_t pfo_sse_cvt(float x) { return sse_cvt(x); }
+
+// ---- FP64 differentiable frame ---------------------------------------------
+struct PFODiff { DiffFrame d; };
+
+PFODiff* pfo_diff_build(const PFCUDASceneDesc* scene, const PFCUDABuildOptions* opts, int width, int height) {
+    PFODiff* f = new PFODiff();
+    if (!make_diff_frame(scene, opts, width, height, f->d)) { delete f; return nullptr; }
+    return f;
+}
+
+void pfo_diff_free(PFODiff* f) { delete f; }
+
+// info[0..4] = points, clip paths, draw paths, flattened lines, depth limit hit
+void pfo_diff_info(const PFODiff* f, uint64_t* info) {
+    info[0] = f->d.np; info[1] = f->d.nclip; info[2] = f->d.ndraw; info[3] = f->d.line_count;
+    info[4] = f->d.limit_hit ? 1 : 0;
+}
+
+// points: 2 per scene point (input space); alpha: one per draw path; image: W x H.
+void pfo_diff_render(PFODiff* f, const double* points, const double* alpha, double background, double* image) {
+    diff_render(f->d, points, alpha, background, image);
+}
+
+// Adjoint of the last pfo_diff_render: dL/dimage -> dL/dpoints (2 per point), dL/dalpha.
+int32_t pfo_diff_grad(PFODiff* f, const double* d_image, double* d_points, double* d_alpha) {
+    if (!f->d.rendered) return -1;
+    diff_grad(f->d, d_image, d_points, d_alpha);
+    return 0;
+}
 
 }  // extern "C"

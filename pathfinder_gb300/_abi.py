@@ -177,6 +177,12 @@ _SIGS = {
     "PFCUDAGetStageTimes": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32]),
     "PFCUDAExclusiveScan": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32]),
     "PFCUDAExclusiveScanNoAlloc": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "PFCUDASetPoints": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int32]),
+    "PFCUDARenderDiff": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDABuildOptions), C.c_uint32, C.c_uint32, C.c_int32,
+                                     C.c_int32, C.c_void_p, C.c_void_p]),
+    "PFCUDARenderDiffAsync": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDABuildOptions), C.c_uint32, C.c_uint32,
+                                          C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "PFCUDABackward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "PFCUDAStatusString": (C.c_char_p, [C.c_int32]),
     "PFCUDASceneGenerate": (C.c_int32, [C.POINTER(PFCUDASceneParams), C.POINTER(C.c_void_p)]),
     "PFCUDASceneGetDesc": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDASceneDesc), C.POINTER(C.c_int32),

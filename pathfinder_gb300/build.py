@@ -27,6 +27,7 @@ NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 UNITS = [
     ("pf_tiler.cu", ["-fmad=false"]),
     ("pf_raster.cu", []),
+    ("pf_adjoint.cu", []),
     ("pf_renderer.cu", []),
     ("pf_noalloc.cu", []),
     ("pf_scenes.cpp", []),
@@ -60,8 +61,6 @@ def _compile(src: str, extra: list[str], verbose: bool) -> str:
     if _newer(obj, [path] + _headers()):
         return obj
     cmd = [nvcc(), "-c", path, "-o", obj] + NVCC_COMMON + extra
-    if src.endswith(".cpp"):
-        cmd += ["-x", "cu"] if False else []
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -53,6 +53,9 @@ struct PathDev {
     int4*     tile_rect;           // [P] tile rect (min x, min y, max x, max y)
     uint32_t* tile_offset;         // [P+1] global tile index of the path's first tile
     uint32_t* col_offset;          // [P+1] offset of its above-rect column backdrops
+    // differentiable frames only (NULL otherwise): paint alpha per draw path
+    const float* alpha_f;          // [draw paths of the batch]
+    const uint32_t* draw_index;    // [P] index of the path among the batch's draw paths
 };
 
 // Per-scene data.
@@ -183,6 +186,20 @@ __device__ __forceinline__ bool clip_to_view(Line& s, float minx, float maxx, fl
     return false;
 }
 
+// The differentiable form keeps each fill's FP32 tile-local endpoints (the
+// 8.8 rounding would make coverage piecewise constant in the control points)
+// and culls only fills of exactly zero width.
+__device__ __forceinline__ bool make_fill_f(const PathCtx& pc, Line s, int32_t tx, int32_t ty, float4& rec,
+                                            uint32_t& g) {
+    if (!(pc.minx <= tx && pc.miny <= ty && tx <= pc.maxx - 1 && ty <= pc.maxy - 1)) return false;
+    const float ulx = (float)tx * 16.0f, uly = (float)ty * 16.0f;
+    rec = make_float4(fminf(fmaxf(s.fx - ulx, 0.0f), 16.0f), fminf(fmaxf(s.fy - uly, 0.0f), 16.0f),
+                      fminf(fmaxf(s.tx - ulx, 0.0f), 16.0f), fminf(fmaxf(s.ty - uly, 0.0f), 16.0f));
+    if (rec.x == rec.z) return false;
+    g = pc.tile_base + (uint32_t)(tx - pc.minx) + (uint32_t)(pc.maxx - pc.minx) * (uint32_t)(ty - pc.miny);
+    return true;
+}
+
 // ObjectBuilder::add_fill (renderer/src/builder.rs:509-553) without the push:
 // returns false when the fill is culled, else the packed LineSegmentU16 and the
 // global tile index.
@@ -205,7 +222,8 @@ __device__ __forceinline__ bool make_fill(const PathCtx& pc, Line s, int32_t tx,
 // process_line_segment (renderer/src/tiler.rs:191-308).  `sink` receives
 // sink.fill(rec, g) for every kept fill in emission order and
 // sink.backdrop(tx, ty, delta) for every backdrop adjustment.
-template <class Sink>
+// DIFF: fills keep FP32 endpoints (make_fill_f) and reach sink.fill as float4.
+template <bool DIFF = false, class Sink>
 __device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink, uint32_t dda_limit,
                                          uint32_t* status) {
     if (!clip_to_view(seg, pc.vminx, pc.vmaxx, pc.vmaxy)) return;
@@ -230,15 +248,19 @@ __device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink
         float next_t = fminf(dir == 1 ? tmx : tmy, 1.0f);
         if (tcx == ttx && tcy == tty) dir = 0;
         float npx = fadd(seg.fx, fmul(vx, next_t)), npy = fadd(seg.fy, fmul(vy, next_t));
-        uint2 rec; uint32_t g;
-        if (make_fill(pc, Line{cx, cy, npx, npy}, tcx, tcy, rec, g)) sink.fill(rec, g);
-        if (stepy < 0 && dir == 2) {
-            if (make_fill(pc, Line{npx, npy, fmul(i2f(tcx), 16.0f), fmul(i2f(tcy), 16.0f)}, tcx, tcy, rec, g))
-                sink.fill(rec, g);
-        } else if (stepy > 0 && last == 2) {
-            if (make_fill(pc, Line{fmul(i2f(tcx), 16.0f), fmul(i2f(tcy), 16.0f), cx, cy}, tcx, tcy, rec, g))
-                sink.fill(rec, g);
-        }
+        auto add = [&](Line l) {
+            uint32_t g;
+            if constexpr (DIFF) {
+                float4 rec;
+                if (make_fill_f(pc, l, tcx, tcy, rec, g)) sink.fill(rec, g);
+            } else {
+                uint2 rec;
+                if (make_fill(pc, l, tcx, tcy, rec, g)) sink.fill(rec, g);
+            }
+        };
+        add(Line{cx, cy, npx, npy});
+        if (stepy < 0 && dir == 2) add(Line{npx, npy, fmul(i2f(tcx), 16.0f), fmul(i2f(tcy), 16.0f)});
+        else if (stepy > 0 && last == 2) add(Line{fmul(i2f(tcx), 16.0f), fmul(i2f(tcy), 16.0f), cx, cy});
         if (stepx < 0 && last == 1) sink.backdrop(tcx, tcy, 1);
         else if (stepx > 0 && dir == 1) sink.backdrop(tcx, tcy, -1);
         if (dir == 0) break;
@@ -404,6 +426,20 @@ __device__ __forceinline__ float resolve_coverage(float c, bool even_odd) {
         c = 1.0f - fabsf(1.0f - m);
     }
     return fminf(1.0f, c);
+}
+
+// resolve_coverage and its derivative d(coverage)/dc, one-sided at the kinks:
+// nonzero d|c|/dc = +1 at c = 0 and 0 once clamped at |c| >= 1; even-odd +1
+// on the rising half of the period (m < 1), -1 on the falling half.
+__device__ __forceinline__ float resolve_coverage_d(float c, bool even_odd, float* dc) {
+    if (!even_odd) {
+        const float a = fabsf(c);
+        *dc = a < 1.0f ? (c >= 0.0f ? 1.0f : -1.0f) : 0.0f;
+        return fminf(1.0f, a);
+    }
+    const float m = c - 2.0f * floorf(c * 0.5f);
+    *dc = m < 1.0f ? 1.0f : -1.0f;
+    return fminf(1.0f, 1.0f - fabsf(1.0f - m));
 }
 
 }  // namespace pf

@@ -56,7 +56,38 @@ struct FrameDev {
     uint32_t* vis;               // [vis_cap] global tile indices
     Counters* counters;
     uint32_t dda_limit;
+    // Differentiable frames (diff != 0): FP32 fills, the curve parameters of
+    // every flattened line, and per visible (screen tile, path tile) entry the
+    // composite tape the adjoint reads back.
+    int diff;
+    float4*   fills_f;           // [fill_cap] tile-local FP32 fills
+    uint32_t* line_seg;          // [line_cap] global segment of each line
+    float2*   line_t;            // [line_cap] curve parameters of the line's ends
+    float*    tape_cov;          // [vis_cap * 256] resolved coverage of the entry
+    float*    tape_dprev;        // [vis_cap * 256] composite value below the entry
+    uint8_t*  tape_code;         // [vis_cap * 256] d(coverage)/d(mask): bits 0-1 own mask, 2-3 clip mask
 };
+
+#ifdef __CUDACC__
+__device__ __forceinline__ bool frame_ok(const FrameDev& f) {
+    return f.counters->tiles <= f.tile_cap && f.counters->columns <= f.col_cap;
+}
+
+// Scene of a global screen tile: the last scene of the frame whose first
+// screen tile is at or before it.
+__device__ __forceinline__ uint32_t scene_of_screen_tile(const FrameDev& f, uint32_t st_global) {
+    uint32_t lo = f.scene_begin, hi = f.scene_begin + f.scene_count;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (f.scenes[mid].screen_offset <= st_global) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+#endif
+
+// 2-bit derivative codes of the tape: 0 -> 0, 1 -> +1, 2 -> -1.
+__host__ __device__ __forceinline__ uint32_t enc_d(float d) { return d > 0.0f ? 1u : (d < 0.0f ? 2u : 0u); }
+__host__ __device__ __forceinline__ float dec_d(uint32_t c) { return c == 1u ? 1.0f : (c == 2u ? -1.0f : 0.0f); }
 
 // scan scratch
 struct ScanTemp { uint32_t* partials; uint32_t cap; };
@@ -99,5 +130,14 @@ void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s);
 // mode 0: RGBA8, 1: R8 single channel, 2: FP32 single channel
 void launch_composite(const FrameDev& f, int mode, void* out, const float4& background, cudaStream_t s);
 void launch_masks(const FrameDev& f, float* alpha_masks, float* tile_cov, cudaStream_t s);
+
+// Differentiable frames: the FP32 composite that records the tape, and the
+// adjoint (dL/dimage -> dL/dmask per alpha tile and dL/dalpha per draw path,
+// then dL/dmask -> dL/dpoints through every flattened line).
+void launch_composite_diff(const FrameDev& f, float* out, const float4& background, cudaStream_t s);
+void launch_composite_bwd(const FrameDev& f, const float* d_image, float* grad_mask, float* grad_alpha,
+                          cudaStream_t s);
+void launch_line_grad(const FrameDev& f, const float* grad_mask, float2* grad_points, cudaStream_t s);
+void launch_points_grad_transform(float2* grad_points, uint32_t n, const float* m4, cudaStream_t s);
 
 }  // namespace pf

@@ -42,10 +42,6 @@ __device__ __forceinline__ bool solid_occludes(int8_t b, bool even_odd) {
     return even_odd ? ((b & 1) != 0) : true;
 }
 
-__device__ __forceinline__ bool frame_ok(const FrameDev& f) {
-    return f.counters->tiles <= f.tile_cap && f.counters->columns <= f.col_cap;
-}
-
 __device__ __forceinline__ uint32_t upper_bound_u32(const uint32_t* a, uint32_t n, uint32_t v) {
     // first index i in [0, n) with a[i] > v
     uint32_t lo = 0, hi = n;
@@ -128,7 +124,11 @@ __global__ void k_propagate(FrameDev f, int clip_pass) {
             f.clips[g] = make_int4((int)kInvalid, 0, (int)kInvalid, 0);
         }
         f.tiles[g] = pack_tile(tx, ty, alpha, gp, color, ctrl, backdrop);
-        if (!is_clip && (f.path.paint[gp] >> 24) == 255u && alpha == kInvalid && solid_occludes(backdrop, even_odd)) {
+        // differentiable frames occlude with the FP32 paint alpha being optimised
+        const bool opaque = is_clip ? false
+                                    : (f.path.alpha_f ? f.path.alpha_f[f.path.draw_index[gp]] >= 1.0f
+                                                      : (f.path.paint[gp] >> 24) == 255u);
+        if (opaque && alpha == kInvalid && solid_occludes(backdrop, even_odd)) {
             uint32_t st;
             if (frame_screen_tile(f, f.scenes[f.path.scene[gp]], tx, ty, &st)) atomicMax(&f.zbuf[st], (int32_t)local);
         }
@@ -204,7 +204,9 @@ __device__ void warp_bitonic_sort(uint32_t* a, uint32_t n) {
 
 struct CovBuf { int acc[256]; int carry[256]; };
 
-// Accumulate the fills of alpha tile `alpha` into `buf` (one warp).
+// Accumulate the fills of alpha tile `alpha` into `buf` (one warp).  DIFF
+// reads the FP32 fills of differentiable frames.
+template <bool DIFF = false>
 __device__ __forceinline__ void warp_accumulate_tile(const FrameDev& f, uint32_t alpha, CovBuf& buf) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
@@ -220,9 +222,14 @@ __device__ __forceinline__ void warp_accumulate_tile(const FrameDev& f, uint32_t
         float x0 = 0.0f, y0 = 0.0f, x1 = 0.0f, y1 = 0.0f;
         int c0 = 0, ncol = 0;
         if (i < b1) {
-            const uint2 rec = f.fills[i];
-            x0 = (float)(rec.x & 0xffffu) * (1.0f / 256.0f); y0 = (float)(rec.x >> 16) * (1.0f / 256.0f);
-            x1 = (float)(rec.y & 0xffffu) * (1.0f / 256.0f); y1 = (float)(rec.y >> 16) * (1.0f / 256.0f);
+            if constexpr (DIFF) {
+                const float4 rec = f.fills_f[i];
+                x0 = rec.x; y0 = rec.y; x1 = rec.z; y1 = rec.w;
+            } else {
+                const uint2 rec = f.fills[i];
+                x0 = (float)(rec.x & 0xffffu) * (1.0f / 256.0f); y0 = (float)(rec.x >> 16) * (1.0f / 256.0f);
+                x1 = (float)(rec.y & 0xffffu) * (1.0f / 256.0f); y1 = (float)(rec.y >> 16) * (1.0f / 256.0f);
+            }
             if (x0 != x1) {
                 c0 = max((int)floorf(fminf(x0, x1)), 0);
                 const int c1 = min((int)ceilf(fmaxf(x0, x1)) - 1, 15);
@@ -319,15 +326,6 @@ __device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint
 // ---------------------------------------------------------------------------
 constexpr uint32_t kWarpListCap = 128;
 
-__device__ __forceinline__ uint32_t scene_of_screen_tile(const FrameDev& f, uint32_t st_global) {
-    uint32_t lo = f.scene_begin, hi = f.scene_begin + f.scene_count;  // last scene with offset <= st
-    while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (f.scenes[mid].screen_offset <= st_global) lo = mid; else hi = mid;
-    }
-    return lo;
-}
-
 template <int MODE, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out, float4 bg) {
     __shared__ WarpScratch scratch[WARPS];
@@ -423,6 +421,130 @@ void launch_composite(const FrameDev& f, int mode, void* out, const float4& bg, 
 }
 
 // ---------------------------------------------------------------------------
+// differentiable frames: FP32 composite that records the adjoint's tape
+// ---------------------------------------------------------------------------
+// Coverage of one path tile for this lane's 8 pixels with d(coverage)/d(mask)
+// codes: bits 0-1 for the mask of tile.alpha (own, or the clip's where the
+// draw tile borrowed it), bits 2-3 for the clip's mask of a combined tile.
+__device__ __forceinline__ void tile_coverage8_diff(const FrameDev& f, int4 rec, uint32_t g, WarpScratch& ws,
+                                                    float cov[8], uint32_t code[8]) {
+    const uint32_t gp = (uint32_t)rec.z;
+    const bool even_odd = (tile_ctrl(rec) & 0x2u) != 0;
+    const float bd = (float)tile_backdrop(rec);
+    bool combine = false;
+    int4 crec = make_int4(0, 0, 0, 0);
+    if (f.path.clip_gpath[gp] >= 0) {
+        crec = f.clips[g];
+        combine = (uint32_t)crec.x != kInvalid && (uint32_t)crec.z != kInvalid;
+    }
+    if (combine) {
+        // min(|d|, |s|) picks one mask per pixel (ties: the draw path's own)
+        int vd[8], vs[8];
+        warp_accumulate_tile<true>(f, (uint32_t)crec.x, ws.b0);
+        warp_accumulate_tile<true>(f, (uint32_t)crec.z, ws.b1);
+        warp_column_values(ws.b0, vd);
+        warp_column_values(ws.b1, vs);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const float wd = (float)vd[k] * kCovInvScale + (float)crec.y;
+            const float wc = (float)vs[k] * kCovInvScale + (float)crec.w;
+            const bool own = fabsf(wd) <= fabsf(wc);
+            float dc;
+            cov[k] = resolve_coverage_d(fminf(fabsf(wd), fabsf(wc)) + bd, even_odd, &dc);
+            const float dm = dc * ((own ? wd : wc) >= 0.0f ? 1.0f : -1.0f);
+            code[k] = own ? enc_d(dm) : (enc_d(dm) << 2);
+        }
+    } else if ((uint32_t)rec.y != kInvalid) {
+        int v[8];
+        warp_accumulate_tile<true>(f, (uint32_t)rec.y, ws.b0);
+        warp_column_values(ws.b0, v);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            float dc;
+            cov[k] = resolve_coverage_d((float)v[k] * kCovInvScale + bd, even_odd, &dc);
+            code[k] = enc_d(dc);
+        }
+    } else {
+        const float c = resolve_coverage(bd, even_odd);
+#pragma unroll
+        for (int k = 0; k < 8; k++) { cov[k] = c; code[k] = 0; }
+    }
+    __syncwarp();
+}
+
+// As k_composite in FP32 single-channel mode, with the paint alpha of the
+// differentiable frame.  Per visible entry e (the screen tile's list in draw
+// order, written back to vis) and pixel, the tape keeps the coverage, the
+// composite value below the entry and the coverage derivative codes.
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_composite_diff(FrameDev f, float* out, float4 bg) {
+    __shared__ WarpScratch scratch[WARPS];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t st = blockIdx.x * WARPS + wid;
+    if (st >= f.screen_count) return;
+    WarpScratch& ws = scratch[wid];
+
+    const SceneDev& sc = f.scenes[scene_of_screen_tile(f, f.screen_begin + st)];
+    const int4 s = sc.screen;
+    const int32_t sw = s.z - s.x;
+    const uint32_t lst = f.screen_begin + st - sc.screen_offset;
+    const int32_t tx = s.x + (int32_t)(lst % (uint32_t)sw), ty = s.y + (int32_t)(lst / (uint32_t)sw);
+    const int col = lane & 15, half = lane >> 4;
+
+    const bool ok = frame_ok(f) && f.counters->fills <= f.fill_cap && f.counters->visible <= f.vis_cap;
+    uint32_t n = 0, base = 0;
+    if (ok) { base = f.screen_base[st]; n = f.screen_base[st + 1] - base; }
+    if (n <= kWarpListCap) {
+        for (uint32_t i = lane; i < n; i += 32) ws.keys[i] = f.vis[base + i];
+        __syncwarp();
+        if (n > 1) {
+            warp_bitonic_sort(ws.keys, n);
+            for (uint32_t i = lane; i < n; i += 32) f.vis[base + i] = ws.keys[i];  // draw order for the adjoint
+        }
+    } else {
+        warp_bitonic_sort(f.vis + base, n);
+    }
+    __syncwarp();
+    const uint32_t* list = n <= kWarpListCap ? ws.keys : f.vis + base;
+
+    float d[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) d[k] = bg.w;
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t g = list[i];
+        const int4 rec = f.tiles[g];
+        float cov[8];
+        uint32_t code[8];
+        tile_coverage8_diff(f, rec, g, ws, cov, code);
+        const float pa = f.path.alpha_f[f.path.draw_index[(uint32_t)rec.z]];
+        const uint64_t t0 = (uint64_t)(base + i) * 256u + (uint32_t)(half * 128 + col);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            f.tape_cov[t0 + k * 16] = cov[k];
+            f.tape_dprev[t0 + k * 16] = d[k];
+            f.tape_code[t0 + k * 16] = (uint8_t)code[k];
+            const float a = pa * cov[k];
+            d[k] = a + d[k] * (1.0f - a);
+        }
+    }
+    const int X = tx * 16 + col;
+    if (X < sc.clip.x || X >= sc.clip.z) return;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int Y = ty * 16 + half * 8 + k;
+        if (Y < sc.clip.y || Y >= sc.clip.w) continue;
+        out[sc.out_offset + (uint64_t)(int64_t)(Y - sc.origin_y) * (uint64_t)(int64_t)sc.pitch +
+            (uint64_t)(int64_t)(X - sc.origin_x)] = d[k];
+    }
+}
+
+void launch_composite_diff(const FrameDev& f, float* out, const float4& bg, cudaStream_t s) {
+    if (f.screen_count == 0) return;
+    count_launch();
+    k_composite_diff<4><<<(f.screen_count + 3) / 4, 128, 0, s>>>(f, out, bg);
+}
+
+// ---------------------------------------------------------------------------
 // readback of raw alpha masks and resolved tile coverage (parity checks)
 // ---------------------------------------------------------------------------
 constexpr int kMaskWarps = 4;
@@ -432,7 +554,8 @@ __global__ void k_alpha_masks(FrameDev f, float* out) {
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t a = blockIdx.x * kMaskWarps + wid;
     if (a >= f.counters->alpha_tiles) return;
-    warp_accumulate_tile(f, a, scratch[wid].b0);
+    if (f.diff) warp_accumulate_tile<true>(f, a, scratch[wid].b0);
+    else warp_accumulate_tile<false>(f, a, scratch[wid].b0);
     int v[8];
     warp_column_values(scratch[wid].b0, v);
     const int col = lane & 15, half = lane >> 4;
@@ -446,7 +569,12 @@ __global__ void k_tile_cov(FrameDev f, float* out) {
     const uint32_t g = blockIdx.x * kMaskWarps + wid;
     if (g >= f.counters->tiles) return;
     float cov[8];
-    tile_coverage8(f, f.tiles[g], g, scratch[wid], cov);
+    if (f.diff) {
+        uint32_t code[8];
+        tile_coverage8_diff(f, f.tiles[g], g, scratch[wid], cov, code);
+    } else {
+        tile_coverage8(f, f.tiles[g], g, scratch[wid], cov);
+    }
     const int col = lane & 15, half = lane >> 4;
 #pragma unroll
     for (int k = 0; k < 8; k++) out[(uint64_t)g * 256 + (half * 8 + k) * 16 + col] = cov[k];

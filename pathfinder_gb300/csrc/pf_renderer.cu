@@ -120,6 +120,23 @@ struct PFCUDARenderer {
     // captured frame
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
+
+    // differentiable frames
+    uint32_t ND = 0;                   // draw paths of the batch
+    std::vector<float> draw_alpha;     // paint alpha / 255 per draw path (default alpha)
+    DevBuf<uint32_t> draw_index;       // [P] path -> draw path index (kInvalid for clip paths)
+    DevBuf<float> alpha_in;            // [ND] alpha of the current differentiable frame
+    DevBuf<float4> fills_f;
+    DevBuf<uint32_t> line_seg;
+    DevBuf<float2> line_t;
+    DevBuf<float> tape_cov, tape_dprev, grad_mask, grad_alpha_tmp;
+    DevBuf<uint8_t> tape_code;
+    bool diff_buffers = false;         // allocate the buffers above with the frame's
+    bool last_diff = false;            // the last enqueued frame was differentiable
+    bool diff_valid = false;           // PFCUDABackward may run on the last frame
+    Range diff_range;
+    bool diff_transformed = false;
+    float diff_m4[4] = {1, 0, 0, 1};
 };
 
 namespace {
@@ -158,8 +175,17 @@ Range make_range(const PFCUDARenderer* r, uint32_t s0, uint32_t count) {
     return g;
 }
 
-FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g) {
+FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool diff = false) {
     FrameDev f{};
+    f.diff = diff ? 1 : 0;
+    f.path.alpha_f = diff ? r->alpha_in.p : nullptr;
+    f.path.draw_index = r->draw_index.p;
+    f.fills_f = r->fills_f.p;
+    f.line_seg = r->line_seg.p;
+    f.line_t = r->line_t.p;
+    f.tape_cov = r->tape_cov.p;
+    f.tape_dprev = r->tape_dprev.p;
+    f.tape_code = r->tape_code.p;
     f.pts = transformed ? r->pts_t.p : r->pts.p;
     f.segs = r->segs.p;
     f.seg_begin = g.g0;
@@ -227,6 +253,12 @@ cudaError_t ensure_frame_buffers(PFCUDARenderer* r) {
         (e = r->vis.ensure((size_t)r->vis_cap + 1)) || (e = r->zbuf.ensure(ST)) || (e = r->screen_cnt.ensure(ST)) ||
         (e = r->screen_base.ensure(ST)) || (e = r->path_tiles.ensure(P)) || (e = r->path_cols.ensure(P)))
         return e;
+    if (r->diff_buffers) {
+        const size_t V = ((size_t)r->vis_cap + 1) * 256;
+        if ((e = r->fills_f.ensure(F)) || (e = r->line_seg.ensure(L)) || (e = r->line_t.ensure(L)) ||
+            (e = r->tape_cov.ensure(V)) || (e = r->tape_dprev.ensure(V)) || (e = r->tape_code.ensure(V)))
+            return e;
+    }
     size_t nmax = std::max<size_t>({(size_t)r->tile_cap, (size_t)r->S, (size_t)r->screen_total, (size_t)r->nord,
                                     (size_t)r->line_cap, (size_t)r->P}) + 1;
     return r->scan_partials.ensure(kMaxScanLanes * (nmax / 2048 + 2));
@@ -239,8 +271,11 @@ bool is_identity(const PFCUDABuildOptions* o) {
            t.vector.y == 0.0f;
 }
 
-// Enqueue one frame over range g.  mode: PF_CUDA_FORMAT_*, or -1 for no composite.
-cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev, const Range& g) {
+// Enqueue one frame over range g.  mode: PF_CUDA_FORMAT_*, or -1 for no
+// composite.  diff: a differentiable frame (FP32 fills, FP32 output and the
+// adjoint's tape; mode is ignored).
+cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev, const Range& g,
+                          bool diff = false) {
     cudaStream_t s = r->stream;
     bool transformed = !is_identity(opts);
     cudaError_t e;
@@ -250,7 +285,9 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
                        opts->transform.vector.x, opts->transform.vector.y};
         launch_transform(r->pts.p, r->pts_t.p, r->NP, m6, s);
     }
-    FrameDev f = frame_dev(r, transformed, g);
+    r->last_diff = diff;
+    if (!diff) r->diff_valid = false;
+    FrameDev f = frame_dev(r, transformed, g, diff);
     ScanTemp tmp{r->scan_partials.p, (uint32_t)r->scan_partials.cap};
     Counters* c = r->counters.p;
     auto mark = [&](int stage) {
@@ -292,12 +329,13 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
                 tmp, s);
     launch_visible(f, true, s);
     mark(7);
-    if (mode >= 0) {
+    if (mode >= 0 || diff) {
         float4 bg = make_float4(0, 0, 0, 0);
         if (r->options.has_background_color)
             bg = make_float4(r->options.background_color.r, r->options.background_color.g,
                              r->options.background_color.b, r->options.background_color.a);
-        launch_composite(f, mode, out_dev, bg, s);
+        if (diff) launch_composite_diff(f, (float*)out_dev, bg, s);
+        else launch_composite(f, mode, out_dev, bg, s);
     }
     mark(8);
     r->launches = launch_counter() - before;
@@ -362,13 +400,14 @@ bool valid_range(const PFCUDARenderer* r, uint32_t first, uint32_t count) {
 }
 
 // Run one frame synchronously with regrow-and-retry.
-int32_t run_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev, const Range& g) {
+int32_t run_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev, const Range& g,
+                  bool diff = false) {
     if (!r->has_scene) return PF_CUDA_ERR_NO_SCENE;
     r->last = g;
     for (int attempt = 0; attempt < 4; attempt++) {
         PF_TRY(ensure_frame_buffers(r));
         PF_TRY(cudaEventRecord(r->ev0, r->stream));
-        PF_TRY(enqueue_frame(r, opts, mode, out_dev, g));
+        PF_TRY(enqueue_frame(r, opts, mode, out_dev, g, diff));
         PF_TRY(cudaEventRecord(r->ev1, r->stream));
         PF_TRY(cudaMemcpyAsync(r->h_counters, r->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, r->stream));
         PF_TRY(cudaStreamSynchronize(r->stream));
@@ -462,6 +501,9 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->col_backdrop.release(); r->zbuf.release(); r->fills.release(); r->fill_e.release(); r->tiles.release();
     r->clips.release(); r->screen_cnt.release(); r->screen_base.release(); r->vis.release();
     r->scan_partials.release(); r->counters.release(); r->out_tmp.release();
+    r->draw_index.release(); r->alpha_in.release(); r->fills_f.release(); r->line_seg.release();
+    r->line_t.release(); r->tape_cov.release(); r->tape_dprev.release(); r->tape_code.release();
+    r->grad_mask.release(); r->grad_alpha_tmp.release();
     if (r->h_counters) cudaFreeHost(r->h_counters);
     if (r->ev0) cudaEventDestroy(r->ev0);
     if (r->ev1) cudaEventDestroy(r->ev1);
@@ -513,6 +555,8 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
         scene_of((size_t)P);
     std::vector<int32_t> clip((size_t)P);
     std::vector<uint8_t> rule((size_t)P), isclip((size_t)P);
+    std::vector<uint32_t> draw_index((size_t)P, kInvalid);
+    std::vector<float> draw_alpha;
     r->scenes.assign(scene_count, SceneInfo());
     r->scenes_host.assign(scene_count, SceneDev{});
     uint32_t point_base = 0, contour_base = 0, gp = 0, screen_total = 0;
@@ -560,6 +604,10 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
             rule[gp] = p.fill_rule;
             isclip[gp] = c ? 1 : 0;
             scene_of[gp] = k;
+            if (!c) {
+                draw_index[gp] = (uint32_t)draw_alpha.size();
+                draw_alpha.push_back((float)p.paint.a / 255.0f);
+            }
         }
         SceneDev& d = r->scenes_host[k];
         d.view_box = make_float4(sc.view_box.origin.x, sc.view_box.origin.y, sc.view_box.lower_right.x,
@@ -590,6 +638,7 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
         (e = r->contour_seg_base.ensure(nord + 1)) || (e = r->first_ord.ensure(Pz + 1)) || (e = r->paint.ensure(Pz)) ||
         (e = r->local_index.ensure(Pz)) || (e = r->scene_of.ensure(Pz)) || (e = r->clip_gpath.ensure(Pz)) ||
         (e = r->rule.ensure(Pz)) || (e = r->is_clip.ensure(Pz)) || (e = r->tile_rect.ensure(Pz)) ||
+        (e = r->draw_index.ensure(Pz)) ||
         (e = r->tile_offset.ensure(Pz + 1)) || (e = r->col_offset.ensure(Pz + 1)) ||
         (e = r->scenes_dev.ensure(scene_count)) || (e = r->scan_partials.ensure(nord / 2048 + 2)))
         return cuda_status(e);
@@ -616,6 +665,7 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
         PF_TRY(cudaMemcpyAsync(r->clip_gpath.p, clip.data(), sizeof(int32_t) * Pz, cudaMemcpyHostToDevice, s));
         PF_TRY(cudaMemcpyAsync(r->rule.p, rule.data(), Pz, cudaMemcpyHostToDevice, s));
         PF_TRY(cudaMemcpyAsync(r->is_clip.p, isclip.data(), Pz, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->draw_index.p, draw_index.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
     }
     // Segment packing on the GPU (SegmentsD3D11::add_path): count, scan, emit.
     PF_TRY(cudaMemsetAsync(r->counters.p, 0, sizeof(Counters), s));
@@ -642,6 +692,9 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
     PF_TRY(upload_scene_records(r));
 
     r->P = (uint32_t)P;
+    r->ND = (uint32_t)draw_alpha.size();
+    r->draw_alpha.swap(draw_alpha);
+    r->diff_valid = false;
     r->NP = (uint32_t)np_total;
     r->NC = (uint32_t)nc_total;
     r->nord = nord;
@@ -846,7 +899,7 @@ int32_t PFCUDAReadMasks(PFCUDARendererRef r, float* out_alpha, uint64_t alpha_ca
     PF_TRY(cudaSetDevice(r->device));
     uint64_t A = r->stats.alpha_tile_count, T = r->stats.tile_count;
     if ((out_alpha && alpha_cap < A) || (out_tile && tile_cap < T)) return PF_CUDA_ERR_CAPACITY;
-    FrameDev f = frame_dev(r, false, r->last);
+    FrameDev f = frame_dev(r, false, r->last, r->last_diff);
     DevBuf<float> a, t;
     if (out_alpha) PF_TRY(a.ensure(A * 256 + 1));
     if (out_tile) PF_TRY(t.ensure(T * 256 + 1));
@@ -869,6 +922,7 @@ int32_t PFCUDAReadRecords(PFCUDARendererRef r, PFCUDAFill* fills, uint32_t* fill
     cudaStream_t s = r->stream;
     const Range& g = r->last;
     const uint64_t F = r->stats.fill_count, T = r->stats.tile_count, NPth = g.p1 - g.p0, NST = g.st1 - g.st0;
+    if (fills && r->last_diff) return PF_CUDA_ERR_INVALID;  // differentiable frames keep FP32 fills only
     if ((fills || fill_tile) && fill_capacity < F) return PF_CUDA_ERR_CAPACITY;
     if ((tiles || clips) && tile_capacity < T) return PF_CUDA_ERR_CAPACITY;
     if ((path_tile_offsets || path_tile_rects) && path_capacity < NPth + 1) return PF_CUDA_ERR_CAPACITY;
@@ -949,6 +1003,102 @@ int32_t PFCUDAExclusiveScan(PFCUDARendererRef r, const uint32_t* in, uint32_t* o
     launch_scan(in, out, nullptr, n, n, 0, nullptr, tmp, r->stream);
     PF_TRY(cudaGetLastError());
     PF_TRY(cudaStreamSynchronize(r->stream));
+    return PF_CUDA_OK;
+}
+
+int32_t PFCUDASetPoints(PFCUDARendererRef r, const PFVector2F* points, uint64_t count, int32_t memory) {
+    if (!r) return PF_CUDA_ERR_INVALID;
+    if (!r->has_scene) return PF_CUDA_ERR_NO_SCENE;
+    if (count != r->NP || (count && !points)) return PF_CUDA_ERR_INVALID;
+    if (memory != PF_MEMORY_HOST && memory != PF_MEMORY_DEVICE) return PF_CUDA_ERR_INVALID;
+    PF_TRY(cudaSetDevice(r->device));
+    r->diff_valid = false;
+    if (count)
+        PF_TRY(cudaMemcpyAsync(r->pts.p, points, sizeof(float2) * count,
+                               memory == PF_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                               r->stream));
+    if (memory == PF_MEMORY_HOST) PF_TRY(cudaStreamSynchronize(r->stream));  // the caller may reuse its buffer
+    return PF_CUDA_OK;
+}
+
+static int32_t diff_prologue(PFCUDARendererRef r, uint32_t first, uint32_t count, int32_t width, int32_t height,
+                             const float* draw_alpha, float* out_device) {
+    if (!r || !out_device) return PF_CUDA_ERR_INVALID;
+    if (!valid_range(r, first, count)) return r->has_scene ? PF_CUDA_ERR_INVALID : PF_CUDA_ERR_NO_SCENE;
+    PF_TRY(cudaSetDevice(r->device));
+    if (width > 0 || height > 0) {
+        bool changed = false;
+        int32_t rc = prepare_plain_targets(r, width, height, &changed);
+        if (rc) return rc;
+        if (changed) PF_TRY(upload_scene_records(r));
+    }
+    PF_TRY(r->alpha_in.ensure((size_t)r->ND + 1));
+    if (r->ND) {
+        if (draw_alpha)
+            PF_TRY(cudaMemcpyAsync(r->alpha_in.p, draw_alpha, sizeof(float) * r->ND, cudaMemcpyDeviceToDevice, r->stream));
+        else
+            PF_TRY(cudaMemcpyAsync(r->alpha_in.p, r->draw_alpha.data(), sizeof(float) * r->ND, cudaMemcpyHostToDevice,
+                                   r->stream));
+    }
+    r->diff_buffers = true;
+    r->diff_valid = false;
+    return PF_CUDA_OK;
+}
+
+static void diff_epilogue(PFCUDARendererRef r, const PFCUDABuildOptions* options, const Range& g) {
+    r->diff_valid = true;
+    r->diff_range = g;
+    r->diff_transformed = !is_identity(options);
+    if (r->diff_transformed) {
+        r->diff_m4[0] = options->transform.m00; r->diff_m4[1] = options->transform.m01;
+        r->diff_m4[2] = options->transform.m10; r->diff_m4[3] = options->transform.m11;
+    }
+}
+
+int32_t PFCUDARenderDiff(PFCUDARendererRef r, const PFCUDABuildOptions* options, uint32_t first, uint32_t count,
+                         int32_t width, int32_t height, const float* draw_alpha, float* out_device) {
+    int32_t rc = diff_prologue(r, first, count, width, height, draw_alpha, out_device);
+    if (rc != PF_CUDA_OK) return rc;
+    const Range g = make_range(r, first, count);
+    rc = run_frame(r, options, PF_CUDA_FORMAT_F32, out_device, g, true);
+    if (rc != PF_CUDA_OK) return rc;
+    diff_epilogue(r, options, g);
+    return PF_CUDA_OK;
+}
+
+int32_t PFCUDARenderDiffAsync(PFCUDARendererRef r, const PFCUDABuildOptions* options, uint32_t first,
+                              uint32_t count, int32_t width, int32_t height, const float* draw_alpha,
+                              float* out_device) {
+    int32_t rc = diff_prologue(r, first, count, width, height, draw_alpha, out_device);
+    if (rc != PF_CUDA_OK) return rc;
+    const Range g = make_range(r, first, count);
+    r->last = g;
+    PF_TRY(ensure_frame_buffers(r));
+    PF_TRY(enqueue_frame(r, options, PF_CUDA_FORMAT_F32, out_device, g, true));
+    diff_epilogue(r, options, g);
+    return PF_CUDA_OK;
+}
+
+int32_t PFCUDABackward(PFCUDARendererRef r, const float* d_image, PFVector2F* d_points, float* d_alpha) {
+    if (!r || !d_image || !d_points) return PF_CUDA_ERR_INVALID;
+    if (!r->diff_valid) return PF_CUDA_ERR_INVALID;
+    PF_TRY(cudaSetDevice(r->device));
+    cudaStream_t s = r->stream;
+    const uint64_t before = launch_counter();
+    PF_TRY(r->grad_mask.ensure(((size_t)r->tile_cap + 1) * 256));  // alpha ids < tiles <= tile_cap
+    if (r->NP) PF_TRY(cudaMemsetAsync(d_points, 0, sizeof(float2) * r->NP, s));
+    float* ga = d_alpha;
+    if (!ga) {
+        PF_TRY(r->grad_alpha_tmp.ensure((size_t)r->ND + 1));
+        ga = r->grad_alpha_tmp.p;
+    }
+    if (r->ND) PF_TRY(cudaMemsetAsync(ga, 0, sizeof(float) * r->ND, s));
+    FrameDev f = frame_dev(r, r->diff_transformed, r->diff_range, true);
+    launch_composite_bwd(f, d_image, r->grad_mask.p, ga, s);
+    launch_line_grad(f, r->grad_mask.p, (float2*)d_points, s);
+    if (r->diff_transformed) launch_points_grad_transform((float2*)d_points, r->NP, r->diff_m4, s);
+    PF_TRY(cudaGetLastError());
+    r->stats.kernel_launches = launch_counter() - before;
     return PF_CUDA_OK;
 }
 

@@ -415,14 +415,23 @@ __global__ void k_check_lines(FrameDev f) {
     }
 }
 
+// DIFF also records each line's segment and curve-parameter interval: the leaf
+// at split path `addr` of depth d covers t in [addr, addr + 1) / 2^d.  The
+// adjoint holds these subdivisions fixed.
+template <bool DIFF>
 __global__ void __launch_bounds__(256) k_flatten_emit(FrameDev f) {
     uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= f.seg_count || f.counters->lines > f.line_cap) return;
     const SegRec sr = f.segs[f.seg_begin + s];
     uint32_t l = f.seg_line_base[s];
-    flatten_segment(f.pts, sr, [&](const Line& ln, uint32_t, int) {
+    flatten_segment(f.pts, sr, [&](const Line& ln, uint32_t addr, int d) {
         f.lines[l] = make_float4(ln.fx, ln.fy, ln.tx, ln.ty);
         f.line_path[l] = (uint32_t)sr.w;
+        if constexpr (DIFF) {
+            const float step = ldexpf(1.0f, -d), t0 = (float)addr * step;
+            f.line_seg[l] = f.seg_begin + s;
+            f.line_t[l] = make_float2(t0, t0 + step);
+        }
         l++;
     }, &f.counters->status);
 }
@@ -430,10 +439,13 @@ __global__ void __launch_bounds__(256) k_flatten_emit(FrameDev f) {
 void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     if (f.seg_count == 0) return;
     const int ft = f.tune.flatten_threads;
-    { count_launch(); k_flatten_count<<<(f.seg_count + ft - 1) / ft, ft, 0, s>>>(f); }
+    const uint32_t blocks = (f.seg_count + ft - 1) / ft;
+    { count_launch(); k_flatten_count<<<blocks, ft, 0, s>>>(f); }
     launch_scan(f.seg_line_count, f.seg_line_base, nullptr, f.seg_count, f.seg_count, 0, &f.counters->lines, tmp, s);
     { count_launch(); k_check_lines<<<1, 1, 0, s>>>(f); }
-    { count_launch(); k_flatten_emit<<<(f.seg_count + ft - 1) / ft, ft, 0, s>>>(f); }
+    count_launch();
+    if (f.diff) k_flatten_emit<true><<<blocks, ft, 0, s>>>(f);
+    else k_flatten_emit<false><<<blocks, ft, 0, s>>>(f);
 }
 
 // ---------------------------------------------------------------------------
@@ -463,7 +475,8 @@ struct CountSink {
     int32_t* tile_delta;
     int32_t* col_backdrop;
     uint32_t n;
-    __device__ __forceinline__ void fill(uint2, uint32_t g) {
+    template <class Rec>
+    __device__ __forceinline__ void fill(Rec, uint32_t g) {
         n++;
         atomicAdd(&tile_fill_count[g], 1u);  // lanes rarely share a tile: aggregation costs more
     }
@@ -477,6 +490,7 @@ struct CountSink {
     }
 };
 
+template <bool DIFF>
 __global__ void __launch_bounds__(512) k_bin_count(FrameDev f) {
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     const uint32_t L = line_total(f);
@@ -484,7 +498,7 @@ __global__ void __launch_bounds__(512) k_bin_count(FrameDev f) {
         const float4 ln = f.lines[l];
         const PathCtx pc = path_ctx(f, f.line_path[l]);
         CountSink sink{&pc, f.tile_fill_count, f.tile_delta, f.col_backdrop, 0};
-        dda_line(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+        dda_line<DIFF>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
         f.line_fill_count[l] = sink.n;
     }
 }
@@ -505,6 +519,20 @@ struct EmitSink {
     __device__ __forceinline__ void backdrop(int32_t, int32_t, int32_t) {}
 };
 
+// FP32 fills of differentiable frames (no emission index: nothing reads it).
+struct EmitSinkF {
+    float4* fills;
+    const uint32_t* tile_fill_base;
+    uint32_t* cursor;
+    uint32_t fill_cap;
+    __device__ __forceinline__ void fill(float4 rec, uint32_t g) {
+        const uint32_t slot = tile_fill_base[g] + atomicSub(&cursor[g], 1u) - 1u;
+        if (slot < fill_cap) fills[slot] = rec;
+    }
+    __device__ __forceinline__ void backdrop(int32_t, int32_t, int32_t) {}
+};
+
+template <bool DIFF>
 __global__ void __launch_bounds__(512) k_bin_emit(FrameDev f) {
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     if (f.counters->fills > f.fill_cap) return;
@@ -513,13 +541,20 @@ __global__ void __launch_bounds__(512) k_bin_emit(FrameDev f) {
         if (f.line_fill_count[l] == 0) continue;
         const float4 ln = f.lines[l];
         const PathCtx pc = path_ctx(f, f.line_path[l]);
-        EmitSink sink{f.fills, f.fill_e, f.tile_fill_base, f.tile_fill_count, f.fill_cap, f.line_fill_base[l]};
-        dda_line(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+        if constexpr (DIFF) {
+            EmitSinkF sink{f.fills_f, f.tile_fill_base, f.tile_fill_count, f.fill_cap};
+            dda_line<true>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+        } else {
+            EmitSink sink{f.fills, f.fill_e, f.tile_fill_base, f.tile_fill_count, f.fill_cap, f.line_fill_base[l]};
+            dda_line(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+        }
     }
 }
 
 void launch_bin_count(const FrameDev& f, cudaStream_t s) {
-    { count_launch(); k_bin_count<<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f); }
+    count_launch();
+    if (f.diff) k_bin_count<true><<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f);
+    else k_bin_count<false><<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f);
 }
 
 __global__ void k_check_fills(FrameDev f) {
@@ -532,7 +567,9 @@ __global__ void k_check_fills(FrameDev f) {
 
 void launch_bin_emit(const FrameDev& f, cudaStream_t s) {
     { count_launch(); k_check_fills<<<1, 1, 0, s>>>(f); }
-    { count_launch(); k_bin_emit<<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f); }
+    count_launch();
+    if (f.diff) k_bin_emit<true><<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f);
+    else k_bin_emit<false><<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f);
 }
 
 }  // namespace pf

@@ -267,6 +267,49 @@ class Renderer:
                                             C.byref(t)), "PFCUDAAutotune")
         return {k: getattr(t, k) for k, _ in t._fields_}
 
+    # --- differentiable frames ----------------------------------------------
+    def set_points(self, points) -> None:
+        """PFCUDASetPoints: replace every uploaded point ([N, 2] float32, host
+        array or CUDA tensor, batch order) without re-uploading the scene."""
+        p, mem = _ptr(points)
+        n = int(points.shape[0])
+        _abi.check(self._lib.PFCUDASetPoints(self._h, C.c_void_p(p), n, mem), "PFCUDASetPoints")
+
+    def render_diff(self, out, first: int = 0, count: int = 1, width: int = 0, height: int = 0, alpha=None,
+                    options: BuildOptions | None = None, sync: bool = True):
+        """PFCUDARenderDiff (sync) or PFCUDARenderDiffAsync into the float32
+        CUDA tensor `out`.  `alpha`: CUDA float32 tensor, one value per draw
+        path of the uploaded batch (None: paint alpha).  width/height > 0 place
+        scenes without a target into a width x height image."""
+        p, mem = _ptr(out)
+        if mem != _abi.PF_MEMORY_DEVICE:
+            raise ValueError("differentiable frames render into device memory")
+        ap = 0
+        if alpha is not None:
+            ap, amem = _ptr(alpha)
+            if amem != _abi.PF_MEMORY_DEVICE:
+                raise ValueError("alpha must be a CUDA tensor")
+        bo = (options or BuildOptions()).to_c()
+        fn = self._lib.PFCUDARenderDiff if sync else self._lib.PFCUDARenderDiffAsync
+        _abi.check(fn(self._h, C.byref(bo), first, count, width, height, C.c_void_p(ap) if ap else None,
+                      C.c_void_p(p)), "PFCUDARenderDiff")
+        return out
+
+    def backward(self, d_image, d_points, d_alpha=None) -> None:
+        """PFCUDABackward of the last render_diff: writes dL/dpoints ([N, 2]
+        CUDA float32) and dL/dalpha (per draw path, optional)."""
+        gi, m0 = _ptr(d_image)
+        gp, m1 = _ptr(d_points)
+        ga = 0
+        if d_alpha is not None:
+            ga, m2 = _ptr(d_alpha)
+            if m2 != _abi.PF_MEMORY_DEVICE:
+                raise ValueError("d_alpha must be a CUDA tensor")
+        if m0 != _abi.PF_MEMORY_DEVICE or m1 != _abi.PF_MEMORY_DEVICE:
+            raise ValueError("the adjoint works on CUDA tensors")
+        _abi.check(self._lib.PFCUDABackward(self._h, C.c_void_p(gi), C.c_void_p(gp), C.c_void_p(ga) if ga else None),
+                   "PFCUDABackward")
+
     def stats(self) -> RenderStats:
         s = _abi.PFCUDARenderStats()
         _abi.check(self._lib.PFCUDAGetStats(self._h, C.byref(s)), "PFCUDAGetStats")
