@@ -79,8 +79,9 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite_bwd(FrameDev f, const 
         float ga = 0.0f;
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            const float c = f.tape_cov[t0 + k * 16], dprev = f.tape_dprev[t0 + k * 16];
-            const uint32_t code = f.tape_code[t0 + k * 16];
+            const uint32_t tw = f.tape[t0 + k * 16];
+            const float c = tape_cov(tw), dprev = tape_dprev(tw);
+            const uint32_t code = tape_code(tw);
             const float dlda = G[k] * (1.0f - dprev);
             ga += dlda * c;
             const float dm = dlda * pa;

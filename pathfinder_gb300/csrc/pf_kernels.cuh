@@ -63,10 +63,26 @@ struct FrameDev {
     float4*   fills_f;           // [fill_cap] tile-local FP32 fills
     uint32_t* line_seg;          // [line_cap] global segment of each line
     float2*   line_t;            // [line_cap] curve parameters of the line's ends
-    float*    tape_cov;          // [vis_cap * 256] resolved coverage of the entry
-    float*    tape_dprev;        // [vis_cap * 256] composite value below the entry
-    uint8_t*  tape_code;         // [vis_cap * 256] d(coverage)/d(mask): bits 0-1 own mask, 2-3 clip mask
+    uint32_t* tape;              // [vis_cap * 256] packed per pixel, see tape_pack
 };
+
+// One tape word per (visible entry, pixel): coverage c and the composite
+// value d below the entry as 14-bit unorms (bits 0-13, 16-29), and the 2-bit
+// derivative codes of dc/d(mask) (bits 14-15: the mask in tile.alpha, bits
+// 30-31: the clip's mask of a combined tile).
+constexpr float kTapeScale = 16383.0f;
+__host__ __device__ __forceinline__ uint32_t tape_q(float v) {
+    v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+    return (uint32_t)(v * kTapeScale + 0.5f);
+}
+__host__ __device__ __forceinline__ uint32_t tape_pack(float cov, float dprev, uint32_t code) {
+    return tape_q(cov) | ((code & 3u) << 14) | (tape_q(dprev) << 16) | ((code >> 2) << 30);
+}
+__host__ __device__ __forceinline__ float tape_cov(uint32_t t) { return (float)(t & 0x3fffu) * (1.0f / kTapeScale); }
+__host__ __device__ __forceinline__ float tape_dprev(uint32_t t) {
+    return (float)((t >> 16) & 0x3fffu) * (1.0f / kTapeScale);
+}
+__host__ __device__ __forceinline__ uint32_t tape_code(uint32_t t) { return ((t >> 14) & 3u) | ((t >> 30) << 2); }
 
 #ifdef __CUDACC__
 __device__ __forceinline__ bool frame_ok(const FrameDev& f) {

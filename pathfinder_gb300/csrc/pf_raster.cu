@@ -520,9 +520,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite_diff(FrameDev f, float
         const uint64_t t0 = (uint64_t)(base + i) * 256u + (uint32_t)(half * 128 + col);
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            f.tape_cov[t0 + k * 16] = cov[k];
-            f.tape_dprev[t0 + k * 16] = d[k];
-            f.tape_code[t0 + k * 16] = (uint8_t)code[k];
+            f.tape[t0 + k * 16] = tape_pack(cov[k], d[k], code[k]);
             const float a = pa * cov[k];
             d[k] = a + d[k] * (1.0f - a);
         }

@@ -129,8 +129,8 @@ struct PFCUDARenderer {
     DevBuf<float4> fills_f;
     DevBuf<uint32_t> line_seg;
     DevBuf<float2> line_t;
-    DevBuf<float> tape_cov, tape_dprev, grad_mask, grad_alpha_tmp;
-    DevBuf<uint8_t> tape_code;
+    DevBuf<uint32_t> tape;
+    DevBuf<float> grad_mask, grad_alpha_tmp;
     bool diff_buffers = false;         // allocate the buffers above with the frame's
     bool last_diff = false;            // the last enqueued frame was differentiable
     bool diff_valid = false;           // PFCUDABackward may run on the last frame
@@ -183,9 +183,7 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.fills_f = r->fills_f.p;
     f.line_seg = r->line_seg.p;
     f.line_t = r->line_t.p;
-    f.tape_cov = r->tape_cov.p;
-    f.tape_dprev = r->tape_dprev.p;
-    f.tape_code = r->tape_code.p;
+    f.tape = r->tape.p;
     f.pts = transformed ? r->pts_t.p : r->pts.p;
     f.segs = r->segs.p;
     f.seg_begin = g.g0;
@@ -256,7 +254,7 @@ cudaError_t ensure_frame_buffers(PFCUDARenderer* r) {
     if (r->diff_buffers) {
         const size_t V = ((size_t)r->vis_cap + 1) * 256;
         if ((e = r->fills_f.ensure(F)) || (e = r->line_seg.ensure(L)) || (e = r->line_t.ensure(L)) ||
-            (e = r->tape_cov.ensure(V)) || (e = r->tape_dprev.ensure(V)) || (e = r->tape_code.ensure(V)))
+            (e = r->tape.ensure(V)))
             return e;
     }
     size_t nmax = std::max<size_t>({(size_t)r->tile_cap, (size_t)r->S, (size_t)r->screen_total, (size_t)r->nord,
@@ -502,7 +500,7 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->clips.release(); r->screen_cnt.release(); r->screen_base.release(); r->vis.release();
     r->scan_partials.release(); r->counters.release(); r->out_tmp.release();
     r->draw_index.release(); r->alpha_in.release(); r->fills_f.release(); r->line_seg.release();
-    r->line_t.release(); r->tape_cov.release(); r->tape_dprev.release(); r->tape_code.release();
+    r->line_t.release(); r->tape.release();
     r->grad_mask.release(); r->grad_alpha_tmp.release();
     if (r->h_counters) cudaFreeHost(r->h_counters);
     if (r->ev0) cudaEventDestroy(r->ev0);

@@ -230,9 +230,13 @@ class Renderer:
 
     def graph_capture(self, batch, out, fmt: int = _abi.PF_CUDA_FORMAT_RGBA8, first: int = 0,
                       count: int | None = None, options: BuildOptions | None = None) -> None:
-        """Capture one frame of the batch range into a CUDA graph."""
-        self.upload_batch(batch)
-        count = len(batch) - first if count is None else count
+        """Capture one frame of the batch range into a CUDA graph (batch=None:
+        the scene(s) already uploaded, with the targets of their last frame)."""
+        if batch is not None:
+            self.upload_batch(batch)
+            count = len(batch) - first if count is None else count
+        elif count is None:
+            count = 1
         p, _ = _ptr(out)
         bo = (options or BuildOptions()).to_c()
         _abi.check(self._lib.PFCUDAGraphCapture(self._h, C.byref(bo), first, count, fmt, C.c_void_p(p)),
