@@ -195,7 +195,7 @@ __device__ __forceinline__ bool make_fill_f(const PathCtx& pc, Line s, int32_t t
     const float ulx = (float)tx * 16.0f, uly = (float)ty * 16.0f;
     rec = make_float4(fminf(fmaxf(s.fx - ulx, 0.0f), 16.0f), fminf(fmaxf(s.fy - uly, 0.0f), 16.0f),
                       fminf(fmaxf(s.tx - ulx, 0.0f), 16.0f), fminf(fmaxf(s.ty - uly, 0.0f), 16.0f));
-    if (rec.x == rec.z) return false;
+    if (!(fabsf(rec.x - rec.z) >= 1e-7f)) return false;  // width below 1e-7 px: area below 2e-6 px^2
     g = pc.tile_base + (uint32_t)(tx - pc.minx) + (uint32_t)(pc.maxx - pc.minx) * (uint32_t)(ty - pc.miny);
     return true;
 }
@@ -346,11 +346,12 @@ __device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Em
 constexpr float kCovScale = 4194304.0f;      // 2^22
 constexpr float kCovInvScale = 1.0f / 4194304.0f;
 
-// Accumulate the part of a fill (x0,y0)->(x1,y1) (tile pixels, x0 != x1)
-// that lies in pixel column px into acc[row][col] and carry[row][col].
-__device__ __forceinline__ void accumulate_fill_column(float x0, float y0, float x1, float y1, int px, int* acc,
+// Accumulate the part of a fill (x0,y0)->(x1,y1) (tile pixels, x0 != x1,
+// slope = dy/dx) that lies in pixel column px into acc[row][col] and
+// carry[row][col].  The row split uses the fast division: its relative error
+// (~2^-22) is at the level of the fixed-point accumulation.
+__device__ __forceinline__ void accumulate_fill_column(float x0, float y0, float x1, float slope, int px, int* acc,
                                                        int* carry) {
-    const float slope = (y1 - y0) / (x1 - x0);
     const float lo = (float)px, hi = (float)(px + 1);
     const float xa = fminf(fmaxf(x0, lo), hi), xb = fminf(fmaxf(x1, lo), hi);
     const float w = xa - xb;  // oriented x-extent (window.x - window.y)
@@ -359,14 +360,14 @@ __device__ __forceinline__ void accumulate_fill_column(float x0, float y0, float
     float ylo = fminf(ya, yb), yhi = fmaxf(ya, yb);
     ylo = fminf(fmaxf(ylo, 0.0f), 16.0f);
     yhi = fminf(fmaxf(yhi, 0.0f), 16.0f);
-    if (yhi - ylo <= 0.0f) {
+    if (!(yhi - ylo > 1e-6f)) {  // flat piece (and no division by a vanishing height)
         const int r = (int)floorf(ylo);
         if (r > 15) return;
         atomicAdd(&acc[r * 16 + px], __float2int_rn(w * ((float)(r + 1) - ylo) * kCovScale));
         if (r + 1 < 16) atomicAdd(&carry[(r + 1) * 16 + px], __float2int_rn(w * kCovScale));
         return;
     }
-    const float inv_h = 1.0f / (yhi - ylo);
+    const float inv_h = __fdividef(1.0f, yhi - ylo);
     const int r0 = (int)floorf(ylo), r1 = min((int)floorf(yhi), 15);
     for (int r = r0; r <= r1; r++) {
         const float yt = fmaxf(ylo, (float)r), yb2 = fminf(yhi, (float)(r + 1));
@@ -376,45 +377,6 @@ __device__ __forceinline__ void accumulate_fill_column(float x0, float y0, float
         const float a = wr * ((float)(r + 1) - 0.5f * (yt + yb2));
         atomicAdd(&acc[r * 16 + px], __float2int_rn(a * kCovScale));
         if (r + 1 < 16) atomicAdd(&carry[(r + 1) * 16 + px], __float2int_rn(wr * kCovScale));
-    }
-}
-
-// Accumulate one fill (8.8 fixed point, tile-local) into acc[row][col] and
-// carry[row][col] (int, 256 each, shared memory).
-__device__ __forceinline__ void accumulate_fill_cells(uint2 rec, int* acc, int* carry) {
-    float x0 = (float)(rec.x & 0xffffu) * (1.0f / 256.0f), y0 = (float)(rec.x >> 16) * (1.0f / 256.0f);
-    float x1 = (float)(rec.y & 0xffffu) * (1.0f / 256.0f), y1 = (float)(rec.y >> 16) * (1.0f / 256.0f);
-    if (x0 == x1) return;
-    float slope = (y1 - y0) / (x1 - x0);
-    float xmin = fminf(x0, x1), xmax = fmaxf(x0, x1);
-    int c0 = (int)floorf(xmin), c1 = (int)ceilf(xmax) - 1;
-    c0 = max(c0, 0); c1 = min(c1, 15);
-    for (int px = c0; px <= c1; px++) {
-        float lo = (float)px, hi = (float)(px + 1);
-        float xa = fminf(fmaxf(x0, lo), hi), xb = fminf(fmaxf(x1, lo), hi);
-        float w = xa - xb;  // oriented x-extent (window.x - window.y)
-        if (w == 0.0f) continue;
-        float ya = y0 + (xa - x0) * slope, yb = y0 + (xb - x0) * slope;
-        float ylo = fminf(ya, yb), yhi = fmaxf(ya, yb);
-        ylo = fminf(fmaxf(ylo, 0.0f), 16.0f); yhi = fminf(fmaxf(yhi, 0.0f), 16.0f);
-        if (yhi - ylo <= 0.0f) {
-            int r = (int)floorf(ylo);
-            if (r > 15) continue;
-            atomicAdd(&acc[r * 16 + px], __float2int_rn(w * ((float)(r + 1) - ylo) * kCovScale));
-            if (r + 1 < 16) atomicAdd(&carry[(r + 1) * 16 + px], __float2int_rn(w * kCovScale));
-            continue;
-        }
-        float inv_h = 1.0f / (yhi - ylo);
-        int r0 = (int)floorf(ylo), r1 = min((int)floorf(yhi), 15);
-        for (int r = r0; r <= r1; r++) {
-            float yt = fmaxf(ylo, (float)r), yb2 = fminf(yhi, (float)(r + 1));
-            float h = yb2 - yt;
-            if (h <= 0.0f) continue;
-            float wr = w * (h * inv_h);
-            float a = wr * ((float)(r + 1) - 0.5f * (yt + yb2));
-            atomicAdd(&acc[r * 16 + px], __float2int_rn(a * kCovScale));
-            if (r + 1 < 16) atomicAdd(&carry[(r + 1) * 16 + px], __float2int_rn(wr * kCovScale));
-        }
     }
 }
 

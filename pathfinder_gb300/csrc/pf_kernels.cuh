@@ -54,6 +54,7 @@ struct FrameDev {
     uint32_t* screen_cnt;        // [screen_count+1]
     uint32_t* screen_base;       // [screen_count+1]
     uint32_t* vis;               // [vis_cap] global tile indices
+    int4*     vis_info;          // [vis_cap] per visible tile: see VisInfo
     Counters* counters;
     uint32_t dda_limit;
     // Differentiable frames (diff != 0): FP32 fills, the curve parameters of
@@ -65,6 +66,16 @@ struct FrameDev {
     float2*   line_t;            // [line_cap] curve parameters of the line's ends
     uint32_t* tape;              // [vis_cap * 256] packed per pixel, see tape_pack
 };
+
+// What the composite needs of a visible tile, gathered by the visibility
+// scatter so that the composite reads one record instead of a chain of
+// dependent loads: x = first fill of its mask, y = fill count, z = paint
+// (RGBA8), w = backdrop (bits 0-7, signed) | even-odd (bit 8) | kind (bits
+// 9-10: 0 solid, 1 one mask, 2 clip-combined: read the tile and clip records).
+enum : uint32_t { kVisSolid = 0, kVisMask = 1, kVisCombine = 2 };
+__host__ __device__ __forceinline__ int32_t vis_meta(int8_t backdrop, bool even_odd, uint32_t kind) {
+    return (int32_t)((uint32_t)(uint8_t)backdrop | ((even_odd ? 1u : 0u) << 8) | (kind << 9));
+}
 
 // One tape word per (visible entry, pixel): coverage c and the composite
 // value d below the entry as 14-bit unorms (bits 0-13, 16-29), and the 2-bit

@@ -160,7 +160,22 @@ __global__ void k_visible(FrameDev f, int scatter) {
             atomicAdd(&f.screen_cnt[st], 1u);
         } else {
             uint32_t slot = f.screen_base[st] + atomicSub(&f.screen_cnt[st], 1u) - 1u;
-            if (slot < f.vis_cap) f.vis[slot] = g;
+            if (slot < f.vis_cap) {
+                f.vis[slot] = g;
+                uint32_t kind = (uint32_t)rec.y == kInvalid ? kVisSolid : kVisMask;
+                if (kind == kVisMask && f.path.clip_gpath[gp] >= 0) {
+                    const int4 crec = f.clips[g];
+                    if ((uint32_t)crec.x != kInvalid && (uint32_t)crec.z != kInvalid) kind = kVisCombine;
+                }
+                uint32_t b0 = 0, nf = 0;
+                if (kind == kVisMask) {
+                    const uint32_t owner = f.alpha_owner[(uint32_t)rec.y];
+                    b0 = f.tile_fill_base[owner];
+                    nf = f.tile_fill_base[owner + 1] - b0;
+                }
+                f.vis_info[slot] = make_int4((int)b0, (int)nf, (int)f.path.paint[gp],
+                                             vis_meta(tile_backdrop(rec), (tile_ctrl(rec) & 0x2u) != 0, kind));
+            }
         }
     }
 }
@@ -184,7 +199,8 @@ void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s) {
 // the first step compares i with i ^ (k - 1), later steps i with i ^ j.  Slots
 // at or beyond n act as +inf and are never touched, so n need not be a power
 // of two.  One warp; `a` in shared or global memory.
-__device__ void warp_bitonic_sort(uint32_t* a, uint32_t n) {
+template <typename K>
+__device__ void warp_bitonic_sort(K* a, uint32_t n) {
     const int lane = threadIdx.x & 31;
     uint32_t N = 1;
     while (N < n) N <<= 1;
@@ -193,7 +209,7 @@ __device__ void warp_bitonic_sort(uint32_t* a, uint32_t n) {
             for (uint32_t i = lane; i < N; i += 32) {
                 uint32_t l = (j == (k >> 1)) ? (i ^ (k - 1)) : (i ^ j);
                 if (l > i && l < n) {
-                    uint32_t x = a[i], y = a[l];
+                    K x = a[i], y = a[l];
                     if (y < x) { a[i] = y; a[l] = x; }
                 }
             }
@@ -202,26 +218,26 @@ __device__ void warp_bitonic_sort(uint32_t* a, uint32_t n) {
     }
 }
 
-struct CovBuf { int acc[256]; int carry[256]; };
+struct __align__(16) CovBuf { int acc[256]; int carry[256]; };  // cleared with int4 stores
 
-// Accumulate the fills of alpha tile `alpha` into `buf` (one warp).  DIFF
+// Accumulate fills [b0, b1) (one alpha tile's) into `buf` (one warp).  DIFF
 // reads the FP32 fills of differentiable frames.
 template <bool DIFF = false>
-__device__ __forceinline__ void warp_accumulate_tile(const FrameDev& f, uint32_t alpha, CovBuf& buf) {
+__device__ __forceinline__ void warp_accumulate_fills(const FrameDev& f, uint32_t b0, uint32_t b1, CovBuf& buf) {
     const int lane = threadIdx.x & 31;
+    int4* z = reinterpret_cast<int4*>(&buf);  // acc and carry: 512 ints
 #pragma unroll
-    for (int k = 0; k < 8; k++) { buf.acc[lane + 32 * k] = 0; buf.carry[lane + 32 * k] = 0; }
+    for (int k = 0; k < 4; k++) z[lane + 32 * k] = make_int4(0, 0, 0, 0);
     __syncwarp();
-    const uint32_t owner = f.alpha_owner[alpha];
-    const uint32_t b0 = f.tile_fill_base[owner], b1 = f.tile_fill_base[owner + 1];
     // Work items are (fill, pixel column) pairs, spread over the lanes: a
     // warp scan of the column counts of 32 fills, then each lane finds the
     // fill of its item with a 5-step search over the scanned counts.
     for (uint32_t base = b0; base < b1; base += 32) {
         const uint32_t i = base + lane;
-        float x0 = 0.0f, y0 = 0.0f, x1 = 0.0f, y1 = 0.0f;
+        float x0 = 0.0f, y0 = 0.0f, x1 = 0.0f, slope = 0.0f;
         int c0 = 0, ncol = 0;
         if (i < b1) {
+            float y1;
             if constexpr (DIFF) {
                 const float4 rec = f.fills_f[i];
                 x0 = rec.x; y0 = rec.y; x1 = rec.z; y1 = rec.w;
@@ -231,6 +247,7 @@ __device__ __forceinline__ void warp_accumulate_tile(const FrameDev& f, uint32_t
                 x1 = (float)(rec.y & 0xffffu) * (1.0f / 256.0f); y1 = (float)(rec.y >> 16) * (1.0f / 256.0f);
             }
             if (x0 != x1) {
+                slope = __fdividef(y1 - y0, x1 - x0);
                 c0 = max((int)floorf(fminf(x0, x1)), 0);
                 const int c1 = min((int)ceilf(fmaxf(x0, x1)) - 1, 15);
                 ncol = max(c1 - c0 + 1, 0);
@@ -252,13 +269,20 @@ __device__ __forceinline__ void warp_accumulate_tile(const FrameDev& f, uint32_t
                 if (v <= k) j += step;
             }
             const float ox0 = __shfl_sync(0xffffffffu, x0, j), oy0 = __shfl_sync(0xffffffffu, y0, j);
-            const float ox1 = __shfl_sync(0xffffffffu, x1, j), oy1 = __shfl_sync(0xffffffffu, y1, j);
+            const float ox1 = __shfl_sync(0xffffffffu, x1, j), osl = __shfl_sync(0xffffffffu, slope, j);
             const int oc0 = __shfl_sync(0xffffffffu, c0, j);
             const int oex = __shfl_sync(0xffffffffu, incl - ncol, j);
-            if (k < total) accumulate_fill_column(ox0, oy0, ox1, oy1, oc0 + (k - oex), buf.acc, buf.carry);
+            if (k < total) accumulate_fill_column(ox0, oy0, ox1, osl, oc0 + (k - oex), buf.acc, buf.carry);
         }
     }
     __syncwarp();
+}
+
+// The same for alpha tile `alpha`, its fill range found through its owner.
+template <bool DIFF = false>
+__device__ __forceinline__ void warp_accumulate_tile(const FrameDev& f, uint32_t alpha, CovBuf& buf) {
+    const uint32_t owner = f.alpha_owner[alpha];
+    warp_accumulate_fills<DIFF>(f, f.tile_fill_base[owner], f.tile_fill_base[owner + 1], buf);
 }
 
 // Lane (col = lane & 15, half = lane >> 4) owns rows half*8 .. half*8+7 of
@@ -283,7 +307,7 @@ __device__ __forceinline__ void warp_column_values(const CovBuf& buf, int out[8]
 struct WarpScratch { uint32_t keys[128]; CovBuf b0, b1; };
 
 // Per-pixel coverage of one path tile for this lane's 8 pixels.
-__device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint32_t g, WarpScratch& ws,
+__device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint32_t g, CovBuf& b0, CovBuf& b1,
                                                float cov[8]) {
     const uint32_t gp = (uint32_t)rec.z;
     const bool even_odd = (tile_ctrl(rec) & 0x2u) != 0;
@@ -297,10 +321,10 @@ __device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint
     if (combine) {
         // tile_clip_combine.fs.glsl:27-30, then sampleMask with the zeroed backdrop
         int vd[8], vs[8];
-        warp_accumulate_tile(f, (uint32_t)crec.x, ws.b0);
-        warp_accumulate_tile(f, (uint32_t)crec.z, ws.b1);
-        warp_column_values(ws.b0, vd);
-        warp_column_values(ws.b1, vs);
+        warp_accumulate_tile(f, (uint32_t)crec.x, b0);
+        warp_accumulate_tile(f, (uint32_t)crec.z, b1);
+        warp_column_values(b0, vd);
+        warp_column_values(b1, vs);
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             float m = fminf(fabsf((float)vd[k] * kCovInvScale + (float)crec.y),
@@ -309,8 +333,8 @@ __device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint
         }
     } else if ((uint32_t)rec.y != kInvalid) {
         int v[8];
-        warp_accumulate_tile(f, (uint32_t)rec.y, ws.b0);
-        warp_column_values(ws.b0, v);
+        warp_accumulate_tile(f, (uint32_t)rec.y, b0);
+        warp_column_values(b0, v);
 #pragma unroll
         for (int k = 0; k < 8; k++) cov[k] = resolve_coverage((float)v[k] * kCovInvScale + bd, even_odd);
     } else {
@@ -326,13 +350,21 @@ __device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint
 // ---------------------------------------------------------------------------
 constexpr uint32_t kWarpListCap = 128;
 
+// Per warp: the screen tile's list as (tile << 32 | position) keys, the
+// visible-tile records by position, and two coverage buffers.
+struct CompositeScratch {
+    unsigned long long keys[kWarpListCap];
+    int4 info[kWarpListCap];
+    CovBuf b0, b1;
+};
+
 template <int MODE, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out, float4 bg) {
-    __shared__ WarpScratch scratch[WARPS];
+    extern __shared__ __align__(16) unsigned char comp_smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t st = blockIdx.x * WARPS + wid;  // frame screen tile
     if (st >= f.screen_count) return;
-    WarpScratch& ws = scratch[wid];
+    CompositeScratch& ws = reinterpret_cast<CompositeScratch*>(comp_smem)[wid];
 
     const SceneDev& sc = f.scenes[scene_of_screen_tile(f, f.screen_begin + st)];
     const int4 s = sc.screen;
@@ -346,26 +378,54 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
     if (ok) { base = f.screen_base[st]; n = f.screen_base[st + 1] - base; }
 
     // draw order = global tile order (paths in order)
-    const uint32_t* list;
-    if (n <= kWarpListCap) {
-        for (uint32_t i = lane; i < n; i += 32) ws.keys[i] = f.vis[base + i];
+    const bool short_list = n <= kWarpListCap;
+    if (short_list) {
+        for (uint32_t i = lane; i < n; i += 32) {
+            ws.keys[i] = ((unsigned long long)f.vis[base + i] << 32) | i;
+            ws.info[i] = f.vis_info[base + i];
+        }
         __syncwarp();
         if (n > 1) warp_bitonic_sort(ws.keys, n);
-        list = ws.keys;
     } else {
         warp_bitonic_sort(f.vis + base, n);  // rare: long lists sort in place in global memory
-        list = f.vis + base;
     }
 
     float d0[8], d1[8], d2[8], d3[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) { d0[k] = bg.x; d1[k] = bg.y; d2[k] = bg.z; d3[k] = bg.w; }
     for (uint32_t i = 0; i < n; i++) {
-        uint32_t g = list[i];
-        int4 rec = f.tiles[g];
         float cov[8];
-        tile_coverage8(f, rec, g, ws, cov);
-        uint32_t paint = f.path.paint[(uint32_t)rec.z];
+        uint32_t paint;
+        uint32_t kind = kVisCombine;
+        int4 info = make_int4(0, 0, 0, 0);
+        uint32_t g;
+        if (short_list) {
+            const unsigned long long key = ws.keys[i];
+            g = (uint32_t)(key >> 32);
+            info = ws.info[(uint32_t)key];
+            kind = ((uint32_t)info.w >> 9) & 3u;
+            paint = (uint32_t)info.z;
+        } else {
+            g = f.vis[base + i];
+        }
+        if (kind == kVisMask) {
+            const bool even_odd = ((uint32_t)info.w >> 8) & 1u;
+            const float bd = (float)(int8_t)(info.w & 0xff);
+            int v[8];
+            warp_accumulate_fills(f, (uint32_t)info.x, (uint32_t)info.x + (uint32_t)info.y, ws.b0);
+            warp_column_values(ws.b0, v);
+            __syncwarp();  // the buffer is cleared by the next tile
+#pragma unroll
+            for (int k = 0; k < 8; k++) cov[k] = resolve_coverage((float)v[k] * kCovInvScale + bd, even_odd);
+        } else if (kind == kVisSolid) {
+            const float c = resolve_coverage((float)(int8_t)(info.w & 0xff), ((uint32_t)info.w >> 8) & 1u);
+#pragma unroll
+            for (int k = 0; k < 8; k++) cov[k] = c;
+        } else {  // clip-combined tile, or a long list: from the tile records
+            const int4 rec = f.tiles[g];
+            tile_coverage8(f, rec, g, ws.b0, ws.b1, cov);
+            paint = f.path.paint[(uint32_t)rec.z];
+        }
         float pa = (float)(paint >> 24) * (1.0f / 255.0f);
         if (MODE == 0) {
             float pr = (float)(paint & 0xffu) * (1.0f / 255.0f);
@@ -404,13 +464,24 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
     }
 }
 
+template <int MODE, int WARPS>
+void launch_composite_warps(const FrameDev& f, void* out, const float4& bg, cudaStream_t s) {
+    constexpr size_t smem = WARPS * sizeof(CompositeScratch);
+    static bool configured = false;  // above 48 KiB needs the opt-in (once per instance)
+    if (!configured) {
+        cudaFuncSetAttribute(k_composite<MODE, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = true;
+    }
+    count_launch();
+    k_composite<MODE, WARPS><<<(f.screen_count + WARPS - 1) / WARPS, WARPS * 32, smem, s>>>(f, out, bg);
+}
+
 template <int MODE>
 void launch_composite_mode(const FrameDev& f, void* out, const float4& bg, cudaStream_t s) {
     const int w = f.tune.comp_warps;
-    const uint32_t blocks = (f.screen_count + w - 1) / w;
-    if (w == 2) { count_launch(); k_composite<MODE, 2><<<blocks, 64, 0, s>>>(f, out, bg); }
-    else if (w == 8) { count_launch(); k_composite<MODE, 8><<<blocks, 256, 0, s>>>(f, out, bg); }
-    else { count_launch(); k_composite<MODE, 4><<<(f.screen_count + 3) / 4, 128, 0, s>>>(f, out, bg); }
+    if (w == 2) launch_composite_warps<MODE, 2>(f, out, bg, s);
+    else if (w == 8) launch_composite_warps<MODE, 8>(f, out, bg, s);
+    else launch_composite_warps<MODE, 4>(f, out, bg, s);
 }
 
 void launch_composite(const FrameDev& f, int mode, void* out, const float4& bg, cudaStream_t s) {
@@ -571,7 +642,7 @@ __global__ void k_tile_cov(FrameDev f, float* out) {
         uint32_t code[8];
         tile_coverage8_diff(f, f.tiles[g], g, scratch[wid], cov, code);
     } else {
-        tile_coverage8(f, f.tiles[g], g, scratch[wid], cov);
+        tile_coverage8(f, f.tiles[g], g, scratch[wid].b0, scratch[wid].b1, cov);
     }
     const int col = lane & 15, half = lane >> 4;
 #pragma unroll

@@ -104,6 +104,7 @@ struct PFCUDARenderer {
     DevBuf<uint32_t> fill_e;
     DevBuf<int4> tiles, clips;
     DevBuf<uint32_t> screen_cnt, screen_base, vis;
+    DevBuf<int4> vis_info;
     DevBuf<uint32_t> scan_partials;
     DevBuf<Counters> counters;
     DevBuf<uint8_t> out_tmp;
@@ -234,6 +235,7 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.screen_cnt = r->screen_cnt.p;
     f.screen_base = r->screen_base.p;
     f.vis = r->vis.p;
+    f.vis_info = r->vis_info.p;
     f.counters = r->counters.p;
     f.dda_limit = 1u << 24;
     return f;
@@ -248,7 +250,7 @@ cudaError_t ensure_frame_buffers(PFCUDARenderer* r) {
         (e = r->tiles.ensure(T)) || (e = r->clips.ensure(T)) || (e = r->col_backdrop.ensure((size_t)r->col_cap + 1)) ||
         (e = r->fills.ensure(F)) || (e = r->fill_e.ensure(F)) || (e = r->lines.ensure(L)) ||
         (e = r->line_path.ensure(L)) || (e = r->line_fill_count.ensure(L)) || (e = r->line_fill_base.ensure(L)) ||
-        (e = r->vis.ensure((size_t)r->vis_cap + 1)) || (e = r->zbuf.ensure(ST)) || (e = r->screen_cnt.ensure(ST)) ||
+        (e = r->vis.ensure((size_t)r->vis_cap + 1)) || (e = r->vis_info.ensure((size_t)r->vis_cap + 1)) || (e = r->zbuf.ensure(ST)) || (e = r->screen_cnt.ensure(ST)) ||
         (e = r->screen_base.ensure(ST)) || (e = r->path_tiles.ensure(P)) || (e = r->path_cols.ensure(P)))
         return e;
     if (r->diff_buffers) {
@@ -497,7 +499,7 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->tile_fill_base.release(); r->tile_alpha.release(); r->alpha_owner.release(); r->tile_delta.release();
     r->tile_delta_scan.release(); r->path_tiles.release(); r->path_cols.release();
     r->col_backdrop.release(); r->zbuf.release(); r->fills.release(); r->fill_e.release(); r->tiles.release();
-    r->clips.release(); r->screen_cnt.release(); r->screen_base.release(); r->vis.release();
+    r->clips.release(); r->screen_cnt.release(); r->screen_base.release(); r->vis.release(); r->vis_info.release();
     r->scan_partials.release(); r->counters.release(); r->out_tmp.release();
     r->draw_index.release(); r->alpha_in.release(); r->fills_f.release(); r->line_seg.release();
     r->line_t.release(); r->tape.release();

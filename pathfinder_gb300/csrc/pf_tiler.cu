@@ -6,10 +6,10 @@
 //   SegmentsD3D11::add_path (renderer/src/builder.rs:804-841) and
 //   ContourIter::next (content/src/outline.rs:1024-1065)  -> k_contour_seg*
 //   Tiler::new bounds / BuiltPath::new tile rect
-//   (renderer/src/tiler.rs:40-66, builder.rs:415-485)     -> k_bound, k_path_scan
-//   generate_fills: process_segment/process_line_segment/add_fill/
-//   adjust_alpha_tile_backdrop (tiler.rs:83-308,
-//   builder.rs:509-616)                                    -> k_tile_count, k_tile_emit
+//   (renderer/src/tiler.rs:40-66, builder.rs:415-485)     -> k_bound, path scans
+//   process_segment (tiler.rs:166-184)                     -> k_flatten_count, k_flatten_emit
+//   process_line_segment/add_fill/adjust_alpha_tile_backdrop
+//   (tiler.rs:191-308, builder.rs:509-616)                 -> k_bin_count, k_bin_emit
 #include "pf_kernels.cuh"
 
 #include <atomic>
@@ -401,7 +401,7 @@ void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
 // segments in path order, each segment's lines depth first.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_flatten_count(FrameDev f) {
-    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= f.seg_count) return;
     uint32_t n = 0;
     flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&, uint32_t, int) { n++; }, &f.counters->status);
@@ -420,16 +420,17 @@ __global__ void k_check_lines(FrameDev f) {
 // adjoint holds these subdivisions fixed.
 template <bool DIFF>
 __global__ void __launch_bounds__(256) k_flatten_emit(FrameDev f) {
-    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= f.seg_count || f.counters->lines > f.line_cap) return;
-    const SegRec sr = f.segs[f.seg_begin + s];
+    const uint32_t sg = f.seg_begin + s;
+    const SegRec sr = f.segs[sg];
     uint32_t l = f.seg_line_base[s];
     flatten_segment(f.pts, sr, [&](const Line& ln, uint32_t addr, int d) {
         f.lines[l] = make_float4(ln.fx, ln.fy, ln.tx, ln.ty);
         f.line_path[l] = (uint32_t)sr.w;
         if constexpr (DIFF) {
             const float step = ldexpf(1.0f, -d), t0 = (float)addr * step;
-            f.line_seg[l] = f.seg_begin + s;
+            f.line_seg[l] = sg;
             f.line_t[l] = make_float2(t0, t0 + step);
         }
         l++;
