@@ -1,0 +1,129 @@
+"""Edge inputs of the CUDA level against the oracle: a transform, a
+background colour, an empty scene, degenerate contours, paths outside or far
+outside the view box, one path large enough to overflow every first-frame
+capacity, and the async path's capacity status."""
+import numpy as np
+import pytest
+
+import pathfinder_gb300 as pf
+from tests.parity import compare_images, compare_masks, compare_records
+
+pytestmark = pytest.mark.gpu
+
+
+def _check(renderer, scene, options=None):
+    import oracle
+    img = renderer.render(scene, options=options)
+    fr = oracle.OracleFrame(scene, options)
+    compare_records(scene, renderer.read_records(scene), fr)
+    compare_masks(renderer, fr)
+    ora, _ = fr.render(scene.width, scene.height)
+    compare_images(img, ora)
+    return img
+
+
+def _star(cx, cy, r0, r1, k, rng=None):
+    c = pf.Contour()
+    for i in range(2 * k):
+        a = np.pi * i / k
+        r = r0 if i % 2 == 0 else r1
+        x, y = cx + r * np.cos(a), cy + r * np.sin(a)
+        if i == 0:
+            c.push_endpoint(x, y)
+        elif rng is not None and i % 3 == 1:
+            c.push_quadratic(x + rng.normal(0, 2), y + rng.normal(0, 2), x, y)
+        else:
+            c.push_endpoint(x, y)
+    c.close()
+    return c
+
+
+def _scene(w, h):
+    s = pf.Scene()
+    s.set_view_box(pf.RectF(0, 0, w, h))
+    return s
+
+
+def test_transform_parity(renderer):
+    s = pf.generate_scene(pf.PF_SCENE_STARS_512, seed=2)
+    bo = pf.BuildOptions(pf.Transform2F(0.83, -0.41, 0.37, 0.91, 40.5, -12.25))
+    _check(renderer, s, bo)
+
+
+def test_background_colour(built):
+    import oracle
+    s = pf.generate_scene(pf.PF_SCENE_STARS_512, seed=3)
+    bg = pf.ColorF(0.1, 0.2, 0.3, 0.6)
+    with pf.Renderer(0, pf.RendererOptions(background_color=bg)) as r:
+        img = r.render(s)
+    ora, _ = oracle.OracleFrame(s).render(s.width, s.height, background=(bg.r, bg.g, bg.b, bg.a))
+    compare_images(img, ora)
+
+
+def test_empty_scene(renderer):
+    s = _scene(64, 48)
+    img = renderer.render(s)
+    assert img.shape == (48, 64, 4) and not img.any()
+    st = renderer.stats()
+    assert st.fill_count == 0 and st.tile_count == 0 and st.visible_tile_count == 0
+
+
+def test_degenerate_contours(renderer):
+    s = _scene(96, 96)
+    for pts in ([], [(10, 10)], [(20, 20), (40, 40)], [(30, 30), (30, 30), (30, 30)],
+                [(10, 50), (50, 50), (90, 50)]):  # empty, point, segment, repeated, collinear
+        c = pf.Contour()
+        for p in pts:
+            c.push_endpoint(*p)
+        if pts:
+            c.close()
+        s.push_draw_path(pf.DrawPath(pf.Outline([c]), pf.ColorU(200, 10, 10, 255)))
+    s.push_draw_path(pf.DrawPath(pf.Outline([_star(48, 48, 30, 12, 7)]), pf.ColorU(10, 200, 10, 180)))
+    _check(renderer, s)
+
+
+def test_paths_outside_and_far_outside_the_view(renderer):
+    s = _scene(128, 96)
+    rng = np.random.default_rng(4)
+    for cx, cy in [(-60, 40), (200, 40), (64, -70), (64, 180), (-50, -50), (190, 150),
+                   (64, 48)]:
+        s.push_draw_path(pf.DrawPath(pf.Outline([_star(cx, cy, 45, 20, 9, rng)]), pf.ColorU(90, 90, 200, 200)))
+    # coordinates far beyond the view on every side, crossing it
+    c = pf.Contour()
+    for p in [(-1e6, -3e5), (2e6, 40.5), (60.25, 1e6), (-4e5, 70.75)]:
+        c.push_endpoint(*p)
+    c.close()
+    s.push_draw_path(pf.DrawPath(pf.Outline([c]), pf.ColorU(10, 160, 60, 128), pf.FillRule.EVEN_ODD))
+    _check(renderer, s)
+
+
+def test_one_path_beyond_every_first_frame_capacity(built):
+    """40,000 edges in one path over 2048^2 (millions of fills): a fresh
+    renderer must grow its buffers and re-run the frame (records still
+    bit-exact)."""
+    rng = np.random.default_rng(5)
+    s = _scene(2048, 2048)
+    s.push_draw_path(pf.DrawPath(pf.Outline([_star(1024, 1024, 1000, 300, 20_000, rng)]),
+                                 pf.ColorU(30, 30, 30, 255)))
+    with pf.Renderer(0) as r:
+        _check(r, s)
+
+
+def test_async_capacity_status_then_regrow(built):
+    torch = pytest.importorskip("torch")
+    from pathfinder_gb300._abi import PF_CUDA_ERR_CAPACITY, PF_CUDA_OK
+    s = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=2, scale=0.05)
+    out = torch.zeros((s.height, s.width, 4), dtype=torch.uint8, device="cuda")
+    with pf.Renderer(0) as r:
+        r.upload_scene(s)
+        codes = []
+        for _ in range(4):  # first-frame capacity guesses may overflow; each status call grows them
+            r.render_async(s, out)
+            code, _ = r.render_status()
+            codes.append(code)
+            if code == PF_CUDA_OK:
+                break
+            assert code == PF_CUDA_ERR_CAPACITY
+        assert codes[-1] == PF_CUDA_OK, codes
+        ref = r.render(s)
+        assert np.array_equal(out.cpu().numpy(), ref)
