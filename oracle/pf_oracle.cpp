@@ -409,12 +409,27 @@ void build_fills(Frame& fr, uint32_t p, uint64_t dda_limit) {
         for_each_segment(c, [&](const Segment& s) { process_segment(ctx, s, 0); });
 }
 
-// Tiler::prepare_tiles (renderer/src/tiler.rs:93-163).
+// The tile of path q at (tx, ty), or NULL outside its tile rect.
+const OTile* tile_at(const Frame& fr, int32_t q, int32_t tx, int32_t ty) {
+    const BuiltPath& cb = fr.built[(uint32_t)q];
+    if (!cb.tile_rect.contains(tx, ty)) return nullptr;
+    return &cb.tiles[(size_t)(ty - cb.tile_rect.miny) * cb.tile_rect.width() + (size_t)(tx - cb.tile_rect.minx)];
+}
+
+// Tiler::prepare_tiles (renderer/src/tiler.rs:93-163).  Draw paths whose
+// clip path is itself clipped (the D3D11 level's clip levels,
+// renderer/src/builder.rs:1124-1220; the CPU tiler has no such case) keep
+// their tiles, flagged as behind a clip chain, unless a level of the chain has
+// no tile or an empty one there.
 void prepare_tiles(Frame& fr, uint32_t p) {
     const PathInput& in = fr.paths[p];
     BuiltPath& bp = fr.built[p];
     const BuiltPath* clip = nullptr;
-    if (!in.is_clip && in.clip_path >= 0) clip = &fr.built[(uint32_t)in.clip_path];
+    bool chain = false;
+    if (!in.is_clip && in.clip_path >= 0) {
+        clip = &fr.built[(uint32_t)in.clip_path];
+        chain = fr.paths[(uint32_t)in.clip_path].clip_path >= 0;
+    }
     int32_t w = bp.tile_rect.width();
     for (size_t i = 0; i < bp.tiles.size(); i++) {
         OTile& t = bp.tiles[i];
@@ -422,7 +437,17 @@ void prepare_tiles(Frame& fr, uint32_t p) {
         int32_t delta = t.backdrop;
         uint32_t draw_alpha = t.alpha_tile_id;
         int8_t draw_backdrop = (int8_t)(uint8_t)(uint32_t)bp.backdrops[column];
-        if (clip) {
+        if (chain) {
+            t.ctrl |= 0x4;
+            bool culled = false;
+            int32_t q = in.clip_path;
+            for (uint32_t it = 0; q >= 0 && it <= fr.clip_count; it++) {
+                const OTile* ct = tile_at(fr, q, t.tile_x, t.tile_y);
+                if (!ct || (ct->alpha_tile_id == kInvalid && ct->backdrop == 0)) { culled = true; break; }
+                q = fr.paths[(uint32_t)q].clip_path;
+            }
+            if (culled) { draw_alpha = kInvalid; draw_backdrop = 0; }
+        } else if (clip) {
             int32_t cx = t.tile_x, cy = t.tile_y;
             if (clip->tile_rect.contains(cx, cy)) {
                 const OTile& ct = clip->tiles[(size_t)(cy - clip->tile_rect.miny) * clip->tile_rect.width() +
@@ -527,6 +552,7 @@ void build_frame(Frame& fr, int threads, uint64_t dda_limit) {
         bool eo = in.fill_rule == PF_FILL_RULE_EVEN_ODD;
         for (const OTile& t : bp.tiles) {
             if (t.alpha_tile_id != kInvalid) continue;
+            if (t.ctrl & 0x4) continue;  // behind a clip chain: may be partly covered
             if (!solid_tile_occludes(t.backdrop, eo)) continue;
             if (!fr.screen.contains(t.tile_x, t.tile_y)) continue;
             int32_t& z = fr.zbuf[(size_t)(t.tile_y - fr.screen.miny) * sw + (t.tile_x - fr.screen.minx)];
@@ -621,12 +647,35 @@ void compute_raw_masks(const Frame& fr, std::vector<T>& masks, int threads) {
     });
 }
 
+// |mask + backdrop| of one tile (the backdrop alone for a solid tile).
+template <typename T>
+void tile_abs_winding(const OTile& t, const std::vector<T>& masks, T* out) {
+    for (int k = 0; k < 256; k++)
+        out[k] = std::fabs((t.alpha_tile_id != kInvalid ? masks[(size_t)t.alpha_tile_id * 256 + k] : (T)0) +
+                           (T)t.backdrop);
+}
+
 template <typename T>
 void tile_coverage(const Frame& fr, uint32_t p, size_t i, const std::vector<T>& masks, T* out) {
     const PathInput& in = fr.paths[p];
     const BuiltPath& bp = fr.built[p];
     const OTile& t = bp.tiles[i];
     bool eo = !in.is_clip && in.fill_rule == PF_FILL_RULE_EVEN_ODD;
+    if (t.ctrl & 0x4) {
+        // behind a clip chain: the minimum over the tile and every level
+        T m[256], mq[256];
+        tile_abs_winding<T>(t, masks, m);
+        int32_t q = in.clip_path;
+        for (uint32_t it = 0; q >= 0 && it <= fr.clip_count; it++) {
+            const OTile* ct = tile_at(fr, q, t.tile_x, t.tile_y);
+            if (!ct) break;  // culled by prepare_tiles
+            tile_abs_winding<T>(*ct, masks, mq);
+            for (int k = 0; k < 256; k++) m[k] = std::min(m[k], mq[k]);
+            q = fr.paths[(uint32_t)q].clip_path;
+        }
+        for (int k = 0; k < 256; k++) out[k] = resolve<T>(m[k], eo);
+        return;
+    }
     if (!bp.clips.empty() && bp.clips[i].dest_tile_id != kInvalid && bp.clips[i].src_tile_id != kInvalid) {
         // tile_clip_combine.fs.glsl:27-30, then sampleMask with backdrop 0.
         const OClip& c = bp.clips[i];
@@ -724,9 +773,10 @@ bool make_frame(const PFCUDASceneDesc* sc, const PFCUDABuildOptions* opts, Frame
         in.is_clip = p < fr.clip_count;
         in.path_index = in.is_clip ? p : p - fr.clip_count;
         in.fill_rule = src.fill_rule;
-        in.clip_path = in.is_clip ? -1 : src.clip_path;
+        in.clip_path = src.clip_path;  // clip paths may be clipped too (clip chains)
         in.paint = src.paint;
-        if (!in.is_clip && src.clip_path >= (int32_t)fr.clip_count) return false;
+        if (src.clip_path >= (int32_t)fr.clip_count) return false;
+        if (in.is_clip && src.clip_path == (int32_t)p) return false;
         if (transform) {
             // Contour::transform (content/src/outline.rs:884-893), Transform2F * Vector2F
             // (geometry/src/transform2d.rs:123-129, :312-318).
@@ -751,6 +801,11 @@ bool make_frame(const PFCUDASceneDesc* sc, const PFCUDABuildOptions* opts, Frame
                 in.contours.push_back(Contour{sc->points + s0, sc->point_flags + s0, s1 - s0});
             }
         }
+    }
+    for (uint32_t p = 0; p < n; p++) {  // no cycles of clip paths
+        uint32_t len = 0;
+        for (int32_t q = fr.paths[p].clip_path; q >= 0; q = fr.paths[(uint32_t)q].clip_path)
+            if (++len > fr.clip_count) return false;
     }
     return true;
 }
@@ -854,6 +909,7 @@ bool make_diff_frame(const PFCUDASceneDesc* sc, const PFCUDABuildOptions* opts, 
         dp.is_clip = p < d.nclip;
         dp.even_odd = src.fill_rule == PF_FILL_RULE_EVEN_ODD;
         if (!dp.is_clip && src.clip_path >= (int32_t)d.nclip) return false;
+        if (dp.is_clip && src.clip_path >= 0) return false;  // clip chains: not differentiable here
         dp.clip = (!dp.is_clip && src.clip_path >= 0) ? src.clip_path : -1;
         for (uint32_t c = 0; c < src.contour_count; c++) {
             const uint32_t s0 = sc->contour_starts[src.first_contour + c];

@@ -57,6 +57,7 @@ struct FrameDev {
     int4*     vis_info;          // [vis_cap] per visible tile: see VisInfo
     Counters* counters;
     uint32_t dda_limit;
+    uint32_t clip_chain_max;     // bound of clip-chain walks (longest chain in the batch)
     // Differentiable frames (diff != 0): FP32 fills, the curve parameters of
     // every flattened line, and per visible (screen tile, path tile) entry the
     // composite tape the adjoint reads back.
@@ -72,7 +73,13 @@ struct FrameDev {
 // dependent loads: x = first fill of its mask, y = fill count, z = paint
 // (RGBA8), w = backdrop (bits 0-7, signed) | even-odd (bit 8) | kind (bits
 // 9-10: 0 solid, 1 one mask, 2 clip-combined: read the tile and clip records).
-enum : uint32_t { kVisSolid = 0, kVisMask = 1, kVisCombine = 2 };
+enum : uint32_t { kVisSolid = 0, kVisMask = 1, kVisCombine = 2, kVisChain = 3 };
+
+// Tile control bit of a draw tile whose clip path is itself clipped: its
+// coverage is the fill rule applied to the minimum of |mask + backdrop| over
+// the tile and its clip chain's tiles (the D3D11 level's per-level
+// min(coverage, clip mask), shaders/d3d11/fill.cs.glsl:77-84).
+constexpr uint32_t kCtrlClipChain = 0x4;
 __host__ __device__ __forceinline__ int32_t vis_meta(int8_t backdrop, bool even_odd, uint32_t kind) {
     return (int32_t)((uint32_t)(uint8_t)backdrop | ((even_odd ? 1u : 0u) << 8) | (kind << 9));
 }

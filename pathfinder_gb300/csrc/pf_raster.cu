@@ -97,7 +97,25 @@ __global__ void k_propagate(FrameDev f, int clip_pass) {
         uint32_t alpha = own_alpha;
         int8_t backdrop = (int8_t)acc;
         const int32_t tx = r.x + ox, ty = r.y + oy;
-        if (clip_gp >= 0) {
+        uint8_t tile_ctrl_bits = ctrl;
+        if (clip_gp >= 0 && f.path.clip_gpath[clip_gp] >= 0) {
+            // Clip chain: the tile stays as built unless a clip level lacks a
+            // tile here or has an empty one (the composite takes the minimum
+            // over the chain).  Clip paths keep their own records, so every
+            // level is final after the clip pass.
+            tile_ctrl_bits = (uint8_t)(ctrl | kCtrlClipChain);
+            bool culled = false;
+            int32_t q = clip_gp;
+            for (uint32_t it = 0; q >= 0 && it <= f.clip_chain_max; it++) {
+                const int4 cr = f.path.tile_rect[q];
+                if (!(cr.x <= tx && cr.y <= ty && tx <= cr.z - 1 && ty <= cr.w - 1)) { culled = true; break; }
+                const int4 ct = f.tiles[f.path.tile_offset[q] + (uint32_t)((ty - cr.y) * (cr.z - cr.x) + (tx - cr.x))];
+                if ((uint32_t)ct.y == kInvalid && tile_backdrop(ct) == 0) { culled = true; break; }
+                q = f.path.clip_gpath[q];
+            }
+            if (culled) { alpha = kInvalid; backdrop = 0; }
+            f.clips[g] = make_int4((int)kInvalid, 0, (int)kInvalid, 0);
+        } else if (clip_gp >= 0) {
             const int4 cr = f.path.tile_rect[clip_gp];
             int4 clip_rec = make_int4((int)kInvalid, 0, (int)kInvalid, 0);
             if (cr.x <= tx && cr.y <= ty && tx <= cr.z - 1 && ty <= cr.w - 1) {
@@ -123,9 +141,10 @@ __global__ void k_propagate(FrameDev f, int clip_pass) {
         } else if (!is_clip) {
             f.clips[g] = make_int4((int)kInvalid, 0, (int)kInvalid, 0);
         }
-        f.tiles[g] = pack_tile(tx, ty, alpha, gp, color, ctrl, backdrop);
-        // differentiable frames occlude with the FP32 paint alpha being optimised
-        const bool opaque = is_clip ? false
+        f.tiles[g] = pack_tile(tx, ty, alpha, gp, color, tile_ctrl_bits, backdrop);
+        // differentiable frames occlude with the FP32 paint alpha being optimised;
+        // a tile behind a clip chain may be partly covered, so it never occludes
+        const bool opaque = (is_clip || (tile_ctrl_bits & kCtrlClipChain)) ? false
                                     : (f.path.alpha_f ? f.path.alpha_f[f.path.draw_index[gp]] >= 1.0f
                                                       : (f.path.paint[gp] >> 24) == 255u);
         if (opaque && alpha == kInvalid && solid_occludes(backdrop, even_odd)) {
@@ -163,7 +182,8 @@ __global__ void k_visible(FrameDev f, int scatter) {
             if (slot < f.vis_cap) {
                 f.vis[slot] = g;
                 uint32_t kind = (uint32_t)rec.y == kInvalid ? kVisSolid : kVisMask;
-                if (kind == kVisMask && f.path.clip_gpath[gp] >= 0) {
+                if (tile_ctrl(rec) & kCtrlClipChain) kind = kVisChain;
+                else if (kind == kVisMask && f.path.clip_gpath[gp] >= 0) {
                     const int4 crec = f.clips[g];
                     if ((uint32_t)crec.x != kInvalid && (uint32_t)crec.z != kInvalid) kind = kVisCombine;
                 }
@@ -307,14 +327,57 @@ __device__ __forceinline__ void warp_column_values(const CovBuf& buf, int out[8]
 struct WarpScratch { uint32_t keys[128]; CovBuf b0, b1; };
 
 // Per-pixel coverage of one path tile for this lane's 8 pixels.
+// |mask + backdrop| of one tile for this lane's 8 pixels (the backdrop alone
+// for a solid tile).
+__device__ __forceinline__ void tile_abs_winding8(const FrameDev& f, int4 rec, CovBuf& b, float m[8]) {
+    const float bd = (float)tile_backdrop(rec);
+    if ((uint32_t)rec.y != kInvalid) {
+        int v[8];
+        warp_accumulate_tile(f, (uint32_t)rec.y, b);
+        warp_column_values(b, v);
+        __syncwarp();  // the buffer is cleared by the next accumulation
+#pragma unroll
+        for (int k = 0; k < 8; k++) m[k] = fabsf((float)v[k] * kCovInvScale + bd);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) m[k] = fabsf(bd);
+    }
+}
+
+// Coverage of a tile behind a clip chain: the fill rule applied to the
+// minimum of |mask + backdrop| over the tile and each clip level's tile at the
+// same coordinates (all present: the propagation culled the tile otherwise).
+__device__ __forceinline__ void chain_coverage8(const FrameDev& f, int4 rec, CovBuf& b, float cov[8]) {
+    float m[8], mq[8];
+    tile_abs_winding8(f, rec, b, m);
+    const int32_t tx = tile_x(rec), ty = tile_y(rec);
+    int32_t q = f.path.clip_gpath[(uint32_t)rec.z];
+    for (uint32_t it = 0; q >= 0 && it <= f.clip_chain_max; it++) {
+        const int4 cr = f.path.tile_rect[q];
+        if (!(cr.x <= tx && cr.y <= ty && tx <= cr.z - 1 && ty <= cr.w - 1)) break;  // culled by propagation
+        const int4 ct = f.tiles[f.path.tile_offset[q] + (uint32_t)((ty - cr.y) * (cr.z - cr.x) + (tx - cr.x))];
+        tile_abs_winding8(f, ct, b, mq);
+#pragma unroll
+        for (int k = 0; k < 8; k++) m[k] = fminf(m[k], mq[k]);
+        q = f.path.clip_gpath[q];
+    }
+    const bool even_odd = (tile_ctrl(rec) & 0x2u) != 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) cov[k] = resolve_coverage(m[k], even_odd);
+}
+
 __device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint32_t g, CovBuf& b0, CovBuf& b1,
                                                float cov[8]) {
     const uint32_t gp = (uint32_t)rec.z;
+    if (tile_ctrl(rec) & kCtrlClipChain) {
+        chain_coverage8(f, rec, b0, cov);
+        return;
+    }
     const bool even_odd = (tile_ctrl(rec) & 0x2u) != 0;
     const float bd = (float)tile_backdrop(rec);
     bool combine = false;
     int4 crec = make_int4(0, 0, 0, 0);
-    if (f.path.clip_gpath[gp] >= 0) {
+    if (tile_ctrl(rec) != 0 && f.path.clip_gpath[gp] >= 0) {  // draw tiles only carry clip records
         crec = f.clips[g];
         combine = (uint32_t)crec.x != kInvalid && (uint32_t)crec.z != kInvalid;
     }
@@ -504,7 +567,7 @@ __device__ __forceinline__ void tile_coverage8_diff(const FrameDev& f, int4 rec,
     const float bd = (float)tile_backdrop(rec);
     bool combine = false;
     int4 crec = make_int4(0, 0, 0, 0);
-    if (f.path.clip_gpath[gp] >= 0) {
+    if (tile_ctrl(rec) != 0 && f.path.clip_gpath[gp] >= 0) {  // draw tiles only carry clip records
         crec = f.clips[g];
         combine = (uint32_t)crec.x != kInvalid && (uint32_t)crec.z != kInvalid;
     }

@@ -122,6 +122,10 @@ struct PFCUDARenderer {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
 
+    // clip chains
+    uint32_t clip_chain_max = 0;       // longest chain of clip paths behind a path
+    bool nested_clips = false;         // some clip path is itself clipped
+
     // differentiable frames
     uint32_t ND = 0;                   // draw paths of the batch
     std::vector<float> draw_alpha;     // paint alpha / 255 per draw path (default alpha)
@@ -238,6 +242,7 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.vis_info = r->vis_info.p;
     f.counters = r->counters.p;
     f.dda_limit = 1u << 24;
+    f.clip_chain_max = r->clip_chain_max;
     return f;
 }
 
@@ -590,8 +595,8 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
             const PFCUDAPath& p = c ? sc.clip_paths[i] : sc.draw_paths[i - sc.clip_path_count];
             if ((uint64_t)p.first_contour + p.contour_count > sc.contour_count) return PF_CUDA_ERR_INVALID;
             if (p.fill_rule > 1 || p.blend_mode != PF_BLEND_MODE_SRC_OVER) return PF_CUDA_ERR_INVALID;
-            if (!c && p.clip_path >= (int32_t)sc.clip_path_count) return PF_CUDA_ERR_INVALID;
-            if (c && p.clip_path >= 0) return PF_CUDA_ERR_INVALID;  // nested clips: not on this path
+            if (p.clip_path >= (int32_t)sc.clip_path_count) return PF_CUDA_ERR_INVALID;
+            if (c && p.clip_path == (int32_t)i) return PF_CUDA_ERR_INVALID;  // a clip path clipping itself
             first_ord[gp] = (uint32_t)ord_contour.size();
             for (uint32_t q = 0; q < p.contour_count; q++) {
                 ord_contour.push_back(contour_base + p.first_contour + q);
@@ -600,7 +605,7 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
             paint[gp] = (uint32_t)p.paint.r | ((uint32_t)p.paint.g << 8) | ((uint32_t)p.paint.b << 16) |
                         ((uint32_t)p.paint.a << 24);
             local[gp] = c ? i : i - sc.clip_path_count;
-            clip[gp] = (!c && p.clip_path >= 0) ? (int32_t)(si.first_path + (uint32_t)p.clip_path) : -1;
+            clip[gp] = p.clip_path >= 0 ? (int32_t)(si.first_path + (uint32_t)p.clip_path) : -1;
             rule[gp] = p.fill_rule;
             isclip[gp] = c ? 1 : 0;
             scene_of[gp] = k;
@@ -626,6 +631,24 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
     }
     hstarts[nc_total] = point_base;
     first_ord[P] = (uint32_t)ord_contour.size();
+    // Clip chains (a clip path clipped by another, the D3D11 level's clip
+    // levels, renderer/src/builder.rs:1124-1220): reject cycles, and keep the
+    // longest chain as the bound of the device-side chain walks.
+    uint32_t chain_max = 0;
+    bool nested = false;
+    for (uint32_t k = 0; k < scene_count; k++) {
+        const SceneInfo& si = r->scenes[k];
+        for (uint32_t q0 = si.first_path; q0 < si.first_path + si.nclip + si.ndraw; q0++) {
+            uint32_t len = 0;
+            for (int32_t q = clip[q0]; q >= 0; q = clip[(uint32_t)q]) {
+                if (++len > si.nclip) return PF_CUDA_ERR_INVALID;  // a cycle of clip paths
+            }
+            chain_max = std::max(chain_max, len);
+            if (isclip[q0] && clip[q0] >= 0) nested = true;
+        }
+    }
+    r->clip_chain_max = chain_max;
+    r->nested_clips = nested;
     const uint32_t nord = (uint32_t)ord_contour.size();
     r->path_local.assign(local.begin(), local.end());
     r->path_is_clip.assign(isclip.begin(), isclip.end());
@@ -1025,6 +1048,7 @@ static int32_t diff_prologue(PFCUDARendererRef r, uint32_t first, uint32_t count
                              const float* draw_alpha, float* out_device) {
     if (!r || !out_device) return PF_CUDA_ERR_INVALID;
     if (!valid_range(r, first, count)) return r->has_scene ? PF_CUDA_ERR_INVALID : PF_CUDA_ERR_NO_SCENE;
+    if (r->nested_clips) return PF_CUDA_ERR_INVALID;  // the adjoint covers single-level clips
     PF_TRY(cudaSetDevice(r->device));
     if (width > 0 || height > 0) {
         bool changed = false;

@@ -97,8 +97,11 @@ class DrawPath:
 
 @dataclass
 class ClipPath:
+    """renderer/src/scene.rs:458-474, 585-612: a clip path may itself be
+    clipped by a previously pushed clip path (a clip chain)."""
     outline: Outline
     fill_rule: FillRule = FillRule.WINDING
+    clip_path: int | None = None
 
 
 _FILL, _TILE, _CLIP, _PATH, _RECT = _abi.record_dtypes()
@@ -153,7 +156,8 @@ class Scene:
         first, count = self._append_outline(clip.outline)
         rec = np.zeros((1,), _PATH)
         rec["first_contour"], rec["contour_count"] = first, count
-        rec["clip_path"], rec["fill_rule"] = -1, int(clip.fill_rule)
+        rec["clip_path"] = -1 if clip.clip_path is None else clip.clip_path
+        rec["fill_rule"] = int(clip.fill_rule)
         self.clip_paths = np.concatenate([self.clip_paths, rec])
         self.epoch += 1
         return len(self.clip_paths) - 1
