@@ -138,7 +138,9 @@ typedef struct PFCUDATile {
     uint32_t alpha_tile_id;     /* 0xffffffff: solid tile */
     uint32_t path_id;           /* index within clip paths or within draw paths */
     uint16_t color;
-    uint8_t  ctrl;
+    uint8_t  ctrl;              /* 0: clip path tile; bit 0 nonzero, bit 1 even-odd; bit 2: behind a
+                                   clip chain (its clip path is itself clipped; coverage is the rule
+                                   applied to the minimum of |mask + backdrop| over the chain) */
     int8_t   backdrop;
 } PFCUDATile;
 /* Clip (renderer/src/gpu_data.rs:436-442). */
