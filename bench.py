@@ -440,6 +440,8 @@ def main():
                     help="svg4k: the 20,000-path 4K frame (default); atlas: the batched glyph atlas; "
                          "diff: forward + adjoint of 256 cubic paths at 1024^2; fit: 64-scene Adam fit")
     ap.add_argument("--fit-steps", type=int, default=200)
+    ap.add_argument("--d3d11", action="store_true",
+                    help="tile with the D3D11 level's semantics (uniform dicing) instead of the CPU tiler's")
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=400)
@@ -485,7 +487,7 @@ def main():
     scene = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=args.seed + rank, scale=args.scale)
     nseg = scene.segment_count
     npts = len(scene.points)
-    r = pf.Renderer(local)
+    r = pf.Renderer(local, pf.RendererOptions(d3d11_semantics=args.d3d11))
     # a dedicated stream: the renderer, the L2 flush and the timing events share it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -599,7 +601,8 @@ def main():
             "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}_scale{args.scale}",
                        "paths": len(scene.draw_paths), "clip_paths": len(scene.clip_paths), "segments": nseg,
                        "points": npts, "width": W, "height": H, "seed": args.seed,
-                       "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}"},
+                       "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}",
+                       "tiling": "d3d11 level (uniform dicing)" if args.d3d11 else "cpu tiler (bit-exact)"},
             "mpx_per_s": round(world * W * H / (ms / 1e3) / 1e6, 3),
             "timing": "CUDA graph replay of the whole frame; ms_per_step_enqueued: the same frame enqueued "
                       "kernel by kernel with stage events",

@@ -105,8 +105,17 @@ typedef struct PFCUDABuildOptions {
 typedef struct PFCUDARendererOptions {
     PFColorF background_color;         /* premultiplied clear colour           */
     int32_t  has_background_color;     /* 0: transparent                       */
-    int32_t  flags;                    /* reserved, 0                          */
+    int32_t  flags;                    /* PF_CUDA_RENDERER_* bits, 0 = default */
 } PFCUDARendererOptions;
+
+/* The D3D11 level's tiling semantics instead of the CPU tiler's (as choosing
+ * RendererLevel::D3D11, renderer/src/gpu/options.rs:41-46): curves diced
+ * uniformly by Sederberg's bound and lines into pieces of at most 16 px, piece
+ * ends rounded to 1/256 px (shaders/d3d11/dice.cs.glsl), binned without the
+ * view-box clip with truncating 8.8 fills (shaders/d3d11/bin.cs.glsl).  Fills
+ * then differ from the CPU tiler's; coverage, resolve and composite do not
+ * change.  Not available for differentiable frames. */
+#define PF_CUDA_RENDERER_D3D11_SEMANTICS 0x1
 
 /* RenderStats (renderer/src/gpu/perf.rs:21-44) + the device counters of the
  * last frame. */

@@ -46,7 +46,7 @@ def lib() -> C.CDLL:
         build()
         l = C.CDLL(LIB_PATH)
         l.pfo_build.restype = C.c_void_p
-        l.pfo_build.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64]
+        l.pfo_build.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_int32]
         l.pfo_free.argtypes = [C.c_void_p]
         l.pfo_counts.argtypes = [C.c_void_p, C.c_void_p]
         l.pfo_fills.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
@@ -90,7 +90,9 @@ def _opts(build_options):
 class OracleFrame:
     """One build of a scene by the CPU tiler restatement."""
 
-    def __init__(self, scene, build_options=None, threads: int = 0, dda_limit: int = 0):
+    def __init__(self, scene, build_options=None, threads: int = 0, dda_limit: int = 0, d3d11: bool = False):
+        """d3d11: the D3D11 level's tiling (uniform dicing, unclipped
+        truncating bins) in place of the CPU tiler's."""
         L = lib()
         self._scene = scene
         self._desc = scene.desc()
@@ -98,7 +100,7 @@ class OracleFrame:
         threads = threads or (os.cpu_count() or 1)
         self.threads = threads
         h = L.pfo_build(C.byref(self._desc), C.byref(self._bo) if self._bo is not None else None, threads,
-                        dda_limit)
+                        dda_limit, 1 if d3d11 else 0)
         if not h:
             raise ValueError("oracle rejected the scene")
         self._h = h

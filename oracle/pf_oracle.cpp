@@ -156,6 +156,7 @@ struct Ctx {
     RectF view_box;
     BuiltPath* bp;
     uint64_t dda_limit;
+    bool d3d11 = false;  // the D3D11 level's binning: no view-box clip, truncating fills
 };
 
 // ObjectBuilder::add_fill (renderer/src/builder.rs:509-553).
@@ -171,6 +172,22 @@ void add_fill(Ctx& ctx, Line seg, int32_t tx, int32_t ty) {
     if (i0 == i2) return;
     uint32_t local = (uint32_t)((tx - bp.tile_rect.minx) + bp.tile_rect.width() * (ty - bp.tile_rect.miny));
     bp.tiles[local].alpha_tile_id = 0;  // get_or_allocate_alpha_tile_index :555-576
+    bp.fills.push_back(OFill{(uint16_t)i0, (uint16_t)i1, (uint16_t)i2, (uint16_t)i3, tx, ty, local});
+}
+
+// addFill of the D3D11 level (shaders/d3d11/bin.cs.glsl:100-125): tile-rect
+// cull, 8.8 conversion by truncation without a clamp to 4095 (a negative
+// value, undefined in GLSL, converts to 0), cull when from.x == to.x.
+void add_fill_d3d11(Ctx& ctx, Line seg, int32_t tx, int32_t ty) {
+    BuiltPath& bp = *ctx.bp;
+    if (!bp.tile_rect.contains(tx, ty)) return;
+    const float ulx = (float)tx * 16.0f, uly = (float)ty * 16.0f;
+    auto q = [](float v) { return (uint32_t)std::min(std::max(v, 0.0f), 65535.0f); };
+    uint32_t i0 = q((seg.fx - ulx) * 256.0f), i1 = q((seg.fy - uly) * 256.0f);
+    uint32_t i2 = q((seg.tx - ulx) * 256.0f), i3 = q((seg.ty - uly) * 256.0f);
+    if (i0 == i2) return;
+    uint32_t local = (uint32_t)((tx - bp.tile_rect.minx) + bp.tile_rect.width() * (ty - bp.tile_rect.miny));
+    bp.tiles[local].alpha_tile_id = 0;
     bp.fills.push_back(OFill{(uint16_t)i0, (uint16_t)i1, (uint16_t)i2, (uint16_t)i3, tx, ty, local});
 }
 
@@ -223,7 +240,11 @@ bool clip_line_segment_to_rect(Line& s, RectF r) {
 void process_line_segment(Ctx& ctx, Line seg) {
     ctx.bp->line_count++;
     RectF clip_box{ctx.view_box.minx, kNegInf, ctx.view_box.maxx, ctx.view_box.maxy};
-    if (!clip_line_segment_to_rect(seg, clip_box)) return;
+    if (!ctx.d3d11 && !clip_line_segment_to_rect(seg, clip_box)) return;
+    auto fill = [&](Line l, int32_t tx, int32_t ty) {
+        if (ctx.d3d11) add_fill_d3d11(ctx, l, tx, ty);
+        else add_fill(ctx, l, tx, ty);
+    };
 
     const float r = 1.0f / 16.0f;
     int32_t ftx = sse_cvt(std::floor(seg.fx * r)), fty = sse_cvt(std::floor(seg.fy * r));
@@ -250,12 +271,12 @@ void process_line_segment(Ctx& ctx, Line seg) {
         if (tcx == ttx && tcy == tty) dir = kNone;
 
         float npx = seg.fx + vx * next_t, npy = seg.fy + vy * next_t;
-        add_fill(ctx, Line{cx, cy, npx, npy}, tcx, tcy);
+        fill(Line{cx, cy, npx, npy}, tcx, tcy);
 
         if (stepy < 0 && dir == kY) {
-            add_fill(ctx, Line{npx, npy, (float)tcx * 16.0f, (float)tcy * 16.0f}, tcx, tcy);
+            fill(Line{npx, npy, (float)tcx * 16.0f, (float)tcy * 16.0f}, tcx, tcy);
         } else if (stepy > 0 && last == kY) {
-            add_fill(ctx, Line{(float)tcx * 16.0f, (float)tcy * 16.0f, cx, cy}, tcx, tcy);
+            fill(Line{(float)tcx * 16.0f, (float)tcy * 16.0f, cx, cy}, tcx, tcy);
         }
 
         if (stepx < 0 && last == kX) adjust_backdrop(ctx, tcx, tcy, 1);
@@ -329,6 +350,68 @@ void process_segment(Ctx& ctx, const Segment& s, int depth) {
     process_segment(ctx, b, depth + 1);
 }
 
+// Uniform dicing of the D3D11 level (shaders/d3d11/dice.cs.glsl:133-217): a
+// curve into n pieces of equal parameter length, n from Sederberg's error
+// bound for tolerance 0.25; a line into pieces of at most 16 px; piece ends
+// rounded to 1/256 px (the packed microline, :83-97).  The FP32 op order is the
+// CUDA level's definition of this mode (dice_seg / dice_count / dice_point).
+void dice_segment(Ctx& ctx, const Segment& s) {
+    const bool curve = s.kind != kLine;
+    float p0x = s.base.fx, p0y = s.base.fy, p3x = s.base.tx, p3y = s.base.ty;
+    float c0x = p0x, c0y = p0y, c1x = p3x, c1y = p3y;
+    if (s.kind == kQuad) {
+        const float third = 1.0f / 3.0f;
+        const float qx2 = s.ctrl.fx + s.ctrl.fx, qy2 = s.ctrl.fy + s.ctrl.fy;
+        c0x = (p0x + qx2) * third; c0y = (p0y + qy2) * third;
+        c1x = (p3x + qx2) * third; c1y = (p3y + qy2) * third;
+    } else if (s.kind == kCubic) {
+        c0x = s.ctrl.fx; c0y = s.ctrl.fy; c1x = s.ctrl.tx; c1y = s.ctrl.ty;
+    }
+    float n;
+    if (curve) {
+        auto dd = [](float a, float b, float c) { return std::fabs((c - 2.0f * b) + a); };
+        const float bx = 6.0f * std::max(dd(p0x, c0x, c1x), dd(c0x, c1x, p3x));
+        const float by = 6.0f * std::max(dd(p0y, c0y, c1y), dd(c0y, c1y, p3y));
+        const float len = std::sqrt(bx * bx + by * by);
+        n = std::sqrt(len / (8.0f * 0.25f));
+    } else {
+        const float dx = p3x - p0x, dy = p3y - p0y;
+        n = std::sqrt(dx * dx + dy * dy) / 16.0f;
+    }
+    const uint32_t kMax = 1u << 16;
+    uint32_t pieces;
+    if (!(n <= (float)kMax)) {
+        ctx.bp->limit_hit = true;
+        pieces = n > (float)kMax ? kMax : 1u;
+    } else {
+        pieces = std::max<uint32_t>((uint32_t)std::ceil(n), 1u);
+    }
+    auto lerp = [](float a, float b, float t) { return a + (b - a) * t; };
+    auto q = [](float v) {
+        return std::nearbyint(std::min(std::max(v, -32768.0f), 32767.0f) * 256.0f) * (1.0f / 256.0f);
+    };
+    float ax = q(p0x), ay = q(p0y);
+    for (uint32_t k = 1; k <= pieces; k++) {
+        const float t = (float)k / (float)pieces;
+        float x, y;
+        if (curve) {
+            const float ux = lerp(p0x, c0x, t), uy = lerp(p0y, c0y, t);
+            const float vx = lerp(c0x, c1x, t), vy = lerp(c0y, c1y, t);
+            const float wx = lerp(c1x, p3x, t), wy = lerp(c1y, p3y, t);
+            const float uvx = lerp(ux, vx, t), uvy = lerp(uy, vy, t);
+            const float vwx = lerp(vx, wx, t), vwy = lerp(vy, wy, t);
+            x = lerp(uvx, vwx, t);
+            y = lerp(uvy, vwy, t);
+        } else {
+            x = lerp(p0x, p3x, t);
+            y = lerp(p0y, p3y, t);
+        }
+        const float bx = q(x), by = q(y);
+        process_line_segment(ctx, Line{ax, ay, bx, by});
+        ax = bx; ay = by;
+    }
+}
+
 // ContourIter::next (content/src/outline.rs:1024-1065) on a closed contour.
 template <typename F>
 void for_each_segment(const Contour& c, F&& f) {
@@ -372,6 +455,7 @@ struct Frame {
     RectI screen{0, 0, 0, 0};
     std::vector<int32_t> zbuf;
     bool limit_hit = false;
+    bool d3d11 = false;  // the D3D11 level's dicing and binning
 };
 
 // Tiler::new + generate_tiles (renderer/src/tiler.rs:40-91) up to generate_fills.
@@ -404,9 +488,12 @@ void build_fills(Frame& fr, uint32_t p, uint64_t dda_limit) {
         }
     if (!in.is_clip && in.clip_path >= 0)
         bp.clips.assign(bp.tiles.size(), OClip{kInvalid, 0, kInvalid, 0});
-    Ctx ctx{fr.view_box, &bp, dda_limit};
+    Ctx ctx{fr.view_box, &bp, dda_limit, fr.d3d11};
     for (const Contour& c : in.contours)
-        for_each_segment(c, [&](const Segment& s) { process_segment(ctx, s, 0); });
+        for_each_segment(c, [&](const Segment& s) {
+            if (fr.d3d11) dice_segment(ctx, s);
+            else process_segment(ctx, s, 0);
+        });
 }
 
 // The tile of path q at (tx, ty), or NULL outside its tile rect.
@@ -1193,10 +1280,12 @@ struct PFOFrame {
 
 extern "C" {
 
+// flags: PF_CUDA_RENDERER_D3D11_SEMANTICS for the D3D11 level's tiling.
 PFOFrame* pfo_build(const PFCUDASceneDesc* scene, const PFCUDABuildOptions* opts, int threads,
-                    uint64_t dda_limit) {
+                    uint64_t dda_limit, int32_t flags) {
     PFOFrame* f = new PFOFrame();
     if (!make_frame(scene, opts, f->fr)) { delete f; return nullptr; }
+    f->fr.d3d11 = (flags & PF_CUDA_RENDERER_D3D11_SEMANTICS) != 0;
     build_frame(f->fr, threads, dda_limit ? dda_limit : (1ull << 24));
     return f;
 }

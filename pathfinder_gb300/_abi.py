@@ -24,6 +24,8 @@ PF_CUDA_ERR_NO_SCENE = 6
 PF_MEMORY_HOST = 0
 PF_MEMORY_DEVICE = 1
 
+PF_CUDA_RENDERER_D3D11_SEMANTICS = 0x1
+
 PF_SCENE_STARS_512 = 1
 PF_SCENE_SVG_4K = 2
 PF_SCENE_GLYPH_ATLAS = 3

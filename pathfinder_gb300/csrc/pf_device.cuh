@@ -219,14 +219,38 @@ __device__ __forceinline__ bool make_fill(const PathCtx& pc, Line s, int32_t tx,
     return true;
 }
 
+// addFill of the D3D11 level (shaders/d3d11/bin.cs.glsl:100-125): tile-rect
+// cull, 8.8 conversion by truncation (no clamp to 4095; a negative value,
+// undefined in GLSL, converts to 0), cull when from.x == to.x.
+__device__ __forceinline__ bool make_fill_d3d11(const PathCtx& pc, Line s, int32_t tx, int32_t ty, uint2& rec,
+                                                uint32_t& g) {
+    if (!(pc.minx <= tx && pc.miny <= ty && tx <= pc.maxx - 1 && ty <= pc.maxy - 1)) return false;
+    const float ulx = fmul(i2f(tx), 16.0f), uly = fmul(i2f(ty), 16.0f);
+    auto q = [](float v) { return (uint32_t)fminf(fmaxf(v, 0.0f), 65535.0f); };  // truncates
+    const uint32_t i0 = q(fmul(fsub(s.fx, ulx), 256.0f)), i1 = q(fmul(fsub(s.fy, uly), 256.0f));
+    const uint32_t i2 = q(fmul(fsub(s.tx, ulx), 256.0f)), i3 = q(fmul(fsub(s.ty, uly), 256.0f));
+    if (i0 == i2) return false;
+    rec.x = i0 | (i1 << 16);
+    rec.y = i2 | (i3 << 16);
+    g = pc.tile_base + (uint32_t)(tx - pc.minx) + (uint32_t)(pc.maxx - pc.minx) * (uint32_t)(ty - pc.miny);
+    return true;
+}
+
+// Fill conversions of the binning pass.
+enum FillMode : int {
+    kFillCpu = 0,    // the CPU tiler: view-box clip, 8.8 round-to-nearest-even clamped to 4095
+    kFillF32 = 1,    // differentiable frames: FP32 tile-local endpoints
+    kFillD3D11 = 2,  // the D3D11 level: no view-box clip, truncating 8.8 conversion
+};
+
 // process_line_segment (renderer/src/tiler.rs:191-308).  `sink` receives
 // sink.fill(rec, g) for every kept fill in emission order and
-// sink.backdrop(tx, ty, delta) for every backdrop adjustment.
-// DIFF: fills keep FP32 endpoints (make_fill_f) and reach sink.fill as float4.
-template <bool DIFF = false, class Sink>
+// sink.backdrop(tx, ty, delta) for every backdrop adjustment.  kFillF32
+// fills reach sink.fill as float4, the others as packed LineSegmentU16.
+template <int MODE = kFillCpu, class Sink>
 __device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink, uint32_t dda_limit,
                                          uint32_t* status) {
-    if (!clip_to_view(seg, pc.vminx, pc.vmaxx, pc.vmaxy)) return;
+    if (MODE != kFillD3D11 && !clip_to_view(seg, pc.vminx, pc.vmaxx, pc.vmaxy)) return;
     const float r = 1.0f / 16.0f;
     int32_t ftx = cvt_rne(floorf(fmul(seg.fx, r))), fty = cvt_rne(floorf(fmul(seg.fy, r)));
     int32_t ttx = cvt_rne(floorf(fmul(seg.tx, r))), tty = cvt_rne(floorf(fmul(seg.ty, r)));
@@ -250,9 +274,12 @@ __device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink
         float npx = fadd(seg.fx, fmul(vx, next_t)), npy = fadd(seg.fy, fmul(vy, next_t));
         auto add = [&](Line l) {
             uint32_t g;
-            if constexpr (DIFF) {
+            if constexpr (MODE == kFillF32) {
                 float4 rec;
                 if (make_fill_f(pc, l, tcx, tcy, rec, g)) sink.fill(rec, g);
+            } else if constexpr (MODE == kFillD3D11) {
+                uint2 rec;
+                if (make_fill_d3d11(pc, l, tcx, tcy, rec, g)) sink.fill(rec, g);
             } else {
                 uint2 rec;
                 if (make_fill(pc, l, tcx, tcy, rec, g)) sink.fill(rec, g);
@@ -278,9 +305,9 @@ __device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink
     }
 }
 
-// process_segment (renderer/src/tiler.rs:166-184) with an explicit stack in
-// place of recursion: calls emit(Line) for every flattened line in the same
-// depth-first order as the reference's recursion.
+// process_segment (renderer/src/tiler.rs:166-184) without recursion: calls
+// emit(Line, addr, depth) for every flattened line in the same depth-first
+// order as the reference's recursion.
 template <class Emit>
 __device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Emit&& emit, uint32_t* status) {
     float2 p0 = pts[sr.x];
@@ -329,6 +356,82 @@ __device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Em
             c = ((addr >> i) & 1u) ? b : a;
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// Uniform dicing of the D3D11 level (shaders/d3d11/dice.cs.glsl:133-217):
+// a curve is cut into n pieces of equal parameter length, n from Sederberg's
+// error bound for tolerance 0.25; a line into n pieces of at most 16 px; the
+// piece ends are rounded to 1/256 px (the packed microline, :83-97).  The FP32
+// op order here is this level's own definition (the oracle repeats it).
+// ---------------------------------------------------------------------------
+constexpr float kDiceTolerance = 0.25f, kMicrolineLength = 16.0f;
+constexpr uint32_t kMaxDicePieces = 1u << 16;
+
+struct DiceSeg { float2 p0, c0, c1, p3; bool curve; };
+
+__device__ __forceinline__ DiceSeg dice_seg(const float2* pts, SegRec sr) {
+    DiceSeg d;
+    d.p0 = pts[sr.x];
+    d.p3 = pts[sr.y];
+    d.curve = sr.z != (int)kSegLine;
+    d.c0 = d.p0; d.c1 = d.p3;
+    if (sr.z == (int)kSegQuad) {
+        const float2 q = pts[sr.x + 1];
+        const float third = 1.0f / 3.0f;
+        const float qx2 = fadd(q.x, q.x), qy2 = fadd(q.y, q.y);
+        d.c0 = make_float2(fmul(fadd(d.p0.x, qx2), third), fmul(fadd(d.p0.y, qy2), third));
+        d.c1 = make_float2(fmul(fadd(d.p3.x, qx2), third), fmul(fadd(d.p3.y, qy2), third));
+    } else if (sr.z == (int)kSegCubic) {
+        d.c0 = pts[sr.x + 1];
+        d.c1 = pts[sr.x + 2];
+    }
+    return d;
+}
+
+// Pieces of one segment (1 .. kMaxDicePieces; *limited when capped or not finite).
+__device__ __forceinline__ uint32_t dice_count(const DiceSeg& d, bool* limited) {
+    float n;
+    if (d.curve) {
+        auto dd = [](float a, float b, float c) { return fabsf(fadd(fsub(c, fmul(2.0f, b)), a)); };
+        const float bx = fmul(6.0f, fmaxf(dd(d.p0.x, d.c0.x, d.c1.x), dd(d.c0.x, d.c1.x, d.p3.x)));
+        const float by = fmul(6.0f, fmaxf(dd(d.p0.y, d.c0.y, d.c1.y), dd(d.c0.y, d.c1.y, d.p3.y)));
+        const float len = __fsqrt_rn(fadd(fmul(bx, bx), fmul(by, by)));
+        n = __fsqrt_rn(fdiv(len, 8.0f * kDiceTolerance));
+    } else {
+        const float dx = fsub(d.p3.x, d.p0.x), dy = fsub(d.p3.y, d.p0.y);
+        n = fdiv(__fsqrt_rn(fadd(fmul(dx, dx), fmul(dy, dy))), kMicrolineLength);
+    }
+    if (!(n <= (float)kMaxDicePieces)) {  // too many pieces, or not finite
+        *limited = true;
+        return n > (float)kMaxDicePieces ? kMaxDicePieces : 1u;
+    }
+    const uint32_t k = (uint32_t)ceilf(n);
+    return k > 1u ? k : 1u;
+}
+
+__device__ __forceinline__ float dice_lerp(float a, float b, float t) { return fadd(a, fmul(fsub(b, a), t)); }
+__device__ __forceinline__ float dice_q(float v) {  // round to 1/256 px (microline packing)
+    return fmul(rintf(fmul(fminf(fmaxf(v, -32768.0f), 32767.0f), 256.0f)), 1.0f / 256.0f);
+}
+
+// Point of piece end k (1 .. n) of the segment, rounded to 1/256 px.
+__device__ __forceinline__ float2 dice_point(const DiceSeg& d, uint32_t k, uint32_t n) {
+    const float t = fdiv((float)k, (float)n);
+    float x, y;
+    if (d.curve) {
+        const float ax = dice_lerp(d.p0.x, d.c0.x, t), ay = dice_lerp(d.p0.y, d.c0.y, t);
+        const float bx = dice_lerp(d.c0.x, d.c1.x, t), by = dice_lerp(d.c0.y, d.c1.y, t);
+        const float cx = dice_lerp(d.c1.x, d.p3.x, t), cy = dice_lerp(d.c1.y, d.p3.y, t);
+        const float abx = dice_lerp(ax, bx, t), aby = dice_lerp(ay, by, t);
+        const float bcx = dice_lerp(bx, cx, t), bcy = dice_lerp(by, cy, t);
+        x = dice_lerp(abx, bcx, t);
+        y = dice_lerp(aby, bcy, t);
+    } else {
+        x = dice_lerp(d.p0.x, d.p3.x, t);
+        y = dice_lerp(d.p0.y, d.p3.y, t);
+    }
+    return make_float2(dice_q(x), dice_q(y));
 }
 
 // ---------------------------------------------------------------------------

@@ -62,6 +62,7 @@ struct FrameDev {
     // every flattened line, and per visible (screen tile, path tile) entry the
     // composite tape the adjoint reads back.
     int diff;
+    int d3d11;                   // the D3D11 level's semantics: uniform dicing, truncating bins
     float4*   fills_f;           // [fill_cap] tile-local FP32 fills
     uint32_t* line_seg;          // [line_cap] global segment of each line
     float2*   line_t;            // [line_cap] curve parameters of the line's ends

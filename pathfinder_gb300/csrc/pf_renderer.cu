@@ -183,6 +183,7 @@ Range make_range(const PFCUDARenderer* r, uint32_t s0, uint32_t count) {
 FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool diff = false) {
     FrameDev f{};
     f.diff = diff ? 1 : 0;
+    f.d3d11 = (!diff && (r->options.flags & PF_CUDA_RENDERER_D3D11_SEMANTICS)) ? 1 : 0;
     f.path.alpha_f = diff ? r->alpha_in.p : nullptr;
     f.path.draw_index = r->draw_index.p;
     f.fills_f = r->fills_f.p;
@@ -470,6 +471,7 @@ int32_t PFCUDARendererCreate(int32_t device_ordinal, const PFCUDARendererOptions
                              PFCUDARendererRef* out_renderer) {
     if (!out_renderer) return PF_CUDA_ERR_INVALID;
     *out_renderer = nullptr;
+    if (options && (options->flags & ~PF_CUDA_RENDERER_D3D11_SEMANTICS)) return PF_CUDA_ERR_INVALID;
     int count = 0;
     cudaError_t e = cudaGetDeviceCount(&count);
     if (e != cudaSuccess || count == 0) return PF_CUDA_ERR_NO_DEVICE;
@@ -527,7 +529,7 @@ int32_t PFCUDARendererSetStream(PFCUDARendererRef r, void* stream) {
 }
 
 int32_t PFCUDARendererSetOptions(PFCUDARendererRef r, const PFCUDARendererOptions* options) {
-    if (!r || !options) return PF_CUDA_ERR_INVALID;
+    if (!r || !options || (options->flags & ~PF_CUDA_RENDERER_D3D11_SEMANTICS)) return PF_CUDA_ERR_INVALID;
     r->options = *options;
     release_graph(r);
     return PF_CUDA_OK;
@@ -1049,6 +1051,7 @@ static int32_t diff_prologue(PFCUDARendererRef r, uint32_t first, uint32_t count
     if (!r || !out_device) return PF_CUDA_ERR_INVALID;
     if (!valid_range(r, first, count)) return r->has_scene ? PF_CUDA_ERR_INVALID : PF_CUDA_ERR_NO_SCENE;
     if (r->nested_clips) return PF_CUDA_ERR_INVALID;  // the adjoint covers single-level clips
+    if (r->options.flags & PF_CUDA_RENDERER_D3D11_SEMANTICS) return PF_CUDA_ERR_INVALID;  // pieces rounded to 1/256 px
     PF_TRY(cudaSetDevice(r->device));
     if (width > 0 || height > 0) {
         bool changed = false;

@@ -404,7 +404,14 @@ __global__ void __launch_bounds__(256) k_flatten_count(FrameDev f) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= f.seg_count) return;
     uint32_t n = 0;
-    flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&, uint32_t, int) { n++; }, &f.counters->status);
+    if (f.d3d11) {
+        bool limited = false;
+        n = dice_count(dice_seg(f.pts, f.segs[f.seg_begin + s]), &limited);
+        if (limited) atomicOr(&f.counters->status, kStatusDepthLimit);
+    } else {
+        flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&, uint32_t, int) { n++; },
+                        &f.counters->status);
+    }
     f.seg_line_count[s] = n;
 }
 
@@ -425,6 +432,19 @@ __global__ void __launch_bounds__(256) k_flatten_emit(FrameDev f) {
     const uint32_t sg = f.seg_begin + s;
     const SegRec sr = f.segs[sg];
     uint32_t l = f.seg_line_base[s];
+    if (!DIFF && f.d3d11) {  // uniform pieces, ends rounded to 1/256 px
+        const DiceSeg d = dice_seg(f.pts, sr);
+        bool limited = false;
+        const uint32_t n = dice_count(d, &limited);
+        float2 a = make_float2(dice_q(d.p0.x), dice_q(d.p0.y));
+        for (uint32_t k = 1; k <= n; k++, l++) {
+            const float2 b = dice_point(d, k, n);
+            f.lines[l] = make_float4(a.x, a.y, b.x, b.y);
+            f.line_path[l] = (uint32_t)sr.w;
+            a = b;
+        }
+        return;
+    }
     flatten_segment(f.pts, sr, [&](const Line& ln, uint32_t addr, int d) {
         f.lines[l] = make_float4(ln.fx, ln.fy, ln.tx, ln.ty);
         f.line_path[l] = (uint32_t)sr.w;
@@ -491,7 +511,7 @@ struct CountSink {
     }
 };
 
-template <bool DIFF>
+template <int MODE>
 __global__ void __launch_bounds__(512) k_bin_count(FrameDev f) {
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     const uint32_t L = line_total(f);
@@ -499,7 +519,7 @@ __global__ void __launch_bounds__(512) k_bin_count(FrameDev f) {
         const float4 ln = f.lines[l];
         const PathCtx pc = path_ctx(f, f.line_path[l]);
         CountSink sink{&pc, f.tile_fill_count, f.tile_delta, f.col_backdrop, 0};
-        dda_line<DIFF>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+        dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
         f.line_fill_count[l] = sink.n;
     }
 }
@@ -533,7 +553,7 @@ struct EmitSinkF {
     __device__ __forceinline__ void backdrop(int32_t, int32_t, int32_t) {}
 };
 
-template <bool DIFF>
+template <int MODE>
 __global__ void __launch_bounds__(512) k_bin_emit(FrameDev f) {
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     if (f.counters->fills > f.fill_cap) return;
@@ -542,20 +562,26 @@ __global__ void __launch_bounds__(512) k_bin_emit(FrameDev f) {
         if (f.line_fill_count[l] == 0) continue;
         const float4 ln = f.lines[l];
         const PathCtx pc = path_ctx(f, f.line_path[l]);
-        if constexpr (DIFF) {
+        if constexpr (MODE == kFillF32) {
             EmitSinkF sink{f.fills_f, f.tile_fill_base, f.tile_fill_count, f.fill_cap};
-            dda_line<true>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+            dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
         } else {
             EmitSink sink{f.fills, f.fill_e, f.tile_fill_base, f.tile_fill_count, f.fill_cap, f.line_fill_base[l]};
-            dda_line(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+            dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
         }
     }
 }
 
+// The binning pass's fill conversion for the frame.
+static int fill_mode(const FrameDev& f) { return f.diff ? kFillF32 : (f.d3d11 ? kFillD3D11 : kFillCpu); }
+
 void launch_bin_count(const FrameDev& f, cudaStream_t s) {
     count_launch();
-    if (f.diff) k_bin_count<true><<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f);
-    else k_bin_count<false><<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f);
+    const uint32_t blocks = 152 * f.tune.bin_blocks_per_sm;
+    const int m = fill_mode(f);
+    if (m == kFillF32) k_bin_count<kFillF32><<<blocks, f.tune.bin_threads, 0, s>>>(f);
+    else if (m == kFillD3D11) k_bin_count<kFillD3D11><<<blocks, f.tune.bin_threads, 0, s>>>(f);
+    else k_bin_count<kFillCpu><<<blocks, f.tune.bin_threads, 0, s>>>(f);
 }
 
 __global__ void k_check_fills(FrameDev f) {
@@ -569,8 +595,11 @@ __global__ void k_check_fills(FrameDev f) {
 void launch_bin_emit(const FrameDev& f, cudaStream_t s) {
     { count_launch(); k_check_fills<<<1, 1, 0, s>>>(f); }
     count_launch();
-    if (f.diff) k_bin_emit<true><<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f);
-    else k_bin_emit<false><<<152 * f.tune.bin_blocks_per_sm, f.tune.bin_threads, 0, s>>>(f);
+    const uint32_t blocks = 152 * f.tune.bin_blocks_per_sm;
+    const int m = fill_mode(f);
+    if (m == kFillF32) k_bin_emit<kFillF32><<<blocks, f.tune.bin_threads, 0, s>>>(f);
+    else if (m == kFillD3D11) k_bin_emit<kFillD3D11><<<blocks, f.tune.bin_threads, 0, s>>>(f);
+    else k_bin_emit<kFillCpu><<<blocks, f.tune.bin_threads, 0, s>>>(f);
 }
 
 }  // namespace pf

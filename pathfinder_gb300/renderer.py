@@ -50,8 +50,11 @@ class BuildOptions:
 
 @dataclass
 class RendererOptions:
-    """renderer/src/gpu/options.rs:19-33."""
+    """renderer/src/gpu/options.rs:19-33.  d3d11_semantics tiles as the D3D11
+    level does (uniform dicing, unclipped truncating bins) instead of as the
+    CPU tiler does (PF_CUDA_RENDERER_D3D11_SEMANTICS)."""
     background_color: ColorF | None = None
+    d3d11_semantics: bool = False
 
     def to_c(self) -> _abi.PFCUDARendererOptions:
         o = _abi.PFCUDARendererOptions()
@@ -59,6 +62,8 @@ class RendererOptions:
             c = self.background_color
             o.background_color = _abi.PFColorF(c.r, c.g, c.b, c.a)
             o.has_background_color = 1
+        if self.d3d11_semantics:
+            o.flags |= _abi.PF_CUDA_RENDERER_D3D11_SEMANTICS
         return o
 
 
