@@ -58,22 +58,92 @@ typedef struct PFTransform2F { float m00, m01, m10, m11; PFVector2F vector; } PF
 #define PF_POINT_FLAG_CONTROL_POINT_1 0x02
 #define PF_FILL_RULE_WINDING  0
 #define PF_FILL_RULE_EVEN_ODD 1
-#define PF_BLEND_MODE_SRC_OVER 0   /* the only blend mode on this path */
+/* BlendMode (content/src/effects.rs:99-167), numbered with the default
+ * (SrcOver) at 0.  Porter-Duff modes blend with the reference's blend states
+ * (renderer/src/gpu/blend.rs); the others mix with the destination as the
+ * reference's composite() does (shaders/tile_fragment.inc.glsl:414-535).
+ * Clear, Copy, SrcIn, DestIn, SrcOut and DestAtop are destructive: the path's
+ * tiles span the whole view box (renderer/src/builder.rs:430-434). */
+#define PF_BLEND_MODE_SRC_OVER     0
+#define PF_BLEND_MODE_CLEAR        1
+#define PF_BLEND_MODE_COPY         2
+#define PF_BLEND_MODE_SRC_IN       3
+#define PF_BLEND_MODE_SRC_OUT      4
+#define PF_BLEND_MODE_SRC_ATOP     5
+#define PF_BLEND_MODE_DEST_IN      6
+#define PF_BLEND_MODE_DEST_OUT     7
+#define PF_BLEND_MODE_DEST_OVER    8
+#define PF_BLEND_MODE_DEST_ATOP    9
+#define PF_BLEND_MODE_XOR          10
+#define PF_BLEND_MODE_LIGHTER      11
+#define PF_BLEND_MODE_DARKEN       12
+#define PF_BLEND_MODE_LIGHTEN      13
+#define PF_BLEND_MODE_MULTIPLY     14
+#define PF_BLEND_MODE_SCREEN       15
+#define PF_BLEND_MODE_HARD_LIGHT   16
+#define PF_BLEND_MODE_OVERLAY      17
+#define PF_BLEND_MODE_COLOR_DODGE  18
+#define PF_BLEND_MODE_COLOR_BURN   19
+#define PF_BLEND_MODE_SOFT_LIGHT   20
+#define PF_BLEND_MODE_DIFFERENCE   21
+#define PF_BLEND_MODE_EXCLUSION    22
+#define PF_BLEND_MODE_HUE          23
+#define PF_BLEND_MODE_SATURATION   24
+#define PF_BLEND_MODE_COLOR        25
+#define PF_BLEND_MODE_LUMINOSITY   26
+#define PF_BLEND_MODE_COUNT        27
+
+/* Gradients (content/src/gradient.rs:27-81). */
+#define PF_GRADIENT_LINEAR      0
+#define PF_GRADIENT_RADIAL      1
+#define PF_GRADIENT_WRAP_CLAMP  0
+#define PF_GRADIENT_WRAP_REPEAT 1
+
+/* ColorStop (content/src/gradient.rs:38-44). */
+typedef struct PFCUDAColorStop {
+    float    offset;                   /* 0 .. 1 */
+    PFColorU color;
+} PFCUDAColorStop;
+
+/* Gradient (content/src/gradient.rs:27-33, 46-72), in scene coordinates.
+ * Stops are ordered by offset, equal offsets in the order given
+ * (Gradient::add, :158-164).  Rendered through a 256-texel ramp sampled with
+ * linear filtering, as the reference's gradient tiles
+ * (renderer/src/paint.rs:855-863). */
+typedef struct PFCUDAGradient {
+    int32_t  kind;                     /* PF_GRADIENT_LINEAR / PF_GRADIENT_RADIAL            */
+    int32_t  wrap;                     /* PF_GRADIENT_WRAP_*                                 */
+    PFVector2F from, to;               /* linear: the line; radial: the line between centres */
+    float    radius0, radius1;         /* radial                                             */
+    PFTransform2F transform;           /* radial: gradient space -> scene space              */
+    const PFCUDAColorStop* stops;      /* host memory                                        */
+    uint32_t stop_count;
+    uint32_t reserved;
+} PFCUDAGradient;
+
+/* Gradient::sample (content/src/gradient.rs:188-211) of the gradient's
+ * stops at t, and the 256-texel colour ramp the composite samples
+ * (texel x = sample((x + 0.5) / 256), renderer/src/paint.rs:855-863).
+ * Host-only; no device or renderer is needed. */
+int32_t PFCUDAGradientSample(const PFCUDAGradient* gradient, float t, PFColorU* out);
+int32_t PFCUDAGradientRamp(const PFCUDAGradient* gradient, PFColorU* out_256);
 
 #define PF_MEMORY_HOST   0
 #define PF_MEMORY_DEVICE 1
 
 /* One path of the scene: a range of contours of the shared outline buffers.
  * Mirrors DrawPath / ClipPath (renderer/src/scene.rs:441-472): outline,
- * paint (a solid colour here), fill rule, optional clip path. */
+ * paint (a colour, or a colour and a gradient), fill rule, blend mode,
+ * optional clip path. */
 typedef struct PFCUDAPath {
     uint32_t first_contour;
     uint32_t contour_count;
     PFColorU paint;          /* draw paths: solid paint; ignored for clip paths  */
     int32_t  clip_path;      /* draw paths: index into clip paths, or -1         */
     uint8_t  fill_rule;      /* PF_FILL_RULE_*                                   */
-    uint8_t  blend_mode;     /* PF_BLEND_MODE_SRC_OVER                           */
-    uint16_t reserved;
+    uint8_t  blend_mode;     /* draw paths: PF_BLEND_MODE_*                      */
+    uint16_t gradient;       /* draw paths: 0 = solid paint, k = gradient k - 1 of the
+                                scene (its colour SrcIn the paint: ramp alpha x paint alpha) */
 } PFCUDAPath;
 
 /* The scene as flat outline buffers.  Every contour is treated as closed
@@ -92,6 +162,8 @@ typedef struct PFCUDASceneDesc {
     uint32_t draw_path_count;
     PFRectF  view_box;                 /* Scene::set_view_box                 */
     int32_t  memory;                   /* PF_MEMORY_* for points/flags/starts */
+    const PFCUDAGradient* gradients;   /* host memory; may be NULL when unused */
+    uint32_t gradient_count;
 } PFCUDASceneDesc;
 
 /* BuildOptions (renderer/src/options.rs:53-61): only the 2-D transform is on
@@ -192,8 +264,9 @@ int32_t PFCUDASceneUpload(PFCUDARendererRef renderer, const PFCUDASceneDesc* sce
  * (renderer/src/gpu/renderer.rs:350-460) with the seven D3D11 dispatches
  * (renderer/src/gpu/d3d11/renderer.rs:427-782) replaced by this library's
  * kernels.  Writes premultiplied RGBA8, row 0 = top, into `out_rgba8`
- * (width*height*4 bytes; host or device memory per out_memory).
- * Synchronises the stream before returning. */
+ * (width*height*4 bytes; host or device memory per out_memory): every pixel
+ * of the view box's 16x16 screen tiles; pixels outside them keep the
+ * buffer's contents.  Synchronises the stream before returning. */
 int32_t PFCUDARenderScene(PFCUDARendererRef renderer,
                           const PFCUDABuildOptions* options,
                           int32_t width, int32_t height,

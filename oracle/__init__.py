@@ -62,6 +62,10 @@ def lib() -> C.CDLL:
         l.pfo_fill_coverage.argtypes = [C.c_void_p, C.c_void_p]
         l.pfo_area_lut_value.restype = C.c_uint8
         l.pfo_area_lut_value.argtypes = [C.c_int, C.c_int, C.c_int]
+        l.pfo_gradient_sample.restype = C.c_int32
+        l.pfo_gradient_sample.argtypes = [C.c_void_p, C.c_float, C.c_void_p]
+        l.pfo_round_f16.restype = C.c_float
+        l.pfo_round_f16.argtypes = [C.c_float]
         l.pfo_sse_cvt.restype = C.c_int32
         l.pfo_sse_cvt.argtypes = [C.c_float]
         l.pfo_diff_build.restype = C.c_void_p

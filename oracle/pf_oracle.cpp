@@ -87,7 +87,112 @@ struct PathInput {
     int32_t clip_path;   // draw paths only
     PFColorU paint;
     uint32_t path_index; // within clip paths or draw paths
+    uint8_t blend = 0;   // draw paths: PF_BLEND_MODE_*
+    uint32_t gradient = 0;  // draw paths: gradient index + 1, 0 = solid paint
+    bool occludes = false;  // BuiltDrawPath::occludes (renderer/src/builder.rs:80-94)
 };
+
+// ---------------------------------------------------------------------------
+// Paint effects: gradients (content/src/gradient.rs, renderer/src/paint.rs)
+// ---------------------------------------------------------------------------
+// Round to the nearest binary16 value, ties to even (the f16::from_f32 of the
+// reference's RGBA16F metadata texture, renderer/src/gpu/renderer.rs:702-763).
+float o_round_f16(float x) {
+    if (std::isnan(x)) return x;
+    double ax = std::fabs((double)x);
+    if (ax >= 65520.0) return x > 0 ? INFINITY : -INFINITY;
+    double q = std::ldexp(1.0, -24);  // subnormal quantum
+    if (ax >= std::ldexp(1.0, -14)) q = std::ldexp(1.0, std::ilogb(ax) - 10);
+    return (float)(std::nearbyint((double)x / q) * q);
+}
+
+// Gradient::add (content/src/gradient.rs:158-164): each stop goes after every
+// stop whose offset is <= its own.
+std::vector<PFCUDAColorStop> o_ordered_stops(const PFCUDAGradient& g) {
+    std::vector<PFCUDAColorStop> out;
+    for (uint32_t i = 0; i < g.stop_count; i++) {
+        size_t k = 0;
+        while (k < out.size() && out[k].offset <= g.stops[i].offset) k++;
+        out.insert(out.begin() + (long)k, g.stops[i]);
+    }
+    return out;
+}
+
+// Gradient::sample (content/src/gradient.rs:188-211) in single precision, with
+// ColorU::to_f32, ColorF::lerp and ColorF::to_u8 (color/src/lib.rs:70-73,
+// 163-171; to_i32x4 rounds to nearest even).
+PFColorU o_gradient_sample(const std::vector<PFCUDAColorStop>& stops, float t) {
+    if (stops.empty()) return PFColorU{0, 0, 0, 0};
+    t = std::fmin(1.0f, std::fmax(0.0f, t));
+    size_t lo = 0, hi = stops.size();  // first stop not (offset < t || offset == 0)
+    while (lo < hi) {
+        size_t mid = (lo + hi) / 2;
+        if (stops[mid].offset < t || stops[mid].offset == 0.0f) lo = mid + 1;
+        else hi = mid;
+    }
+    size_t upper = std::min(lo, stops.size() - 1);
+    size_t lower = upper > 0 ? upper - 1 : upper;
+    const PFCUDAColorStop &a = stops[lower], &b = stops[upper];
+    float denom = b.offset - a.offset;
+    if (denom == 0.0f) return a.color;
+    float ratio = std::fmin((t - a.offset) / denom, 1.0f);
+    const float k = 1.0f / 255.0f;
+    float ca[4] = {a.color.r * k, a.color.g * k, a.color.b * k, a.color.a * k};
+    float cb[4] = {b.color.r * k, b.color.g * k, b.color.b * k, b.color.a * k};
+    uint8_t o[4];
+    for (int c = 0; c < 4; c++) o[c] = (uint8_t)sse_cvt((ca[c] + (cb[c] - ca[c]) * ratio) * 255.0f);
+    return PFColorU{o[0], o[1], o[2], o[3]};
+}
+
+struct OGrad {
+    int32_t kind = 0, wrap = 0;
+    float g[6] = {0, 0, 0, 0, 0, 0};  // scene -> colour texture coordinate (row-major 2x3)
+    float fx = 0, fy = 0, vx = 0, vy = 0, r0 = 0, r1 = 0;  // radial, rounded to binary16
+    PFColorU ramp[256];
+    bool opaque = true;
+};
+
+// The gradient's colour ramp (renderer/src/paint.rs:855-863) and texture
+// transform (:603-616): linear, the projection onto the gradient line; radial,
+// Transform2F::inverse of its transform (geometry/src/transform2d.rs:60-72,
+// 294-298).  A degenerate linear gradient samples u = 0 here (the reference
+// divides by zero); a singular radial transform is rejected.
+bool o_build_gradient(const PFCUDAGradient& in, OGrad& g) {
+    if (in.kind != PF_GRADIENT_LINEAR && in.kind != PF_GRADIENT_RADIAL) return false;
+    if (in.wrap != PF_GRADIENT_WRAP_CLAMP && in.wrap != PF_GRADIENT_WRAP_REPEAT) return false;
+    if (in.stop_count && !in.stops) return false;
+    g.kind = in.kind;
+    g.wrap = in.wrap;
+    std::vector<PFCUDAColorStop> stops = o_ordered_stops(in);
+    for (int x = 0; x < 256; x++) g.ramp[x] = o_gradient_sample(stops, ((float)x + 0.5f) / 256.0f);
+    g.opaque = true;  // Gradient::is_opaque (content/src/gradient.rs:215-217)
+    for (const PFCUDAColorStop& st : stops) g.opaque = g.opaque && st.color.a == 255;
+    if (in.kind == PF_GRADIENT_LINEAR) {
+        float dx = in.to.x - in.from.x, dy = in.to.y - in.from.y;
+        float l2 = dx * dx + dy * dy;  // LineSegment2F::square_length
+        if (l2 > 0.0f) {
+            float m0x = dx / l2, m0y = dy / l2;
+            g.g[0] = m0x;
+            g.g[1] = m0y;
+            g.g[2] = m0x * -in.from.x + m0y * -in.from.y;
+        }
+    } else {
+        const PFTransform2F& t = in.transform;
+        float det = t.m00 * t.m11 - t.m01 * t.m10;
+        if (det == 0.0f) return false;
+        float r = 1.0f / det;
+        float a = r * t.m11, b = r * -t.m01, c = r * -t.m10, d = r * t.m00;
+        g.g[0] = a; g.g[1] = b; g.g[2] = -(a * t.vector.x + b * t.vector.y);
+        g.g[3] = c; g.g[4] = d; g.g[5] = -(c * t.vector.x + d * t.vector.y);
+        g.fx = o_round_f16(in.from.x);
+        g.fy = o_round_f16(in.from.y);
+        g.vx = o_round_f16(in.to.x - in.from.x);
+        g.vy = o_round_f16(in.to.y - in.from.y);
+        g.r0 = o_round_f16(in.radius0);
+        g.r1 = o_round_f16(in.radius1);
+    }
+    return true;
+}
 
 // Outline bounds (content/src/outline.rs:180-193 push_contour, :1086-1092
 // union_rect): union of every point, control points included.
@@ -454,6 +559,8 @@ struct Frame {
     std::vector<uint32_t> alpha_owner;        // alpha id -> global tile index owning the fills
     RectI screen{0, 0, 0, 0};
     std::vector<int32_t> zbuf;
+    std::vector<OGrad> grads;                 // the scene's gradients
+    float inv[6] = {1, 0, 0, 0, 1, 0};        // frame pixel -> scene (inverse build transform)
     bool limit_hit = false;
     bool d3d11 = false;  // the D3D11 level's dicing and binning
 };
@@ -468,6 +575,12 @@ void build_fills(Frame& fr, uint32_t p, uint64_t dda_limit) {
         RectF isect;
         if (rect_intersection(ob, fr.view_box, &isect)) bounds = isect;
     }
+    // A destructive blend mode tiles the whole view box (renderer/src/builder.rs:430-434,
+    // BlendMode::is_destructive, content/src/effects.rs:233-262).
+    const uint8_t m = in.blend;
+    if (!in.is_clip && (m == PF_BLEND_MODE_CLEAR || m == PF_BLEND_MODE_COPY || m == PF_BLEND_MODE_SRC_IN ||
+                        m == PF_BLEND_MODE_SRC_OUT || m == PF_BLEND_MODE_DEST_IN || m == PF_BLEND_MODE_DEST_ATOP))
+        bounds = fr.view_box;
     bp.tile_rect = round_rect_out_to_tile_bounds(bounds);
     int32_t w = bp.tile_rect.width(), h = bp.tile_rect.height();
     if (w < 0) w = 0;
@@ -634,7 +747,7 @@ void build_frame(Frame& fr, int threads, uint64_t dda_limit) {
     fr.zbuf.assign((size_t)sw * (size_t)sh, 0);
     for (uint32_t d = 0; d < fr.draw_count; d++) {
         const PathInput& in = fr.paths[fr.clip_count + d];
-        if (in.paint.a != 255) continue;
+        if (!in.occludes) continue;
         const BuiltPath& bp = fr.built[fr.clip_count + d];
         bool eo = in.fill_rule == PF_FILL_RULE_EVEN_ODD;
         for (const OTile& t : bp.tiles) {
@@ -783,6 +896,167 @@ void tile_coverage(const Frame& fr, uint32_t p, size_t i, const std::vector<T>& 
     for (int k = 0; k < 256; k++) out[k] = c;
 }
 
+// Paint effects of the composite.  The colour texture transform of a
+// gradient for this frame is its own map composed with the inverse build
+// transform (renderer/src/paint.rs:637; Transform2F * Transform2F,
+// geometry/src/transform2d.rs:115-121, 301-310) in single precision, then
+// rounded to binary16 as the metadata texture stores it.
+void o_frame_transform(const Frame& fr, const OGrad& g, float t[6]) {
+    const float* G = g.g;
+    const float* R = fr.inv;
+    t[0] = o_round_f16(G[0] * R[0] + G[1] * R[3]);
+    t[1] = o_round_f16(G[0] * R[1] + G[1] * R[4]);
+    t[2] = o_round_f16((G[0] * R[2] + G[1] * R[5]) + G[2]);
+    t[3] = o_round_f16(G[3] * R[0] + G[4] * R[3]);
+    t[4] = o_round_f16(G[3] * R[1] + G[4] * R[4]);
+    t[5] = o_round_f16((G[3] * R[2] + G[4] * R[5]) + G[5]);
+}
+
+// Linear filtering of the ramp at u (a 256-texel RGBA8 row, clamp to edge or
+// repeat in u: TextureSamplingFlags::REPEAT_U, renderer/src/paint.rs:469-474).
+// A NaN coordinate gives transparent black.
+template <typename T>
+void o_ramp_sample(const OGrad& g, T u, T out[4]) {
+    if (g.wrap == PF_GRADIENT_WRAP_REPEAT) u = u - std::floor(u);
+    if (std::isnan(u)) { out[0] = out[1] = out[2] = out[3] = (T)0; return; }
+    u = std::min(std::max(u, (T)-1), (T)2);
+    T x = u * (T)256 - (T)0.5;
+    T x0 = std::floor(x), w1 = x - x0;
+    int i0 = (int)x0, i1 = i0 + 1;
+    if (g.wrap == PF_GRADIENT_WRAP_REPEAT) { i0 &= 255; i1 &= 255; }
+    else { i0 = std::min(std::max(i0, 0), 255); i1 = std::min(std::max(i1, 0), 255); }
+    const PFColorU a = g.ramp[i0], b = g.ramp[i1];
+    const T ca[4] = {(T)a.r, (T)a.g, (T)a.b, (T)a.a}, cb[4] = {(T)b.r, (T)b.g, (T)b.b, (T)b.a};
+    for (int c = 0; c < 4; c++) out[c] = (ca[c] * ((T)1 - w1) + cb[c] * w1) / (T)255;
+}
+
+// The gradient's straight colour at pixel centre (px, py): linear, the ramp at
+// u; radial, filterRadialGradient (shaders/tile_fragment.inc.glsl:274-307).
+template <typename T>
+void o_gradient_color(const OGrad& g, const float t[6], T px, T py, T out[4]) {
+    T u = (T)t[0] * px + (T)t[1] * py + (T)t[2];
+    if (g.kind == PF_GRADIENT_LINEAR) { o_ramp_sample<T>(g, u, out); return; }
+    T v = (T)t[3] * px + (T)t[4] * py + (T)t[5];
+    T dpx = u - (T)g.fx, dpy = v - (T)g.fy, dcx = g.vx, dcy = g.vy;
+    T dr = (T)g.r1 - (T)g.r0, r0 = g.r0;
+    T a = (dcx * dcx + dcy * dcy) - dr * dr;
+    T b = (dpx * dcx + dpy * dcy) + r0 * dr;
+    T c = (dpx * dpx + dpy * dpy) - r0 * r0;
+    T disc = b * b - a * c;
+    out[0] = out[1] = out[2] = out[3] = (T)0;
+    if (disc != (T)0) {
+        T sq = std::sqrt(disc);
+        T lo = (sq + b) / a, hi = (-sq + b) / a;
+        if (lo > hi) std::swap(lo, hi);
+        o_ramp_sample<T>(g, lo >= (T)0 ? lo : hi, out);
+    }
+}
+
+template <typename T> T o_clamp01(T v) { return std::min(std::max(v, (T)0), (T)1); }
+
+// compositeRGB, one separable channel (shaders/tile_fragment.inc.glsl:420-517).
+template <typename T>
+T o_blend_channel(uint32_t mode, T d, T s) {
+    auto screen = [](T dd, T ss) { return dd + ss - dd * ss; };
+    auto hard = [&](T dd, T ss) { return ss <= (T)0.5 ? dd * (T)2 * ss : screen(dd, (T)2 * ss - (T)1); };
+    auto dodge = [](T dd, T ss) { return dd == (T)0 ? (T)0 : (ss == (T)1 ? (T)1 : dd / ((T)1 - ss)); };
+    switch (mode) {
+    case PF_BLEND_MODE_MULTIPLY: return d * s;
+    case PF_BLEND_MODE_SCREEN: return screen(d, s);
+    case PF_BLEND_MODE_OVERLAY: return hard(s, d);
+    case PF_BLEND_MODE_DARKEN: return std::min(d, s);
+    case PF_BLEND_MODE_LIGHTEN: return std::max(d, s);
+    case PF_BLEND_MODE_COLOR_DODGE: return dodge(d, s);
+    case PF_BLEND_MODE_COLOR_BURN: return (T)1 - dodge((T)1 - d, (T)1 - s);
+    case PF_BLEND_MODE_HARD_LIGHT: return hard(d, s);
+    case PF_BLEND_MODE_SOFT_LIGHT: {
+        T dark = d <= (T)0.25 ? (((T)16 * d - (T)12) * d + (T)4) * d : std::sqrt(d);
+        T factor = s <= (T)0.5 ? d * ((T)1 - d) : dark - d;
+        return d + (s * (T)2 - (T)1) * factor;
+    }
+    case PF_BLEND_MODE_DIFFERENCE: return std::fabs(d - s);
+    default: return d + s - (T)2 * d * s;  // Exclusion
+    }
+}
+
+// compositeRGBToHSL / compositeHSLToRGB (shaders/tile_fragment.inc.glsl:431-448).
+template <typename T>
+void o_rgb_to_hsl(const T rgb[3], T hsl[3]) {
+    const T pi3 = (T)1.0471975511965976;
+    T v = std::max(std::max(rgb[0], rgb[1]), rgb[2]), lo = std::min(std::min(rgb[0], rgb[1]), rgb[2]);
+    T c = v - lo, l = lo + (v - lo) * (T)0.5;
+    T tx, ty, tz;
+    if (rgb[0] == v) { tx = 0; ty = rgb[1]; tz = rgb[2]; }
+    else if (rgb[1] == v) { tx = 2; ty = rgb[2]; tz = rgb[0]; }
+    else { tx = 4; ty = rgb[0]; tz = rgb[1]; }
+    hsl[0] = pi3 * (c != (T)0 ? (tx * c + ty - tz) / c : (T)0);
+    hsl[1] = v != (T)0 ? c / v : (T)0;
+    hsl[2] = l;
+}
+template <typename T>
+void o_hsl_to_rgb(const T hsl[3], T rgb[3]) {
+    const T six_pi = (T)1.9098593171027443;
+    T a = hsl[1] * std::min(hsl[2], (T)1 - hsl[2]);
+    const T k0[3] = {0, 8, 4};
+    for (int i = 0; i < 3; i++) {
+        T k = k0[i] + hsl[0] * six_pi;
+        k = k - (T)12 * std::floor(k / (T)12);
+        rgb[i] = hsl[2] - std::min(std::max(std::min(k - (T)3, (T)9 - k), (T)-1), (T)1) * a;
+    }
+}
+
+// One pixel of a draw: straight source colour s, alpha a (paint alpha x
+// coverage), premultiplied destination dst (4 channels, or alpha alone).
+// Porter-Duff modes by their blend factors (renderer/src/gpu/blend.rs:42-144;
+// Copy writes the source unblended); the others by the shader's composite()
+// (shaders/tile_fragment.inc.glsl:519-537, output alpha 1).  Each result is
+// clamped to [0, 1] as a UNORM framebuffer holds it.
+template <typename T>
+void o_blend(uint32_t mode, const T s[3], T a, T* dst, int channels) {
+    T& da_ref = dst[channels == 4 ? 3 : 0];
+    const T da = da_ref;
+    if (mode <= PF_BLEND_MODE_LIGHTER) {
+        T fs = 1, fd = (T)1 - a;
+        switch (mode) {
+        case PF_BLEND_MODE_CLEAR: fs = 0; fd = 0; break;
+        case PF_BLEND_MODE_COPY: fs = 1; fd = 0; break;
+        case PF_BLEND_MODE_SRC_IN: fs = da; fd = 0; break;
+        case PF_BLEND_MODE_SRC_OUT: fs = (T)1 - da; fd = 0; break;
+        case PF_BLEND_MODE_SRC_ATOP: fs = da; fd = (T)1 - a; break;
+        case PF_BLEND_MODE_DEST_IN: fs = 0; fd = a; break;
+        case PF_BLEND_MODE_DEST_OUT: fs = 0; fd = (T)1 - a; break;
+        case PF_BLEND_MODE_DEST_OVER: fs = (T)1 - da; fd = 1; break;
+        case PF_BLEND_MODE_DEST_ATOP: fs = (T)1 - da; fd = a; break;
+        case PF_BLEND_MODE_XOR: fs = (T)1 - da; fd = (T)1 - a; break;
+        case PF_BLEND_MODE_LIGHTER: fs = 1; fd = 1; break;
+        default: break;  // SrcOver
+        }
+        if (channels == 4)
+            for (int c = 0; c < 3; c++) dst[c] = o_clamp01(s[c] * a * fs + dst[c] * fd);
+        da_ref = o_clamp01(a * fs + da * fd);
+        return;
+    }
+    if (channels == 4) {
+        T b[3];
+        if (mode >= PF_BLEND_MODE_HUE) {
+            T dh[3], sh[3];
+            o_rgb_to_hsl<T>(dst, dh);
+            o_rgb_to_hsl<T>(s, sh);
+            T h[3] = {dh[0], dh[1], dh[2]};
+            if (mode == PF_BLEND_MODE_HUE) h[0] = sh[0];
+            else if (mode == PF_BLEND_MODE_SATURATION) h[1] = sh[1];
+            else if (mode == PF_BLEND_MODE_COLOR) { h[0] = sh[0]; h[1] = sh[1]; }
+            else h[2] = sh[2];
+            o_hsl_to_rgb<T>(h, b);
+        } else {
+            for (int c = 0; c < 3; c++) b[c] = o_blend_channel<T>(mode, dst[c], s[c]);
+        }
+        for (int c = 0; c < 3; c++)
+            dst[c] = o_clamp01(a * ((T)1 - da) * s[c] + a * da * b[c] + ((T)1 - a) * dst[c]);
+    }
+    da_ref = 1;
+}
+
 // Tile composite (shaders/d3d11/tile.cs.glsl:91-159 with calculateColor,
 // shaders/tile_fragment.inc.glsl:560-613, and SrcOver, renderer/src/gpu/blend.rs:54-62):
 // back to front in draw order; occluded tiles (path index < z) are skipped
@@ -816,6 +1090,28 @@ void composite(const Frame& fr, const std::vector<T>& masks, int w, int h, const
                 tile_coverage<T>(fr, p, i, masks, cov.data());
                 T col[4] = {(T)in.paint.r / (T)255, (T)in.paint.g / (T)255, (T)in.paint.b / (T)255,
                             (T)in.paint.a / (T)255};
+                if (in.blend != PF_BLEND_MODE_SRC_OVER || in.gradient != 0) {
+                    const OGrad* g = in.gradient ? &fr.grads[in.gradient - 1] : nullptr;
+                    float tt[6];
+                    if (g) o_frame_transform(fr, *g, tt);
+                    for (int py = 0; py < 16; py++) {
+                        int Y = t.tile_y * 16 + py;
+                        if (Y < 0 || Y >= h) continue;
+                        for (int px = 0; px < 16; px++) {
+                            int X = t.tile_x * 16 + px;
+                            if (X < 0 || X >= w) continue;
+                            T src[4] = {col[0], col[1], col[2], col[3]};
+                            if (g) {  // combineColor0 SrcIn (shaders/tile_fragment.inc.glsl:81-89)
+                                T tex[4];
+                                o_gradient_color<T>(*g, tt, (T)X + (T)0.5, (T)Y + (T)0.5, tex);
+                                src[0] = tex[0]; src[1] = tex[1]; src[2] = tex[2]; src[3] = tex[3] * col[3];
+                            }
+                            o_blend<T>(in.blend, src, src[3] * cov[py * 16 + px], &fb[((size_t)Y * w + X) * channels],
+                                       channels);
+                        }
+                    }
+                    continue;
+                }
                 for (int py = 0; py < 16; py++) {
                     int Y = t.tile_y * 16 + py;
                     if (Y < 0 || Y >= h) continue;
@@ -854,6 +1150,20 @@ bool make_frame(const PFCUDASceneDesc* sc, const PFCUDABuildOptions* opts, Frame
                       tf.vector.x == 0.0f && tf.vector.y == 0.0f);
     }
     fr.transformed.assign(transform ? n : 0, {});
+    if (sc->gradient_count && !sc->gradients) return false;
+    fr.grads.assign(sc->gradient_count, OGrad());
+    for (uint32_t q = 0; q < sc->gradient_count; q++)
+        if (!o_build_gradient(sc->gradients[q], fr.grads[q])) return false;
+    if (transform) {
+        // render_transform = the build transform's inverse (renderer/src/builder.rs:168-171)
+        float det = tf.m00 * tf.m11 - tf.m01 * tf.m10;
+        if (det != 0.0f) {
+            float r = 1.0f / det;
+            float a = r * tf.m11, b = r * -tf.m01, c = r * -tf.m10, d = r * tf.m00;
+            float inv[6] = {a, b, -(a * tf.vector.x + b * tf.vector.y), c, d, -(c * tf.vector.x + d * tf.vector.y)};
+            std::copy(inv, inv + 6, fr.inv);
+        }
+    }
     for (uint32_t p = 0; p < n; p++) {
         const PFCUDAPath& src = p < fr.clip_count ? sc->clip_paths[p] : sc->draw_paths[p - fr.clip_count];
         PathInput& in = fr.paths[p];
@@ -862,6 +1172,15 @@ bool make_frame(const PFCUDASceneDesc* sc, const PFCUDABuildOptions* opts, Frame
         in.fill_rule = src.fill_rule;
         in.clip_path = src.clip_path;  // clip paths may be clipped too (clip chains)
         in.paint = src.paint;
+        if (!in.is_clip) {
+            if (src.blend_mode >= PF_BLEND_MODE_COUNT || src.gradient > sc->gradient_count) return false;
+            in.blend = src.blend_mode;
+            in.gradient = src.gradient;
+            // opaque paint (Paint::is_opaque, renderer/src/paint.rs:163-177) with a
+            // blend mode that hides the backdrop (content/src/effects.rs:202-230)
+            bool opaque = src.paint.a == 255 && (src.gradient == 0 || fr.grads[src.gradient - 1].opaque);
+            in.occludes = opaque && (src.blend_mode == PF_BLEND_MODE_SRC_OVER || src.blend_mode == PF_BLEND_MODE_CLEAR);
+        }
         if (src.clip_path >= (int32_t)fr.clip_count) return false;
         if (in.is_clip && src.clip_path == (int32_t)p) return false;
         if (transform) {
@@ -1460,5 +1779,15 @@ int32_t pfo_diff_grad(PFODiff* f, const double* d_image, double* d_points, doubl
     diff_grad(f->d, d_image, d_points, d_alpha);
     return 0;
 }
+
+
+// Gradient::sample of the gradient's stops (ordered as Gradient::add orders them).
+int32_t pfo_gradient_sample(const PFCUDAGradient* g, float t, PFColorU* out) {
+    if (!g || !out || (g->stop_count && !g->stops)) return 1;
+    *out = o_gradient_sample(o_ordered_stops(*g), t);
+    return 0;
+}
+
+float pfo_round_f16(float x) { return o_round_f16(x); }
 
 }  // extern "C"

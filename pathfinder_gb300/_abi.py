@@ -26,6 +26,18 @@ PF_MEMORY_DEVICE = 1
 
 PF_CUDA_RENDERER_D3D11_SEMANTICS = 0x1
 
+# BlendMode (content/src/effects.rs:99-160), SrcOver first
+BLEND_MODES = ["src_over", "clear", "copy", "src_in", "src_out", "src_atop", "dest_in", "dest_out",
+               "dest_over", "dest_atop", "xor", "lighter", "darken", "lighten", "multiply", "screen",
+               "hard_light", "overlay", "color_dodge", "color_burn", "soft_light", "difference",
+               "exclusion", "hue", "saturation", "color", "luminosity"]
+PF_BLEND_MODE_COUNT = len(BLEND_MODES)
+
+PF_GRADIENT_LINEAR = 0
+PF_GRADIENT_RADIAL = 1
+PF_GRADIENT_WRAP_CLAMP = 0
+PF_GRADIENT_WRAP_REPEAT = 1
+
 PF_SCENE_STARS_512 = 1
 PF_SCENE_SVG_4K = 2
 PF_SCENE_GLYPH_ATLAS = 3
@@ -68,7 +80,17 @@ class PFTransform2F(C.Structure):
 class PFCUDAPath(C.Structure):
     _fields_ = [("first_contour", C.c_uint32), ("contour_count", C.c_uint32), ("paint", PFColorU),
                 ("clip_path", C.c_int32), ("fill_rule", C.c_uint8), ("blend_mode", C.c_uint8),
-                ("reserved", C.c_uint16)]
+                ("gradient", C.c_uint16)]
+
+
+class PFCUDAColorStop(C.Structure):
+    _fields_ = [("offset", C.c_float), ("color", PFColorU)]
+
+
+class PFCUDAGradient(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("wrap", C.c_int32), ("from_", PFVector2F), ("to", PFVector2F),
+                ("radius0", C.c_float), ("radius1", C.c_float), ("transform", PFTransform2F),
+                ("stops", C.c_void_p), ("stop_count", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class PFCUDASceneDesc(C.Structure):
@@ -76,7 +98,8 @@ class PFCUDASceneDesc(C.Structure):
                 ("clip_paths", C.c_void_p), ("draw_paths", C.c_void_p),
                 ("point_count", C.c_uint32), ("contour_count", C.c_uint32),
                 ("clip_path_count", C.c_uint32), ("draw_path_count", C.c_uint32),
-                ("view_box", PFRectF), ("memory", C.c_int32)]
+                ("view_box", PFRectF), ("memory", C.c_int32),
+                ("gradients", C.c_void_p), ("gradient_count", C.c_uint32)]
 
 
 class PFCUDABuildOptions(C.Structure):
@@ -140,12 +163,14 @@ def record_dtypes():
     clip = np.dtype([("dest_tile_id", "<u4"), ("dest_backdrop", "<i4"), ("src_tile_id", "<u4"),
                      ("src_backdrop", "<i4")])
     path = np.dtype([("first_contour", "<u4"), ("contour_count", "<u4"), ("paint", "u1", (4,)),
-                     ("clip_path", "<i4"), ("fill_rule", "u1"), ("blend_mode", "u1"), ("reserved", "<u2")])
+                     ("clip_path", "<i4"), ("fill_rule", "u1"), ("blend_mode", "u1"), ("gradient", "<u2")])
     rect = np.dtype([("x0", "<i4"), ("y0", "<i4"), ("x1", "<i4"), ("y1", "<i4")])
     return fill, tile, clip, path, rect
 
 
 _SIGS = {
+    "PFCUDAGradientSample": (C.c_int32, [C.POINTER(PFCUDAGradient), C.c_float, C.POINTER(PFColorU)]),
+    "PFCUDAGradientRamp": (C.c_int32, [C.POINTER(PFCUDAGradient), C.c_void_p]),
     "PFCUDARendererCreate": (C.c_int32, [C.c_int32, C.POINTER(PFCUDARendererOptions), C.POINTER(C.c_void_p)]),
     "PFCUDARendererDestroy": (C.c_int32, [C.c_void_p]),
     "PFCUDARendererSetStream": (C.c_int32, [C.c_void_p, C.c_void_p]),

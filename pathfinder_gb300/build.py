@@ -20,7 +20,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpathfinder_cuda.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+# Host code: no multiply-add contraction (gcc contracts by default on aarch64),
+# so the host-side single-precision arithmetic is the same on every machine.
+NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                       "-I" + os.path.join(ROOT, "include"), "--expt-relaxed-constexpr"]
 
 # (source, extra flags)
@@ -31,6 +33,7 @@ UNITS = [
     ("pf_renderer.cu", []),
     ("pf_noalloc.cu", []),
     ("pf_scenes.cpp", []),
+    ("pf_paint.cu", []),
 ]
 
 

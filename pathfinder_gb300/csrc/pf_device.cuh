@@ -10,6 +10,7 @@
 
 #include <cstdint>
 #include <climits>
+#include <cmath>
 #include <cuda_runtime.h>
 
 namespace pf {
@@ -19,7 +20,7 @@ namespace pf {
 // ---------------------------------------------------------------------------
 constexpr uint32_t kInvalid = 0xffffffffu;
 constexpr int kTileSize = 16;             // renderer/src/tiles.rs:19-20
-constexpr int kMaxFlattenDepth = 32;      // explicit-stack bound (see DESIGN)
+constexpr int kMaxFlattenDepth = 32;      // depth bound of the subdivision walk
 constexpr uint32_t kSegLine = 1, kSegQuad = 2, kSegCubic = 3;
 
 // status bits (device word, OR-ed)
@@ -56,7 +57,49 @@ struct PathDev {
     // differentiable frames only (NULL otherwise): paint alpha per draw path
     const float* alpha_f;          // [draw paths of the batch]
     const uint32_t* draw_index;    // [P] index of the path among the batch's draw paths
+    // paint: blend mode (PF_BLEND_MODE_*) and gradient (index + 1, 0 = none) per path
+    const uint8_t*  blend;         // [P]
+    const uint32_t* gradient;      // [P]
+    const uint8_t*  occludes;      // [P] opaque paint with a blend mode that hides what lies below
 };
+
+// Blend modes whose paths cover the whole view box (BlendMode::is_destructive,
+// content/src/effects.rs:233-262).
+__host__ __device__ __forceinline__ bool blend_is_destructive(uint32_t m) {
+    return m == 1u /* Clear */ || m == 2u /* Copy */ || m == 3u /* SrcIn */ || m == 4u /* SrcOut */ ||
+           m == 6u /* DestIn */ || m == 9u /* DestAtop */;
+}
+
+// A gradient of the batch (ramp of 256 RGBA8 texels in `ramps`).
+// `g` maps scene coordinates to the colour texture coordinate before the
+// frame's inverse build transform is composed in: linear, u = g0 x + g1 y + g2
+// (the projection onto the gradient line); radial, the inverse of the
+// gradient's transform.  The radial filter parameters are stored rounded to
+// binary16, as the reference's RGBA16F metadata texture holds them
+// (renderer/src/gpu/renderer.rs:702-763).
+struct GradDev {
+    int32_t kind, wrap;            // PF_GRADIENT_*
+    float g[6];                    // row-major 2x3: [m11 m12 m13; m21 m22 m23]
+    float from_x, from_y;          // radial: first centre
+    float vec_x, vec_y;            // radial: vector between the centres
+    float r0, r1;                  // radial: radii
+};
+
+// Round a float to the nearest binary16 value (ties to even), kept as float;
+// overflow gives infinity.  Used for the metadata the reference stores as f16.
+__host__ __device__ inline float round_f16(float x) {
+    if (!(x == x)) return x;
+    const float ax = fabsf(x);
+    if (ax >= 65520.0f) return x > 0.0f ? INFINITY : -INFINITY;
+    if (ax < 6.103515625e-05f) {  // below 2^-14: fixed quantum 2^-24
+        const float q = 5.9604644775390625e-08f;
+        return nearbyintf(x / q) * q;
+    }
+    int e;
+    frexpf(ax, &e);                          // ax = m * 2^e, m in [0.5, 1)
+    const float q = ldexpf(1.0f, e - 11);    // 11 significant bits
+    return nearbyintf(x / q) * q;
+}
 
 // Per-scene data.
 struct SceneDev {

@@ -58,6 +58,10 @@ struct FrameDev {
     Counters* counters;
     uint32_t dda_limit;
     uint32_t clip_chain_max;     // bound of clip-chain walks (longest chain in the batch)
+    // paint
+    const GradDev*  grads;       // [gradients of the batch]
+    const uint32_t* ramps;       // [gradients * 256] RGBA8 texels
+    float inv_m[6];              // frame pixel -> scene coordinates (inverse build transform)
     // Differentiable frames (diff != 0): FP32 fills, the curve parameters of
     // every flattened line, and per visible (screen tile, path tile) entry the
     // composite tape the adjoint reads back.
@@ -73,7 +77,9 @@ struct FrameDev {
 // scatter so that the composite reads one record instead of a chain of
 // dependent loads: x = first fill of its mask, y = fill count, z = paint
 // (RGBA8), w = backdrop (bits 0-7, signed) | even-odd (bit 8) | kind (bits
-// 9-10: 0 solid, 1 one mask, 2 clip-combined: read the tile and clip records).
+// 9-10: 0 solid, 1 one mask, 2 clip-combined: read the tile and clip records,
+// 3 clip chain) | blend mode (bits 11-15) | gradient index + 1 (bits 16-31,
+// 0 = solid paint).  Bits 11-31 are zero for solid SrcOver paint.
 enum : uint32_t { kVisSolid = 0, kVisMask = 1, kVisCombine = 2, kVisChain = 3 };
 
 // Tile control bit of a draw tile whose clip path is itself clipped: its
@@ -81,8 +87,13 @@ enum : uint32_t { kVisSolid = 0, kVisMask = 1, kVisCombine = 2, kVisChain = 3 };
 // the tile and its clip chain's tiles (the D3D11 level's per-level
 // min(coverage, clip mask), shaders/d3d11/fill.cs.glsl:77-84).
 constexpr uint32_t kCtrlClipChain = 0x4;
-__host__ __device__ __forceinline__ int32_t vis_meta(int8_t backdrop, bool even_odd, uint32_t kind) {
-    return (int32_t)((uint32_t)(uint8_t)backdrop | ((even_odd ? 1u : 0u) << 8) | (kind << 9));
+__host__ __device__ __forceinline__ int32_t vis_meta(int8_t backdrop, bool even_odd, uint32_t kind,
+                                                     uint32_t paint_fx = 0) {
+    return (int32_t)((uint32_t)(uint8_t)backdrop | ((even_odd ? 1u : 0u) << 8) | (kind << 9) | (paint_fx << 11));
+}
+// blend mode | (gradient index + 1) << 5, the paint effect bits of a visible record
+__host__ __device__ __forceinline__ uint32_t paint_fx_bits(uint32_t blend, uint32_t gradient1) {
+    return (blend & 31u) | (gradient1 << 5);
 }
 
 // One tape word per (visible entry, pixel): coverage c and the composite
@@ -126,6 +137,14 @@ __host__ __device__ __forceinline__ float dec_d(uint32_t c) { return c == 1u ? 1
 
 // scan scratch
 struct ScanTemp { uint32_t* partials; uint32_t cap; };
+
+}  // namespace pf
+struct PFCUDAGradient;
+struct PFCUDAColorStop;
+namespace pf {
+// Gradient paints (host): the record of one gradient and its 256-texel ramp;
+// returns a PF_CUDA_* status.
+int32_t build_gradient(const PFCUDAGradient& g, GradDev* out, uint32_t* ramp, bool* opaque);
 
 // Number of kernels this library has launched (host counter).
 uint64_t launch_counter();

@@ -17,6 +17,7 @@
 // index within the clip or draw paths).  Screen-tile arrays (z-buffer, list
 // counts) are indexed from the first screen tile of the frame's scene range.
 #include "pf_kernels.cuh"
+#include "pathfinder_cuda.h"
 
 namespace pf {
 
@@ -146,7 +147,7 @@ __global__ void k_propagate(FrameDev f, int clip_pass) {
         // a tile behind a clip chain may be partly covered, so it never occludes
         const bool opaque = (is_clip || (tile_ctrl_bits & kCtrlClipChain)) ? false
                                     : (f.path.alpha_f ? f.path.alpha_f[f.path.draw_index[gp]] >= 1.0f
-                                                      : (f.path.paint[gp] >> 24) == 255u);
+                                                      : f.path.occludes[gp] != 0);
         if (opaque && alpha == kInvalid && solid_occludes(backdrop, even_odd)) {
             uint32_t st;
             if (frame_screen_tile(f, f.scenes[f.path.scene[gp]], tx, ty, &st)) atomicMax(&f.zbuf[st], (int32_t)local);
@@ -194,7 +195,8 @@ __global__ void k_visible(FrameDev f, int scatter) {
                     nf = f.tile_fill_base[owner + 1] - b0;
                 }
                 f.vis_info[slot] = make_int4((int)b0, (int)nf, (int)f.path.paint[gp],
-                                             vis_meta(tile_backdrop(rec), (tile_ctrl(rec) & 0x2u) != 0, kind));
+                                             vis_meta(tile_backdrop(rec), (tile_ctrl(rec) & 0x2u) != 0, kind,
+                                                      paint_fx_bits(f.path.blend[gp], f.path.gradient[gp])));
             }
         }
     }
@@ -409,6 +411,205 @@ __device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint
 }
 
 // ---------------------------------------------------------------------------
+// paint effects: gradient colour (tile_fragment.inc.glsl:75-90, 274-307,
+// 560-613) and blend modes (renderer/src/gpu/blend.rs:42-160 for the
+// Porter-Duff modes, the shader's composite(), tile_fragment.inc.glsl:414-537,
+// for the others).  Solid SrcOver tiles never come here.
+// ---------------------------------------------------------------------------
+// The colour texture transform of a gradient for this frame: the gradient's
+// map composed with the inverse build transform (`transform *=
+// render_transform`, renderer/src/paint.rs:637; Transform2F * Transform2F,
+// geometry/src/transform2d.rs:115-121, 301-310) and rounded to binary16 as the
+// metadata texture stores it (renderer/src/gpu/renderer.rs:711-719).
+__device__ __forceinline__ void gradient_frame_transform(const FrameDev& f, const GradDev& gd, float t[6]) {
+    const float* G = gd.g;
+    const float* R = f.inv_m;
+    t[0] = round_f16(fadd(fmul(G[0], R[0]), fmul(G[1], R[3])));
+    t[1] = round_f16(fadd(fmul(G[0], R[1]), fmul(G[1], R[4])));
+    t[2] = round_f16(fadd(fadd(fmul(G[0], R[2]), fmul(G[1], R[5])), G[2]));
+    t[3] = round_f16(fadd(fmul(G[3], R[0]), fmul(G[4], R[3])));
+    t[4] = round_f16(fadd(fmul(G[3], R[1]), fmul(G[4], R[4])));
+    t[5] = round_f16(fadd(fadd(fmul(G[3], R[2]), fmul(G[4], R[5])), G[5]));
+}
+
+__device__ __forceinline__ float4 unpack_unorm8(uint32_t v) {
+    const float s = 1.0f / 255.0f;
+    return make_float4((float)(v & 0xffu) * s, (float)((v >> 8) & 0xffu) * s, (float)((v >> 16) & 0xffu) * s,
+                       (float)(v >> 24) * s);
+}
+
+// Linear filtering of the 256-texel ramp at texture coordinate u, clamped to
+// the edge texels or repeated (TextureSamplingFlags::REPEAT_U,
+// renderer/src/paint.rs:469-474).  A NaN coordinate (the reference leaves it
+// to the sampler) gives transparent black.
+__device__ __forceinline__ float4 ramp_sample(const uint32_t* ramp, float u, int32_t wrap) {
+    if (wrap == PF_GRADIENT_WRAP_REPEAT) u = u - floorf(u);
+    if (!(u == u)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    u = fminf(fmaxf(u, -1.0f), 2.0f);
+    const float x = u * 256.0f - 0.5f;
+    const float x0 = floorf(x), w1 = x - x0;
+    int i0 = (int)x0, i1 = i0 + 1;
+    if (wrap == PF_GRADIENT_WRAP_REPEAT) { i0 &= 255; i1 &= 255; }
+    else { i0 = min(max(i0, 0), 255); i1 = min(max(i1, 0), 255); }
+    const float4 c0 = unpack_unorm8(__ldg(ramp + i0)), c1 = unpack_unorm8(__ldg(ramp + i1));
+    const float w0 = 1.0f - w1;
+    return make_float4(c0.x * w0 + c1.x * w1, c0.y * w0 + c1.y * w1, c0.z * w0 + c1.z * w1,
+                       c0.w * w0 + c1.w * w1);
+}
+
+// Separable blend functions (compositeRGB, tile_fragment.inc.glsl:420-517),
+// one channel: d destination, s source.
+__device__ __forceinline__ float blend_screen(float d, float s) { return d + s - d * s; }
+__device__ __forceinline__ float blend_hard_light(float d, float s) {
+    return s <= 0.5f ? d * 2.0f * s : blend_screen(d, 2.0f * s - 1.0f);
+}
+__device__ __forceinline__ float blend_color_dodge(float d, float s) {
+    return d == 0.0f ? 0.0f : (s == 1.0f ? 1.0f : d / (1.0f - s));
+}
+__device__ __forceinline__ float blend_separable(uint32_t mode, float d, float s) {
+    switch (mode) {
+    case PF_BLEND_MODE_MULTIPLY: return d * s;
+    case PF_BLEND_MODE_SCREEN: return blend_screen(d, s);
+    case PF_BLEND_MODE_OVERLAY: return blend_hard_light(s, d);
+    case PF_BLEND_MODE_DARKEN: return fminf(d, s);
+    case PF_BLEND_MODE_LIGHTEN: return fmaxf(d, s);
+    case PF_BLEND_MODE_COLOR_DODGE: return blend_color_dodge(d, s);
+    case PF_BLEND_MODE_COLOR_BURN: return 1.0f - blend_color_dodge(1.0f - d, 1.0f - s);
+    case PF_BLEND_MODE_HARD_LIGHT: return blend_hard_light(d, s);
+    case PF_BLEND_MODE_SOFT_LIGHT: {
+        const float dark = d <= 0.25f ? ((16.0f * d - 12.0f) * d + 4.0f) * d : sqrtf(d);
+        const float factor = s <= 0.5f ? d * (1.0f - d) : dark - d;
+        return d + (s * 2.0f - 1.0f) * factor;
+    }
+    case PF_BLEND_MODE_DIFFERENCE: return fabsf(d - s);
+    default: return d + s - 2.0f * d * s;  // Exclusion
+    }
+}
+
+__device__ __forceinline__ float blend_divide(float n, float d) { return d != 0.0f ? n / d : 0.0f; }
+
+// compositeRGBToHSL / compositeHSLToRGB (tile_fragment.inc.glsl:431-448): the
+// reference's own HSL variant (saturation c / v), restated as written.
+__device__ __forceinline__ float3 blend_rgb_to_hsl(float r, float g, float b) {
+    const float v = fmaxf(fmaxf(r, g), b), lo = fminf(fminf(r, g), b);
+    const float c = v - lo, l = lo + (v - lo) * 0.5f;
+    float tx, ty, tz;
+    if (r == v) { tx = 0.0f; ty = g; tz = b; }
+    else if (g == v) { tx = 2.0f; ty = b; tz = r; }
+    else { tx = 4.0f; ty = r; tz = g; }
+    const float h = 1.0471975511965976f * blend_divide(tx * c + ty - tz, c);
+    return make_float3(h, blend_divide(c, v), l);
+}
+__device__ __forceinline__ float blend_hsl_channel(float k0, float h, float s, float l) {
+    const float a = s * fminf(l, 1.0f - l);
+    float k = k0 + h * 1.9098593171027443f;
+    k = k - 12.0f * floorf(k / 12.0f);  // GLSL mod
+    return l - fminf(fmaxf(fminf(k - 3.0f, 9.0f - k), -1.0f), 1.0f) * a;
+}
+
+// One pixel: straight source colour (sr, sg, sb), source alpha a (paint alpha
+// x coverage), premultiplied destination d.  The framebuffer is UNORM, so
+// every result is clamped to [0, 1].
+__device__ __forceinline__ void blend_pixel(uint32_t mode, float sr, float sg, float sb, float a, float& d0,
+                                            float& d1, float& d2, float& d3) {
+    const float da = d3;
+    if (mode <= PF_BLEND_MODE_LIGHTER) {
+        float fs, fd;  // source and destination factors (blend.rs:42-144; Copy: no blending)
+        switch (mode) {
+        case PF_BLEND_MODE_CLEAR: fs = 0.0f; fd = 0.0f; break;
+        case PF_BLEND_MODE_COPY: fs = 1.0f; fd = 0.0f; break;
+        case PF_BLEND_MODE_SRC_IN: fs = da; fd = 0.0f; break;
+        case PF_BLEND_MODE_SRC_OUT: fs = 1.0f - da; fd = 0.0f; break;
+        case PF_BLEND_MODE_SRC_ATOP: fs = da; fd = 1.0f - a; break;
+        case PF_BLEND_MODE_DEST_IN: fs = 0.0f; fd = a; break;
+        case PF_BLEND_MODE_DEST_OUT: fs = 0.0f; fd = 1.0f - a; break;
+        case PF_BLEND_MODE_DEST_OVER: fs = 1.0f - da; fd = 1.0f; break;
+        case PF_BLEND_MODE_DEST_ATOP: fs = 1.0f - da; fd = a; break;
+        case PF_BLEND_MODE_XOR: fs = 1.0f - da; fd = 1.0f - a; break;
+        case PF_BLEND_MODE_LIGHTER: fs = 1.0f; fd = 1.0f; break;
+        default: fs = 1.0f; fd = 1.0f - a; break;  // SrcOver
+        }
+        d0 = __saturatef(sr * a * fs + d0 * fd);
+        d1 = __saturatef(sg * a * fs + d1 * fd);
+        d2 = __saturatef(sb * a * fs + d2 * fd);
+        d3 = __saturatef(a * fs + da * fd);
+        return;
+    }
+    float b0, b1, b2;
+    if (mode >= PF_BLEND_MODE_HUE) {
+        const float3 dh = blend_rgb_to_hsl(d0, d1, d2), sh = blend_rgb_to_hsl(sr, sg, sb);
+        float h = dh.x, s = dh.y, l = dh.z;  // compositeHSL (tile_fragment.inc.glsl:471-482)
+        if (mode == PF_BLEND_MODE_HUE) h = sh.x;
+        else if (mode == PF_BLEND_MODE_SATURATION) s = sh.y;
+        else if (mode == PF_BLEND_MODE_COLOR) { h = sh.x; s = sh.y; }
+        else l = sh.z;
+        b0 = blend_hsl_channel(0.0f, h, s, l);
+        b1 = blend_hsl_channel(8.0f, h, s, l);
+        b2 = blend_hsl_channel(4.0f, h, s, l);
+    } else {
+        b0 = blend_separable(mode, d0, sr);
+        b1 = blend_separable(mode, d1, sg);
+        b2 = blend_separable(mode, d2, sb);
+    }
+    // composite() (tile_fragment.inc.glsl:519-537): output alpha 1
+    const float ws = a * (1.0f - da), wb = a * da, wd = 1.0f - a;
+    d0 = __saturatef(ws * sr + wb * b0 + wd * d0);
+    d1 = __saturatef(ws * sg + wb * b1 + wd * d1);
+    d2 = __saturatef(ws * sb + wb * b2 + wd * d2);
+    d3 = 1.0f;
+}
+
+// Composite one visible tile with paint effects into this lane's 8 pixels
+// (column col, rows half*8 .. half*8+7 of screen tile (tx, ty)).
+__device__ __forceinline__ void composite_paint_tile(const FrameDev& f, uint32_t fx, uint32_t paint, const float cov[8],
+                                                     int32_t tx, int32_t ty, int col, int half, float d0[8],
+                                                     float d1[8], float d2[8], float d3[8]) {
+    const uint32_t mode = fx & 31u, grad1 = fx >> 5;
+    const float4 base = unpack_unorm8(paint);
+    if (grad1 == 0) {
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            blend_pixel(mode, base.x, base.y, base.z, base.w * cov[k], d0[k], d1[k], d2[k], d3[k]);
+        return;
+    }
+    const GradDev& gd = f.grads[grad1 - 1];
+    const uint32_t* ramp = f.ramps + (size_t)(grad1 - 1) * 256u;
+    float t[6];
+    gradient_frame_transform(f, gd, t);
+    const int32_t wrap = gd.wrap;
+    const bool radial = gd.kind == PF_GRADIENT_RADIAL;
+    // filterRadialGradient (tile_fragment.inc.glsl:274-307): per-tile terms
+    const float dr = gd.r1 - gd.r0;
+    const float qa = (gd.vec_x * gd.vec_x + gd.vec_y * gd.vec_y) - dr * dr;
+    const float px = (float)(tx * 16 + col) + 0.5f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const float py = (float)(ty * 16 + half * 8 + k) + 0.5f;
+        const float u = t[0] * px + t[1] * py + t[2];
+        float4 c;
+        if (!radial) {
+            c = ramp_sample(ramp, u, wrap);
+        } else {
+            const float v = t[3] * px + t[4] * py + t[5];
+            const float dpx = u - gd.from_x, dpy = v - gd.from_y;
+            const float qb = (dpx * gd.vec_x + dpy * gd.vec_y) + gd.r0 * dr;
+            const float qc = (dpx * dpx + dpy * dpy) - gd.r0 * gd.r0;
+            const float disc = qb * qb - qa * qc;
+            c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (disc != 0.0f) {
+                const float sq = sqrtf(disc);
+                float lo = (sq + qb) / qa, hi = (-sq + qb) / qa;
+                if (lo > hi) { const float tmp = lo; lo = hi; hi = tmp; }
+                c = ramp_sample(ramp, lo >= 0.0f ? lo : hi, wrap);
+            }
+        }
+        // combineColor0 SrcIn (tile_fragment.inc.glsl:81-89): the texel's colour,
+        // its alpha times the base colour's
+        blend_pixel(mode, c.x, c.y, c.z, c.w * base.w * cov[k], d0[k], d1[k], d2[k], d3[k]);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // fused fill + composite: one warp per screen tile, no block barriers
 // ---------------------------------------------------------------------------
 constexpr uint32_t kWarpListCap = 128;
@@ -458,7 +659,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
     for (int k = 0; k < 8; k++) { d0[k] = bg.x; d1[k] = bg.y; d2[k] = bg.z; d3[k] = bg.w; }
     for (uint32_t i = 0; i < n; i++) {
         float cov[8];
-        uint32_t paint;
+        uint32_t paint, fx = 0;
         uint32_t kind = kVisCombine;
         int4 info = make_int4(0, 0, 0, 0);
         uint32_t g;
@@ -468,6 +669,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
             info = ws.info[(uint32_t)key];
             kind = ((uint32_t)info.w >> 9) & 3u;
             paint = (uint32_t)info.z;
+            fx = (uint32_t)info.w >> 11;
         } else {
             g = f.vis[base + i];
         }
@@ -487,10 +689,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
         } else {  // clip-combined tile, or a long list: from the tile records
             const int4 rec = f.tiles[g];
             tile_coverage8(f, rec, g, ws.b0, ws.b1, cov);
-            paint = f.path.paint[(uint32_t)rec.z];
+            const uint32_t gp = (uint32_t)rec.z;
+            paint = f.path.paint[gp];
+            fx = paint_fx_bits(f.path.blend[gp], f.path.gradient[gp]);
         }
         float pa = (float)(paint >> 24) * (1.0f / 255.0f);
-        if (MODE == 0) {
+        if (fx != 0) {
+            composite_paint_tile(f, fx, paint, cov, tx, ty, col, half, d0, d1, d2, d3);
+        } else if (MODE == 0) {
             float pr = (float)(paint & 0xffu) * (1.0f / 255.0f);
             float pg = (float)((paint >> 8) & 0xffu) * (1.0f / 255.0f);
             float pb = (float)((paint >> 16) & 0xffu) * (1.0f / 255.0f);

@@ -87,7 +87,9 @@ struct PFCUDARenderer {
     DevBuf<SegRec> segs;
     DevBuf<uint32_t> first_ord, paint, local_index, scene_of;
     DevBuf<int32_t> clip_gpath;
-    DevBuf<uint8_t> rule, is_clip;
+    DevBuf<uint8_t> rule, is_clip, blend, occludes;
+    DevBuf<uint32_t> gradient, ramps;
+    DevBuf<GradDev> grads;
     DevBuf<SceneDev> scenes_dev;
     std::vector<SceneDev> scenes_host;
 
@@ -125,6 +127,7 @@ struct PFCUDARenderer {
     // clip chains
     uint32_t clip_chain_max = 0;       // longest chain of clip paths behind a path
     bool nested_clips = false;         // some clip path is itself clipped
+    bool paint_effects = false;        // some path has a gradient or a blend mode other than SrcOver
 
     // differentiable frames
     uint32_t ND = 0;                   // draw paths of the batch
@@ -199,6 +202,12 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.path.clip_gpath = r->clip_gpath.p;
     f.path.rule = r->rule.p;
     f.path.is_clip = r->is_clip.p;
+    f.path.blend = r->blend.p;
+    f.path.gradient = r->gradient.p;
+    f.path.occludes = r->occludes.p;
+    f.grads = r->grads.p;
+    f.ramps = r->ramps.p;
+    f.inv_m[0] = 1.0f; f.inv_m[4] = 1.0f;
     f.path.local_index = r->local_index.p;
     f.path.scene = r->scene_of.p;
     f.path.tile_rect = r->tile_rect.p;
@@ -294,6 +303,16 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     r->last_diff = diff;
     if (!diff) r->diff_valid = false;
     FrameDev f = frame_dev(r, transformed, g, diff);
+    if (transformed) {  // gradients are evaluated at pixel centres mapped back to scene space
+        const PFTransform2F& t = opts->transform;
+        const float det = t.m00 * t.m11 - t.m01 * t.m10;
+        if (det != 0.0f) {
+            const float inv = 1.0f / det;
+            const float a = t.m11 * inv, b = -t.m01 * inv, c = -t.m10 * inv, d = t.m00 * inv;
+            f.inv_m[0] = a; f.inv_m[1] = b; f.inv_m[2] = -(a * t.vector.x + b * t.vector.y);
+            f.inv_m[3] = c; f.inv_m[4] = d; f.inv_m[5] = -(c * t.vector.x + d * t.vector.y);
+        }
+    }
     ScanTemp tmp{r->scan_partials.p, (uint32_t)r->scan_partials.cap};
     Counters* c = r->counters.p;
     auto mark = [&](int stage) {
@@ -508,7 +527,8 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->col_backdrop.release(); r->zbuf.release(); r->fills.release(); r->fill_e.release(); r->tiles.release();
     r->clips.release(); r->screen_cnt.release(); r->screen_base.release(); r->vis.release(); r->vis_info.release();
     r->scan_partials.release(); r->counters.release(); r->out_tmp.release();
-    r->draw_index.release(); r->alpha_in.release(); r->fills_f.release(); r->line_seg.release();
+    r->draw_index.release(); r->blend.release(); r->occludes.release(); r->gradient.release();
+    r->grads.release(); r->ramps.release(); r->alpha_in.release(); r->fills_f.release(); r->line_seg.release();
     r->line_t.release(); r->tape.release();
     r->grad_mask.release(); r->grad_alpha_tmp.release();
     if (r->h_counters) cudaFreeHost(r->h_counters);
@@ -564,6 +584,10 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
     std::vector<uint8_t> rule((size_t)P), isclip((size_t)P);
     std::vector<uint32_t> draw_index((size_t)P, kInvalid);
     std::vector<float> draw_alpha;
+    std::vector<uint8_t> blend((size_t)P, 0), occl((size_t)P, 0);
+    std::vector<uint32_t> gradv((size_t)P, 0), ramps;
+    std::vector<GradDev> grads;
+    std::vector<uint8_t> grad_opaque;
     r->scenes.assign(scene_count, SceneInfo());
     r->scenes_host.assign(scene_count, SceneDev{});
     uint32_t point_base = 0, contour_base = 0, gp = 0, screen_total = 0;
@@ -592,11 +616,24 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
         si.screen_offset = screen_total;
         si.screen_count = (uint32_t)sw * (uint32_t)sh;
         screen_total += si.screen_count;
+        if (sc.gradient_count && !sc.gradients) return PF_CUDA_ERR_INVALID;
+        const uint32_t grad_base = (uint32_t)grads.size();
+        for (uint32_t q = 0; q < sc.gradient_count; q++) {
+            if (grads.size() >= 0xfffeu) return PF_CUDA_ERR_INVALID;  // 16-bit ids in the visible records
+            GradDev gd;
+            bool opaque = false;
+            ramps.resize(ramps.size() + 256);
+            int32_t rc = build_gradient(sc.gradients[q], &gd, ramps.data() + ramps.size() - 256, &opaque);
+            if (rc != PF_CUDA_OK) return rc;
+            grads.push_back(gd);
+            grad_opaque.push_back(opaque ? 1 : 0);
+        }
         for (uint32_t i = 0; i < sc.clip_path_count + sc.draw_path_count; i++, gp++) {
             const bool c = i < sc.clip_path_count;
             const PFCUDAPath& p = c ? sc.clip_paths[i] : sc.draw_paths[i - sc.clip_path_count];
             if ((uint64_t)p.first_contour + p.contour_count > sc.contour_count) return PF_CUDA_ERR_INVALID;
-            if (p.fill_rule > 1 || p.blend_mode != PF_BLEND_MODE_SRC_OVER) return PF_CUDA_ERR_INVALID;
+            if (p.fill_rule > 1 || p.blend_mode >= PF_BLEND_MODE_COUNT) return PF_CUDA_ERR_INVALID;
+            if (!c && p.gradient > sc.gradient_count) return PF_CUDA_ERR_INVALID;
             if (p.clip_path >= (int32_t)sc.clip_path_count) return PF_CUDA_ERR_INVALID;
             if (c && p.clip_path == (int32_t)i) return PF_CUDA_ERR_INVALID;  // a clip path clipping itself
             first_ord[gp] = (uint32_t)ord_contour.size();
@@ -614,6 +651,12 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
             if (!c) {
                 draw_index[gp] = (uint32_t)draw_alpha.size();
                 draw_alpha.push_back((float)p.paint.a / 255.0f);
+                blend[gp] = p.blend_mode;
+                gradv[gp] = p.gradient ? grad_base + p.gradient : 0u;  // global index + 1
+                // BuiltDrawPath::occludes (renderer/src/builder.rs:80-94): opaque paint and
+                // BlendMode::occludes_backdrop (content/src/effects.rs:202-230)
+                const bool opaque = p.paint.a == 255 && (p.gradient == 0 || grad_opaque[grad_base + p.gradient - 1]);
+                occl[gp] = opaque && (p.blend_mode == PF_BLEND_MODE_SRC_OVER || p.blend_mode == PF_BLEND_MODE_CLEAR);
             }
         }
         SceneDev& d = r->scenes_host[k];
@@ -651,6 +694,8 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
     }
     r->clip_chain_max = chain_max;
     r->nested_clips = nested;
+    r->paint_effects = !grads.empty();
+    for (uint32_t q = 0; q < P; q++) r->paint_effects = r->paint_effects || blend[q] != PF_BLEND_MODE_SRC_OVER;
     const uint32_t nord = (uint32_t)ord_contour.size();
     r->path_local.assign(local.begin(), local.end());
     r->path_is_clip.assign(isclip.begin(), isclip.end());
@@ -663,7 +708,9 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
         (e = r->contour_seg_base.ensure(nord + 1)) || (e = r->first_ord.ensure(Pz + 1)) || (e = r->paint.ensure(Pz)) ||
         (e = r->local_index.ensure(Pz)) || (e = r->scene_of.ensure(Pz)) || (e = r->clip_gpath.ensure(Pz)) ||
         (e = r->rule.ensure(Pz)) || (e = r->is_clip.ensure(Pz)) || (e = r->tile_rect.ensure(Pz)) ||
-        (e = r->draw_index.ensure(Pz)) ||
+        (e = r->draw_index.ensure(Pz)) || (e = r->blend.ensure(Pz)) || (e = r->occludes.ensure(Pz)) ||
+        (e = r->gradient.ensure(Pz)) || (e = r->grads.ensure(grads.size() + 1)) ||
+        (e = r->ramps.ensure(ramps.size() + 1)) ||
         (e = r->tile_offset.ensure(Pz + 1)) || (e = r->col_offset.ensure(Pz + 1)) ||
         (e = r->scenes_dev.ensure(scene_count)) || (e = r->scan_partials.ensure(nord / 2048 + 2)))
         return cuda_status(e);
@@ -691,6 +738,13 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
         PF_TRY(cudaMemcpyAsync(r->rule.p, rule.data(), Pz, cudaMemcpyHostToDevice, s));
         PF_TRY(cudaMemcpyAsync(r->is_clip.p, isclip.data(), Pz, cudaMemcpyHostToDevice, s));
         PF_TRY(cudaMemcpyAsync(r->draw_index.p, draw_index.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->blend.p, blend.data(), Pz, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->occludes.p, occl.data(), Pz, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->gradient.p, gradv.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
+    }
+    if (!grads.empty()) {
+        PF_TRY(cudaMemcpyAsync(r->grads.p, grads.data(), sizeof(GradDev) * grads.size(), cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->ramps.p, ramps.data(), sizeof(uint32_t) * ramps.size(), cudaMemcpyHostToDevice, s));
     }
     // Segment packing on the GPU (SegmentsD3D11::add_path): count, scan, emit.
     PF_TRY(cudaMemsetAsync(r->counters.p, 0, sizeof(Counters), s));
@@ -756,6 +810,13 @@ static int32_t render_plain(PFCUDARendererRef r, const PFCUDABuildOptions* optio
     if (out_memory == PF_MEMORY_HOST) {
         PF_TRY(r->out_tmp.ensure(bytes));
         dst = r->out_tmp.p;
+        // Pixels outside every scene's screen tiles are not written: they keep
+        // the caller's values, as they do in a device buffer.
+        bool covered = false;
+        for (const SceneInfo& si : r->scenes)
+            covered = covered || (!si.explicit_target && si.screen.x <= 0 && si.screen.y <= 0 &&
+                                  (int64_t)si.screen.z * 16 >= width && (int64_t)si.screen.w * 16 >= height);
+        if (!covered) PF_TRY(cudaMemcpyAsync(dst, out, bytes, cudaMemcpyHostToDevice, r->stream));
     } else if (out_memory != PF_MEMORY_DEVICE) {
         return PF_CUDA_ERR_INVALID;
     }
@@ -1051,6 +1112,7 @@ static int32_t diff_prologue(PFCUDARendererRef r, uint32_t first, uint32_t count
     if (!r || !out_device) return PF_CUDA_ERR_INVALID;
     if (!valid_range(r, first, count)) return r->has_scene ? PF_CUDA_ERR_INVALID : PF_CUDA_ERR_NO_SCENE;
     if (r->nested_clips) return PF_CUDA_ERR_INVALID;  // the adjoint covers single-level clips
+    if (r->paint_effects) return PF_CUDA_ERR_INVALID;  // and solid paint with SrcOver
     if (r->options.flags & PF_CUDA_RENDERER_D3D11_SEMANTICS) return PF_CUDA_ERR_INVALID;  // pieces rounded to 1/256 px
     PF_TRY(cudaSetDevice(r->device));
     if (width > 0 || height > 0) {

@@ -68,7 +68,7 @@ PFCUDAPath make_path(uint32_t first_contour, uint32_t count, PFColorU paint, int
     p.clip_path = clip;
     p.fill_rule = rule;
     p.blend_mode = PF_BLEND_MODE_SRC_OVER;
-    p.reserved = 0;
+    p.gradient = 0;
     return p;
 }
 

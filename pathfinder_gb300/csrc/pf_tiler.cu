@@ -343,6 +343,11 @@ __global__ void k_bound(FrameDev f, const uint32_t* __restrict__ ord_contour, co
             bx1 = smin(mxx, v.z); by1 = smin(mxy, v.w);
         }
     }
+    if (!f.path.is_clip[gp] && blend_is_destructive(f.path.blend[gp])) {
+        // a destructive blend mode tiles the whole view box (renderer/src/builder.rs:430-434)
+        const float4 v = sc.view_box;
+        bx0 = v.x; by0 = v.y; bx1 = v.z; by1 = v.w;
+    }
     // round_rect_out_to_tile_bounds (renderer/src/tiles.rs:64-66)
     const float q = 1.0f / 16.0f;
     int4 r;

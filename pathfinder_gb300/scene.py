@@ -89,10 +89,15 @@ class Outline:
 
 @dataclass
 class DrawPath:
+    """renderer/src/scene.rs:441-456, 509-583.  ``paint`` is the solid colour, or
+    the base colour of ``gradient`` (only its alpha counts then: the gradient
+    combines SrcIn over it); ``blend_mode`` is a BlendMode."""
     outline: Outline
     paint: ColorU = ColorU(0, 0, 0, 255)
     fill_rule: FillRule = FillRule.WINDING
     clip_path: int | None = None
+    blend_mode: int = 0
+    gradient: object = None  # paint.Gradient
 
 
 @dataclass
@@ -128,7 +133,9 @@ class Scene:
         self.width = 0
         self.height = 0
         self.cells = None  # glyph atlas cells, when generated
+        self.gradients: list = []  # paint.Gradient, indexed by draw path records' gradient - 1
         self._pending: list = []
+        self._keep: list = []
 
     # --- the reference's mutators -----------------------------------------
     def set_view_box(self, rect: RectF) -> None:
@@ -169,9 +176,24 @@ class Scene:
         rec["paint"] = (path.paint.r, path.paint.g, path.paint.b, path.paint.a)
         rec["clip_path"] = -1 if path.clip_path is None else path.clip_path
         rec["fill_rule"] = int(path.fill_rule)
+        rec["blend_mode"] = int(path.blend_mode)
+        if path.gradient is not None:
+            rec["gradient"] = self.push_gradient(path.gradient) + 1
         self.draw_paths = np.concatenate([self.draw_paths, rec])
         self.epoch += 1
         return len(self.draw_paths) - 1
+
+    def push_gradient(self, gradient) -> int:
+        """Index of ``gradient`` among the scene's gradients (added once per object,
+        as Palette::push_paint dedupes paints, renderer/src/paint.rs:381-390)."""
+        for i, g in enumerate(self.gradients):
+            if g is gradient:
+                return i
+        if len(self.gradients) >= 0xfffe:
+            raise ValueError("too many gradients in one scene")
+        self.gradients.append(gradient)
+        self.epoch += 1
+        return len(self.gradients) - 1
 
     # --- C ABI view -----------------------------------------------------------
     def desc(self) -> _abi.PFCUDASceneDesc:
@@ -193,6 +215,15 @@ class Scene:
         vb = self.view_box
         d.view_box = _abi.PFRectF(_abi.PFVector2F(vb.x0, vb.y0), _abi.PFVector2F(vb.x1, vb.y1))
         d.memory = _abi.PF_MEMORY_HOST
+        if self.gradients:
+            arr = (_abi.PFCUDAGradient * len(self.gradients))()
+            keep = [arr]
+            for i, g in enumerate(self.gradients):
+                arr[i], stops = g.to_c()
+                keep.append(stops)
+            self._keep = keep  # the descriptor points into these
+            d.gradients = C.addressof(arr)
+            d.gradient_count = len(self.gradients)
         return d
 
     @property

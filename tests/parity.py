@@ -50,7 +50,12 @@ def compare_masks(renderer, fr, tol=COVERAGE_TOL):
 
 def compare_images(gpu, ora, max_diff=2, frac_exact=0.99):
     d = np.abs(gpu.astype(np.int32) - ora.astype(np.int32))
-    assert d.max() <= max_diff, f"image max diff {d.max()}"
+    if d.max() > max_diff:
+        dm = d.max(-1) if d.ndim == 3 else d
+        ys, xs = np.nonzero(dm > max_diff)
+        where = ", ".join(f"({y},{x}) gpu={gpu[y, x].tolist()} ora={ora[y, x].tolist()}" for y, x in zip(ys[:4], xs[:4]))
+        raise AssertionError(f"image max diff {d.max()} at {len(ys)} pixels, x {xs.min()}..{xs.max()}, "
+                             f"y {ys.min()}..{ys.max()}: {where}")
     exact = float((d == 0).mean())
     assert exact >= frac_exact, f"only {exact:.4f} of channels exact"
     return int(d.max()), exact

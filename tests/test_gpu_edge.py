@@ -127,3 +127,21 @@ def test_async_capacity_status_then_regrow(built):
         assert codes[-1] == PF_CUDA_OK, codes
         ref = r.render(s)
         assert np.array_equal(out.cpu().numpy(), ref)
+
+
+def test_view_box_away_from_origin_keeps_other_pixels(renderer):
+    """Pixels outside the view box's screen tiles keep the buffer's contents,
+    for host buffers as for device buffers, whatever the renderer drew before."""
+    rng = np.random.default_rng(3)
+    big = pf.Scene()
+    big.set_view_box(pf.RectF(0, 0, 640, 96))
+    big.push_draw_path(pf.DrawPath(pf.Outline([_star(320, 48, 20, 300, 7, rng)]), pf.ColorU(200, 30, 40, 255)))
+    renderer.render(big)  # leaves content in the renderer's staging image
+    s = pf.Scene()
+    s.set_view_box(pf.RectF(500, 8, 640, 96))
+    s.push_draw_path(pf.DrawPath(pf.Outline([_star(570, 50, 10, 40, 5, rng)]), pf.ColorU(20, 90, 200, 230)))
+    out = np.full((96, 640, 4), 77, np.uint8)
+    img = renderer.render(s, out=out)
+    x0 = (500 // 16) * 16  # first screen tile column
+    assert (img[:, :x0] == 77).all()
+    assert (img[40:60, 560:580, 3] > 0).any()
