@@ -144,6 +144,7 @@ def run_reference(args) -> None:
     pbuild.build()
     oracle.build()
     scene = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=args.seed)
+    paints = add_paints(scene, args.seed) if args.paints else None
     nseg = scene.segment_count
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
@@ -159,14 +160,43 @@ def run_reference(args) -> None:
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded, PF_SCENE_SVG_4K)",
-        "config": {"workload": WORKLOAD, "paths": 20000, "segments": nseg, "width": W, "height": H,
-                   "seed": args.seed},
+        "config": {"workload": WORKLOAD + ("_paints" if paints else ""), "paths": 20000, "segments": nseg,
+                   "width": W, "height": H, "seed": args.seed, **({"paints": paints} if paints else {})},
         "cpu_baseline": {"value": round(value, 4), "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} full frames of the 4K scene (tiling + FP32 coverage + composite)"},
         "e2e": {"value": round(value, 4), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "mpx_per_s": round(W * H / (ms / 1e3) / 1e6, 3),
     }
     print(json.dumps(line), flush=True)
+
+
+def add_paints(scene, seed: int) -> str:
+    """Seeded paint effects over the generated scene: a quarter of the draw
+    paths take one of 64 gradients (linear and radial, clamp and repeat, four
+    random stops), a tenth take a blend mode other than SrcOver (uniform over
+    the other 26).  Returns the description for the JSON line."""
+    import numpy as np
+    import pathfinder_gb300 as pf
+    rng = np.random.default_rng(seed + 7)
+    w, h = scene.width, scene.height
+    for k in range(64):
+        if k % 2 == 0:
+            g = pf.Gradient.linear((rng.uniform(0, w), rng.uniform(0, h)), (rng.uniform(0, w), rng.uniform(0, h)))
+        else:
+            g = pf.Gradient.radial((rng.uniform(0, w), rng.uniform(0, h)), (0.0, rng.uniform(50, 800)))
+        g.set_wrap(pf.GradientWrap.REPEAT if k % 4 >= 2 else pf.GradientWrap.CLAMP)
+        for _ in range(4):
+            g.add_color_stop(pf.ColorU(*[int(v) for v in rng.integers(0, 256, 3)], int(rng.integers(96, 256))),
+                             float(rng.uniform(0, 1)))
+        scene.push_gradient(g)
+    n = len(scene.draw_paths)
+    pick = rng.random(n) < 0.25
+    scene.draw_paths["gradient"][pick] = rng.integers(1, 65, int(pick.sum()))
+    bm = rng.random(n) < 0.10
+    scene.draw_paths["blend_mode"][bm] = rng.integers(1, 27, int(bm.sum()))
+    scene.epoch += 1
+    return (f"{int(pick.sum())} paths with one of 64 gradients (linear/radial, clamp/repeat), "
+            f"{int(bm.sum())} with a blend mode other than SrcOver")
 
 
 def cpu_baseline(scene, nseg: int, budget_s: float = 12.0) -> dict:
@@ -442,6 +472,8 @@ def main():
     ap.add_argument("--fit-steps", type=int, default=200)
     ap.add_argument("--d3d11", action="store_true",
                     help="tile with the D3D11 level's semantics (uniform dicing) instead of the CPU tiler's")
+    ap.add_argument("--paints", action="store_true",
+                    help="add seeded gradients and blend modes to the 4K scene's paths")
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=400)
@@ -485,6 +517,7 @@ def main():
 
     # replicas only: each rank renders its own scene (seed + rank)
     scene = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=args.seed + rank, scale=args.scale)
+    paints = add_paints(scene, args.seed + rank) if args.paints else None
     nseg = scene.segment_count
     npts = len(scene.points)
     r = pf.Renderer(local, pf.RendererOptions(d3d11_semantics=args.d3d11))
@@ -598,7 +631,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded PF_SCENE_SVG_4K: 20,000 log-normal star paths, 40/30/30 line/quad/cubic)",
-            "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}_scale{args.scale}",
+            "config": {"workload": (WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}_scale{args.scale}")
+                                   + ("_paints" if paints else ""),
+                       **({"paints": paints} if paints else {}),
                        "paths": len(scene.draw_paths), "clip_paths": len(scene.clip_paths), "segments": nseg,
                        "points": npts, "width": W, "height": H, "seed": args.seed,
                        "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}",

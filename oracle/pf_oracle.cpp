@@ -1037,6 +1037,10 @@ void o_blend(uint32_t mode, const T s[3], T a, T* dst, int channels) {
         return;
     }
     if (channels == 4) {
+        // the destination composite() reads is a copy of the RGBA8 framebuffer
+        // (renderer/src/gpu/d3d9/renderer.rs:405-407): quantised to 8 bits
+        for (int c = 0; c < 3; c++) dst[c] = std::nearbyint(o_clamp01(dst[c]) * (T)255) / (T)255;
+        const T dq = std::nearbyint(o_clamp01(da) * (T)255) / (T)255;
         T b[3];
         if (mode >= PF_BLEND_MODE_HUE) {
             T dh[3], sh[3];
@@ -1052,7 +1056,7 @@ void o_blend(uint32_t mode, const T s[3], T a, T* dst, int channels) {
             for (int c = 0; c < 3; c++) b[c] = o_blend_channel<T>(mode, dst[c], s[c]);
         }
         for (int c = 0; c < 3; c++)
-            dst[c] = o_clamp01(a * ((T)1 - da) * s[c] + a * da * b[c] + ((T)1 - a) * dst[c]);
+            dst[c] = o_clamp01(a * ((T)1 - dq) * s[c] + a * dq * b[c] + ((T)1 - a) * dst[c]);
     }
     da_ref = 1;
 }

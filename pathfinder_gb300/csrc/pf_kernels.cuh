@@ -58,6 +58,7 @@ struct FrameDev {
     Counters* counters;
     uint32_t dda_limit;
     uint32_t clip_chain_max;     // bound of clip-chain walks (longest chain in the batch)
+    uint32_t paint_effects;      // some path of the batch has a gradient or a blend mode other than SrcOver
     // paint
     const GradDev*  grads;       // [gradients of the batch]
     const uint32_t* ramps;       // [gradients * 256] RGBA8 texels

@@ -196,7 +196,8 @@ __global__ void k_visible(FrameDev f, int scatter) {
                 }
                 f.vis_info[slot] = make_int4((int)b0, (int)nf, (int)f.path.paint[gp],
                                              vis_meta(tile_backdrop(rec), (tile_ctrl(rec) & 0x2u) != 0, kind,
-                                                      paint_fx_bits(f.path.blend[gp], f.path.gradient[gp])));
+                                                      f.paint_effects ? paint_fx_bits(f.path.blend[gp], f.path.gradient[gp])
+                                                                      : 0u));
             }
         }
     }
@@ -535,6 +536,13 @@ __device__ __forceinline__ void blend_pixel(uint32_t mode, float sr, float sg, f
         d3 = __saturatef(a * fs + da * fd);
         return;
     }
+    // composite() reads the destination from a copy of the RGBA8 framebuffer
+    // (copy_alpha_tiles_to_dest_blend_texture, renderer/src/gpu/d3d9/
+    // renderer.rs:405-407): the destination it sees is quantised to 8 bits.
+    d0 = rintf(__saturatef(d0) * 255.0f) * (1.0f / 255.0f);
+    d1 = rintf(__saturatef(d1) * 255.0f) * (1.0f / 255.0f);
+    d2 = rintf(__saturatef(d2) * 255.0f) * (1.0f / 255.0f);
+    const float dq = rintf(__saturatef(da) * 255.0f) * (1.0f / 255.0f);
     float b0, b1, b2;
     if (mode >= PF_BLEND_MODE_HUE) {
         const float3 dh = blend_rgb_to_hsl(d0, d1, d2), sh = blend_rgb_to_hsl(sr, sg, sb);
@@ -552,7 +560,7 @@ __device__ __forceinline__ void blend_pixel(uint32_t mode, float sr, float sg, f
         b2 = blend_separable(mode, d2, sb);
     }
     // composite() (tile_fragment.inc.glsl:519-537): output alpha 1
-    const float ws = a * (1.0f - da), wb = a * da, wd = 1.0f - a;
+    const float ws = a * (1.0f - dq), wb = a * dq, wd = 1.0f - a;
     d0 = __saturatef(ws * sr + wb * b0 + wd * d0);
     d1 = __saturatef(ws * sg + wb * b1 + wd * d1);
     d2 = __saturatef(ws * sb + wb * b2 + wd * d2);
@@ -622,7 +630,7 @@ struct CompositeScratch {
     CovBuf b0, b1;
 };
 
-template <int MODE, int WARPS>
+template <int MODE, int WARPS, bool PAINT>
 __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out, float4 bg) {
     extern __shared__ __align__(16) unsigned char comp_smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -669,7 +677,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
             info = ws.info[(uint32_t)key];
             kind = ((uint32_t)info.w >> 9) & 3u;
             paint = (uint32_t)info.z;
-            fx = (uint32_t)info.w >> 11;
+            if (PAINT) fx = (uint32_t)info.w >> 11;
         } else {
             g = f.vis[base + i];
         }
@@ -691,10 +699,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
             tile_coverage8(f, rec, g, ws.b0, ws.b1, cov);
             const uint32_t gp = (uint32_t)rec.z;
             paint = f.path.paint[gp];
-            fx = paint_fx_bits(f.path.blend[gp], f.path.gradient[gp]);
+            if (PAINT) fx = paint_fx_bits(f.path.blend[gp], f.path.gradient[gp]);
         }
         float pa = (float)(paint >> 24) * (1.0f / 255.0f);
-        if (fx != 0) {
+        if (PAINT && fx != 0) {
             composite_paint_tile(f, fx, paint, cov, tx, ty, col, half, d0, d1, d2, d3);
         } else if (MODE == 0) {
             float pr = (float)(paint & 0xffu) * (1.0f / 255.0f);
@@ -733,16 +741,23 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
     }
 }
 
-template <int MODE, int WARPS>
-void launch_composite_warps(const FrameDev& f, void* out, const float4& bg, cudaStream_t s) {
+// Solid SrcOver batches run the instance without the paint-effect path.
+template <int MODE, int WARPS, bool PAINT>
+void launch_composite_instance(const FrameDev& f, void* out, const float4& bg, cudaStream_t s) {
     constexpr size_t smem = WARPS * sizeof(CompositeScratch);
     static bool configured = false;  // above 48 KiB needs the opt-in (once per instance)
     if (!configured) {
-        cudaFuncSetAttribute(k_composite<MODE, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_composite<MODE, WARPS, PAINT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         configured = true;
     }
     count_launch();
-    k_composite<MODE, WARPS><<<(f.screen_count + WARPS - 1) / WARPS, WARPS * 32, smem, s>>>(f, out, bg);
+    k_composite<MODE, WARPS, PAINT><<<(f.screen_count + WARPS - 1) / WARPS, WARPS * 32, smem, s>>>(f, out, bg);
+}
+
+template <int MODE, int WARPS>
+void launch_composite_warps(const FrameDev& f, void* out, const float4& bg, cudaStream_t s) {
+    if (f.paint_effects) launch_composite_instance<MODE, WARPS, true>(f, out, bg, s);
+    else launch_composite_instance<MODE, WARPS, false>(f, out, bg, s);
 }
 
 template <int MODE>

@@ -253,6 +253,7 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.counters = r->counters.p;
     f.dda_limit = 1u << 24;
     f.clip_chain_max = r->clip_chain_max;
+    f.paint_effects = r->paint_effects ? 1u : 0u;
     return f;
 }
 

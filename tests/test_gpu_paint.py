@@ -127,3 +127,12 @@ def test_differentiable_frame_rejects_paint_effects(renderer):
     out = torch.zeros((s.height, s.width), dtype=torch.float32, device="cuda")
     with pytest.raises(PFCUDAError):
         renderer.render_diff(out, width=s.width, height=s.height)
+
+
+def test_svg4k_with_paints_reduced(renderer):
+    """The bench's paint workload (gradients on a quarter of the paths, blend
+    modes on a tenth) at a tenth of the 4K scene's paths."""
+    import bench
+    s = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=3, scale=0.1)
+    bench.add_paints(s, 3)
+    _check(renderer, s, frac_exact=0.95)
