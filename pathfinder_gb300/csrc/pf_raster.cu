@@ -504,7 +504,7 @@ __device__ __forceinline__ float3 blend_rgb_to_hsl(float r, float g, float b) {
 __device__ __forceinline__ float blend_hsl_channel(float k0, float h, float s, float l) {
     const float a = s * fminf(l, 1.0f - l);
     float k = k0 + h * 1.9098593171027443f;
-    k = k - 12.0f * floorf(k / 12.0f);  // GLSL mod
+    k = k - 12.0f * floorf(k * (1.0f / 12.0f));  // GLSL mod(k, 12)
     return l - fminf(fmaxf(fminf(k - 3.0f, 9.0f - k), -1.0f), 1.0f) * a;
 }
 
@@ -568,52 +568,71 @@ __device__ __forceinline__ void blend_pixel(uint32_t mode, float sr, float sg, f
 }
 
 // Composite one visible tile with paint effects into this lane's 8 pixels
-// (column col, rows half*8 .. half*8+7 of screen tile (tx, ty)).
+// (column col, rows half*8 .. half*8+7 of screen tile (tx, ty)).  The pixel
+// loop stays rolled, with the destination in a local array: unrolled, the
+// blend modes' code overflows the instruction cache.
 __device__ __forceinline__ void composite_paint_tile(const FrameDev& f, uint32_t fx, uint32_t paint, const float cov[8],
                                                      int32_t tx, int32_t ty, int col, int half, float d0[8],
                                                      float d1[8], float d2[8], float d3[8]) {
     const uint32_t mode = fx & 31u, grad1 = fx >> 5;
     const float4 base = unpack_unorm8(paint);
-    if (grad1 == 0) {
-#pragma unroll
-        for (int k = 0; k < 8; k++)
-            blend_pixel(mode, base.x, base.y, base.z, base.w * cov[k], d0[k], d1[k], d2[k], d3[k]);
-        return;
-    }
-    const GradDev& gd = f.grads[grad1 - 1];
-    const uint32_t* ramp = f.ramps + (size_t)(grad1 - 1) * 256u;
-    float t[6];
-    gradient_frame_transform(f, gd, t);
-    const int32_t wrap = gd.wrap;
-    const bool radial = gd.kind == PF_GRADIENT_RADIAL;
-    // filterRadialGradient (tile_fragment.inc.glsl:274-307): per-tile terms
-    const float dr = gd.r1 - gd.r0;
-    const float qa = (gd.vec_x * gd.vec_x + gd.vec_y * gd.vec_y) - dr * dr;
-    const float px = (float)(tx * 16 + col) + 0.5f;
+    float4 dd[8];
+    float cv[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) {
-        const float py = (float)(ty * 16 + half * 8 + k) + 0.5f;
-        const float u = t[0] * px + t[1] * py + t[2];
-        float4 c;
-        if (!radial) {
-            c = ramp_sample(ramp, u, wrap);
-        } else {
-            const float v = t[3] * px + t[4] * py + t[5];
-            const float dpx = u - gd.from_x, dpy = v - gd.from_y;
-            const float qb = (dpx * gd.vec_x + dpy * gd.vec_y) + gd.r0 * dr;
-            const float qc = (dpx * dpx + dpy * dpy) - gd.r0 * gd.r0;
-            const float disc = qb * qb - qa * qc;
-            c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (disc != 0.0f) {
-                const float sq = sqrtf(disc);
-                float lo = (sq + qb) / qa, hi = (-sq + qb) / qa;
-                if (lo > hi) { const float tmp = lo; lo = hi; hi = tmp; }
-                c = ramp_sample(ramp, lo >= 0.0f ? lo : hi, wrap);
+        dd[k] = make_float4(d0[k], d1[k], d2[k], d3[k]);
+        cv[k] = cov[k];
+    }
+    const GradDev* gd = grad1 ? &f.grads[grad1 - 1] : nullptr;
+    const uint32_t* ramp = f.ramps + (size_t)(grad1 ? grad1 - 1 : 0) * 256u;
+    float t[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    int32_t wrap = 0;
+    bool radial = false;
+    float fx0 = 0.0f, fy0 = 0.0f, vx = 0.0f, vy = 0.0f, r0 = 0.0f, dr = 0.0f, qa = 0.0f;
+    if (gd) {
+        gradient_frame_transform(f, *gd, t);
+        wrap = gd->wrap;
+        radial = gd->kind == PF_GRADIENT_RADIAL;
+        // filterRadialGradient (tile_fragment.inc.glsl:274-307): per-tile terms
+        fx0 = gd->from_x; fy0 = gd->from_y; vx = gd->vec_x; vy = gd->vec_y; r0 = gd->r0;
+        dr = gd->r1 - gd->r0;
+        qa = (vx * vx + vy * vy) - dr * dr;
+    }
+    const float px = (float)(tx * 16 + col) + 0.5f;
+#pragma unroll 1
+    for (int k = 0; k < 8; k++) {
+        float4 c = base;
+        float a = base.w * cv[k];
+        if (gd) {
+            const float py = (float)(ty * 16 + half * 8 + k) + 0.5f;
+            const float u = t[0] * px + t[1] * py + t[2];
+            if (!radial) {
+                c = ramp_sample(ramp, u, wrap);
+            } else {
+                const float v = t[3] * px + t[4] * py + t[5];
+                const float dpx = u - fx0, dpy = v - fy0;
+                const float qb = (dpx * vx + dpy * vy) + r0 * dr;
+                const float qc = (dpx * dpx + dpy * dpy) - r0 * r0;
+                const float disc = qb * qb - qa * qc;
+                c = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (disc != 0.0f) {
+                    const float sq = sqrtf(disc);
+                    float lo = (sq + qb) / qa, hi = (-sq + qb) / qa;
+                    if (lo > hi) { const float tmp = lo; lo = hi; hi = tmp; }
+                    c = ramp_sample(ramp, lo >= 0.0f ? lo : hi, wrap);
+                }
             }
+            // combineColor0 SrcIn (tile_fragment.inc.glsl:81-89): the texel's
+            // colour, its alpha times the base colour's
+            a = c.w * base.w * cv[k];
         }
-        // combineColor0 SrcIn (tile_fragment.inc.glsl:81-89): the texel's colour,
-        // its alpha times the base colour's
-        blend_pixel(mode, c.x, c.y, c.z, c.w * base.w * cov[k], d0[k], d1[k], d2[k], d3[k]);
+        float4 d = dd[k];
+        blend_pixel(mode, c.x, c.y, c.z, a, d.x, d.y, d.z, d.w);
+        dd[k] = d;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        d0[k] = dd[k].x; d1[k] = dd[k].y; d2[k] = dd[k].z; d3[k] = dd[k].w;
     }
 }
 
