@@ -74,8 +74,16 @@ __global__ void k_propagate(FrameDev f, int clip_pass) {
     if (!frame_ok(f) || f.path_count == 0) return;
     const uint32_t T = (uint32_t)f.counters->tiles;
     const uint32_t* offs = f.path.tile_offset + f.path_begin;
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < T; g += gridDim.x * blockDim.x) {
-        const uint32_t gp = f.path_begin + upper_bound_u32(offs, f.path_count + 1, g) - 1;
+    // A one-scene frame has its clip paths' tiles first: each pass visits only
+    // its own tiles and searches only its own paths.
+    uint32_t g_begin = 0, g_end = T, p_lo = 0, p_n = f.path_count + 1;
+    if (f.scene_count == 1) {
+        const uint32_t nclip = f.scenes[f.scene_begin].clip_count;
+        if (clip_pass) { g_end = offs[nclip]; p_n = nclip + 1; }
+        else { g_begin = offs[nclip]; p_lo = nclip; p_n = f.path_count + 1 - nclip; }
+    }
+    for (uint32_t g = g_begin + blockIdx.x * blockDim.x + threadIdx.x; g < g_end; g += gridDim.x * blockDim.x) {
+        const uint32_t gp = f.path_begin + p_lo + upper_bound_u32(offs + p_lo, p_n, g) - 1;
         const bool is_clip = f.path.is_clip[gp] != 0;
         if (is_clip != (clip_pass != 0)) continue;
         const int4 r = f.path.tile_rect[gp];
