@@ -191,7 +191,7 @@ def add_paints(scene, seed: int) -> str:
         scene.push_gradient(g)
     n = len(scene.draw_paths)
     pick = rng.random(n) < 0.25
-    scene.draw_paths["gradient"][pick] = rng.integers(1, 65, int(pick.sum()))
+    scene.draw_paths["overlay"][pick] = rng.integers(1, 65, int(pick.sum()))
     bm = rng.random(n) < 0.10
     scene.draw_paths["blend_mode"][bm] = rng.integers(1, 27, int(bm.sum()))
     scene.epoch += 1

@@ -128,12 +128,38 @@ typedef struct PFCUDAGradient {
 int32_t PFCUDAGradientSample(const PFCUDAGradient* gradient, float t, PFColorU* out);
 int32_t PFCUDAGradientRamp(const PFCUDAGradient* gradient, PFColorU* out_256);
 
+/* Image patterns (Pattern, content/src/pattern.rs:21-200, with PatternSource::
+ * Image).  The image is placed as the reference's texture allocator places it:
+ * on its own texture page, with one transparent texel of border on each axis
+ * that does not repeat (renderer/src/paint.rs:498-530); pattern space (0, 0)
+ * is the page's corner.  PatternFilter (content/src/effects.rs:64-95): a
+ * one-direction Gaussian blur, or a colour matrix (5 columns of RGBA, the
+ * feColorMatrix layout: out = M * colour + column 4).  The text filter
+ * belongs to the text front-end and is not on this path. */
+#define PF_PATTERN_REPEAT_X      0x1
+#define PF_PATTERN_REPEAT_Y      0x2
+#define PF_PATTERN_NO_SMOOTHING  0x4   /* nearest texel instead of linear filtering */
+#define PF_PATTERN_FILTER_NONE          0
+#define PF_PATTERN_FILTER_BLUR_X        1
+#define PF_PATTERN_FILTER_BLUR_Y        2
+#define PF_PATTERN_FILTER_COLOR_MATRIX  3
+
+typedef struct PFCUDAPattern {
+    const PFColorU* pixels;            /* width * height texels, row 0 first, straight alpha */
+    uint32_t width, height;            /* >= 1                                            */
+    PFTransform2F transform;           /* pattern space -> scene space                    */
+    uint32_t flags;                    /* PF_PATTERN_* bits                               */
+    int32_t  filter;                   /* PF_PATTERN_FILTER_*                             */
+    float    blur_sigma;               /* BLUR_X / BLUR_Y: > 0                            */
+    float    color_matrix[20];         /* COLOR_MATRIX: columns 0-4, RGBA each            */
+} PFCUDAPattern;
+
 #define PF_MEMORY_HOST   0
 #define PF_MEMORY_DEVICE 1
 
 /* One path of the scene: a range of contours of the shared outline buffers.
  * Mirrors DrawPath / ClipPath (renderer/src/scene.rs:441-472): outline,
- * paint (a colour, or a colour and a gradient), fill rule, blend mode,
+ * paint (a colour, or a colour with a gradient or pattern overlay), fill rule, blend mode,
  * optional clip path. */
 typedef struct PFCUDAPath {
     uint32_t first_contour;
@@ -142,8 +168,9 @@ typedef struct PFCUDAPath {
     int32_t  clip_path;      /* draw paths: index into clip paths, or -1         */
     uint8_t  fill_rule;      /* PF_FILL_RULE_*                                   */
     uint8_t  blend_mode;     /* draw paths: PF_BLEND_MODE_*                      */
-    uint16_t gradient;       /* draw paths: 0 = solid paint, k = gradient k - 1 of the
-                                scene (its colour SrcIn the paint: ramp alpha x paint alpha) */
+    uint16_t overlay;        /* draw paths: 0 = solid paint; 1 <= k <= gradient_count:
+                                gradients[k - 1]; above: patterns[k - 1 - gradient_count].
+                                The overlay's colour SrcIn the paint (its alpha x paint alpha) */
 } PFCUDAPath;
 
 /* The scene as flat outline buffers.  Every contour is treated as closed
@@ -164,6 +191,8 @@ typedef struct PFCUDASceneDesc {
     int32_t  memory;                   /* PF_MEMORY_* for points/flags/starts */
     const PFCUDAGradient* gradients;   /* host memory; may be NULL when unused */
     uint32_t gradient_count;
+    const PFCUDAPattern* patterns;     /* host memory; may be NULL when unused */
+    uint32_t pattern_count;
 } PFCUDASceneDesc;
 
 /* BuildOptions (renderer/src/options.rs:53-61): only the 2-D transform is on

@@ -144,13 +144,22 @@ PFColorU o_gradient_sample(const std::vector<PFCUDAColorStop>& stops, float t) {
     return PFColorU{o[0], o[1], o[2], o[3]};
 }
 
+// A paint overlay: a gradient (kind PF_GRADIENT_*) or an image pattern (kind 2).
 struct OGrad {
     int32_t kind = 0, wrap = 0;
     float g[6] = {0, 0, 0, 0, 0, 0};  // scene -> colour texture coordinate (row-major 2x3)
     float fx = 0, fy = 0, vx = 0, vy = 0, r0 = 0, r1 = 0;  // radial, rounded to binary16
     PFColorU ramp[256];
     bool opaque = true;
+    // patterns: the texture page (image inside a transparent border on axes that do not repeat)
+    std::vector<PFColorU> page;
+    int32_t pw = 0, ph = 0;
+    uint32_t flags = 0;
+    int32_t filter = 0;
+    float blur[6] = {0, 0, 0, 0, 0, 0};  // offset x, y, support, Gaussian x, y, z (binary16)
+    float matrix[20] = {};               // colour matrix columns (binary16)
 };
+const int32_t kOPattern = 2;
 
 // The gradient's colour ramp (renderer/src/paint.rs:855-863) and texture
 // transform (:603-616): linear, the projection onto the gradient line; radial,
@@ -190,6 +199,62 @@ bool o_build_gradient(const PFCUDAGradient& in, OGrad& g) {
         g.vy = o_round_f16(in.to.y - in.from.y);
         g.r0 = o_round_f16(in.radius0);
         g.r1 = o_round_f16(in.radius1);
+    }
+    return true;
+}
+
+// An image pattern on its own texture page (renderer/src/paint.rs:498-560):
+// one transparent texel of border on each axis that does not repeat; page UV
+// = scale(1 / page size) * inverse(pattern transform) (:617-623) in single
+// precision with the reference's product order (geometry/src/transform2d.rs:
+// 60-72, 115-129, 294-310); filter parameters as compute_filter_params writes
+// them (renderer/src/gpu/renderer.rs:988-1040), rounded to binary16.
+bool o_build_pattern(const PFCUDAPattern& in, OGrad& g) {
+    if (!in.pixels || in.width == 0 || in.height == 0 || in.width > 16384 || in.height > 16384) return false;
+    if (in.flags & ~7u) return false;
+    if (in.filter < 0 || in.filter > PF_PATTERN_FILTER_COLOR_MATRIX) return false;
+    const bool blur = in.filter == PF_PATTERN_FILTER_BLUR_X || in.filter == PF_PATTERN_FILTER_BLUR_Y;
+    if (blur && !(in.blur_sigma > 0.0f && in.blur_sigma <= 256.0f)) return false;
+    const PFTransform2F& t = in.transform;
+    float det = t.m00 * t.m11 - t.m01 * t.m10;
+    if (det == 0.0f) return false;
+    g.kind = kOPattern;
+    g.flags = in.flags;
+    g.filter = in.filter;
+    const int bx = (in.flags & PF_PATTERN_REPEAT_X) ? 0 : 1, by = (in.flags & PF_PATTERN_REPEAT_Y) ? 0 : 1;
+    g.pw = (int)in.width + 2 * bx;
+    g.ph = (int)in.height + 2 * by;
+    g.page.assign((size_t)g.pw * g.ph, PFColorU{0, 0, 0, 0});
+    g.opaque = true;  // Image::is_opaque (content/src/pattern.rs:208-212)
+    for (uint32_t y = 0; y < in.height; y++)
+        for (uint32_t x = 0; x < in.width; x++) {
+            PFColorU c = in.pixels[(size_t)y * in.width + x];
+            g.page[(size_t)(y + by) * g.pw + (x + bx)] = c;
+            g.opaque = g.opaque && c.a == 255;
+        }
+    float r = 1.0f / det;
+    float a = r * t.m11, b = r * -t.m01, c = r * -t.m10, d = r * t.m00;
+    float ivx = -(a * t.vector.x + b * t.vector.y), ivy = -(c * t.vector.x + d * t.vector.y);
+    float sx = 1.0f / (float)g.pw, sy = 1.0f / (float)g.ph;
+    // [sx 0; 0 sy] * [a b; c d] with the zero products kept, as F32x4 lanes compute it
+    g.g[0] = sx * a + 0.0f * c;
+    g.g[1] = sx * b + 0.0f * d;
+    g.g[3] = 0.0f * a + sy * c;
+    g.g[4] = 0.0f * b + sy * d;
+    g.g[2] = (sx * ivx + 0.0f * ivy) + 0.0f;
+    g.g[5] = (0.0f * ivx + sy * ivy) + 0.0f;
+    if (blur) {
+        float sigma_inv = 1.0f / in.blur_sigma;
+        float gx = 0.3989422804014327f * sigma_inv, gy = std::exp(-0.5f * sigma_inv * sigma_inv), gz = gy * gy;
+        float support = std::ceil(1.5f * in.blur_sigma) * 2.0f;
+        g.blur[0] = in.filter == PF_PATTERN_FILTER_BLUR_X ? 1.0f : 0.0f;
+        g.blur[1] = in.filter == PF_PATTERN_FILTER_BLUR_Y ? 1.0f : 0.0f;
+        g.blur[2] = o_round_f16(support);
+        g.blur[3] = o_round_f16(gx);
+        g.blur[4] = o_round_f16(gy);
+        g.blur[5] = o_round_f16(gz);
+    } else if (in.filter == PF_PATTERN_FILTER_COLOR_MATRIX) {
+        for (int k = 0; k < 20; k++) g.matrix[k] = o_round_f16(in.color_matrix[k]);
     }
     return true;
 }
@@ -559,7 +624,7 @@ struct Frame {
     std::vector<uint32_t> alpha_owner;        // alpha id -> global tile index owning the fills
     RectI screen{0, 0, 0, 0};
     std::vector<int32_t> zbuf;
-    std::vector<OGrad> grads;                 // the scene's gradients
+    std::vector<OGrad> grads;                 // the scene's overlays: gradients, then patterns
     float inv[6] = {1, 0, 0, 0, 1, 0};        // frame pixel -> scene (inverse build transform)
     bool limit_hit = false;
     bool d3d11 = false;  // the D3D11 level's dicing and binning
@@ -930,11 +995,87 @@ void o_ramp_sample(const OGrad& g, T u, T out[4]) {
     for (int c = 0; c < 4; c++) out[c] = (ca[c] * ((T)1 - w1) + cb[c] * w1) / (T)255;
 }
 
+// One sample of a pattern's page at UV (u, v): linear filtering or the
+// nearest texel, each axis repeated or clamped to the edge
+// (renderer/src/paint.rs:537-548).  A NaN coordinate gives transparent black.
+template <typename T>
+void o_page_sample(const OGrad& g, T u, T v, T out[4]) {
+    const bool rx = (g.flags & PF_PATTERN_REPEAT_X) != 0, ry = (g.flags & PF_PATTERN_REPEAT_Y) != 0;
+    if (rx) u = u - std::floor(u);
+    if (ry) v = v - std::floor(v);
+    if (std::isnan(u) || std::isnan(v)) { out[0] = out[1] = out[2] = out[3] = (T)0; return; }
+    u = std::min(std::max(u, (T)-1), (T)2);
+    v = std::min(std::max(v, (T)-1), (T)2);
+    const int W = g.pw, H = g.ph;
+    auto wx_ = [&](long i) { return (int)(rx ? ((i % W) + W) % W : std::min<long>(std::max<long>(i, 0), W - 1)); };
+    auto wy_ = [&](long i) { return (int)(ry ? ((i % H) + H) % H : std::min<long>(std::max<long>(i, 0), H - 1)); };
+    auto texel = [&](int x, int y, T c[4]) {
+        const PFColorU p = g.page[(size_t)y * W + x];
+        c[0] = (T)p.r / (T)255; c[1] = (T)p.g / (T)255; c[2] = (T)p.b / (T)255; c[3] = (T)p.a / (T)255;
+    };
+    if (g.flags & PF_PATTERN_NO_SMOOTHING) {
+        texel(wx_((long)std::floor(u * (T)W)), wy_((long)std::floor(v * (T)H)), out);
+        return;
+    }
+    T x = u * (T)W - (T)0.5, y = v * (T)H - (T)0.5;
+    T x0 = std::floor(x), y0 = std::floor(y), fx = x - x0, fy = y - y0;
+    int ix0 = wx_((long)x0), ix1 = wx_((long)x0 + 1), iy0 = wy_((long)y0), iy1 = wy_((long)y0 + 1);
+    T c00[4], c10[4], c01[4], c11[4];
+    texel(ix0, iy0, c00); texel(ix1, iy0, c10); texel(ix0, iy1, c01); texel(ix1, iy1, c11);
+    for (int k = 0; k < 4; k++) {
+        T top = c00[k] + (c10[k] - c00[k]) * fx, bot = c01[k] + (c11[k] - c01[k]) * fx;
+        out[k] = top + (bot - top) * fy;
+    }
+}
+
+// A pattern's colour through its filter: filterBlur (shaders/
+// tile_fragment.inc.glsl:309-347) or filterColorMatrix (:349-359).
+template <typename T>
+void o_pattern_color(const OGrad& g, T u, T v, T out[4]) {
+    if (g.filter == PF_PATTERN_FILTER_COLOR_MATRIX) {
+        T c[4];
+        o_page_sample<T>(g, u, v, c);
+        const float* m = g.matrix;
+        for (int k = 0; k < 4; k++)
+            out[k] = (T)m[k] * c[0] + (T)m[4 + k] * c[1] + (T)m[8 + k] * c[2] + (T)m[12 + k] * c[3] + (T)m[16 + k];
+        return;
+    }
+    if (g.filter != PF_PATTERN_FILTER_BLUR_X && g.filter != PF_PATTERN_FILTER_BLUR_Y) {
+        o_page_sample<T>(g, u, v, out);
+        return;
+    }
+    const T sx = (T)g.blur[0] / (T)g.pw, sy = (T)g.blur[1] / (T)g.ph;
+    const int support = (int)g.blur[2];
+    T gx = g.blur[3], gy = g.blur[4];
+    const T gz = g.blur[5];
+    T sum = gx, c[4];
+    o_page_sample<T>(g, u, v, c);
+    for (int k = 0; k < 4; k++) c[k] *= gx;
+    gx *= gy; gy *= gz;
+    for (int i = 1; i <= support; i += 2) {
+        T partial = gx;
+        gx *= gy; gy *= gz;
+        partial += gx;
+        T o = (T)i + gx / partial;
+        T a[4], b[4];
+        o_page_sample<T>(g, u - sx * o, v - sy * o, a);
+        o_page_sample<T>(g, u + sx * o, v + sy * o, b);
+        for (int k = 0; k < 4; k++) c[k] += (a[k] + b[k]) * partial;
+        sum += (T)2 * partial;
+        gx *= gy; gy *= gz;
+    }
+    for (int k = 0; k < 4; k++) out[k] = c[k] / sum;
+}
+
 // The gradient's straight colour at pixel centre (px, py): linear, the ramp at
 // u; radial, filterRadialGradient (shaders/tile_fragment.inc.glsl:274-307).
 template <typename T>
 void o_gradient_color(const OGrad& g, const float t[6], T px, T py, T out[4]) {
     T u = (T)t[0] * px + (T)t[1] * py + (T)t[2];
+    if (g.kind == kOPattern) {
+        o_pattern_color<T>(g, u, (T)t[3] * px + (T)t[4] * py + (T)t[5], out);
+        return;
+    }
     if (g.kind == PF_GRADIENT_LINEAR) { o_ramp_sample<T>(g, u, out); return; }
     T v = (T)t[3] * px + (T)t[4] * py + (T)t[5];
     T dpx = u - (T)g.fx, dpy = v - (T)g.fy, dcx = g.vx, dcy = g.vy;
@@ -1154,10 +1295,12 @@ bool make_frame(const PFCUDASceneDesc* sc, const PFCUDABuildOptions* opts, Frame
                       tf.vector.x == 0.0f && tf.vector.y == 0.0f);
     }
     fr.transformed.assign(transform ? n : 0, {});
-    if (sc->gradient_count && !sc->gradients) return false;
-    fr.grads.assign(sc->gradient_count, OGrad());
+    if ((sc->gradient_count && !sc->gradients) || (sc->pattern_count && !sc->patterns)) return false;
+    fr.grads.assign((size_t)sc->gradient_count + sc->pattern_count, OGrad());
     for (uint32_t q = 0; q < sc->gradient_count; q++)
         if (!o_build_gradient(sc->gradients[q], fr.grads[q])) return false;
+    for (uint32_t q = 0; q < sc->pattern_count; q++)
+        if (!o_build_pattern(sc->patterns[q], fr.grads[sc->gradient_count + q])) return false;
     if (transform) {
         // render_transform = the build transform's inverse (renderer/src/builder.rs:168-171)
         float det = tf.m00 * tf.m11 - tf.m01 * tf.m10;
@@ -1177,12 +1320,13 @@ bool make_frame(const PFCUDASceneDesc* sc, const PFCUDABuildOptions* opts, Frame
         in.clip_path = src.clip_path;  // clip paths may be clipped too (clip chains)
         in.paint = src.paint;
         if (!in.is_clip) {
-            if (src.blend_mode >= PF_BLEND_MODE_COUNT || src.gradient > sc->gradient_count) return false;
+            if (src.blend_mode >= PF_BLEND_MODE_COUNT || src.overlay > sc->gradient_count + sc->pattern_count)
+                return false;
             in.blend = src.blend_mode;
-            in.gradient = src.gradient;
+            in.gradient = src.overlay;
             // opaque paint (Paint::is_opaque, renderer/src/paint.rs:163-177) with a
             // blend mode that hides the backdrop (content/src/effects.rs:202-230)
-            bool opaque = src.paint.a == 255 && (src.gradient == 0 || fr.grads[src.gradient - 1].opaque);
+            bool opaque = src.paint.a == 255 && (src.overlay == 0 || fr.grads[src.overlay - 1].opaque);
             in.occludes = opaque && (src.blend_mode == PF_BLEND_MODE_SRC_OVER || src.blend_mode == PF_BLEND_MODE_CLEAR);
         }
         if (src.clip_path >= (int32_t)fr.clip_count) return false;

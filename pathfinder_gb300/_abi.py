@@ -38,6 +38,14 @@ PF_GRADIENT_RADIAL = 1
 PF_GRADIENT_WRAP_CLAMP = 0
 PF_GRADIENT_WRAP_REPEAT = 1
 
+PF_PATTERN_REPEAT_X = 0x1
+PF_PATTERN_REPEAT_Y = 0x2
+PF_PATTERN_NO_SMOOTHING = 0x4
+PF_PATTERN_FILTER_NONE = 0
+PF_PATTERN_FILTER_BLUR_X = 1
+PF_PATTERN_FILTER_BLUR_Y = 2
+PF_PATTERN_FILTER_COLOR_MATRIX = 3
+
 PF_SCENE_STARS_512 = 1
 PF_SCENE_SVG_4K = 2
 PF_SCENE_GLYPH_ATLAS = 3
@@ -80,7 +88,7 @@ class PFTransform2F(C.Structure):
 class PFCUDAPath(C.Structure):
     _fields_ = [("first_contour", C.c_uint32), ("contour_count", C.c_uint32), ("paint", PFColorU),
                 ("clip_path", C.c_int32), ("fill_rule", C.c_uint8), ("blend_mode", C.c_uint8),
-                ("gradient", C.c_uint16)]
+                ("overlay", C.c_uint16)]
 
 
 class PFCUDAColorStop(C.Structure):
@@ -93,13 +101,20 @@ class PFCUDAGradient(C.Structure):
                 ("stops", C.c_void_p), ("stop_count", C.c_uint32), ("reserved", C.c_uint32)]
 
 
+class PFCUDAPattern(C.Structure):
+    _fields_ = [("pixels", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("transform", PFTransform2F), ("flags", C.c_uint32), ("filter", C.c_int32),
+                ("blur_sigma", C.c_float), ("color_matrix", C.c_float * 20)]
+
+
 class PFCUDASceneDesc(C.Structure):
     _fields_ = [("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_starts", C.c_void_p),
                 ("clip_paths", C.c_void_p), ("draw_paths", C.c_void_p),
                 ("point_count", C.c_uint32), ("contour_count", C.c_uint32),
                 ("clip_path_count", C.c_uint32), ("draw_path_count", C.c_uint32),
                 ("view_box", PFRectF), ("memory", C.c_int32),
-                ("gradients", C.c_void_p), ("gradient_count", C.c_uint32)]
+                ("gradients", C.c_void_p), ("gradient_count", C.c_uint32),
+                ("patterns", C.c_void_p), ("pattern_count", C.c_uint32)]
 
 
 class PFCUDABuildOptions(C.Structure):
@@ -163,7 +178,7 @@ def record_dtypes():
     clip = np.dtype([("dest_tile_id", "<u4"), ("dest_backdrop", "<i4"), ("src_tile_id", "<u4"),
                      ("src_backdrop", "<i4")])
     path = np.dtype([("first_contour", "<u4"), ("contour_count", "<u4"), ("paint", "u1", (4,)),
-                     ("clip_path", "<i4"), ("fill_rule", "u1"), ("blend_mode", "u1"), ("gradient", "<u2")])
+                     ("clip_path", "<i4"), ("fill_rule", "u1"), ("blend_mode", "u1"), ("overlay", "<u2")])
     rect = np.dtype([("x0", "<i4"), ("y0", "<i4"), ("x1", "<i4"), ("y1", "<i4")])
     return fill, tile, clip, path, rect
 

@@ -57,9 +57,9 @@ struct PathDev {
     // differentiable frames only (NULL otherwise): paint alpha per draw path
     const float* alpha_f;          // [draw paths of the batch]
     const uint32_t* draw_index;    // [P] index of the path among the batch's draw paths
-    // paint: blend mode (PF_BLEND_MODE_*) and gradient (index + 1, 0 = none) per path
+    // paint: blend mode (PF_BLEND_MODE_*) and overlay (index + 1, 0 = none) per path
     const uint8_t*  blend;         // [P]
-    const uint32_t* gradient;      // [P]
+    const uint32_t* overlay;       // [P]
     const uint8_t*  occludes;      // [P] opaque paint with a blend mode that hides what lies below
 };
 
@@ -70,19 +70,28 @@ __host__ __device__ __forceinline__ bool blend_is_destructive(uint32_t m) {
            m == 6u /* DestIn */ || m == 9u /* DestAtop */;
 }
 
-// A gradient of the batch (ramp of 256 RGBA8 texels in `ramps`).
-// `g` maps scene coordinates to the colour texture coordinate before the
-// frame's inverse build transform is composed in: linear, u = g0 x + g1 y + g2
-// (the projection onto the gradient line); radial, the inverse of the
-// gradient's transform.  The radial filter parameters are stored rounded to
-// binary16, as the reference's RGBA16F metadata texture holds them
+// A paint overlay of the batch: a gradient (a ramp of 256 RGBA8 texels) or an
+// image pattern (a texture page), both in `texels`.  `g` maps scene
+// coordinates to the colour texture coordinate before the frame's inverse
+// build transform is composed in: linear gradients, u = g0 x + g1 y + g2 (the
+// projection onto the line); radial gradients, the inverse of the gradient's
+// transform; patterns, page UV = scale(1 / page size) * inverse(pattern
+// transform).  Filter parameters are stored rounded to binary16, as the
+// reference's RGBA16F metadata texture holds them
 // (renderer/src/gpu/renderer.rs:702-763).
-struct GradDev {
-    int32_t kind, wrap;            // PF_GRADIENT_*
+constexpr int32_t kOverlayPattern = 2;  // after PF_GRADIENT_LINEAR / PF_GRADIENT_RADIAL
+struct OverlayDev {
+    int32_t kind, wrap;            // PF_GRADIENT_* or kOverlayPattern; gradient wrap
     float g[6];                    // row-major 2x3: [m11 m12 m13; m21 m22 m23]
     float from_x, from_y;          // radial: first centre
     float vec_x, vec_y;            // radial: vector between the centres
     float r0, r1;                  // radial: radii
+    uint32_t texel_offset;         // first texel of the ramp or page in `texels`
+    uint32_t page_w, page_h;       // page size (ramps: 256 x 1)
+    uint32_t flags;                // patterns: PF_PATTERN_* bits
+    int32_t filter;                // patterns: PF_PATTERN_FILTER_*
+    float blur[6];                 // blur: source offset (x, y), support, Gaussian coefficients (x, y, z)
+    float matrix[20];              // colour matrix columns
 };
 
 // Round a float to the nearest binary16 value (ties to even), kept as float;

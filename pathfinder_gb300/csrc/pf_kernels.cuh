@@ -3,6 +3,8 @@
 
 #include "pf_device.cuh"
 
+#include <vector>
+
 namespace pf {
 
 // Launch shapes chosen by the autotuner (outputs do not depend on them).
@@ -60,8 +62,8 @@ struct FrameDev {
     uint32_t clip_chain_max;     // bound of clip-chain walks (longest chain in the batch)
     uint32_t paint_effects;      // some path of the batch has a gradient or a blend mode other than SrcOver
     // paint
-    const GradDev*  grads;       // [gradients of the batch]
-    const uint32_t* ramps;       // [gradients * 256] RGBA8 texels
+    const OverlayDev* overlays;  // [paint overlays of the batch: gradients, then patterns]
+    const uint32_t* texels;      // gradient ramps and pattern pages, RGBA8
     float inv_m[6];              // frame pixel -> scene coordinates (inverse build transform)
     // Differentiable frames (diff != 0): FP32 fills, the curve parameters of
     // every flattened line, and per visible (screen tile, path tile) entry the
@@ -141,11 +143,14 @@ struct ScanTemp { uint32_t* partials; uint32_t cap; };
 
 }  // namespace pf
 struct PFCUDAGradient;
+struct PFCUDAPattern;
 struct PFCUDAColorStop;
 namespace pf {
-// Gradient paints (host): the record of one gradient and its 256-texel ramp;
+// Paint overlays (host): the record of one gradient with its 256-texel ramp,
+// or of one image pattern with its texture page, appended to `texels`;
 // returns a PF_CUDA_* status.
-int32_t build_gradient(const PFCUDAGradient& g, GradDev* out, uint32_t* ramp, bool* opaque);
+int32_t build_gradient(const PFCUDAGradient& g, OverlayDev* out, std::vector<uint32_t>& texels, bool* opaque);
+int32_t build_pattern(const PFCUDAPattern& p, OverlayDev* out, std::vector<uint32_t>& texels, bool* opaque);
 
 // Number of kernels this library has launched (host counter).
 uint64_t launch_counter();

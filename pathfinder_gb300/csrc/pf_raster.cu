@@ -204,7 +204,7 @@ __global__ void k_visible(FrameDev f, int scatter) {
                 }
                 f.vis_info[slot] = make_int4((int)b0, (int)nf, (int)f.path.paint[gp],
                                              vis_meta(tile_backdrop(rec), (tile_ctrl(rec) & 0x2u) != 0, kind,
-                                                      f.paint_effects ? paint_fx_bits(f.path.blend[gp], f.path.gradient[gp])
+                                                      f.paint_effects ? paint_fx_bits(f.path.blend[gp], f.path.overlay[gp])
                                                                       : 0u));
             }
         }
@@ -430,7 +430,7 @@ __device__ __forceinline__ void tile_coverage8(const FrameDev& f, int4 rec, uint
 // render_transform`, renderer/src/paint.rs:637; Transform2F * Transform2F,
 // geometry/src/transform2d.rs:115-121, 301-310) and rounded to binary16 as the
 // metadata texture stores it (renderer/src/gpu/renderer.rs:711-719).
-__device__ __forceinline__ void gradient_frame_transform(const FrameDev& f, const GradDev& gd, float t[6]) {
+__device__ __forceinline__ void gradient_frame_transform(const FrameDev& f, const OverlayDev& gd, float t[6]) {
     const float* G = gd.g;
     const float* R = f.inv_m;
     t[0] = round_f16(fadd(fmul(G[0], R[0]), fmul(G[1], R[3])));
@@ -575,6 +575,71 @@ __device__ __forceinline__ void blend_pixel(uint32_t mode, float sr, float sg, f
     d3 = 1.0f;
 }
 
+// One sample of a pattern's texture page at UV (u, v): linear filtering or the
+// nearest texel (NEAREST_MIN | NEAREST_MAG, renderer/src/paint.rs:545-548),
+// each axis repeated or clamped to the edge (REPEAT_U / REPEAT_V, :537-543);
+// the non-repeating axes' edges are the page's transparent border.  A NaN
+// coordinate gives transparent black.
+__device__ __forceinline__ float4 page_sample(const uint32_t* tex, int W, int H, uint32_t flags, float u, float v) {
+    const bool rx = (flags & PF_PATTERN_REPEAT_X) != 0, ry = (flags & PF_PATTERN_REPEAT_Y) != 0;
+    if (rx) u = u - floorf(u);
+    if (ry) v = v - floorf(v);
+    if (!(u == u) || !(v == v)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    u = fminf(fmaxf(u, -1.0f), 2.0f);
+    v = fminf(fmaxf(v, -1.0f), 2.0f);
+    auto wrap_x = [&](int i) { return rx ? ((i % W) + W) % W : min(max(i, 0), W - 1); };
+    auto wrap_y = [&](int i) { return ry ? ((i % H) + H) % H : min(max(i, 0), H - 1); };
+    if (flags & PF_PATTERN_NO_SMOOTHING)
+        return unpack_unorm8(__ldg(tex + wrap_y((int)floorf(v * (float)H)) * W + wrap_x((int)floorf(u * (float)W))));
+    const float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
+    const float x0 = floorf(x), y0 = floorf(y), wx = x - x0, wy = y - y0;
+    const int ix0 = wrap_x((int)x0), ix1 = wrap_x((int)x0 + 1), iy0 = wrap_y((int)y0), iy1 = wrap_y((int)y0 + 1);
+    const float4 c00 = unpack_unorm8(__ldg(tex + iy0 * W + ix0)), c10 = unpack_unorm8(__ldg(tex + iy0 * W + ix1));
+    const float4 c01 = unpack_unorm8(__ldg(tex + iy1 * W + ix0)), c11 = unpack_unorm8(__ldg(tex + iy1 * W + ix1));
+    auto lerp4 = [](float4 a, float4 b, float t) {
+        return make_float4(a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t, a.w + (b.w - a.w) * t);
+    };
+    return lerp4(lerp4(c00, c10, wx), lerp4(c01, c11, wx), wy);
+}
+
+// A pattern's colour at UV (u, v) through its filter: filterNone, filterBlur
+// (shaders/tile_fragment.inc.glsl:309-347, the incremental Gaussian with two
+// taps per linear fetch) or filterColorMatrix (:349-359).
+__device__ __noinline__ float4 pattern_color(const OverlayDev& od, const uint32_t* tex, float u, float v) {
+    const int W = (int)od.page_w, H = (int)od.page_h;
+    if (od.filter == PF_PATTERN_FILTER_COLOR_MATRIX) {
+        const float4 c = page_sample(tex, W, H, od.flags, u, v);
+        const float* m = od.matrix;
+        return make_float4(m[0] * c.x + m[4] * c.y + m[8] * c.z + m[12] * c.w + m[16],
+                           m[1] * c.x + m[5] * c.y + m[9] * c.z + m[13] * c.w + m[17],
+                           m[2] * c.x + m[6] * c.y + m[10] * c.z + m[14] * c.w + m[18],
+                           m[3] * c.x + m[7] * c.y + m[11] * c.z + m[15] * c.w + m[19]);
+    }
+    if (od.filter != PF_PATTERN_FILTER_BLUR_X && od.filter != PF_PATTERN_FILTER_BLUR_Y)
+        return page_sample(tex, W, H, od.flags, u, v);
+    const float sx = od.blur[0] / (float)W, sy = od.blur[1] / (float)H;
+    const int support = (int)od.blur[2];
+    float gx = od.blur[3], gy = od.blur[4];
+    const float gz = od.blur[5];
+    float sum = gx;
+    float4 c = page_sample(tex, W, H, od.flags, u, v);
+    c = make_float4(c.x * gx, c.y * gx, c.z * gx, c.w * gx);
+    gx *= gy; gy *= gz;
+    for (int i = 1; i <= support; i += 2) {
+        float partial = gx;
+        gx *= gy; gy *= gz;
+        partial += gx;
+        const float o = (float)i + gx / partial;
+        const float4 a = page_sample(tex, W, H, od.flags, u - sx * o, v - sy * o);
+        const float4 b = page_sample(tex, W, H, od.flags, u + sx * o, v + sy * o);
+        c.x += (a.x + b.x) * partial; c.y += (a.y + b.y) * partial;
+        c.z += (a.z + b.z) * partial; c.w += (a.w + b.w) * partial;
+        sum += 2.0f * partial;
+        gx *= gy; gy *= gz;
+    }
+    return make_float4(c.x / sum, c.y / sum, c.z / sum, c.w / sum);
+}
+
 // Composite one visible tile with paint effects into this lane's 8 pixels
 // (column col, rows half*8 .. half*8+7 of screen tile (tx, ty)).  The pixel
 // loop stays rolled, with the destination in a local array: unrolled, the
@@ -591,16 +656,17 @@ __device__ __forceinline__ void composite_paint_tile(const FrameDev& f, uint32_t
         dd[k] = make_float4(d0[k], d1[k], d2[k], d3[k]);
         cv[k] = cov[k];
     }
-    const GradDev* gd = grad1 ? &f.grads[grad1 - 1] : nullptr;
-    const uint32_t* ramp = f.ramps + (size_t)(grad1 ? grad1 - 1 : 0) * 256u;
+    const OverlayDev* gd = grad1 ? &f.overlays[grad1 - 1] : nullptr;
+    const uint32_t* ramp = f.texels + (gd ? gd->texel_offset : 0u);
     float t[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     int32_t wrap = 0;
-    bool radial = false;
+    bool radial = false, pattern = false;
     float fx0 = 0.0f, fy0 = 0.0f, vx = 0.0f, vy = 0.0f, r0 = 0.0f, dr = 0.0f, qa = 0.0f;
     if (gd) {
         gradient_frame_transform(f, *gd, t);
         wrap = gd->wrap;
         radial = gd->kind == PF_GRADIENT_RADIAL;
+        pattern = gd->kind == kOverlayPattern;
         // filterRadialGradient (tile_fragment.inc.glsl:274-307): per-tile terms
         fx0 = gd->from_x; fy0 = gd->from_y; vx = gd->vec_x; vy = gd->vec_y; r0 = gd->r0;
         dr = gd->r1 - gd->r0;
@@ -614,7 +680,9 @@ __device__ __forceinline__ void composite_paint_tile(const FrameDev& f, uint32_t
         if (gd) {
             const float py = (float)(ty * 16 + half * 8 + k) + 0.5f;
             const float u = t[0] * px + t[1] * py + t[2];
-            if (!radial) {
+            if (pattern) {
+                c = pattern_color(*gd, ramp, u, t[3] * px + t[4] * py + t[5]);
+            } else if (!radial) {
                 c = ramp_sample(ramp, u, wrap);
             } else {
                 const float v = t[3] * px + t[4] * py + t[5];
@@ -726,7 +794,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
             tile_coverage8(f, rec, g, ws.b0, ws.b1, cov);
             const uint32_t gp = (uint32_t)rec.z;
             paint = f.path.paint[gp];
-            if (PAINT) fx = paint_fx_bits(f.path.blend[gp], f.path.gradient[gp]);
+            if (PAINT) fx = paint_fx_bits(f.path.blend[gp], f.path.overlay[gp]);
         }
         float pa = (float)(paint >> 24) * (1.0f / 255.0f);
         if (PAINT && fx != 0) {

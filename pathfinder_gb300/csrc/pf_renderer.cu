@@ -88,8 +88,8 @@ struct PFCUDARenderer {
     DevBuf<uint32_t> first_ord, paint, local_index, scene_of;
     DevBuf<int32_t> clip_gpath;
     DevBuf<uint8_t> rule, is_clip, blend, occludes;
-    DevBuf<uint32_t> gradient, ramps;
-    DevBuf<GradDev> grads;
+    DevBuf<uint32_t> overlay, texels;
+    DevBuf<OverlayDev> overlays;
     DevBuf<SceneDev> scenes_dev;
     std::vector<SceneDev> scenes_host;
 
@@ -203,10 +203,10 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.path.rule = r->rule.p;
     f.path.is_clip = r->is_clip.p;
     f.path.blend = r->blend.p;
-    f.path.gradient = r->gradient.p;
+    f.path.overlay = r->overlay.p;
     f.path.occludes = r->occludes.p;
-    f.grads = r->grads.p;
-    f.ramps = r->ramps.p;
+    f.overlays = r->overlays.p;
+    f.texels = r->texels.p;
     f.inv_m[0] = 1.0f; f.inv_m[4] = 1.0f;
     f.path.local_index = r->local_index.p;
     f.path.scene = r->scene_of.p;
@@ -528,8 +528,8 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->col_backdrop.release(); r->zbuf.release(); r->fills.release(); r->fill_e.release(); r->tiles.release();
     r->clips.release(); r->screen_cnt.release(); r->screen_base.release(); r->vis.release(); r->vis_info.release();
     r->scan_partials.release(); r->counters.release(); r->out_tmp.release();
-    r->draw_index.release(); r->blend.release(); r->occludes.release(); r->gradient.release();
-    r->grads.release(); r->ramps.release(); r->alpha_in.release(); r->fills_f.release(); r->line_seg.release();
+    r->draw_index.release(); r->blend.release(); r->occludes.release(); r->overlay.release();
+    r->overlays.release(); r->texels.release(); r->alpha_in.release(); r->fills_f.release(); r->line_seg.release();
     r->line_t.release(); r->tape.release();
     r->grad_mask.release(); r->grad_alpha_tmp.release();
     if (r->h_counters) cudaFreeHost(r->h_counters);
@@ -586,9 +586,9 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
     std::vector<uint32_t> draw_index((size_t)P, kInvalid);
     std::vector<float> draw_alpha;
     std::vector<uint8_t> blend((size_t)P, 0), occl((size_t)P, 0);
-    std::vector<uint32_t> gradv((size_t)P, 0), ramps;
-    std::vector<GradDev> grads;
-    std::vector<uint8_t> grad_opaque;
+    std::vector<uint32_t> overlayv((size_t)P, 0), texels;
+    std::vector<OverlayDev> overlays;
+    std::vector<uint8_t> overlay_opaque;
     r->scenes.assign(scene_count, SceneInfo());
     r->scenes_host.assign(scene_count, SceneDev{});
     uint32_t point_base = 0, contour_base = 0, gp = 0, screen_total = 0;
@@ -617,24 +617,26 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
         si.screen_offset = screen_total;
         si.screen_count = (uint32_t)sw * (uint32_t)sh;
         screen_total += si.screen_count;
-        if (sc.gradient_count && !sc.gradients) return PF_CUDA_ERR_INVALID;
-        const uint32_t grad_base = (uint32_t)grads.size();
-        for (uint32_t q = 0; q < sc.gradient_count; q++) {
-            if (grads.size() >= 0xfffeu) return PF_CUDA_ERR_INVALID;  // 16-bit ids in the visible records
-            GradDev gd;
+        if ((sc.gradient_count && !sc.gradients) || (sc.pattern_count && !sc.patterns)) return PF_CUDA_ERR_INVALID;
+        if ((uint64_t)overlays.size() + sc.gradient_count + sc.pattern_count > 0xfffeu)
+            return PF_CUDA_ERR_INVALID;  // 16-bit overlay ids in the visible records
+        const uint32_t ov_base = (uint32_t)overlays.size();
+        for (uint32_t q = 0; q < sc.gradient_count + sc.pattern_count; q++) {
+            OverlayDev od;
             bool opaque = false;
-            ramps.resize(ramps.size() + 256);
-            int32_t rc = build_gradient(sc.gradients[q], &gd, ramps.data() + ramps.size() - 256, &opaque);
+            const int32_t rc = q < sc.gradient_count
+                                   ? build_gradient(sc.gradients[q], &od, texels, &opaque)
+                                   : build_pattern(sc.patterns[q - sc.gradient_count], &od, texels, &opaque);
             if (rc != PF_CUDA_OK) return rc;
-            grads.push_back(gd);
-            grad_opaque.push_back(opaque ? 1 : 0);
+            overlays.push_back(od);
+            overlay_opaque.push_back(opaque ? 1 : 0);
         }
         for (uint32_t i = 0; i < sc.clip_path_count + sc.draw_path_count; i++, gp++) {
             const bool c = i < sc.clip_path_count;
             const PFCUDAPath& p = c ? sc.clip_paths[i] : sc.draw_paths[i - sc.clip_path_count];
             if ((uint64_t)p.first_contour + p.contour_count > sc.contour_count) return PF_CUDA_ERR_INVALID;
             if (p.fill_rule > 1 || p.blend_mode >= PF_BLEND_MODE_COUNT) return PF_CUDA_ERR_INVALID;
-            if (!c && p.gradient > sc.gradient_count) return PF_CUDA_ERR_INVALID;
+            if (!c && p.overlay > sc.gradient_count + sc.pattern_count) return PF_CUDA_ERR_INVALID;
             if (p.clip_path >= (int32_t)sc.clip_path_count) return PF_CUDA_ERR_INVALID;
             if (c && p.clip_path == (int32_t)i) return PF_CUDA_ERR_INVALID;  // a clip path clipping itself
             first_ord[gp] = (uint32_t)ord_contour.size();
@@ -653,10 +655,10 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
                 draw_index[gp] = (uint32_t)draw_alpha.size();
                 draw_alpha.push_back((float)p.paint.a / 255.0f);
                 blend[gp] = p.blend_mode;
-                gradv[gp] = p.gradient ? grad_base + p.gradient : 0u;  // global index + 1
+                overlayv[gp] = p.overlay ? ov_base + p.overlay : 0u;  // global index + 1
                 // BuiltDrawPath::occludes (renderer/src/builder.rs:80-94): opaque paint and
                 // BlendMode::occludes_backdrop (content/src/effects.rs:202-230)
-                const bool opaque = p.paint.a == 255 && (p.gradient == 0 || grad_opaque[grad_base + p.gradient - 1]);
+                const bool opaque = p.paint.a == 255 && (p.overlay == 0 || overlay_opaque[ov_base + p.overlay - 1]);
                 occl[gp] = opaque && (p.blend_mode == PF_BLEND_MODE_SRC_OVER || p.blend_mode == PF_BLEND_MODE_CLEAR);
             }
         }
@@ -695,7 +697,7 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
     }
     r->clip_chain_max = chain_max;
     r->nested_clips = nested;
-    r->paint_effects = !grads.empty();
+    r->paint_effects = !overlays.empty();
     for (uint32_t q = 0; q < P; q++) r->paint_effects = r->paint_effects || blend[q] != PF_BLEND_MODE_SRC_OVER;
     const uint32_t nord = (uint32_t)ord_contour.size();
     r->path_local.assign(local.begin(), local.end());
@@ -710,8 +712,8 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
         (e = r->local_index.ensure(Pz)) || (e = r->scene_of.ensure(Pz)) || (e = r->clip_gpath.ensure(Pz)) ||
         (e = r->rule.ensure(Pz)) || (e = r->is_clip.ensure(Pz)) || (e = r->tile_rect.ensure(Pz)) ||
         (e = r->draw_index.ensure(Pz)) || (e = r->blend.ensure(Pz)) || (e = r->occludes.ensure(Pz)) ||
-        (e = r->gradient.ensure(Pz)) || (e = r->grads.ensure(grads.size() + 1)) ||
-        (e = r->ramps.ensure(ramps.size() + 1)) ||
+        (e = r->overlay.ensure(Pz)) || (e = r->overlays.ensure(overlays.size() + 1)) ||
+        (e = r->texels.ensure(texels.size() + 1)) ||
         (e = r->tile_offset.ensure(Pz + 1)) || (e = r->col_offset.ensure(Pz + 1)) ||
         (e = r->scenes_dev.ensure(scene_count)) || (e = r->scan_partials.ensure(nord / 2048 + 2)))
         return cuda_status(e);
@@ -741,11 +743,12 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
         PF_TRY(cudaMemcpyAsync(r->draw_index.p, draw_index.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
         PF_TRY(cudaMemcpyAsync(r->blend.p, blend.data(), Pz, cudaMemcpyHostToDevice, s));
         PF_TRY(cudaMemcpyAsync(r->occludes.p, occl.data(), Pz, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->gradient.p, gradv.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->overlay.p, overlayv.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
     }
-    if (!grads.empty()) {
-        PF_TRY(cudaMemcpyAsync(r->grads.p, grads.data(), sizeof(GradDev) * grads.size(), cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->ramps.p, ramps.data(), sizeof(uint32_t) * ramps.size(), cudaMemcpyHostToDevice, s));
+    if (!overlays.empty()) {
+        PF_TRY(cudaMemcpyAsync(r->overlays.p, overlays.data(), sizeof(OverlayDev) * overlays.size(),
+                               cudaMemcpyHostToDevice, s));
+        PF_TRY(cudaMemcpyAsync(r->texels.p, texels.data(), sizeof(uint32_t) * texels.size(), cudaMemcpyHostToDevice, s));
     }
     // Segment packing on the GPU (SegmentsD3D11::add_path): count, scan, emit.
     PF_TRY(cudaMemsetAsync(r->counters.p, 0, sizeof(Counters), s));

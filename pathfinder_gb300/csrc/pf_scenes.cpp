@@ -68,7 +68,7 @@ PFCUDAPath make_path(uint32_t first_contour, uint32_t count, PFColorU paint, int
     p.clip_path = clip;
     p.fill_rule = rule;
     p.blend_mode = PF_BLEND_MODE_SRC_OVER;
-    p.gradient = 0;
+    p.overlay = 0;
     return p;
 }
 
@@ -356,6 +356,10 @@ int32_t PFCUDASceneGetDesc(PFCUDASceneBuffersRef s, PFCUDASceneDesc* d, int32_t*
     d->draw_path_count = (uint32_t)s->b.draw_paths.size();
     d->view_box = s->view_box;
     d->memory = PF_MEMORY_HOST;
+    d->gradients = nullptr;  // generated scenes have solid paint
+    d->gradient_count = 0;
+    d->patterns = nullptr;
+    d->pattern_count = 0;
     if (w) *w = s->width;
     if (h) *h = s->height;
     return PF_CUDA_OK;

@@ -1,10 +1,11 @@
-"""Paint effects of a draw path: blend modes and gradients.
+"""Paint effects of a draw path: blend modes, gradients and image patterns.
 
 Mirrors the reference's BlendMode (content/src/effects.rs:99-160), Gradient
-and ColorStop (content/src/gradient.rs:27-72, 121-260).  A draw path's paint
-is its solid colour, or that colour as the base colour of a gradient overlay
-(Paint, renderer/src/paint.rs:52-150: the gradient's texel colour with its
-alpha times the base colour's alpha).
+and ColorStop (content/src/gradient.rs:27-72, 121-260), Pattern with an image
+source and its filters (content/src/pattern.rs, effects.rs:64-95).  A draw
+path's paint is its solid colour, or that colour as the base colour of a
+gradient or pattern overlay (Paint, renderer/src/paint.rs:52-150: the
+overlay's texel colour with its alpha times the base colour's alpha).
 """
 from __future__ import annotations
 
@@ -159,3 +160,68 @@ class Gradient:
         g.stops = C.addressof(stops) if self.stops else None
         g.stop_count = len(self.stops)
         return g, stops
+
+
+class PatternFilterKind(IntEnum):
+    """PatternFilter (content/src/effects.rs:64-95) without the text filter."""
+    NONE = _abi.PF_PATTERN_FILTER_NONE
+    BLUR_X = _abi.PF_PATTERN_FILTER_BLUR_X
+    BLUR_Y = _abi.PF_PATTERN_FILTER_BLUR_Y
+    COLOR_MATRIX = _abi.PF_PATTERN_FILTER_COLOR_MATRIX
+
+
+@dataclass(eq=False)
+class Pattern:
+    """An image pattern (content/src/pattern.rs:21-200, PatternSource::Image).
+
+    ``pixels``: (height, width, 4) uint8 straight-alpha RGBA; ``transform``:
+    pattern space -> scene, (m00, m01, m10, m11, tx, ty)."""
+    pixels: np.ndarray
+    transform: tuple = (1.0, 0.0, 0.0, 1.0, 0.0, 0.0)
+    repeat_x: bool = False
+    repeat_y: bool = False
+    smoothing: bool = True
+    filter: PatternFilterKind = PatternFilterKind.NONE
+    blur_sigma: float = 0.0
+    color_matrix: tuple = tuple([1.0, 0, 0, 0, 0, 1.0, 0, 0, 0, 0, 1.0, 0, 0, 0, 0, 1.0, 0, 0, 0, 0])
+
+    @classmethod
+    def from_image(cls, pixels) -> "Pattern":
+        """Pattern::from_image (content/src/pattern.rs:97-99): identity transform, no filter."""
+        return cls(np.ascontiguousarray(pixels, np.uint8))
+
+    def apply_transform(self, transform) -> None:
+        """Pattern::apply_transform (content/src/pattern.rs:119-122): after the existing one."""
+        self.transform = tuple(float(v) for v in _transform_mul(_as_tuple(transform), self.transform))
+
+    def set_blur(self, sigma: float, direction: str = "x") -> None:
+        self.filter = PatternFilterKind.BLUR_X if direction == "x" else PatternFilterKind.BLUR_Y
+        self.blur_sigma = float(sigma)
+
+    def set_color_matrix(self, columns) -> None:
+        """Five RGBA columns (the feColorMatrix layout: out = M * colour + column 4)."""
+        m = np.asarray(columns, np.float32).reshape(20)
+        self.filter = PatternFilterKind.COLOR_MATRIX
+        self.color_matrix = tuple(float(v) for v in m)
+
+    def is_opaque(self) -> bool:
+        """Image::is_opaque (content/src/pattern.rs:208-212)."""
+        return bool((np.asarray(self.pixels)[..., 3] == 255).all())
+
+    def to_c(self):
+        """(PFCUDAPattern, the pixel array it points at: keep both alive)."""
+        px = np.ascontiguousarray(self.pixels, np.uint8)
+        if px.ndim != 3 or px.shape[2] != 4:
+            raise ValueError("pattern pixels must be (height, width, 4) uint8")
+        p = _abi.PFCUDAPattern()
+        p.pixels = px.ctypes.data
+        p.height, p.width = px.shape[0], px.shape[1]
+        t = self.transform
+        p.transform = _abi.PFTransform2F(t[0], t[1], t[2], t[3], _abi.PFVector2F(t[4], t[5]))
+        p.flags = ((_abi.PF_PATTERN_REPEAT_X if self.repeat_x else 0) | (_abi.PF_PATTERN_REPEAT_Y if self.repeat_y else 0)
+                   | (0 if self.smoothing else _abi.PF_PATTERN_NO_SMOOTHING))
+        p.filter = int(self.filter)
+        p.blur_sigma = self.blur_sigma
+        for k in range(20):
+            p.color_matrix[k] = self.color_matrix[k]
+        return p, px

@@ -98,6 +98,7 @@ class DrawPath:
     clip_path: int | None = None
     blend_mode: int = 0
     gradient: object = None  # paint.Gradient
+    pattern: object = None   # paint.Pattern (a path takes a gradient or a pattern)
 
 
 @dataclass
@@ -133,7 +134,8 @@ class Scene:
         self.width = 0
         self.height = 0
         self.cells = None  # glyph atlas cells, when generated
-        self.gradients: list = []  # paint.Gradient, indexed by draw path records' gradient - 1
+        self.gradients: list = []  # paint.Gradient: overlays 1..len(gradients)
+        self.patterns: list = []   # paint.Pattern: the overlays after the gradients
         self._pending: list = []
         self._keep: list = []
 
@@ -177,8 +179,12 @@ class Scene:
         rec["clip_path"] = -1 if path.clip_path is None else path.clip_path
         rec["fill_rule"] = int(path.fill_rule)
         rec["blend_mode"] = int(path.blend_mode)
+        if path.gradient is not None and path.pattern is not None:
+            raise ValueError("a draw path takes a gradient or a pattern, not both")
         if path.gradient is not None:
-            rec["gradient"] = self.push_gradient(path.gradient) + 1
+            rec["overlay"] = self.push_gradient(path.gradient) + 1
+        elif path.pattern is not None:
+            rec["overlay"] = self.PATTERN_OVERLAY_BASE + self.push_pattern(path.pattern)
         self.draw_paths = np.concatenate([self.draw_paths, rec])
         self.epoch += 1
         return len(self.draw_paths) - 1
@@ -194,6 +200,20 @@ class Scene:
         self.gradients.append(gradient)
         self.epoch += 1
         return len(self.gradients) - 1
+
+    # Pattern overlays are recorded as BASE + index and numbered after the
+    # gradients when the descriptor is made (the gradient count may still grow).
+    PATTERN_OVERLAY_BASE = 0x8000
+
+    def push_pattern(self, pattern) -> int:
+        for i, p in enumerate(self.patterns):
+            if p is pattern:
+                return i
+        if len(self.patterns) >= 0x7ffe:
+            raise ValueError("too many patterns in one scene")
+        self.patterns.append(pattern)
+        self.epoch += 1
+        return len(self.patterns) - 1
 
     # --- C ABI view -----------------------------------------------------------
     def desc(self) -> _abi.PFCUDASceneDesc:
@@ -215,15 +235,31 @@ class Scene:
         vb = self.view_box
         d.view_box = _abi.PFRectF(_abi.PFVector2F(vb.x0, vb.y0), _abi.PFVector2F(vb.x1, vb.y1))
         d.memory = _abi.PF_MEMORY_HOST
+        keep = []
         if self.gradients:
             arr = (_abi.PFCUDAGradient * len(self.gradients))()
-            keep = [arr]
+            keep.append(arr)
             for i, g in enumerate(self.gradients):
                 arr[i], stops = g.to_c()
                 keep.append(stops)
-            self._keep = keep  # the descriptor points into these
             d.gradients = C.addressof(arr)
             d.gradient_count = len(self.gradients)
+        if self.patterns:
+            parr = (_abi.PFCUDAPattern * len(self.patterns))()
+            keep.append(parr)
+            for i, p in enumerate(self.patterns):
+                parr[i], px = p.to_c()
+                keep.append(px)
+            d.patterns = C.addressof(parr)
+            d.pattern_count = len(self.patterns)
+        ov = self.draw_paths["overlay"] if len(self.draw_paths) else np.zeros((0,), np.uint16)
+        pat = ov >= self.PATTERN_OVERLAY_BASE
+        if pat.any():  # the descriptor numbers the patterns after the gradients
+            dp = self.draw_paths.copy()
+            dp["overlay"][pat] = ov[pat] - self.PATTERN_OVERLAY_BASE + len(self.gradients) + 1
+            keep.append(dp)
+            d.draw_paths = dp.ctypes.data
+        self._keep = keep  # the descriptor points into these
         return d
 
     @property

@@ -105,3 +105,49 @@ def gradient_scene(seed=0, W=160, H=128, clip=True):
     s.push_draw_path(pf.DrawPath(rect(0.55 * W, 0.05 * H, 0.98 * W, 0.6 * H), pf.ColorU(255, 255, 255, 255),
                                  gradient=grads[5]))
     return s
+
+
+def image(rng, w, h, opaque=False):
+    """A seeded straight-alpha RGBA8 image: smooth colour ramps with noise."""
+    y, x = np.mgrid[0:h, 0:w]
+    img = np.zeros((h, w, 4), np.float64)
+    img[..., 0] = 255 * x / max(1, w - 1)
+    img[..., 1] = 255 * y / max(1, h - 1)
+    img[..., 2] = 128 + 127 * np.sin(x * 0.7 + y * 0.3)
+    img[..., 3] = 255 if opaque else 60 + 195 * ((x + y) % 7) / 6
+    img[..., :3] += rng.normal(0, 20, (h, w, 3))
+    return np.clip(np.rint(img), 0, 255).astype(np.uint8)
+
+
+def pattern_scene(seed=0, W=160, H=128, filters=True):
+    """Image patterns with every repeat/smoothing combination, rotated and
+    scaled, with blur and colour-matrix filters, over a backdrop."""
+    rng = np.random.default_rng(seed)
+    s = pf.Scene()
+    s.set_view_box(pf.RectF(0, 0, W, H))
+    backdrop(s, rng, W, H, n=2)
+    k = 0
+    for rx in (False, True):
+        for ry in (False, True):
+            for smooth in (True, False):
+                p = pf.Pattern.from_image(image(rng, int(rng.integers(5, 24)), int(rng.integers(5, 24)), opaque=k % 3 == 0))
+                p.repeat_x, p.repeat_y, p.smoothing = rx, ry, smooth
+                a, sc = rng.uniform(0, 2 * np.pi), rng.uniform(0.6, 3.0)
+                p.apply_transform((sc * np.cos(a), -sc * np.sin(a), sc * np.sin(a), sc * np.cos(a),
+                                   rng.uniform(0, W), rng.uniform(0, H)))
+                if filters and k % 4 == 1:
+                    p.set_blur(float(rng.uniform(0.5, 3.0)), "x" if k % 8 == 1 else "y")
+                elif filters and k % 4 == 3:
+                    cols = np.zeros((5, 4), np.float32)
+                    cols[0] = (0.3, 0.3, 0.3, 0)   # r -> greyish
+                    cols[1] = (0.59, 0.59, 0.2, 0)
+                    cols[2] = (0.11, 0.11, 0.8, 0)
+                    cols[3] = (0, 0, 0, 1)
+                    cols[4] = (0.05, -0.05, 0.1, 0)
+                    p.set_color_matrix(cols)
+                base = pf.ColorU(255, 255, 255, 255 if k % 2 == 0 else 190)
+                s.push_draw_path(pf.DrawPath(blob(rng, rng.uniform(0.2 * W, 0.8 * W), rng.uniform(0.2 * H, 0.8 * H),
+                                                  rng.uniform(0.2, 0.4) * min(W, H), 11, rng), base, pattern=p,
+                                             blend_mode=int(pf.BlendMode.MULTIPLY) if k == 6 else 0))
+                k += 1
+    return s

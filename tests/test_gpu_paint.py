@@ -1,4 +1,5 @@
 """Paint effects on the GPU: every blend mode, every gradient kind and wrap,
+image patterns with their filters,
 gradients under a build transform, in batches and in the alpha-only format.
 Records bit-exact with the oracle (destructive modes tile the view box,
 occlusion follows the paint's opacity and blend mode), images within 2/255
@@ -33,6 +34,19 @@ def test_blend_mode_parity(renderer, mode):
 @pytest.mark.parametrize("seed", [0, 1, 2])
 def test_gradient_parity(renderer, seed):
     _check(renderer, ps.gradient_scene(seed))
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_pattern_parity(renderer, seed):
+    """Image patterns: every repeat/smoothing combination, rotated and
+    scaled, blur and colour-matrix filters."""
+    _check(renderer, ps.pattern_scene(seed))
+
+
+def test_pattern_under_transform(renderer):
+    s = ps.pattern_scene(5, W=256, H=192)
+    t = pf.Transform2F(0.9, 0.35, -0.3, 1.1, 12.5, -7.0)
+    _check(renderer, s, pf.BuildOptions(t))
 
 
 def test_gradient_under_transform(renderer):
@@ -112,7 +126,7 @@ def test_invalid_paint_rejected(renderer):
     with pytest.raises(PFCUDAError):
         renderer.render(s)
     s = ps.gradient_scene(0)
-    s.draw_paths["gradient"][-1] = 99
+    s.draw_paths["overlay"][-1] = 99
     s.epoch += 1
     with pytest.raises(PFCUDAError):
         renderer.render(s)

@@ -210,7 +210,7 @@ def test_scene_records_paint_fields(built):
     rng = np.random.default_rng(1)
     s = ps.gradient_scene(1)
     assert len(s.gradients) == 7
-    g = s.draw_paths["gradient"]
+    g = s.draw_paths["overlay"]
     assert g.max() == 7 and (g[-1] == g[-3])  # the rectangle reuses gradient 6
     s2 = ps.blend_scene(pf.BlendMode.XOR)
     assert (s2.draw_paths["blend_mode"] == int(pf.BlendMode.XOR)).sum() == 2
@@ -227,7 +227,80 @@ def test_invalid_paint_rejected(built):
     with pytest.raises(ValueError):
         oracle.OracleFrame(s)
     s = ps.blend_scene(pf.BlendMode.SRC_OVER)
-    s.draw_paths["gradient"][0] = 5  # the scene has no gradients
+    s.draw_paths["overlay"][0] = 5  # the scene has no gradients
     s.epoch += 1
     with pytest.raises(ValueError):
         oracle.OracleFrame(s)
+
+
+# --- image patterns ------------------------------------------------------------
+def _pattern_render(pattern, W=48, H=32):
+    # view box sides are multiples of the tile size: the CPU tiler clips
+    # edges to the view box, so a partial last tile column would stay empty
+    s = pf.Scene()
+    s.set_view_box(pf.RectF(0, 0, W, H))
+    s.push_draw_path(pf.DrawPath(ps.rect(-4, -4, W + 4, H + 4), pf.ColorU(255, 255, 255, 255), pattern=pattern))
+    return _render(s)[1]
+
+
+def test_pattern_placement_nearest(built):
+    """Nearest sampling with the identity transform: a non-repeating axis
+    has the page's transparent border at pattern coordinate 0 (the image
+    starts one texel in, renderer/src/paint.rs:498-530, 617-623); a
+    repeating axis tiles the image from 0."""
+    rng = np.random.default_rng(1)
+    img = ps.image(rng, 7, 5, opaque=True)
+    for rx, ry in ((False, False), (True, True), (True, False)):
+        p = pf.Pattern.from_image(img)
+        p.repeat_x, p.repeat_y, p.smoothing = rx, ry, False
+        out = _pattern_render(p)
+        for y in range(32):
+            for x in range(48):
+                ix = x % 7 if rx else x - 1
+                iy = y % 5 if ry else y - 1
+                want = img[iy, ix] / 255.0 if (0 <= ix < 7 and 0 <= iy < 5) else np.zeros(4)
+                want = np.concatenate([want[:3] * want[3], want[3:]])
+                assert np.abs(out[y, x] - want).max() < 1e-9, (rx, ry, x, y)
+
+
+def test_pattern_filters(built):
+    """A colour matrix swapping red and blue; a blur of a constant image."""
+    rng = np.random.default_rng(2)
+    img = ps.image(rng, 6, 6, opaque=True)
+    p = pf.Pattern.from_image(img)
+    p.repeat_x = p.repeat_y = True
+    p.smoothing = False
+    cols = np.zeros((5, 4), np.float32)
+    cols[0] = (0, 0, 1, 0)
+    cols[1] = (0, 1, 0, 0)
+    cols[2] = (1, 0, 0, 0)
+    cols[3] = (0, 0, 0, 1)
+    plain = _pattern_render(p)
+    p.set_color_matrix(cols)
+    swapped = _pattern_render(p)
+    assert np.abs(swapped[..., [2, 1, 0, 3]] - plain).max() < 1e-9
+    flat = np.zeros((8, 8, 4), np.uint8)
+    flat[...] = (40, 120, 200, 255)
+    q = pf.Pattern.from_image(flat)
+    q.repeat_x = q.repeat_y = True
+    for sigma, d in ((0.7, "x"), (2.5, "y"), (9.0, "x")):
+        q.set_blur(sigma, d)
+        out = _pattern_render(q)
+        assert np.abs(out - np.array([40, 120, 200, 255]) / 255.0).max() < 1e-6, sigma
+
+
+def test_pattern_occlusion_follows_image_opacity(built):
+    """Image::is_opaque decides occlusion (content/src/pattern.rs:193-195,
+    208-212), also for a non-repeating pattern whose page border is
+    transparent: the tiles it covers hide what lies below."""
+    import oracle
+    rng = np.random.default_rng(3)
+    s = pf.Scene()
+    s.set_view_box(pf.RectF(0, 0, 64, 64))
+    s.push_draw_path(pf.DrawPath(ps.rect(0, 0, 64, 64), pf.ColorU(10, 200, 30, 255)))
+    p = pf.Pattern.from_image(ps.image(rng, 4, 4, opaque=True))
+    s.push_draw_path(pf.DrawPath(ps.rect(-8, -8, 72, 72), pf.ColorU(255, 255, 255, 255), pattern=p))
+    z = oracle.OracleFrame(s).zbuffer()
+    assert (z == 1).all()
+    img = _render(s)[1]
+    assert np.abs(img[40:, 40:]).max() == 0  # transparent: the green below is culled
