@@ -173,8 +173,9 @@ def run_reference(args) -> None:
 def add_paints(scene, seed: int) -> str:
     """Seeded paint effects over the generated scene: a quarter of the draw
     paths take one of 64 gradients (linear and radial, clamp and repeat, four
-    random stops), a tenth take a blend mode other than SrcOver (uniform over
-    the other 26).  Returns the description for the JSON line."""
+    random stops), a twentieth of the rest one of 8 image patterns, a tenth
+    take a blend mode other than SrcOver (uniform over the other 26).
+    Returns the description for the JSON line."""
     import numpy as np
     import pathfinder_gb300 as pf
     rng = np.random.default_rng(seed + 7)
@@ -189,14 +190,32 @@ def add_paints(scene, seed: int) -> str:
             g.add_color_stop(pf.ColorU(*[int(v) for v in rng.integers(0, 256, 3)], int(rng.integers(96, 256))),
                              float(rng.uniform(0, 1)))
         scene.push_gradient(g)
+    patterns = []
+    for k in range(8):  # 64x64 images: repeat/clamp, linear/nearest, a blur, a colour matrix
+        px = rng.integers(0, 256, (64, 64, 4)).astype(np.uint8)
+        px[..., 3] = np.maximum(px[..., 3], 96)
+        p = pf.Pattern.from_image(px)
+        p.repeat_x, p.repeat_y, p.smoothing = k % 2 == 0, k % 4 < 2, k != 3
+        s = float(rng.uniform(0.5, 4.0))
+        p.apply_transform((s, 0.0, 0.0, s, rng.uniform(0, w), rng.uniform(0, h)))
+        if k == 5:
+            p.set_blur(2.0, "x")
+        elif k == 6:
+            p.set_color_matrix(np.array([[0.3, 0.3, 0.3, 0], [0.59, 0.59, 0.59, 0], [0.11, 0.11, 0.11, 0],
+                                         [0, 0, 0, 1], [0, 0, 0, 0]], np.float32))
+        patterns.append(p)
     n = len(scene.draw_paths)
     pick = rng.random(n) < 0.25
     scene.draw_paths["overlay"][pick] = rng.integers(1, 65, int(pick.sum()))
+    patt = (~pick) & (rng.random(n) < 0.05)
+    scene.draw_paths["overlay"][patt] = [scene.PATTERN_OVERLAY_BASE + scene.push_pattern(patterns[int(i)])
+                                         for i in rng.integers(0, 8, int(patt.sum()))]
     bm = rng.random(n) < 0.10
     scene.draw_paths["blend_mode"][bm] = rng.integers(1, 27, int(bm.sum()))
     scene.epoch += 1
     return (f"{int(pick.sum())} paths with one of 64 gradients (linear/radial, clamp/repeat), "
-            f"{int(bm.sum())} with a blend mode other than SrcOver")
+            f"{int(patt.sum())} with one of 8 64x64 image patterns (repeat/clamp, linear/nearest, a blur, "
+            f"a colour matrix), {int(bm.sum())} with a blend mode other than SrcOver")
 
 
 def cpu_baseline(scene, nseg: int, budget_s: float = 12.0) -> dict:

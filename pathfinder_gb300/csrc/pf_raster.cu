@@ -587,8 +587,9 @@ __device__ __forceinline__ float4 page_sample(const uint32_t* tex, int W, int H,
     if (!(u == u) || !(v == v)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     u = fminf(fmaxf(u, -1.0f), 2.0f);
     v = fminf(fmaxf(v, -1.0f), 2.0f);
-    auto wrap_x = [&](int i) { return rx ? ((i % W) + W) % W : min(max(i, 0), W - 1); };
-    auto wrap_y = [&](int i) { return ry ? ((i % H) + H) % H : min(max(i, 0), H - 1); };
+    // after the wrap above, repeated indices lie in [-1, size]: one correction suffices
+    auto wrap_x = [&](int i) { return rx ? (i < 0 ? i + W : (i >= W ? i - W : i)) : min(max(i, 0), W - 1); };
+    auto wrap_y = [&](int i) { return ry ? (i < 0 ? i + H : (i >= H ? i - H : i)) : min(max(i, 0), H - 1); };
     if (flags & PF_PATTERN_NO_SMOOTHING)
         return unpack_unorm8(__ldg(tex + wrap_y((int)floorf(v * (float)H)) * W + wrap_x((int)floorf(u * (float)W))));
     const float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
