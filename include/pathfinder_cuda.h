@@ -484,6 +484,64 @@ int32_t PFCUDARenderDiffAsync(PFCUDARendererRef renderer, const PFCUDABuildOptio
 int32_t PFCUDABackward(PFCUDARendererRef renderer, const float* d_image, PFVector2F* d_points,
                        float* d_alpha);
 
+/* ---- stroke to fill ----------------------------------------------------------
+ * OutlineStrokeToFill (content/src/stroke.rs:24-190): each contour of an
+ * outline is offset by half the line width on both sides, segment by segment,
+ * with the stroke's joins between pieces and its caps at the ends of open
+ * contours; a closed contour gives two closed contours, an open one gives one.
+ * The result is an outline to fill with the nonzero rule, as the reference's
+ * front-ends use it.  Runs on the GPU, with the reference's single-precision
+ * op order: the same input gives the same output points. */
+#define PF_LINE_CAP_BUTT    0
+#define PF_LINE_CAP_SQUARE  1
+#define PF_LINE_CAP_ROUND   2
+#define PF_LINE_JOIN_MITER  0
+#define PF_LINE_JOIN_BEVEL  1
+#define PF_LINE_JOIN_ROUND  2
+
+/* StrokeStyle (content/src/stroke.rs:45-56); miter_limit for PF_LINE_JOIN_MITER
+ * (LineJoin::Miter(f32); the default style is width 1, butt, miter 10). */
+typedef struct PFCUDAStrokeStyle {
+    float   line_width;
+    int32_t line_cap;      /* PF_LINE_CAP_*  */
+    int32_t line_join;     /* PF_LINE_JOIN_* */
+    float   miter_limit;
+} PFCUDAStrokeStyle;
+
+/* Outlines to stroke.  Contour c owns points [contour_starts[c],
+ * contour_starts[c+1]) and is closed when contour_closed[c] != 0; outline o owns
+ * contours [outline_starts[o], outline_starts[o+1]) and is stroked with
+ * styles[o].  All arrays in `memory`. */
+typedef struct PFCUDAStrokeInput {
+    const PFVector2F* points;
+    const uint8_t*    point_flags;      /* PF_POINT_FLAG_* bits */
+    const uint32_t*   contour_starts;   /* contour_count + 1 */
+    const uint8_t*    contour_closed;   /* contour_count */
+    const uint32_t*   outline_starts;   /* outline_count + 1 */
+    const PFCUDAStrokeStyle* styles;    /* outline_count */
+    uint32_t point_count, contour_count, outline_count;
+    int32_t  memory;                    /* PF_MEMORY_* */
+} PFCUDAStrokeInput;
+
+/* The stroked outlines: closed contours as flat buffers (in `memory`).  Input
+ * contour c gives output contours in order (two for a closed contour, forward
+ * then backward; one for an open one); outline_starts (outline_count + 1)
+ * gives each outline's output contours.  point_count / contour_count are
+ * written; with too little capacity the call returns PF_CUDA_ERR_CAPACITY,
+ * writes the sizes needed and nothing else. */
+typedef struct PFCUDAStrokeOutput {
+    PFVector2F* points;
+    uint8_t*    point_flags;
+    uint32_t*   contour_starts;         /* contour_capacity + 1 */
+    uint32_t*   outline_starts;         /* outline_count + 1 */
+    uint64_t    point_capacity, contour_capacity;
+    uint64_t    point_count, contour_count;
+    int32_t     memory;
+} PFCUDAStrokeOutput;
+
+/* Synchronous on the renderer's stream. */
+int32_t PFCUDAStrokeToFill(PFCUDARendererRef renderer, const PFCUDAStrokeInput* input, PFCUDAStrokeOutput* output);
+
 /* Human-readable text for a status code (static storage). */
 const char* PFCUDAStatusString(int32_t status);
 

@@ -21,6 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "pf_oracle.cpp")
+SRCS = [SRC, os.path.join(HERE, "pf_oracle_stroke.cpp")]
 LIB_PATH = os.path.join(HERE, "libpforacle.so")
 
 CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-Wall"]
@@ -28,9 +29,10 @@ CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
 
 def build(force: bool = False) -> str:
     """Compile the oracle with g++ (no FMA contraction: SSE op order)."""
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC):
+    if not force and os.path.exists(LIB_PATH) and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(s)
+                                                       for s in SRCS):
         return LIB_PATH
-    cmd = ["g++"] + CXXFLAGS + ["-o", LIB_PATH, SRC, "-lpthread"]
+    cmd = ["g++"] + CXXFLAGS + ["-I", os.path.join(ROOT, "include"), "-o", LIB_PATH] + SRCS + ["-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")
@@ -244,3 +246,30 @@ def area_lut_value(u: int, v: int, k: int) -> int:
 
 def sse_cvt(x: float) -> int:
     return int(lib().pfo_sse_cvt(x))
+
+
+def stroke(stroke_input):
+    """The oracle's stroke-to-fill of a host-memory PFCUDAStrokeInput:
+    (points (N, 2) float32, flags (N,) uint8, contour_starts, outline_starts,
+    depth_limit_hit)."""
+    L = lib()
+    L.pfo_stroke.restype = C.c_void_p
+    L.pfo_stroke.argtypes = [C.c_void_p]
+    L.pfo_stroke_counts.argtypes = [C.c_void_p, C.c_void_p]
+    L.pfo_stroke_read.argtypes = [C.c_void_p] * 5
+    L.pfo_stroke_free.argtypes = [C.c_void_p]
+    h = L.pfo_stroke(C.byref(stroke_input))
+    if not h:
+        raise ValueError("oracle rejected the stroke input")
+    try:
+        n = np.zeros((3,), np.uint64)
+        L.pfo_stroke_counts(h, n.ctypes.data)
+        npts, nc = int(n[0]), int(n[1])
+        pts = np.zeros((npts, 2), np.float32)
+        flags = np.zeros((npts,), np.uint8)
+        cs = np.zeros((nc + 1,), np.uint32)
+        os_ = np.zeros((stroke_input.outline_count + 1,), np.uint32)
+        L.pfo_stroke_read(h, pts.ctypes.data, flags.ctypes.data, cs.ctypes.data, os_.ctypes.data)
+        return pts, flags, cs, os_, bool(n[2])
+    finally:
+        L.pfo_stroke_free(h)

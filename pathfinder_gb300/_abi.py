@@ -46,6 +46,13 @@ PF_PATTERN_FILTER_BLUR_X = 1
 PF_PATTERN_FILTER_BLUR_Y = 2
 PF_PATTERN_FILTER_COLOR_MATRIX = 3
 
+PF_LINE_CAP_BUTT = 0
+PF_LINE_CAP_SQUARE = 1
+PF_LINE_CAP_ROUND = 2
+PF_LINE_JOIN_MITER = 0
+PF_LINE_JOIN_BEVEL = 1
+PF_LINE_JOIN_ROUND = 2
+
 PF_SCENE_STARS_512 = 1
 PF_SCENE_SVG_4K = 2
 PF_SCENE_GLYPH_ATLAS = 3
@@ -117,6 +124,25 @@ class PFCUDASceneDesc(C.Structure):
                 ("patterns", C.c_void_p), ("pattern_count", C.c_uint32)]
 
 
+class PFCUDAStrokeStyle(C.Structure):
+    _fields_ = [("line_width", C.c_float), ("line_cap", C.c_int32), ("line_join", C.c_int32),
+                ("miter_limit", C.c_float)]
+
+
+class PFCUDAStrokeInput(C.Structure):
+    _fields_ = [("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_starts", C.c_void_p),
+                ("contour_closed", C.c_void_p), ("outline_starts", C.c_void_p), ("styles", C.c_void_p),
+                ("point_count", C.c_uint32), ("contour_count", C.c_uint32), ("outline_count", C.c_uint32),
+                ("memory", C.c_int32)]
+
+
+class PFCUDAStrokeOutput(C.Structure):
+    _fields_ = [("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_starts", C.c_void_p),
+                ("outline_starts", C.c_void_p), ("point_capacity", C.c_uint64),
+                ("contour_capacity", C.c_uint64), ("point_count", C.c_uint64), ("contour_count", C.c_uint64),
+                ("memory", C.c_int32)]
+
+
 class PFCUDABuildOptions(C.Structure):
     _fields_ = [("transform", PFTransform2F), ("has_transform", C.c_int32)]
 
@@ -184,6 +210,7 @@ def record_dtypes():
 
 
 _SIGS = {
+    "PFCUDAStrokeToFill": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDAStrokeInput), C.POINTER(PFCUDAStrokeOutput)]),
     "PFCUDAGradientSample": (C.c_int32, [C.POINTER(PFCUDAGradient), C.c_float, C.POINTER(PFColorU)]),
     "PFCUDAGradientRamp": (C.c_int32, [C.POINTER(PFCUDAGradient), C.c_void_p]),
     "PFCUDARendererCreate": (C.c_int32, [C.c_int32, C.POINTER(PFCUDARendererOptions), C.POINTER(C.c_void_p)]),

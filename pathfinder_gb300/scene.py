@@ -59,6 +59,7 @@ class Contour:
     def __init__(self):
         self.points: list[tuple[float, float]] = []
         self.flags: list[int] = []
+        self.closed = False  # Contour::closed: whether a stroke joins the ends
 
     def push_endpoint(self, x: float, y: float) -> "Contour":
         self.points.append((x, y)); self.flags.append(0)
@@ -74,7 +75,10 @@ class Contour:
         return self
 
     def close(self) -> "Contour":
-        """Contours are always closed on this path (Outline::close_all_contours)."""
+        """Contour::close.  Fills treat every contour as closed
+        (Outline::close_all_contours); strokes join a closed contour's ends
+        instead of capping them."""
+        self.closed = True
         return self
 
 
