@@ -506,18 +506,31 @@ void split_half(const Segment& s, Segment* a, Segment* b) {
     b->base = Line{p0123x, p0123y, p3x, p3y}; b->ctrl = Line{p123x, p123y, p23x, p23y}; b->kind = kCubic;
 }
 
-// process_segment (renderer/src/tiler.rs:166-184), recursive as in the reference.
-void process_segment(Ctx& ctx, const Segment& s, int depth) {
-    if (s.kind == kQuad) { process_segment(ctx, to_cubic(s), depth); return; }
+// process_segment (renderer/src/tiler.rs:166-184), recursive as in the reference,
+// with the CUDA tiler's bound of 2^20 lines per input segment (depth first; the
+// walk stops there and flags the limit).  Returns false once stopped.
+const uint32_t kMaxSegmentLines = 1u << 20;
+bool process_segment(Ctx& ctx, const Segment& s, int depth, uint32_t* emitted) {
+    if (s.kind == kQuad) return process_segment(ctx, to_cubic(s), depth, emitted);
     if (s.kind == kLine || is_flat(s) || depth >= 32) {
         if (depth >= 32 && s.kind == kCubic && !is_flat(s)) ctx.bp->limit_hit = true;
         process_line_segment(ctx, s.base);
-        return;
+        if (++*emitted >= kMaxSegmentLines) { ctx.bp->limit_hit = true; return false; }
+        return true;
     }
     Segment a, b;
     split_half(s, &a, &b);
-    process_segment(ctx, a, depth + 1);
-    process_segment(ctx, b, depth + 1);
+    if (!process_segment(ctx, a, depth + 1, emitted)) return false;
+    return process_segment(ctx, b, depth + 1, emitted);
+}
+
+// A segment with a non-finite coordinate gives no fills (as on the GPU).
+bool segment_finite(const Segment& s) {
+    auto f = [](float v) { return std::isfinite(v); };
+    if (!f(s.base.fx) || !f(s.base.fy) || !f(s.base.tx) || !f(s.base.ty)) return false;
+    if (s.kind == kQuad) return f(s.ctrl.fx) && f(s.ctrl.fy);
+    if (s.kind == kCubic) return f(s.ctrl.fx) && f(s.ctrl.fy) && f(s.ctrl.tx) && f(s.ctrl.ty);
+    return true;
 }
 
 // Uniform dicing of the D3D11 level (shaders/d3d11/dice.cs.glsl:133-217): a
@@ -669,8 +682,10 @@ void build_fills(Frame& fr, uint32_t p, uint64_t dda_limit) {
     Ctx ctx{fr.view_box, &bp, dda_limit, fr.d3d11};
     for (const Contour& c : in.contours)
         for_each_segment(c, [&](const Segment& s) {
+            if (!segment_finite(s)) { bp.limit_hit = true; return; }
+            uint32_t emitted = 0;
             if (fr.d3d11) dice_segment(ctx, s);
-            else process_segment(ctx, s, 0);
+            else process_segment(ctx, s, 0, &emitted);
         });
 }
 

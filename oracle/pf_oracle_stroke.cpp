@@ -240,11 +240,13 @@ void add_join(OutContour& c, float distance, int join, float miter_limit, V join
             c.push(miter_endpoint, 0);
         }
     } else if (join == PF_LINE_JOIN_ROUND) {
+        // a chord end at the join point has no direction: the reference would
+        // push NaN points (normalising a zero vector); no join is pushed here
+        const V cf = vsub(prev_tangent.t, join_point), ct = vsub(next_tangent.t, join_point);
+        if ((cf.x == 0.0f && cf.y == 0.0f) || (ct.x == 0.0f && ct.y == 0.0f)) return;
         const float scale = std::fabs(distance);
         const T2 transform = t2_translate(t2_scale(scale), join_point);
-        const V chord_from = vnormalize(vsub(prev_tangent.t, join_point));
-        const V chord_to = vnormalize(vsub(next_tangent.t, join_point));
-        c.push_arc_from_unit_chord(transform, L{chord_from, chord_to});
+        c.push_arc_from_unit_chord(transform, L{vnormalize(cf), vnormalize(ct)});
     }
 }
 
@@ -290,7 +292,8 @@ bool error_within_tolerance(const Seg& self, const Seg& other, float distance) {
     return true;
 }
 
-struct Stroker { Style st; OutContour out; bool depth_limit = false; };
+struct Stroker { Style st; OutContour out; bool depth_limit = false; uint32_t pieces = 0; };
+const uint32_t kMaxStrokePieces = 1u << 16;  // per segment, as the CUDA stroker bounds it
 
 // Offset::add_to_contour (:256-279)
 void add_to_contour(Stroker& k, const Seg& s, float distance, int join, V join_point) {
@@ -303,40 +306,44 @@ void add_to_contour(Stroker& k, const Seg& s, float distance, int join, V join_p
 
 // Offset::offset (:238-254), with the recursion bounded at depth 32 as the
 // CUDA stroker bounds it (the reference recurses without bound).
-void offset_segment(Stroker& k, const Seg& s, float distance, int join, int depth) {
+// Returns false once the segment's piece budget is spent (the walk stops).
+bool offset_segment(Stroker& k, const Seg& s, float distance, int join, int depth) {
     const V join_point = s.base.f;
     if (vsqlen(lvec(s.base)) < kTolerance * kTolerance) {
         add_to_contour(k, s, distance, join, join_point);
-        return;
+        if (++k.pieces >= kMaxStrokePieces) { k.depth_limit = true; return false; }
+        return true;
     }
     const Seg cand = offset_once(s, distance);
     if (error_within_tolerance(s, cand, distance) || depth >= 32) {
         if (depth >= 32 && !error_within_tolerance(s, cand, distance)) k.depth_limit = true;
         add_to_contour(k, cand, distance, join, join_point);
-        return;
+        if (++k.pieces >= kMaxStrokePieces) { k.depth_limit = true; return false; }
+        return true;
     }
     Seg a, b;
     seg_split(s, 0.5f, &a, &b);
-    offset_segment(k, a, distance, join, depth + 1);
-    offset_segment(k, b, distance, join, depth + 1);
+    if (!offset_segment(k, a, distance, join, depth + 1)) return false;
+    return offset_segment(k, b, distance, join, depth + 1);
 }
 
 // ContourIter (content/src/outline.rs:1020-1065) with ContourIterFlags::empty()
 std::vector<Seg> contour_segments(const PFVector2F* pts, const uint8_t* flags, uint32_t n, bool closed) {
     std::vector<Seg> out;
-    auto P = [&](uint32_t i) { return V{pts[i].x, pts[i].y}; };
+    // indices past the end (a contour ending on a control point; the reference
+    // would read out of bounds) clamp to the last point, as the CUDA stroker does
+    auto P = [&](uint32_t i) { const uint32_t j = i < n ? i : n - 1; return V{pts[j].x, pts[j].y}; };
     auto is_end = [&](uint32_t i) {
         return (flags[i] & (PF_POINT_FLAG_CONTROL_POINT_0 | PF_POINT_FLAG_CONTROL_POINT_1)) == 0;
     };
     uint32_t index = 1;
-    for (;;) {
-        if ((index == n && !closed) || index == n + 1 || n == 0) break;
+    while (n != 0 && index <= n && !(index == n && !closed)) {
         const V p0 = P(index - 1);
         if (index == n) { index++; out.push_back(seg_line(L{p0, P(0)})); continue; }
         const uint32_t i1 = index++;
         if (is_end(i1)) { out.push_back(seg_line(L{p0, P(i1)})); continue; }
         const uint32_t i2 = index++;
-        if (is_end(i2)) { out.push_back(seg_quad(L{p0, P(i2)}, P(i1))); continue; }
+        if (i2 >= n || is_end(i2)) { out.push_back(seg_quad(L{p0, P(i2)}, P(i1))); continue; }
         const uint32_t i3 = index++;
         out.push_back(seg_cubic(L{p0, P(i3)}, L{P(i1), P(i2)}));
     }
@@ -411,13 +418,17 @@ void stroke_contour(StrokeResult& r, const Style& st, const PFVector2F* pts, con
     Stroker k;
     k.st = st;
     // offset_forward (:208-215): the first segment joins with Bevel
-    for (size_t i = 0; i < segs.size(); i++)
+    for (size_t i = 0; i < segs.size(); i++) {
+        k.pieces = 0;
         offset_segment(k, segs[i], -radius, i == 0 ? PF_LINE_JOIN_BEVEL : st.join, 0);
+    }
     if (closed) push_stroked_contour(r, k, true, first);
     else add_cap(k);
     // offset_backward (:217-230): reversed segments in reverse order
-    for (size_t i = 0; i < segs.size(); i++)
+    for (size_t i = 0; i < segs.size(); i++) {
+        k.pieces = 0;
         offset_segment(k, seg_reversed(segs[segs.size() - 1 - i]), -radius, i == 0 ? PF_LINE_JOIN_BEVEL : st.join, 0);
+    }
     if (!closed) add_cap(k);
     push_stroked_contour(r, k, closed, first);
 }

@@ -8,6 +8,7 @@ hand-written kernels of ``libpathfinder_cuda.so``.  There is no CPU fallback.
 from .scene import (ClipPath, ColorF, ColorU, Contour, DrawPath, FillRule, Outline, RectF, Scene,
                     generate_scene)
 from .paint import BlendMode, ColorStop, Gradient, GradientKind, GradientWrap, Pattern, PatternFilterKind
+from .stroke import LineCap, LineJoin, StrokeStyle
 from .renderer import (BuildOptions, Renderer, RendererLevel, RendererOptions, RenderStats, Transform2F)
 from . import _abi
 from .batch import SceneBatch, target
@@ -26,5 +27,6 @@ __all__ = [
     "ClipPath", "ColorF", "ColorU", "Contour", "DrawPath", "FillRule", "Outline", "RectF", "Scene",
     "generate_scene", "BuildOptions", "Renderer", "RendererLevel", "RendererOptions", "RenderStats",
     "Transform2F", "PF_SCENE_STARS_512", "PF_SCENE_SVG_4K", "PF_SCENE_GLYPH_ATLAS", "PF_SCENE_CUBIC_1K",
-    "PF_SCENE_EDGE_CASES", "BlendMode", "ColorStop", "Gradient", "GradientKind", "GradientWrap", "Pattern", "PatternFilterKind",
+    "PF_SCENE_EDGE_CASES", "BlendMode", "ColorStop", "Gradient", "GradientKind", "GradientWrap", "Pattern", "PatternFilterKind", "LineCap",
+    "LineJoin", "StrokeStyle",
 ]

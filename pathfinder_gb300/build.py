@@ -34,6 +34,7 @@ UNITS = [
     ("pf_noalloc.cu", []),
     ("pf_scenes.cpp", []),
     ("pf_paint.cu", []),
+    ("pf_stroke.cu", ["-fmad=false"]),
 ]
 
 

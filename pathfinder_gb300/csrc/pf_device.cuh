@@ -360,10 +360,18 @@ __device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink
 // process_segment (renderer/src/tiler.rs:166-184) without recursion: calls
 // emit(Line, addr, depth) for every flattened line in the same depth-first
 // order as the reference's recursion.
+// A segment with a non-finite coordinate gives no lines and flags the frame
+// malformed (the reference's recursion would not end on it); a segment gives
+// at most kMaxSegmentLines lines (depth first), then flags the depth limit, so
+// huge coordinates cannot make the walk exponential.
+constexpr uint32_t kMaxSegmentLines = 1u << 20;
+__host__ __device__ __forceinline__ bool finite2(float2 p) { return isfinite(p.x) && isfinite(p.y); }
+
 template <class Emit>
 __device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Emit&& emit, uint32_t* status) {
     float2 p0 = pts[sr.x];
     float2 pe = pts[sr.y];
+    if (!finite2(p0) || !finite2(pe)) { atomicOr(status, kStatusMalformed); return; }
     if (sr.z == (int)kSegLine) {
         emit(Line{p0.x, p0.y, pe.x, pe.y}, 0u, 0);
         return;
@@ -371,12 +379,15 @@ __device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Em
     Cubic c;
     if (sr.z == (int)kSegQuad) {
         float2 q = pts[sr.x + 1];
+        if (!finite2(q)) { atomicOr(status, kStatusMalformed); return; }
         c = quad_to_cubic(p0.x, p0.y, q.x, q.y, pe.x, pe.y);
     } else {
         float2 c0 = pts[sr.x + 1], c1 = pts[sr.x + 2];
+        if (!finite2(c0) || !finite2(c1)) { atomicOr(status, kStatusMalformed); return; }
         c.base = Line{p0.x, p0.y, pe.x, pe.y};
         c.ctrl = Line{c0.x, c0.y, c1.x, c1.y};
     }
+    uint32_t emitted = 0;
     // Depth-first without a stack: the current node is named by its split
     // path `addr` (d bits, first split most significant; the leaf covers
     // [addr, addr + 1) / 2^d of the curve parameter).  Descending left splits
@@ -398,6 +409,7 @@ __device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Em
         }
         if (!flat) atomicOr(status, kStatusDepthLimit);
         emit(c.base, addr, d);
+        if (++emitted >= kMaxSegmentLines) { atomicOr(status, kStatusDepthLimit); break; }
         while (d > 0 && (addr & 1u)) { addr >>= 1; d--; }  // climb past right children
         if (d == 0) break;
         addr |= 1u;  // the right sibling
@@ -421,6 +433,9 @@ constexpr float kDiceTolerance = 0.25f, kMicrolineLength = 16.0f;
 constexpr uint32_t kMaxDicePieces = 1u << 16;
 
 struct DiceSeg { float2 p0, c0, c1, p3; bool curve; };
+__device__ __forceinline__ bool dice_finite(const DiceSeg& d) {
+    return finite2(d.p0) && finite2(d.c0) && finite2(d.c1) && finite2(d.p3);
+}
 
 __device__ __forceinline__ DiceSeg dice_seg(const float2* pts, SegRec sr) {
     DiceSeg d;

@@ -144,6 +144,8 @@ struct ScanTemp { uint32_t* partials; uint32_t cap; };
 }  // namespace pf
 struct PFCUDAGradient;
 struct PFCUDAPattern;
+struct PFCUDAStrokeInput;
+struct PFCUDAStrokeOutput;
 struct PFCUDAColorStop;
 namespace pf {
 // Paint overlays (host): the record of one gradient with its 256-texel ramp,
@@ -151,6 +153,13 @@ namespace pf {
 // returns a PF_CUDA_* status.
 int32_t build_gradient(const PFCUDAGradient& g, OverlayDev* out, std::vector<uint32_t>& texels, bool* opaque);
 int32_t build_pattern(const PFCUDAPattern& p, OverlayDev* out, std::vector<uint32_t>& texels, bool* opaque);
+
+// Stroke to fill (pf_stroke.cu): grow-only device work buffers and one
+// synchronous run on stream s; returns a PF_CUDA_* status.
+struct StrokeWork;
+StrokeWork* stroke_work_create();
+void stroke_work_destroy(StrokeWork* w);
+int32_t stroke_run(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, PFCUDAStrokeOutput* out);
 
 // Number of kernels this library has launched (host counter).
 uint64_t launch_counter();

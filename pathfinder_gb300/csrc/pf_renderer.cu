@@ -128,6 +128,7 @@ struct PFCUDARenderer {
     uint32_t clip_chain_max = 0;       // longest chain of clip paths behind a path
     bool nested_clips = false;         // some clip path is itself clipped
     bool paint_effects = false;        // some path has a gradient or a blend mode other than SrcOver
+    StrokeWork* stroke = nullptr;      // stroke-to-fill work buffers, made on first use
 
     // differentiable frames
     uint32_t ND = 0;                   // draw paths of the batch
@@ -538,6 +539,7 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     for (int i = 0; i <= PF_CUDA_STAGE_COUNT; i++)
         if (r->stage_ev[i]) cudaEventDestroy(r->stage_ev[i]);
     if (r->own_stream) cudaStreamDestroy(r->own_stream);
+    stroke_work_destroy(r->stroke);
     delete r;
     return PF_CUDA_OK;
 }
@@ -1083,6 +1085,13 @@ int32_t PFCUDAGetStageTimes(PFCUDARendererRef r, float* out_ms, int32_t capacity
         out_ms[i] = ms;
     }
     return PF_CUDA_OK;
+}
+
+int32_t PFCUDAStrokeToFill(PFCUDARendererRef r, const PFCUDAStrokeInput* input, PFCUDAStrokeOutput* output) {
+    if (!r || !input || !output) return PF_CUDA_ERR_INVALID;
+    PF_TRY(cudaSetDevice(r->device));
+    if (!r->stroke) r->stroke = stroke_work_create();
+    return stroke_run(r->stroke, r->stream, input, output);
 }
 
 int32_t PFCUDAExclusiveScan(PFCUDARendererRef r, const uint32_t* in, uint32_t* out, uint32_t n) {

@@ -411,7 +411,9 @@ __global__ void __launch_bounds__(256) k_flatten_count(FrameDev f) {
     uint32_t n = 0;
     if (f.d3d11) {
         bool limited = false;
-        n = dice_count(dice_seg(f.pts, f.segs[f.seg_begin + s]), &limited);
+        const DiceSeg dsg = dice_seg(f.pts, f.segs[f.seg_begin + s]);
+        if (dice_finite(dsg)) n = dice_count(dsg, &limited);
+        else atomicOr(&f.counters->status, kStatusMalformed);  // no pieces for non-finite input
         if (limited) atomicOr(&f.counters->status, kStatusDepthLimit);
     } else {
         flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&, uint32_t, int) { n++; },
@@ -440,7 +442,7 @@ __global__ void __launch_bounds__(256) k_flatten_emit(FrameDev f) {
     if (!DIFF && f.d3d11) {  // uniform pieces, ends rounded to 1/256 px
         const DiceSeg d = dice_seg(f.pts, sr);
         bool limited = false;
-        const uint32_t n = dice_count(d, &limited);
+        const uint32_t n = dice_finite(d) ? dice_count(d, &limited) : 0u;
         float2 a = make_float2(dice_q(d.p0.x), dice_q(d.p0.y));
         for (uint32_t k = 1; k <= n; k++, l++) {
             const float2 b = dice_point(d, k, n);

@@ -319,6 +319,39 @@ class Renderer:
         _abi.check(self._lib.PFCUDABackward(self._h, C.c_void_p(gi), C.c_void_p(gp), C.c_void_p(ga) if ga else None),
                    "PFCUDABackward")
 
+    def stroke_to_fill_buffers(self, items):
+        """PFCUDAStrokeToFill over [(Outline, StrokeStyle)]: the stroked outlines as
+        (points (N, 2) float32, flags (N,) uint8, contour_starts, outline_starts)."""
+        from .stroke import StrokeBatch
+        b = StrokeBatch(items)
+        d = b.desc()
+        cap_p = max(64, 8 * len(b.points) + 64 * b.contour_count)
+        cap_c = 2 * b.contour_count
+        for _ in range(2):
+            pts = np.zeros((cap_p, 2), np.float32)
+            flags = np.zeros((cap_p,), np.uint8)
+            cs = np.zeros((cap_c + 1,), np.uint32)
+            os_ = np.zeros((b.outline_count + 1,), np.uint32)
+            o = _abi.PFCUDAStrokeOutput()
+            o.points, o.point_flags = pts.ctypes.data, flags.ctypes.data
+            o.contour_starts, o.outline_starts = cs.ctypes.data, os_.ctypes.data
+            o.point_capacity, o.contour_capacity = cap_p, cap_c
+            o.memory = _abi.PF_MEMORY_HOST
+            rc = self._lib.PFCUDAStrokeToFill(self._h, C.byref(d), C.byref(o))
+            if rc == _abi.PF_CUDA_ERR_CAPACITY and (o.point_count > cap_p or o.contour_count > cap_c):
+                cap_p, cap_c = int(o.point_count), int(o.contour_count)
+                continue
+            _abi.check(rc, "PFCUDAStrokeToFill")
+            n, nc = int(o.point_count), int(o.contour_count)
+            return pts[:n], flags[:n], cs[:nc + 1], os_
+        raise RuntimeError("PFCUDAStrokeToFill: capacity did not converge")
+
+    def stroke_to_fill(self, items):
+        """OutlineStrokeToFill (content/src/stroke.rs:24-190) for many outlines at
+        once on the GPU: [(Outline, StrokeStyle)] -> [Outline] of closed contours."""
+        from .stroke import outlines_from_buffers
+        return outlines_from_buffers(*self.stroke_to_fill_buffers(items))
+
     def stats(self) -> RenderStats:
         s = _abi.PFCUDARenderStats()
         _abi.check(self._lib.PFCUDAGetStats(self._h, C.byref(s)), "PFCUDAGetStats")

@@ -145,3 +145,34 @@ def test_view_box_away_from_origin_keeps_other_pixels(renderer):
     x0 = (500 // 16) * 16  # first screen tile column
     assert (img[:, :x0] == 77).all()
     assert (img[40:60, 560:580, 3] > 0).any()
+
+
+def _bad_point_scene(kind):
+    s = pf.Scene()
+    s.set_view_box(pf.RectF(0, 0, 64, 64))
+    s.push_draw_path(pf.DrawPath(pf.Outline([_star(32, 32, 10, 25, 6)]), pf.ColorU(90, 160, 30, 255)))
+    c = pf.Contour()
+    c.push_endpoint(5, 5)
+    if kind == "nan":
+        c.push_cubic(float("nan"), 10, 30, 40, 50, 50)
+    else:  # finite but never flat: the walk is bounded per segment
+        c.push_cubic(1e30, -1e30, -1e30, 1e30, 50, 50)
+    c.push_endpoint(5, 50)
+    s.push_draw_path(pf.DrawPath(pf.Outline([c]), pf.ColorU(200, 30, 40, 255)))
+    return s
+
+
+@pytest.mark.parametrize("kind", ["nan", "huge"])
+def test_non_finite_and_huge_control_points(renderer, kind):
+    """A non-finite segment gives no fills and the frame reports malformed
+    input; a finite segment that never flattens is cut at 2^20 lines and the
+    frame reports the limit.  Both end promptly, with fills identical to the
+    oracle's for the same rules."""
+    import oracle
+    from pathfinder_gb300._abi import PFCUDAError
+    s = _bad_point_scene(kind)
+    with pytest.raises(PFCUDAError):
+        renderer.render(s)
+    fr = oracle.OracleFrame(s)
+    assert fr.limit_hit
+    compare_records(s, renderer.read_records(s), fr)

@@ -50,3 +50,22 @@ def test_resolved_coverage_is_a_fraction(built):
     fr = oracle.OracleFrame(pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=4, scale=0.01))
     _, cov = fr.masks()
     assert cov.min() >= 0.0 and cov.max() <= 1.0
+
+
+def test_non_finite_and_huge_segments_end(built):
+    """The oracle's tiler ends on a NaN control point (no fills for that
+    segment) and on a never-flat cubic (2^20 lines), flagging both."""
+    import time
+    import oracle
+    import pathfinder_gb300 as pf
+    for ctrl in ((float("nan"), 10.0), (1e30, -1e30)):
+        s = pf.Scene()
+        s.set_view_box(pf.RectF(0, 0, 64, 64))
+        c = pf.Contour()
+        c.push_endpoint(5, 5)
+        c.push_cubic(ctrl[0], ctrl[1], -1e30 if ctrl[0] == 1e30 else 30, 40, 50, 50)
+        c.push_endpoint(5, 50)
+        s.push_draw_path(pf.DrawPath(pf.Outline([c]), pf.ColorU(200, 30, 40, 255)))
+        t = time.time()
+        fr = oracle.OracleFrame(s)
+        assert fr.limit_hit and time.time() - t < 60

@@ -125,3 +125,13 @@ def test_open_contour_edge_cases(built):
     ol = pf.Outline([c0, c1, c2, c3])
     pts, flags, cs, os_, _ = _stroke([(ol, StrokeStyle(2.0, LineCap.ROUND, LineJoin.ROUND))])
     assert list(os_) == [0, 5]  # open: 1 each, closed: 2
+
+
+def test_huge_input_is_bounded(built):
+    import time
+    c = pf.Contour()
+    c.push_endpoint(0, 0)
+    c.push_cubic(1e30, -1e30, -1e30, 1e30, 50, 50)
+    t = time.time()
+    _, _, _, _, lim = _stroke([(pf.Outline([c]), StrokeStyle(3.0))])
+    assert lim and time.time() - t < 60
