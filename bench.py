@@ -309,6 +309,135 @@ def run_atlas(args) -> None:
     r.close()
 
 
+def stroke_workload(seed: int, scale: float = 1.0):
+    """The 4K scene's outlines as strokes: every draw path's contours, half of
+    them open, seeded widths 0.5-8 px with every cap and join (miter limit 4).
+    Returns (StrokeBatch, input segments)."""
+    import numpy as np
+    import pathfinder_gb300 as pf
+    from pathfinder_gb300.stroke import LineCap, LineJoin, StrokeBatch, StrokeStyle
+    scene = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=seed, scale=scale)
+    rng = np.random.default_rng(seed + 11)
+    items, nseg = [], 0
+    starts, pts, fl = scene.contour_starts, scene.points, scene.flags
+    for rec in scene.draw_paths:
+        fc, n = int(rec["first_contour"]), int(rec["contour_count"])
+        ol = pf.Outline()
+        for c in range(fc, fc + n):
+            a, b = int(starts[c]), int(starts[c + 1])
+            ct = pf.Contour()
+            ct.points = pts[a:b].tolist()
+            ct.flags = fl[a:b].tolist()
+            ct.closed = bool(rng.integers(0, 2))
+            ends = int(np.count_nonzero((fl[a + 1:b] & 3) == 0))
+            nseg += (ends + 1 if ct.closed else ends) if b > a else 0
+            ol.contours.append(ct)
+        items.append((ol, StrokeStyle(float(rng.uniform(0.5, 8.0)), LineCap(int(rng.integers(0, 3))),
+                                      LineJoin(int(rng.integers(0, 3))), 4.0)))
+    return StrokeBatch(items), nseg
+
+
+def run_strokes(args) -> None:
+    """Stroke to fill of the 4K scene's 20,000 outlines (2.1M segments) on the
+    GPU, inputs and outputs resident in device memory; e2e through the C ABI
+    with host buffers; CPU baseline: the oracle's single-threaded stroker."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    from pathfinder_gb300 import build as pbuild
+    pbuild.build()
+    import pathfinder_gb300 as pf
+    from pathfinder_gb300 import _abi
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    batch, nseg = stroke_workload(args.seed, args.scale)
+    r = pf.Renderer(0)
+    r.set_stream(stream.cuda_stream)
+    dev = {k: torch.from_numpy(np.ascontiguousarray(getattr(batch, k))).cuda()
+           for k in ("points", "flags", "contour_starts", "contour_closed", "outline_starts")}
+    styles = torch.frombuffer(bytearray(bytes(batch.styles)), dtype=torch.uint8).cuda()
+    d = _abi.PFCUDAStrokeInput()
+    d.points, d.point_flags = dev["points"].data_ptr(), dev["flags"].data_ptr()
+    d.contour_starts, d.contour_closed = dev["contour_starts"].data_ptr(), dev["contour_closed"].data_ptr()
+    d.outline_starts, d.styles = dev["outline_starts"].data_ptr(), styles.data_ptr()
+    d.point_count, d.contour_count, d.outline_count = len(batch.points), batch.contour_count, batch.outline_count
+    d.memory = _abi.PF_MEMORY_DEVICE
+    o = _abi.PFCUDAStrokeOutput()
+    o.memory = _abi.PF_MEMORY_DEVICE
+    L = r._lib
+    rc = L.PFCUDAStrokeToFill(r._h, C.byref(d), C.byref(o))
+    assert rc == _abi.PF_CUDA_ERR_CAPACITY, rc
+    npts, ncont = int(o.point_count), int(o.contour_count)
+    out_pts = torch.empty((npts, 2), dtype=torch.float32, device="cuda")
+    out_fl = torch.empty((npts,), dtype=torch.uint8, device="cuda")
+    out_cs = torch.empty((ncont + 1,), dtype=torch.int32, device="cuda")
+    out_os = torch.empty((batch.outline_count + 1,), dtype=torch.int32, device="cuda")
+    o.points, o.point_flags = out_pts.data_ptr(), out_fl.data_ptr()
+    o.contour_starts, o.outline_starts = out_cs.data_ptr(), out_os.data_ptr()
+    o.point_capacity, o.contour_capacity = npts, ncont
+    for _ in range(args.warmup):
+        assert L.PFCUDAStrokeToFill(r._h, C.byref(d), C.byref(o)) == 0
+    sampler = ClockSampler(0)
+    sampler.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in evs:
+        a.record(stream)
+        L.PFCUDAStrokeToFill(r._h, C.byref(d), C.byref(o))
+        b.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    # e2e: host arrays in, host arrays out, through the Python API
+    e2e = []
+    for _ in range(max(3, min(args.steps, 10))):
+        t0 = time.perf_counter()
+        _stroke_host(r, batch, npts, ncont)
+        e2e.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * sum(e2e) / len(e2e)
+    line = {
+        "metric": "Mseg/s stroked", "value": round(nseg / (ms / 1e3) / 1e6, 3), "unit": "Mseg/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (the seeded PF_SCENE_SVG_4K outlines, half open, widths 0.5-8 px, every cap and join)",
+        "config": {"workload": "stroke_4k_20000_paths" if args.scale == 1.0 else f"stroke_4k_scale{args.scale}",
+                   "outlines": batch.outline_count, "contours": batch.contour_count, "segments": nseg,
+                   "input_points": len(batch.points), "output_points": npts, "output_contours": ncont},
+        "e2e": {"value": round(nseg / (e2e_ms / 1e3) / 1e6, 3), "unit": "Mseg/s",
+                "h2d_bytes_per_step": int(batch.points.nbytes + batch.flags.nbytes + batch.contour_starts.nbytes),
+                "d2h_bytes_per_step": int(npts * 9 + (ncont + 1) * 4), "ms_per_step": round(e2e_ms, 3)},
+        "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        t0 = time.perf_counter()
+        oracle.stroke(batch.desc())
+        cpu_s = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": round(nseg / cpu_s / 1e6, 4), "unit": "Mseg/s", "cores": 1, "kind": "port",
+                                "sample": f"the whole workload once on one host thread ({cpu_s:.2f} s)"}
+    print(json.dumps(line), flush=True)
+    r.close()
+
+
+def _stroke_host(r, batch, npts, ncont):
+    """PFCUDAStrokeToFill with host input and output buffers (the e2e leg)."""
+    import ctypes as C
+    import numpy as np
+    from pathfinder_gb300 import _abi
+    pts = np.empty((npts, 2), np.float32)
+    fl = np.empty((npts,), np.uint8)
+    cs = np.empty((ncont + 1,), np.uint32)
+    os_ = np.empty((batch.outline_count + 1,), np.uint32)
+    o = _abi.PFCUDAStrokeOutput()
+    o.points, o.point_flags, o.contour_starts, o.outline_starts = (pts.ctypes.data, fl.ctypes.data, cs.ctypes.data,
+                                                                   os_.ctypes.data)
+    o.point_capacity, o.contour_capacity, o.memory = npts, ncont, _abi.PF_MEMORY_HOST
+    d = batch.desc()
+    _abi.check(r._lib.PFCUDAStrokeToFill(r._h, C.byref(d), C.byref(o)), "PFCUDAStrokeToFill")
+    return pts, fl, cs, os_
+
+
 def _diff_common(args):
     import torch
     from pathfinder_gb300 import build as pbuild
@@ -485,9 +614,10 @@ def run_fit(args) -> None:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="svg4k", choices=["svg4k", "atlas", "diff", "fit"],
+    ap.add_argument("--workload", default="svg4k", choices=["svg4k", "atlas", "diff", "fit", "strokes"],
                     help="svg4k: the 20,000-path 4K frame (default); atlas: the batched glyph atlas; "
-                         "diff: forward + adjoint of 256 cubic paths at 1024^2; fit: 64-scene Adam fit")
+                         "diff: forward + adjoint of 256 cubic paths at 1024^2; fit: 64-scene Adam fit; "
+                         "strokes: stroke to fill of the 4K scene's outlines")
     ap.add_argument("--fit-steps", type=int, default=200)
     ap.add_argument("--d3d11", action="store_true",
                     help="tile with the D3D11 level's semantics (uniform dicing) instead of the CPU tiler's")
@@ -517,6 +647,9 @@ def main():
         return
     if args.workload == "fit":
         run_fit(args)
+        return
+    if args.workload == "strokes":
+        run_strokes(args)
         return
 
     import torch
