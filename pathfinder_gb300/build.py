@@ -35,6 +35,7 @@ UNITS = [
     ("pf_scenes.cpp", []),
     ("pf_paint.cu", []),
     ("pf_stroke.cu", ["-fmad=false"]),
+    ("pf_pack.cu", []),
 ]
 
 

@@ -5,6 +5,8 @@
 
 #include <vector>
 
+struct PFCUDAPath;
+
 namespace pf {
 
 // Launch shapes chosen by the autotuner (outputs do not depend on them).
@@ -167,11 +169,67 @@ void count_launch(uint32_t n = 1);
 
 
 void launch_transform(const float2* in, float2* out, uint32_t n, const float* m6, cudaStream_t s);
-void launch_contour_segcount(const uint32_t* ord_contour, uint32_t nord, const uint32_t* contour_starts,
-                             const uint8_t* flags, uint32_t* seg_count, uint32_t* status, cudaStream_t s);
-void launch_contour_segemit(const uint32_t* ord_contour, const uint32_t* ord_path, uint32_t nord,
-                            const uint32_t* contour_starts, const uint8_t* flags, const uint32_t* seg_base,
-                            SegRec* segs, cudaStream_t s);
+// Segments per contour reference and their records. The reference count is
+// the device-side *d_n clamped to the buffers' capacity cap (d_n NULL: cap).
+// contour_total: contours behind contour_starts (a reference past it is malformed).
+void launch_contour_segcount(const uint32_t* ord_contour, const uint64_t* d_n, uint32_t cap,
+                             const uint32_t* contour_starts, uint32_t contour_total, const uint8_t* flags,
+                             uint32_t* seg_count, uint32_t* status, cudaStream_t s);
+void launch_contour_segemit(const uint32_t* ord_contour, const uint32_t* ord_path, const uint64_t* d_n, uint32_t cap,
+                            const uint32_t* contour_starts, uint32_t contour_total, const uint8_t* flags,
+                            const uint32_t* seg_base, SegRec* segs, cudaStream_t s);
+
+// ---- scene packing at upload (pf_pack.cu) ----------------------------------
+// One scene of an upload batch, as the packing kernels see it.
+struct ScenePackDev {
+    uint32_t first_path, nclip, ndraw;     // global index of the scene's path 0; clip, draw paths
+    uint32_t contour_base, contour_count;  // global index of the scene's contour 0; contours
+    uint32_t point_base, point_count;      // global index of the scene's point 0; points
+    uint32_t draw_base;                    // global draw index of the scene's draw path 0
+    uint32_t overlay_base, overlay_count;  // global overlay index of the scene's overlay 1, minus 1; count
+};
+// What the host reads back after packing.
+struct PackInfo {
+    uint64_t nord;       // contour references of all paths (a 32-bit scan total)
+    uint64_t segs;       // segments of all references
+    uint64_t refs;       // the same references summed in 64 bits: nord is valid while refs < 2^31
+    uint32_t status;     // kStatusMalformed: an invalid record or index
+    uint32_t chain_max;  // longest chain of clip paths behind a path
+    uint32_t flags;      // kPackNestedClips | kPackBlendModes
+    uint32_t pad;
+};
+constexpr uint32_t kPackNestedClips = 1u, kPackBlendModes = 2u;
+// The per-path tables a frame reads (indexed by global path; draw-indexed for alpha).
+struct PathTablesDev {
+    uint32_t* ncont;        // contour references (0 for an invalid record); scanned into first_ord
+    uint32_t* paint;        // RGBA8
+    uint32_t* local;        // index within the scene's clip paths or draw paths
+    uint32_t* scene_of;
+    int32_t* clip;          // global clip path, or -1
+    uint8_t* rule;
+    uint8_t* is_clip;
+    uint32_t* draw_index;   // kInvalid for clip paths
+    float* alpha;           // default paint alpha of each draw path (draw-indexed)
+    uint8_t* blend;
+    uint32_t* overlay;      // global overlay + 1, or 0
+    uint8_t* occludes;
+};
+// Global contour boundaries from each scene's own (validated) boundaries.
+void launch_pack_starts(const uint32_t* raw, uint32_t* starts, const ScenePackDev* scenes, uint32_t scene_count,
+                        uint32_t boundary_count, uint32_t point_total, PackInfo* info, cudaStream_t s);
+void launch_pack_paths(const PFCUDAPath* paths, uint32_t path_count, const ScenePackDev* scenes,
+                       uint32_t scene_count, const uint8_t* overlay_opaque, const PathTablesDev& t, PackInfo* info,
+                       cudaStream_t s);
+// ord_contour / ord_path from first_ord (references past cap are dropped: the host grows and re-runs).
+void launch_pack_order(const PFCUDAPath* paths, uint32_t path_count, const ScenePackDev* scenes,
+                       const uint32_t* scene_of, const uint32_t* ncont, const uint32_t* first_ord, uint32_t cap,
+                       uint32_t* ord_contour, uint32_t* ord_path, cudaStream_t s);
+void launch_pack_chains(const int32_t* clip, const uint8_t* is_clip, const uint32_t* scene_of,
+                        const ScenePackDev* scenes, uint32_t path_count, PackInfo* info, cudaStream_t s);
+// Per scene: [first segment, end segment).
+void launch_pack_ranges(const ScenePackDev* scenes, uint32_t scene_count, const uint32_t* first_ord,
+                        const uint32_t* seg_base, const uint64_t* d_nord, uint32_t cap, uint32_t* ranges,
+                        cudaStream_t s);
 void launch_bound(const FrameDev& f, const uint32_t* ord_contour, const uint32_t* contour_starts, cudaStream_t s);
 void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s);
 void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s);

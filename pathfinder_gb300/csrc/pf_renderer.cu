@@ -41,6 +41,57 @@ struct DevBuf {
     void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
 };
 
+// Pinned host staging for the scene tables built at upload. A copy from
+// pageable memory waits for the driver's bounce buffer, so a dozen small
+// tables cost a dozen round trips; from here each copy is one async enqueue.
+// `done` is recorded after the last copy that reads the staging, and the next
+// upload waits on it before writing.
+struct HostStage {
+    uint8_t* p = nullptr;
+    size_t cap = 0, used = 0;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+    cudaError_t begin(size_t n) {
+        cudaError_t e = cudaSuccess;
+        if (pending && (e = cudaEventSynchronize(done))) return e;
+        pending = false;
+        used = 0;
+        if (n <= cap && p) return cudaSuccess;
+        if (p) { cudaFreeHost(p); p = nullptr; cap = 0; }
+        const size_t want = std::max<size_t>(n, 1u << 16);
+        if ((e = cudaHostAlloc((void**)&p, want, cudaHostAllocDefault))) return e;
+        cap = want;
+        return cudaSuccess;
+    }
+    static size_t room(size_t bytes) { return (bytes + 15) & ~size_t(15); }
+    template <typename T>
+    T* take(size_t n) {
+        T* q = (T*)(p + used);
+        used += room(n * sizeof(T));
+        return q;
+    }
+    template <typename T>
+    const T* put(const std::vector<T>& v) {
+        T* q = take<T>(v.size());
+        if (!v.empty()) std::memcpy(q, v.data(), v.size() * sizeof(T));
+        return q;
+    }
+    cudaError_t mark(cudaStream_t s) {
+        if (!done) {
+            cudaError_t e = cudaEventCreateWithFlags(&done, cudaEventDisableTiming);
+            if (e) return e;
+        }
+        pending = true;
+        return cudaEventRecord(done, s);
+    }
+    void release() {
+        if (pending && done) cudaEventSynchronize(done);
+        if (p) cudaFreeHost(p);
+        if (done) cudaEventDestroy(done);
+        p = nullptr; cap = 0; done = nullptr; pending = false;
+    }
+};
+
 inline int32_t cvt_rne_host(float x) {
     if (!(x >= -2147483648.0f && x < 2147483648.0f)) return INT32_MIN;
     return (int32_t)std::nearbyint(x);
@@ -72,6 +123,11 @@ struct PFCUDARenderer {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
+    // Uploads copy the points on their own stream, beside the packing
+    // kernels (which read only the point flags); the frame stream waits on
+    // points_done before anything that reads points.
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t points_done = nullptr, prior_done = nullptr;
     PFCUDARendererOptions options{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -79,11 +135,17 @@ struct PFCUDARenderer {
     bool has_scene = false;
     uint32_t P = 0, NP = 0, NC = 0, nord = 0, S = 0, screen_total = 0;
     std::vector<SceneInfo> scenes;
-    std::vector<uint32_t> path_local;  // host copy: index within clip / draw paths
-    std::vector<uint8_t> path_is_clip;
     DevBuf<float2> pts, pts_t;
     DevBuf<uint8_t> flags;
     DevBuf<uint32_t> starts, ord_contour, ord_path, contour_segs, contour_seg_base;
+    uint32_t ord_cap = 0;               // contour references the order buffers hold
+    // upload staging on the device: the caller's records and the packing results
+    DevBuf<uint32_t> starts_raw, path_ncont, scene_ranges;
+    DevBuf<PFCUDAPath> path_in;
+    DevBuf<ScenePackDev> scene_pack;
+    DevBuf<PackInfo> pack_info;
+    DevBuf<uint8_t> overlay_opaque;
+    DevBuf<float> alpha_default;        // paint alpha / 255 per draw path (the default alpha)
     DevBuf<SegRec> segs;
     DevBuf<uint32_t> first_ord, paint, local_index, scene_of;
     DevBuf<int32_t> clip_gpath;
@@ -111,6 +173,7 @@ struct PFCUDARenderer {
     DevBuf<Counters> counters;
     DevBuf<uint8_t> out_tmp;
     Counters* h_counters = nullptr;  // pinned
+    HostStage stage;                 // pinned scene tables
 
     uint32_t tile_cap = 0, col_cap = 0, fill_cap = 0, vis_cap = 0, line_cap = 0;
     Range last;
@@ -124,6 +187,11 @@ struct PFCUDARenderer {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
 
+    // plain frames replayed from a graph while their key (every pointer, size
+    // and option that a launch of the frame reads) repeats
+    std::vector<uint8_t> replay_key;
+    cudaGraphExec_t replay_exec = nullptr;
+
     // clip chains
     uint32_t clip_chain_max = 0;       // longest chain of clip paths behind a path
     bool nested_clips = false;         // some clip path is itself clipped
@@ -132,7 +200,6 @@ struct PFCUDARenderer {
 
     // differentiable frames
     uint32_t ND = 0;                   // draw paths of the batch
-    std::vector<float> draw_alpha;     // paint alpha / 255 per draw path (default alpha)
     DevBuf<uint32_t> draw_index;       // [P] path -> draw path index (kInvalid for clip paths)
     DevBuf<float> alpha_in;            // [ND] alpha of the current differentiable frame
     DevBuf<float4> fills_f;
@@ -281,6 +348,12 @@ cudaError_t ensure_frame_buffers(PFCUDARenderer* r) {
     return r->scan_partials.ensure(kMaxScanLanes * (nmax / 2048 + 2));
 }
 
+float4 background_of(const PFCUDARenderer* r) {
+    if (!r->options.has_background_color) return make_float4(0, 0, 0, 0);
+    return make_float4(r->options.background_color.r, r->options.background_color.g, r->options.background_color.b,
+                       r->options.background_color.a);
+}
+
 bool is_identity(const PFCUDABuildOptions* o) {
     if (!o || !o->has_transform) return true;
     const PFTransform2F& t = o->transform;
@@ -357,10 +430,7 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     launch_visible(f, true, s);
     mark(7);
     if (mode >= 0 || diff) {
-        float4 bg = make_float4(0, 0, 0, 0);
-        if (r->options.has_background_color)
-            bg = make_float4(r->options.background_color.r, r->options.background_color.g,
-                             r->options.background_color.b, r->options.background_color.a);
+        const float4 bg = background_of(r);
         if (diff) launch_composite_diff(f, (float*)out_dev, bg, s);
         else launch_composite(f, mode, out_dev, bg, s);
     }
@@ -422,8 +492,95 @@ void set_target(PFCUDARenderer* r, uint32_t k, const PFCUDASceneTarget& t) {
     d.out_offset = t.out_offset;
 }
 
+// The scene of global path gp (the last scene starting at or before it).
+const SceneInfo& scene_of_path(const PFCUDARenderer* r, uint32_t gp) {
+    auto it = std::upper_bound(r->scenes.begin(), r->scenes.end(), gp,
+                               [](uint32_t v, const SceneInfo& si) { return v < si.first_path; });
+    return it == r->scenes.begin() ? r->scenes.front() : *(it - 1);
+}
+
+bool path_is_clip_of(const PFCUDARenderer* r, uint32_t gp) {
+    const SceneInfo& si = scene_of_path(r, gp);
+    return gp - si.first_path < si.nclip;
+}
+
+// Index of global path gp within its scene's clip paths or draw paths.
+uint32_t path_local_of(const PFCUDARenderer* r, uint32_t gp, bool* is_clip) {
+    const SceneInfo& si = scene_of_path(r, gp);
+    const uint32_t i = gp - si.first_path;
+    if (is_clip) *is_clip = i < si.nclip;
+    return i < si.nclip ? i : i - si.nclip;
+}
+
 bool valid_range(const PFCUDARenderer* r, uint32_t first, uint32_t count) {
     return r->has_scene && count > 0 && first < r->scenes.size() && count <= r->scenes.size() - first;
+}
+
+// Everything the launches of a plain frame read on the host: two frames with
+// equal keys enqueue the same kernels with the same arguments. Scene contents
+// stay out of it: they are read on the device, so a graph of the frame
+// replays correctly after an upload that kept every buffer and size.
+std::vector<uint8_t> frame_key(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev,
+                               const Range& g) {
+    const bool transformed = !is_identity(opts);
+    const FrameDev f = frame_dev(r, transformed, g, false);
+    std::vector<uint8_t> k;
+    auto put = [&k](const void* p, size_t n) { k.insert(k.end(), (const uint8_t*)p, (const uint8_t*)p + n); };
+    put(&f, sizeof f);
+    const void* ptrs[] = {r->pts.p, r->ord_contour.p, r->starts.p, r->scan_partials.p, out_dev};
+    put(ptrs, sizeof ptrs);
+    const uint64_t vals[] = {r->scan_partials.cap, r->NP, (uint64_t)(int64_t)mode, transformed ? 1u : 0u};
+    put(vals, sizeof vals);
+    const float4 bg = background_of(r);
+    put(&bg, sizeof bg);
+    if (transformed) put(&opts->transform, sizeof opts->transform);
+    return k;
+}
+
+void drop_replay(PFCUDARenderer* r) {
+    if (r->replay_exec) cudaGraphExecDestroy(r->replay_exec);
+    r->replay_exec = nullptr;
+    r->replay_key.clear();
+}
+
+// A plain frame whose key repeats the previous one's runs as one graph
+// launch, captured at the key's second frame (a key seen once is not worth a
+// capture); any other frame is enqueued kernel by kernel.
+cudaError_t enqueue_plain(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev, const Range& g) {
+    std::vector<uint8_t> key = frame_key(r, opts, mode, out_dev, g);
+    if (key != r->replay_key) {
+        drop_replay(r);
+        r->replay_key.swap(key);
+        return enqueue_frame(r, opts, mode, out_dev, g);
+    }
+    if (!r->replay_exec) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(r->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+            (void)cudaGetLastError();
+            return enqueue_frame(r, opts, mode, out_dev, g);
+        }
+        cudaError_t e = cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            return enqueue_frame(r, opts, mode, out_dev, g);
+        }
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e1 = enqueue_frame(r, opts, mode, out_dev, g);
+        const cudaError_t e2 = cudaStreamEndCapture(r->stream, &graph);
+        if (e1 != cudaSuccess || e2 != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return e1 != cudaSuccess ? e1 : e2;
+        }
+        e = cudaGraphInstantiate(&r->replay_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            r->replay_exec = nullptr;
+            return e;
+        }
+    }
+    r->last_diff = false;
+    r->diff_valid = false;
+    return cudaGraphLaunch(r->replay_exec, r->stream);
 }
 
 // Run one frame synchronously with regrow-and-retry.
@@ -434,7 +591,8 @@ int32_t run_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, v
     for (int attempt = 0; attempt < 4; attempt++) {
         PF_TRY(ensure_frame_buffers(r));
         PF_TRY(cudaEventRecord(r->ev0, r->stream));
-        PF_TRY(enqueue_frame(r, opts, mode, out_dev, g, diff));
+        if (diff || r->profiling) PF_TRY(enqueue_frame(r, opts, mode, out_dev, g, diff));
+        else PF_TRY(enqueue_plain(r, opts, mode, out_dev, g));
         PF_TRY(cudaEventRecord(r->ev1, r->stream));
         PF_TRY(cudaMemcpyAsync(r->h_counters, r->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, r->stream));
         PF_TRY(cudaStreamSynchronize(r->stream));
@@ -502,6 +660,9 @@ int32_t PFCUDARendererCreate(int32_t device_ordinal, const PFCUDARendererOptions
     r->device = device_ordinal;
     if (options) r->options = *options;
     if ((e = cudaStreamCreateWithFlags(&r->own_stream, cudaStreamNonBlocking)) ||
+        (e = cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking)) ||
+        (e = cudaEventCreateWithFlags(&r->points_done, cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&r->prior_done, cudaEventDisableTiming)) ||
         (e = cudaEventCreate(&r->ev0)) || (e = cudaEventCreate(&r->ev1)) ||
         (e = cudaMallocHost((void**)&r->h_counters, sizeof(Counters))) || (e = r->counters.ensure(1))) {
         PFCUDARendererDestroy(r);
@@ -530,15 +691,25 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->clips.release(); r->screen_cnt.release(); r->screen_base.release(); r->vis.release(); r->vis_info.release();
     r->scan_partials.release(); r->counters.release(); r->out_tmp.release();
     r->draw_index.release(); r->blend.release(); r->occludes.release(); r->overlay.release();
+    r->starts_raw.release(); r->path_ncont.release(); r->scene_ranges.release(); r->path_in.release();
+    r->scene_pack.release(); r->pack_info.release(); r->overlay_opaque.release(); r->alpha_default.release();
     r->overlays.release(); r->texels.release(); r->alpha_in.release(); r->fills_f.release(); r->line_seg.release();
     r->line_t.release(); r->tape.release();
     r->grad_mask.release(); r->grad_alpha_tmp.release();
     if (r->h_counters) cudaFreeHost(r->h_counters);
+    r->stage.release();
+    drop_replay(r);
     if (r->ev0) cudaEventDestroy(r->ev0);
     if (r->ev1) cudaEventDestroy(r->ev1);
     for (int i = 0; i <= PF_CUDA_STAGE_COUNT; i++)
         if (r->stage_ev[i]) cudaEventDestroy(r->stage_ev[i]);
     if (r->own_stream) cudaStreamDestroy(r->own_stream);
+    if (r->copy_stream) {
+        cudaStreamSynchronize(r->copy_stream);
+        cudaStreamDestroy(r->copy_stream);
+    }
+    if (r->points_done) cudaEventDestroy(r->points_done);
+    if (r->prior_done) cudaEventDestroy(r->prior_done);
     stroke_work_destroy(r->stroke);
     delete r;
     return PF_CUDA_OK;
@@ -558,57 +729,24 @@ int32_t PFCUDARendererSetOptions(PFCUDARendererRef r, const PFCUDARendererOption
     return PF_CUDA_OK;
 }
 
-int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scenes, const PFCUDASceneTarget* targets,
-                               uint32_t scene_count) {
-    if (!r || !scenes || scene_count == 0) return PF_CUDA_ERR_INVALID;
-    PF_TRY(cudaSetDevice(r->device));
+// The scene tables of an upload whose point copies are already enqueued. The
+// host lays out the scenes (O(scenes) work) and stages the caller's records;
+// the per-path tables, the contour order, the clip chains and the segment
+// records are built on the device (pf_pack.cu, then the segment kernels).
+static int32_t upload_tables(PFCUDARendererRef r, const PFCUDASceneDesc* scenes, const PFCUDASceneTarget* targets,
+                             uint32_t scene_count, uint64_t np_total, uint64_t nc_total, uint64_t P) {
     cudaStream_t s = r->stream;
-    release_graph(r);
-    r->has_scene = false;
-
-    // ---- validate and lay out the batch on the host --------------------------
-    uint64_t np_total = 0, nc_total = 0, P = 0;
-    for (uint32_t k = 0; k < scene_count; k++) {
-        const PFCUDASceneDesc& sc = scenes[k];
-        if (sc.memory != PF_MEMORY_HOST && sc.memory != PF_MEMORY_DEVICE) return PF_CUDA_ERR_INVALID;
-        if ((sc.clip_path_count && !sc.clip_paths) || (sc.draw_path_count && !sc.draw_paths)) return PF_CUDA_ERR_INVALID;
-        if (sc.contour_count && !sc.contour_starts) return PF_CUDA_ERR_INVALID;
-        if (sc.point_count && (!sc.points || !sc.point_flags)) return PF_CUDA_ERR_INVALID;
-        np_total += sc.point_count;
-        nc_total += (uint64_t)sc.contour_count + 1;  // each scene keeps its own end boundary
-        P += (uint64_t)sc.clip_path_count + sc.draw_path_count;
-    }
-    if (np_total >= 0x7fffffffull || nc_total >= 0x7fffffffull || P >= 0x7fffffffull) return PF_CUDA_ERR_INVALID;
-
-    std::vector<uint32_t> hstarts((size_t)nc_total + 1, 0);
-    std::vector<uint32_t> first_ord((size_t)P + 1, 0), ord_contour, ord_path, paint((size_t)P), local((size_t)P),
-        scene_of((size_t)P);
-    std::vector<int32_t> clip((size_t)P);
-    std::vector<uint8_t> rule((size_t)P), isclip((size_t)P);
-    std::vector<uint32_t> draw_index((size_t)P, kInvalid);
-    std::vector<float> draw_alpha;
-    std::vector<uint8_t> blend((size_t)P, 0), occl((size_t)P, 0);
-    std::vector<uint32_t> overlayv((size_t)P, 0), texels;
+    const size_t Pz = (size_t)P;
+    const uint32_t nb = (uint32_t)nc_total;  // contour boundary slots: contours + 1 per scene
+    std::vector<uint32_t> texels;
     std::vector<OverlayDev> overlays;
     std::vector<uint8_t> overlay_opaque;
+    std::vector<ScenePackDev> packs(scene_count);
     r->scenes.assign(scene_count, SceneInfo());
     r->scenes_host.assign(scene_count, SceneDev{});
-    uint32_t point_base = 0, contour_base = 0, gp = 0, screen_total = 0;
+    uint32_t point_base = 0, contour_base = 0, gp = 0, screen_total = 0, draw_base = 0;
     for (uint32_t k = 0; k < scene_count; k++) {
         const PFCUDASceneDesc& sc = scenes[k];
-        std::vector<uint32_t> st(sc.contour_count + 1, 0);
-        if (sc.contour_count) {
-            if (sc.memory == PF_MEMORY_HOST)
-                std::memcpy(st.data(), sc.contour_starts, sizeof(uint32_t) * (sc.contour_count + 1));
-            else
-                PF_TRY(cudaMemcpy(st.data(), sc.contour_starts, sizeof(uint32_t) * (sc.contour_count + 1),
-                                  cudaMemcpyDeviceToHost));
-        }
-        for (uint32_t c = 0; c < sc.contour_count; c++)
-            if (st[c] > st[c + 1] || st[c + 1] > sc.point_count) return PF_CUDA_ERR_INVALID;
-        // contour c of the scene is global contour contour_base + c; its end is
-        // the next boundary, so the scene's boundaries (count + 1) are copied whole
-        for (uint32_t c = 0; c <= sc.contour_count; c++) hstarts[contour_base + c] = point_base + st[c];
         SceneInfo& si = r->scenes[k];
         si.first_path = gp;
         si.nclip = sc.clip_path_count;
@@ -633,37 +771,8 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
             overlays.push_back(od);
             overlay_opaque.push_back(opaque ? 1 : 0);
         }
-        for (uint32_t i = 0; i < sc.clip_path_count + sc.draw_path_count; i++, gp++) {
-            const bool c = i < sc.clip_path_count;
-            const PFCUDAPath& p = c ? sc.clip_paths[i] : sc.draw_paths[i - sc.clip_path_count];
-            if ((uint64_t)p.first_contour + p.contour_count > sc.contour_count) return PF_CUDA_ERR_INVALID;
-            if (p.fill_rule > 1 || p.blend_mode >= PF_BLEND_MODE_COUNT) return PF_CUDA_ERR_INVALID;
-            if (!c && p.overlay > sc.gradient_count + sc.pattern_count) return PF_CUDA_ERR_INVALID;
-            if (p.clip_path >= (int32_t)sc.clip_path_count) return PF_CUDA_ERR_INVALID;
-            if (c && p.clip_path == (int32_t)i) return PF_CUDA_ERR_INVALID;  // a clip path clipping itself
-            first_ord[gp] = (uint32_t)ord_contour.size();
-            for (uint32_t q = 0; q < p.contour_count; q++) {
-                ord_contour.push_back(contour_base + p.first_contour + q);
-                ord_path.push_back(gp);
-            }
-            paint[gp] = (uint32_t)p.paint.r | ((uint32_t)p.paint.g << 8) | ((uint32_t)p.paint.b << 16) |
-                        ((uint32_t)p.paint.a << 24);
-            local[gp] = c ? i : i - sc.clip_path_count;
-            clip[gp] = p.clip_path >= 0 ? (int32_t)(si.first_path + (uint32_t)p.clip_path) : -1;
-            rule[gp] = p.fill_rule;
-            isclip[gp] = c ? 1 : 0;
-            scene_of[gp] = k;
-            if (!c) {
-                draw_index[gp] = (uint32_t)draw_alpha.size();
-                draw_alpha.push_back((float)p.paint.a / 255.0f);
-                blend[gp] = p.blend_mode;
-                overlayv[gp] = p.overlay ? ov_base + p.overlay : 0u;  // global index + 1
-                // BuiltDrawPath::occludes (renderer/src/builder.rs:80-94): opaque paint and
-                // BlendMode::occludes_backdrop (content/src/effects.rs:202-230)
-                const bool opaque = p.paint.a == 255 && (p.overlay == 0 || overlay_opaque[ov_base + p.overlay - 1]);
-                occl[gp] = opaque && (p.blend_mode == PF_BLEND_MODE_SRC_OVER || p.blend_mode == PF_BLEND_MODE_CLEAR);
-            }
-        }
+        packs[k] = ScenePackDev{gp, sc.clip_path_count, sc.draw_path_count, contour_base, sc.contour_count,
+                                point_base, sc.point_count, draw_base, ov_base, sc.gradient_count + sc.pattern_count};
         SceneDev& d = r->scenes_host[k];
         d.view_box = make_float4(sc.view_box.origin.x, sc.view_box.origin.y, sc.view_box.lower_right.x,
                                  sc.view_box.lower_right.y);
@@ -676,109 +785,150 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
             set_target(r, k, targets[k]);
             si.explicit_target = true;
         }
+        gp += sc.clip_path_count + sc.draw_path_count;
+        draw_base += sc.draw_path_count;
         point_base += sc.point_count;
         contour_base += sc.contour_count + 1;
     }
-    hstarts[nc_total] = point_base;
-    first_ord[P] = (uint32_t)ord_contour.size();
-    // Clip chains (a clip path clipped by another, the D3D11 level's clip
-    // levels, renderer/src/builder.rs:1124-1220): reject cycles, and keep the
-    // longest chain as the bound of the device-side chain walks.
-    uint32_t chain_max = 0;
-    bool nested = false;
-    for (uint32_t k = 0; k < scene_count; k++) {
-        const SceneInfo& si = r->scenes[k];
-        for (uint32_t q0 = si.first_path; q0 < si.first_path + si.nclip + si.ndraw; q0++) {
-            uint32_t len = 0;
-            for (int32_t q = clip[q0]; q >= 0; q = clip[(uint32_t)q]) {
-                if (++len > si.nclip) return PF_CUDA_ERR_INVALID;  // a cycle of clip paths
-            }
-            chain_max = std::max(chain_max, len);
-            if (isclip[q0] && clip[q0] >= 0) nested = true;
-        }
-    }
-    r->clip_chain_max = chain_max;
-    r->nested_clips = nested;
-    r->paint_effects = !overlays.empty();
-    for (uint32_t q = 0; q < P; q++) r->paint_effects = r->paint_effects || blend[q] != PF_BLEND_MODE_SRC_OVER;
-    const uint32_t nord = (uint32_t)ord_contour.size();
-    r->path_local.assign(local.begin(), local.end());
-    r->path_is_clip.assign(isclip.begin(), isclip.end());
 
-    // ---- device copies ---------------------------------------------------------
+    // ---- device buffers --------------------------------------------------------
+    // Contour references: one per contour of each path; more only when paths
+    // share contours, found after packing (the buffers then grow and the
+    // order is packed again).
+    uint32_t cap = std::max(r->ord_cap, nb);
     cudaError_t e;
-    const size_t Pz = (size_t)P;
-    if ((e = r->pts.ensure(np_total)) || (e = r->flags.ensure(np_total)) || (e = r->starts.ensure(nc_total + 1)) ||
-        (e = r->ord_contour.ensure(nord)) || (e = r->ord_path.ensure(nord)) || (e = r->contour_segs.ensure(nord + 1)) ||
-        (e = r->contour_seg_base.ensure(nord + 1)) || (e = r->first_ord.ensure(Pz + 1)) || (e = r->paint.ensure(Pz)) ||
-        (e = r->local_index.ensure(Pz)) || (e = r->scene_of.ensure(Pz)) || (e = r->clip_gpath.ensure(Pz)) ||
-        (e = r->rule.ensure(Pz)) || (e = r->is_clip.ensure(Pz)) || (e = r->tile_rect.ensure(Pz)) ||
-        (e = r->draw_index.ensure(Pz)) || (e = r->blend.ensure(Pz)) || (e = r->occludes.ensure(Pz)) ||
-        (e = r->overlay.ensure(Pz)) || (e = r->overlays.ensure(overlays.size() + 1)) ||
-        (e = r->texels.ensure(texels.size() + 1)) ||
-        (e = r->tile_offset.ensure(Pz + 1)) || (e = r->col_offset.ensure(Pz + 1)) ||
-        (e = r->scenes_dev.ensure(scene_count)) || (e = r->scan_partials.ensure(nord / 2048 + 2)))
+    auto ensure_order = [&](uint32_t c) -> cudaError_t {
+        cudaError_t x;
+        if ((x = r->ord_contour.ensure((size_t)c + 1)) || (x = r->ord_path.ensure((size_t)c + 1)) ||
+            (x = r->contour_segs.ensure((size_t)c + 1)) || (x = r->contour_seg_base.ensure((size_t)c + 1)) ||
+            (x = r->scan_partials.ensure(std::max<size_t>(Pz, c) / 2048 + 2)))
+            return x;
+        r->ord_cap = c;
+        return cudaSuccess;
+    };
+    if ((e = ensure_order(cap)) || (e = r->starts.ensure((size_t)nb + 1)) || (e = r->starts_raw.ensure((size_t)nb + 1)) ||
+        (e = r->path_in.ensure(Pz + 1)) || (e = r->scene_pack.ensure(scene_count)) ||
+        (e = r->path_ncont.ensure(Pz + 1)) || (e = r->first_ord.ensure(Pz + 1)) || (e = r->paint.ensure(Pz + 1)) ||
+        (e = r->local_index.ensure(Pz + 1)) || (e = r->scene_of.ensure(Pz + 1)) || (e = r->clip_gpath.ensure(Pz + 1)) ||
+        (e = r->rule.ensure(Pz + 1)) || (e = r->is_clip.ensure(Pz + 1)) || (e = r->tile_rect.ensure(Pz + 1)) ||
+        (e = r->draw_index.ensure(Pz + 1)) || (e = r->alpha_default.ensure((size_t)draw_base + 1)) ||
+        (e = r->blend.ensure(Pz + 1)) || (e = r->occludes.ensure(Pz + 1)) || (e = r->overlay.ensure(Pz + 1)) ||
+        (e = r->overlays.ensure(overlays.size() + 1)) || (e = r->overlay_opaque.ensure(overlays.size() + 1)) ||
+        (e = r->texels.ensure(texels.size() + 1)) || (e = r->tile_offset.ensure(Pz + 1)) ||
+        (e = r->col_offset.ensure(Pz + 1)) || (e = r->scenes_dev.ensure(scene_count)) ||
+        (e = r->pack_info.ensure(1)) || (e = r->scene_ranges.ensure(2 * (size_t)scene_count)))
         return cuda_status(e);
-    point_base = 0;
+
+    // ---- the caller's records through the pinned staging ----------------------
+    const size_t stage_bytes = HostStage::room(4 * (size_t)nb) + HostStage::room(sizeof(PFCUDAPath) * Pz) +
+                               HostStage::room(sizeof(ScenePackDev) * scene_count) +
+                               HostStage::room(sizeof(OverlayDev) * overlays.size()) +
+                               HostStage::room(4 * texels.size()) + HostStage::room(overlay_opaque.size()) +
+                               HostStage::room(sizeof(PackInfo)) + HostStage::room(8 * (size_t)scene_count);
+    if ((e = r->stage.begin(stage_bytes))) return cuda_status(e);
+    HostStage& hs = r->stage;
+    uint32_t* raw = hs.take<uint32_t>(nb);
+    PFCUDAPath* paths = hs.take<PFCUDAPath>(Pz);
+    for (uint32_t k = 0; k < scene_count; k++) {
+        const PFCUDASceneDesc& sc = scenes[k];
+        const ScenePackDev& pk = packs[k];
+        // contour c of the scene is global contour contour_base + c; its end is
+        // the next boundary, so the scene's boundaries (count + 1) are copied whole
+        if (sc.contour_count == 0) raw[pk.contour_base] = 0;
+        else if (sc.memory == PF_MEMORY_HOST)
+            std::memcpy(raw + pk.contour_base, sc.contour_starts, sizeof(uint32_t) * ((size_t)sc.contour_count + 1));
+        if (sc.clip_path_count)
+            std::memcpy(paths + pk.first_path, sc.clip_paths, sizeof(PFCUDAPath) * sc.clip_path_count);
+        if (sc.draw_path_count)
+            std::memcpy(paths + pk.first_path + sc.clip_path_count, sc.draw_paths,
+                        sizeof(PFCUDAPath) * sc.draw_path_count);
+    }
+    auto h2d = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+        return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
+    };
+    if ((e = h2d(r->starts_raw.p, raw, 4 * (size_t)nb)) || (e = h2d(r->path_in.p, paths, sizeof(PFCUDAPath) * Pz)) ||
+        (e = h2d(r->scene_pack.p, hs.put(packs), sizeof(ScenePackDev) * scene_count)) ||
+        (e = h2d(r->overlays.p, hs.put(overlays), sizeof(OverlayDev) * overlays.size())) ||
+        (e = h2d(r->texels.p, hs.put(texels), 4 * texels.size())) ||
+        (e = h2d(r->overlay_opaque.p, hs.put(overlay_opaque), overlay_opaque.size())))
+        return cuda_status(e);
+    // The points queue behind the small copies above (copies in one direction
+    // share an engine in issue order), so the packing below starts at once.
     for (uint32_t k = 0; k < scene_count; k++) {
         const PFCUDASceneDesc& sc = scenes[k];
         const cudaMemcpyKind kind = sc.memory == PF_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-        if (sc.point_count) {
-            PF_TRY(cudaMemcpyAsync(r->pts.p + point_base, sc.points, sizeof(float2) * sc.point_count, kind, s));
-            PF_TRY(cudaMemcpyAsync(r->flags.p + point_base, sc.point_flags, sc.point_count, kind, s));
-        }
-        point_base += sc.point_count;
+        if (sc.point_count)
+            PF_TRY(cudaMemcpyAsync(r->pts.p + packs[k].point_base, sc.points, sizeof(float2) * sc.point_count, kind,
+                                   r->copy_stream));
     }
-    PF_TRY(cudaMemcpyAsync(r->starts.p, hstarts.data(), sizeof(uint32_t) * (nc_total + 1), cudaMemcpyHostToDevice, s));
-    if (nord) {
-        PF_TRY(cudaMemcpyAsync(r->ord_contour.p, ord_contour.data(), sizeof(uint32_t) * nord, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->ord_path.p, ord_path.data(), sizeof(uint32_t) * nord, cudaMemcpyHostToDevice, s));
+    PF_TRY(cudaEventRecord(r->points_done, r->copy_stream));
+    for (uint32_t k = 0; k < scene_count; k++) {  // boundaries already in device memory
+        const PFCUDASceneDesc& sc = scenes[k];
+        if (sc.contour_count && sc.memory == PF_MEMORY_DEVICE)
+            PF_TRY(cudaMemcpyAsync(r->starts_raw.p + packs[k].contour_base, sc.contour_starts,
+                                   sizeof(uint32_t) * ((size_t)sc.contour_count + 1), cudaMemcpyDeviceToDevice, s));
     }
-    if (P) {
-        PF_TRY(cudaMemcpyAsync(r->first_ord.p, first_ord.data(), sizeof(uint32_t) * (Pz + 1), cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->paint.p, paint.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->local_index.p, local.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->scene_of.p, scene_of.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->clip_gpath.p, clip.data(), sizeof(int32_t) * Pz, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->rule.p, rule.data(), Pz, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->is_clip.p, isclip.data(), Pz, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->draw_index.p, draw_index.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->blend.p, blend.data(), Pz, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->occludes.p, occl.data(), Pz, cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->overlay.p, overlayv.data(), sizeof(uint32_t) * Pz, cudaMemcpyHostToDevice, s));
-    }
-    if (!overlays.empty()) {
-        PF_TRY(cudaMemcpyAsync(r->overlays.p, overlays.data(), sizeof(OverlayDev) * overlays.size(),
-                               cudaMemcpyHostToDevice, s));
-        PF_TRY(cudaMemcpyAsync(r->texels.p, texels.data(), sizeof(uint32_t) * texels.size(), cudaMemcpyHostToDevice, s));
-    }
-    // Segment packing on the GPU (SegmentsD3D11::add_path): count, scan, emit.
-    PF_TRY(cudaMemsetAsync(r->counters.p, 0, sizeof(Counters), s));
-    launch_contour_segcount(r->ord_contour.p, nord, r->starts.p, r->flags.p, r->contour_segs.p, &r->counters.p->status, s);
+    PackInfo* hinfo = hs.take<PackInfo>(1);
+    uint32_t* hranges = hs.take<uint32_t>(2 * (size_t)scene_count);
+
+    // ---- packing on the device -------------------------------------------------
+    PackInfo* info = r->pack_info.p;
     ScanTemp tmp{r->scan_partials.p, (uint32_t)r->scan_partials.cap};
-    launch_scan(r->contour_segs.p, r->contour_seg_base.p, nullptr, nord, nord, 0, &r->counters.p->lines, tmp, s);
-    std::vector<uint32_t> seg_base(nord + 1, 0);
-    PF_TRY(cudaMemcpyAsync(r->h_counters, r->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, s));
-    PF_TRY(cudaMemcpyAsync(seg_base.data(), r->contour_seg_base.p, sizeof(uint32_t) * (nord + 1), cudaMemcpyDeviceToHost, s));
-    PF_TRY(cudaStreamSynchronize(s));
-    if (r->h_counters->status & kStatusMalformed) return PF_CUDA_ERR_INVALID;
-    const uint32_t S = (uint32_t)r->h_counters->lines;
-    if ((e = r->segs.ensure(S + 1)) || (e = r->seg_line_count.ensure(S + 1)) || (e = r->seg_line_base.ensure(S + 1)))
+    PF_TRY(cudaMemsetAsync(info, 0, sizeof(PackInfo), s));
+    launch_pack_starts(r->starts_raw.p, r->starts.p, r->scene_pack.p, scene_count, nb, (uint32_t)np_total, info, s);
+    const PathTablesDev t{r->path_ncont.p, r->paint.p,      r->local_index.p,   r->scene_of.p,
+                          r->clip_gpath.p, r->rule.p,       r->is_clip.p,       r->draw_index.p,
+                          r->alpha_default.p, r->blend.p,   r->overlay.p,       r->occludes.p};
+    launch_pack_paths(r->path_in.p, (uint32_t)P, r->scene_pack.p, scene_count, r->overlay_opaque.p, t, info, s);
+    launch_scan(r->path_ncont.p, r->first_ord.p, nullptr, (uint32_t)P, (uint32_t)P, 0, &info->nord, tmp, s);
+    launch_pack_chains(r->clip_gpath.p, r->is_clip.p, r->scene_of.p, r->scene_pack.p, (uint32_t)P, info, s);
+    // Segments per contour reference (SegmentsD3D11::add_path): count, scan,
+    // and the scene ranges, then one read-back.
+    auto pack_segments = [&]() -> cudaError_t {
+        tmp = ScanTemp{r->scan_partials.p, (uint32_t)r->scan_partials.cap};
+        launch_pack_order(r->path_in.p, (uint32_t)P, r->scene_pack.p, r->scene_of.p, r->path_ncont.p, r->first_ord.p,
+                          cap, r->ord_contour.p, r->ord_path.p, s);
+        launch_contour_segcount(r->ord_contour.p, &info->nord, cap, r->starts.p, nb, r->flags.p, r->contour_segs.p,
+                                &info->status, s);
+        launch_scan(r->contour_segs.p, r->contour_seg_base.p, &info->nord, 0, cap, 0, &info->segs, tmp, s);
+        launch_pack_ranges(r->scene_pack.p, scene_count, r->first_ord.p, r->contour_seg_base.p, &info->nord, cap,
+                           r->scene_ranges.p, s);
+        cudaError_t x;
+        if ((x = cudaGetLastError()) ||
+            (x = cudaMemcpyAsync(hinfo, info, sizeof(PackInfo), cudaMemcpyDeviceToHost, s)) ||
+            (scene_count && (x = cudaMemcpyAsync(hranges, r->scene_ranges.p, 8 * (size_t)scene_count,
+                                                 cudaMemcpyDeviceToHost, s))) ||
+            (x = hs.mark(s)))
+            return x;
+        return cudaStreamSynchronize(s);
+    };
+    if ((e = pack_segments())) return cuda_status(e);
+    if ((hinfo->status & kStatusMalformed) || hinfo->refs >= 0x7fffffffull) return PF_CUDA_ERR_INVALID;
+    if (hinfo->nord > cap) {  // paths share contours: grow and pack the order again
+        cap = (uint32_t)hinfo->nord;
+        if ((e = ensure_order(cap)) || (e = pack_segments())) return cuda_status(e);
+        if (hinfo->status & kStatusMalformed) return PF_CUDA_ERR_INVALID;
+    }
+    const uint32_t nord = (uint32_t)hinfo->nord;
+    if (hinfo->segs >= 0x7fffffffull) return PF_CUDA_ERR_INVALID;
+    const uint32_t S = (uint32_t)hinfo->segs;
+    if ((e = r->segs.ensure((size_t)S + 1)) || (e = r->seg_line_count.ensure((size_t)S + 1)) ||
+        (e = r->seg_line_base.ensure((size_t)S + 1)))
         return cuda_status(e);
-    launch_contour_segemit(r->ord_contour.p, r->ord_path.p, nord, r->starts.p, r->flags.p, r->contour_seg_base.p,
-                           r->segs.p, s);
+    launch_contour_segemit(r->ord_contour.p, r->ord_path.p, &info->nord, cap, r->starts.p, nb, r->flags.p,
+                           r->contour_seg_base.p, r->segs.p, s);
     PF_TRY(cudaGetLastError());
     for (uint32_t k = 0; k < scene_count; k++) {
-        SceneInfo& si = r->scenes[k];
-        const uint32_t pend = si.first_path + si.nclip + si.ndraw;
-        si.seg_begin = seg_base[first_ord[si.first_path]];
-        si.seg_end = seg_base[first_ord[pend]];
+        r->scenes[k].seg_begin = hranges[2 * k];
+        r->scenes[k].seg_end = hranges[2 * k + 1];
     }
     PF_TRY(upload_scene_records(r));
 
+    r->clip_chain_max = hinfo->chain_max;
+    r->nested_clips = (hinfo->flags & kPackNestedClips) != 0;
+    r->paint_effects = !overlays.empty() || (hinfo->flags & kPackBlendModes) != 0;
     r->P = (uint32_t)P;
-    r->ND = (uint32_t)draw_alpha.size();
-    r->draw_alpha.swap(draw_alpha);
+    r->ND = draw_base;
     r->diff_valid = false;
     r->NP = (uint32_t)np_total;
     r->NC = (uint32_t)nc_total;
@@ -791,8 +941,61 @@ int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scene
     r->fill_cap = std::max<uint32_t>(r->fill_cap, std::max<uint32_t>(1u << 18, 4 * S));
     r->line_cap = std::max<uint32_t>(r->line_cap, std::max<uint32_t>(1u << 16, 2 * S));
     r->vis_cap = std::max<uint32_t>(r->vis_cap, r->tile_cap);
-    r->has_scene = true;
-    PF_TRY(cudaStreamSynchronize(s));
+    r->has_scene = true;  // the segment records complete in stream order before any frame
+    return PF_CUDA_OK;
+}
+
+int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scenes, const PFCUDASceneTarget* targets,
+                               uint32_t scene_count) {
+    if (!r || !scenes || scene_count == 0) return PF_CUDA_ERR_INVALID;
+    PF_TRY(cudaSetDevice(r->device));
+    cudaStream_t s = r->stream;
+    release_graph(r);
+    r->has_scene = false;
+
+    uint64_t np_total = 0, nc_total = 0, P = 0;
+    for (uint32_t k = 0; k < scene_count; k++) {
+        const PFCUDASceneDesc& sc = scenes[k];
+        if (sc.memory != PF_MEMORY_HOST && sc.memory != PF_MEMORY_DEVICE) return PF_CUDA_ERR_INVALID;
+        if ((sc.clip_path_count && !sc.clip_paths) || (sc.draw_path_count && !sc.draw_paths)) return PF_CUDA_ERR_INVALID;
+        if (sc.contour_count && !sc.contour_starts) return PF_CUDA_ERR_INVALID;
+        if (sc.point_count && (!sc.points || !sc.point_flags)) return PF_CUDA_ERR_INVALID;
+        np_total += sc.point_count;
+        nc_total += (uint64_t)sc.contour_count + 1;  // each scene keeps its own end boundary
+        P += (uint64_t)sc.clip_path_count + sc.draw_path_count;
+    }
+    if (np_total >= 0x7fffffffull || nc_total >= 0x7fffffffull || P >= 0x7fffffffull) return PF_CUDA_ERR_INVALID;
+
+    // The point arrays are the bulk of an upload: their copies go first, so
+    // that from pinned memory they run while the tables are built. The flags
+    // go on the frame stream (segment packing reads them); the points, eight
+    // times larger, on the copy stream, after every earlier frame on the frame
+    // stream (which may still read the old points).
+    cudaError_t e;
+    if ((e = r->pts.ensure(np_total)) || (e = r->flags.ensure(np_total))) return cuda_status(e);
+    PF_TRY(cudaEventRecord(r->prior_done, s));
+    PF_TRY(cudaStreamWaitEvent(r->copy_stream, r->prior_done, 0));
+    uint64_t point_base = 0;
+    for (uint32_t k = 0; k < scene_count; k++) {
+        const PFCUDASceneDesc& sc = scenes[k];
+        const cudaMemcpyKind kind = sc.memory == PF_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+        if (sc.point_count)
+            PF_TRY(cudaMemcpyAsync(r->flags.p + point_base, sc.point_flags, sc.point_count, kind, s));
+        point_base += sc.point_count;
+    }
+    const int32_t rc = upload_tables(r, scenes, targets, scene_count, np_total, nc_total, P);
+    // Later work on the frame stream sees the points, and no copy that reads
+    // the caller's arrays outlives the call.
+    const cudaError_t e1 = cudaStreamWaitEvent(s, r->points_done, 0);
+    const cudaError_t e2 = cudaEventSynchronize(r->points_done);
+    if (rc != PF_CUDA_OK) {
+        cudaStreamSynchronize(s);
+        return rc;
+    }
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+        r->has_scene = false;
+        return cuda_status(e1 != cudaSuccess ? e1 : e2);
+    }
     return PF_CUDA_OK;
 }
 
@@ -813,7 +1016,22 @@ static int32_t render_plain(PFCUDARendererRef r, const PFCUDABuildOptions* optio
     const size_t elem = format == PF_CUDA_FORMAT_RGBA8 ? 4 : (format == PF_CUDA_FORMAT_R8 ? 1 : 4);
     const size_t bytes = (size_t)width * (size_t)height * elem;
     void* dst = out;
+    bool staged = false;
     if (out_memory == PF_MEMORY_HOST) {
+        // Page-locked host memory is mapped into the device's address space:
+        // the composite writes the frame there itself (no device copy and no
+        // separate device-to-host pass), and pixels outside the screen tiles
+        // keep the caller's values. Pageable memory goes through a device copy.
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, out) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+            dst = pa.devicePointer;
+        else
+            staged = true;
+        (void)cudaGetLastError();
+    } else if (out_memory != PF_MEMORY_DEVICE) {
+        return PF_CUDA_ERR_INVALID;
+    }
+    if (staged) {
         PF_TRY(r->out_tmp.ensure(bytes));
         dst = r->out_tmp.p;
         // Pixels outside every scene's screen tiles are not written: they keep
@@ -823,11 +1041,9 @@ static int32_t render_plain(PFCUDARendererRef r, const PFCUDABuildOptions* optio
             covered = covered || (!si.explicit_target && si.screen.x <= 0 && si.screen.y <= 0 &&
                                   (int64_t)si.screen.z * 16 >= width && (int64_t)si.screen.w * 16 >= height);
         if (!covered) PF_TRY(cudaMemcpyAsync(dst, out, bytes, cudaMemcpyHostToDevice, r->stream));
-    } else if (out_memory != PF_MEMORY_DEVICE) {
-        return PF_CUDA_ERR_INVALID;
     }
     rc = run_frame(r, options, format, dst, make_range(r, 0, (uint32_t)r->scenes.size()));
-    if (rc == PF_CUDA_OK && out_memory == PF_MEMORY_HOST) {
+    if (rc == PF_CUDA_OK && staged) {
         PF_TRY(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, r->stream));
         PF_TRY(cudaStreamSynchronize(r->stream));
     }
@@ -1047,14 +1263,14 @@ int32_t PFCUDAReadRecords(PFCUDARendererRef r, PFCUDAFill* fills, uint32_t* fill
         PF_TRY(cudaStreamSynchronize(s));
         // device records carry the global path index; report the index within
         // the clip paths or the draw paths, as TileObjectPrimitive::path_id
-        for (uint64_t i = 0; i < T; i++) tiles[i].path_id = r->path_local[tiles[i].path_id];
+        for (uint64_t i = 0; i < T; i++) tiles[i].path_id = path_local_of(r, tiles[i].path_id, nullptr);
     }
     if (clips && T) {
         PF_TRY(cudaMemcpyAsync(clips, r->clips.p, T * sizeof(PFCUDAClip), cudaMemcpyDeviceToHost, s));
         PF_TRY(cudaStreamSynchronize(s));
         // tiles of clip paths carry no clip record
         for (uint64_t q = 0; q < NPth; q++)
-            if (r->path_is_clip[g.p0 + q])
+            if (path_is_clip_of(r, g.p0 + q))
                 for (uint32_t t = off[q]; t < off[q + 1]; t++) clips[t] = PFCUDAClip{0xffffffffu, 0, 0xffffffffu, 0};
     }
     if (path_tile_offsets) std::memcpy(path_tile_offsets, off.data(), (NPth + 1) * sizeof(uint32_t));
@@ -1139,7 +1355,7 @@ static int32_t diff_prologue(PFCUDARendererRef r, uint32_t first, uint32_t count
         if (draw_alpha)
             PF_TRY(cudaMemcpyAsync(r->alpha_in.p, draw_alpha, sizeof(float) * r->ND, cudaMemcpyDeviceToDevice, r->stream));
         else
-            PF_TRY(cudaMemcpyAsync(r->alpha_in.p, r->draw_alpha.data(), sizeof(float) * r->ND, cudaMemcpyHostToDevice,
+            PF_TRY(cudaMemcpyAsync(r->alpha_in.p, r->alpha_default.p, sizeof(float) * r->ND, cudaMemcpyDeviceToDevice,
                                    r->stream));
     }
     r->diff_buffers = true;

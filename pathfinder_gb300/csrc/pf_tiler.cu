@@ -234,13 +234,21 @@ __device__ __forceinline__ bool is_endpoint(const uint8_t* flags, uint32_t i) {
     return (flags[i] & 3u) == 0;
 }
 
-__global__ void k_contour_segcount(const uint32_t* __restrict__ ord_contour, uint32_t nord,
-                                   const uint32_t* __restrict__ starts, const uint8_t* __restrict__ flags,
-                                   uint32_t* __restrict__ seg_count, uint32_t* status) {
+__global__ void k_contour_segcount(const uint32_t* __restrict__ ord_contour, const uint64_t* d_n, uint32_t cap,
+                                   const uint32_t* __restrict__ starts, uint32_t ncont,
+                                   const uint8_t* __restrict__ flags, uint32_t* __restrict__ seg_count,
+                                   uint32_t* status) {
     uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (k >= nord) return;
+    if (k >= scan_count(d_n, cap)) return;
     uint32_t c = ord_contour[k];
+    if (c >= ncont) {
+        if (lane == 0) {
+            atomicOr(status, kStatusMalformed);
+            seg_count[k] = 0;
+        }
+        return;
+    }
     uint32_t a = starts[c], b = starts[c + 1];
     uint32_t n = b > a ? b - a : 0;
     uint32_t count = 0;
@@ -260,13 +268,14 @@ __global__ void k_contour_segcount(const uint32_t* __restrict__ ord_contour, uin
 }
 
 __global__ void k_contour_segemit(const uint32_t* __restrict__ ord_contour, const uint32_t* __restrict__ ord_path,
-                                  uint32_t nord, const uint32_t* __restrict__ starts,
-                                  const uint8_t* __restrict__ flags, const uint32_t* __restrict__ seg_base,
-                                  SegRec* __restrict__ segs) {
+                                  const uint64_t* d_n, uint32_t cap, const uint32_t* __restrict__ starts,
+                                  uint32_t ncont, const uint8_t* __restrict__ flags,
+                                  const uint32_t* __restrict__ seg_base, SegRec* __restrict__ segs) {
     uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (k >= nord) return;
+    if (k >= scan_count(d_n, cap)) return;
     uint32_t c = ord_contour[k], gp = ord_path[k];
+    if (c >= ncont) return;  // counted as no segments
     uint32_t a = starts[c], b = starts[c + 1];
     uint32_t n = b > a ? b - a : 0;
     uint32_t out = seg_base[k];
@@ -289,19 +298,23 @@ __global__ void k_contour_segemit(const uint32_t* __restrict__ ord_contour, cons
     }
 }
 
-void launch_contour_segcount(const uint32_t* ord_contour, uint32_t nord, const uint32_t* starts, const uint8_t* flags,
-                             uint32_t* seg_count, uint32_t* status, cudaStream_t s) {
-    if (nord == 0) return;
-    uint32_t blocks = (nord * 32 + 255) / 256;
-    { count_launch(); k_contour_segcount<<<blocks, 256, 0, s>>>(ord_contour, nord, starts, flags, seg_count, status); }
+void launch_contour_segcount(const uint32_t* ord_contour, const uint64_t* d_n, uint32_t cap, const uint32_t* starts,
+                             uint32_t contour_total, const uint8_t* flags, uint32_t* seg_count, uint32_t* status,
+                             cudaStream_t s) {
+    if (cap == 0) return;
+    const uint32_t blocks = (uint32_t)(((uint64_t)cap * 32 + 255) / 256);
+    count_launch();
+    k_contour_segcount<<<blocks, 256, 0, s>>>(ord_contour, d_n, cap, starts, contour_total, flags, seg_count, status);
 }
 
-void launch_contour_segemit(const uint32_t* ord_contour, const uint32_t* ord_path, uint32_t nord,
-                            const uint32_t* starts, const uint8_t* flags, const uint32_t* seg_base, SegRec* segs,
-                            cudaStream_t s) {
-    if (nord == 0) return;
-    uint32_t blocks = (nord * 32 + 255) / 256;
-    { count_launch(); k_contour_segemit<<<blocks, 256, 0, s>>>(ord_contour, ord_path, nord, starts, flags, seg_base, segs); }
+void launch_contour_segemit(const uint32_t* ord_contour, const uint32_t* ord_path, const uint64_t* d_n, uint32_t cap,
+                            const uint32_t* starts, uint32_t contour_total, const uint8_t* flags,
+                            const uint32_t* seg_base, SegRec* segs, cudaStream_t s) {
+    if (cap == 0) return;
+    const uint32_t blocks = (uint32_t)(((uint64_t)cap * 32 + 255) / 256);
+    count_launch();
+    k_contour_segemit<<<blocks, 256, 0, s>>>(ord_contour, ord_path, d_n, cap, starts, contour_total, flags, seg_base,
+                                             segs);
 }
 
 // ---------------------------------------------------------------------------

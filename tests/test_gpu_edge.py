@@ -147,6 +147,54 @@ def test_view_box_away_from_origin_keeps_other_pixels(renderer):
     assert (img[40:60, 560:580, 3] > 0).any()
 
 
+def test_pinned_host_output_matches_pageable(renderer):
+    """A page-locked host buffer is written by the composite in place: the
+    image equals the pageable render, and pixels outside the screen tiles
+    keep the caller's values."""
+    import torch
+    rng = np.random.default_rng(5)
+    s = pf.Scene()
+    s.set_view_box(pf.RectF(0, 0, 333, 200))
+    for _ in range(40):
+        s.push_draw_path(pf.DrawPath(pf.Outline([_star(*rng.uniform(0, 333, 2), 5, 60, 7, rng)]),
+                                     pf.ColorU(*rng.integers(0, 256, 4).tolist())))
+    ref = renderer.render(s, out=np.zeros((200, 333, 4), np.uint8))
+    pinned = torch.full((200, 333, 4), 9, dtype=torch.uint8).pin_memory()
+    img = renderer.render(s, out=pinned.numpy())
+    assert np.array_equal(img, ref)
+    # a view box away from the origin: the first tile columns are not drawn
+    s.set_view_box(pf.RectF(100, 8, 333, 200))
+    pinned.fill_(77)
+    img = renderer.render(s, out=pinned.numpy())
+    ref = renderer.render(s, out=np.full((200, 333, 4), 77, np.uint8))
+    assert np.array_equal(img, ref)
+    assert (img[:, :96] == 77).all()
+
+
+def _layout_scene(dx, seed=11):
+    rng = np.random.default_rng(seed)
+    s = _scene(256, 160)
+    for _ in range(30):
+        cx, cy = rng.uniform(20, 236), rng.uniform(20, 140)
+        s.push_draw_path(pf.DrawPath(pf.Outline([_star(cx + dx, cy, 4, 30, 6, rng)]),
+                                     pf.ColorU(*rng.integers(0, 256, 4).tolist())))
+    return s
+
+
+def test_repeated_frames_follow_uploads(renderer):
+    """Frames that repeat their layout run as one captured graph from the
+    second on: the third frame replays it, and a later upload that keeps every
+    size (the same paths moved) shows in the replayed frame."""
+    a, b = _layout_scene(0.0), _layout_scene(7.25)
+    for _ in range(3):
+        _check(renderer, a)
+    _check(renderer, b)
+    opts = pf.BuildOptions(pf.Transform2F(0.75, 0.1, -0.05, 0.8, 12.5, 3.0))
+    for _ in range(3):
+        _check(renderer, b, opts)
+    _check(renderer, a, opts)
+
+
 def _bad_point_scene(kind):
     s = pf.Scene()
     s.set_view_box(pf.RectF(0, 0, 64, 64))
