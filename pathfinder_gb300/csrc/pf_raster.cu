@@ -172,6 +172,10 @@ void launch_propagate(const FrameDev& f, bool clip_pass, cudaStream_t s) {
 // visibility: count per screen tile, then scatter global tile indices
 // ---------------------------------------------------------------------------
 __global__ void k_visible(FrameDev f, int scatter) {
+    if (scatter && blockIdx.x == 0 && threadIdx.x == 0 && f.counters->visible > f.vis_cap) {
+        atomicOr(&f.counters->status, kStatusVisibleCapacity);  // the visibility scan's total
+        f.counters->needed_visible = f.counters->visible;
+    }
     uint64_t T = f.counters->tiles;
     if (!frame_ok(f)) return;
     if (scatter && f.counters->visible > f.vis_cap) return;
@@ -211,15 +215,7 @@ __global__ void k_visible(FrameDev f, int scatter) {
     }
 }
 
-__global__ void k_check_visible(FrameDev f) {
-    if (f.counters->visible > f.vis_cap) {
-        atomicOr(&f.counters->status, kStatusVisibleCapacity);
-        f.counters->needed_visible = f.counters->visible;
-    }
-}
-
 void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s) {
-    if (scatter) { count_launch(); k_check_visible<<<1, 1, 0, s>>>(f); }
     { count_launch(); k_visible<<<152 * 8, 256, 0, s>>>(f, scatter ? 1 : 0); }
 }
 

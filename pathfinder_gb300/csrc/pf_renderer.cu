@@ -418,12 +418,10 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     mark(4);
     launch_bin_emit(f, s);
     mark(5);
-    if ((e = cudaMemsetAsync(r->zbuf.p, 0, sizeof(int32_t) * nst, s))) return e;
     // clip paths first: draw tiles of clipped paths read their clip's finished tiles
     launch_propagate(f, true, s);
     launch_propagate(f, false, s);
     mark(6);
-    if ((e = cudaMemsetAsync(r->screen_cnt.p, 0, sizeof(uint32_t) * nst, s))) return e;
     launch_visible(f, false, s);
     launch_scan(r->screen_cnt.p, r->screen_base.p, nullptr, (uint32_t)(nst - 1), (uint32_t)(nst - 1), 0, &c->visible,
                 tmp, s);

@@ -380,19 +380,22 @@ void launch_bound(const FrameDev& f, const uint32_t* ord_contour, const uint32_t
     { count_launch(); k_bound<<<blocks, 256, 0, s>>>(f, ord_contour, starts); }
 }
 
-// capacity checks after the path scans
-__global__ void k_check_tiles(FrameDev f) {
-    uint64_t T = f.counters->tiles, C = f.counters->columns;
-    if (T > f.tile_cap) {
-        atomicOr(&f.counters->status, kStatusTileCapacity);
-        f.counters->needed_tiles = T;
-    }
-    if (C > f.col_cap) atomicOr(&f.counters->status, kStatusColumnCapacity);
-}
-
-// zero the per-tile accumulators of this frame
+// Zero the per-tile accumulators and the per-screen-tile z-buffer and counts
+// of this frame; block 0 also checks the path scans' totals against the
+// capacities (one kernel instead of a check kernel and two memsets).
 __global__ void k_zero_tiles(FrameDev f) {
     uint64_t T = f.counters->tiles, C = f.counters->columns;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (T > f.tile_cap) {
+            atomicOr(&f.counters->status, kStatusTileCapacity);
+            f.counters->needed_tiles = T;
+        }
+        if (C > f.col_cap) atomicOr(&f.counters->status, kStatusColumnCapacity);
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= f.screen_count; i += gridDim.x * blockDim.x) {
+        f.zbuf[i] = 0;
+        f.screen_cnt[i] = 0;
+    }
     if (T > f.tile_cap || C > f.col_cap) return;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < T || i < C;
          i += (uint64_t)gridDim.x * blockDim.x) {
@@ -409,7 +412,6 @@ void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     lanes.in[1] = f.path_cols + f.path_begin; lanes.out[1] = f.path.col_offset + f.path_begin;
     lanes.total[1] = &f.counters->columns;
     launch_scan_multi(lanes, nullptr, f.path_count, tmp, s);
-    { count_launch(); k_check_tiles<<<1, 1, 0, s>>>(f); }
     { count_launch(); k_zero_tiles<<<152 * 8, 256, 0, s>>>(f); }
 }
 
@@ -435,19 +437,16 @@ __global__ void __launch_bounds__(256) k_flatten_count(FrameDev f) {
     f.seg_line_count[s] = n;
 }
 
-__global__ void k_check_lines(FrameDev f) {
-    if (f.counters->lines > f.line_cap) {
-        atomicOr(&f.counters->status, kStatusLineCapacity);
-        f.counters->needed_lines = f.counters->lines;
-    }
-}
-
 // DIFF also records each line's segment and curve-parameter interval: the leaf
 // at split path `addr` of depth d covers t in [addr, addr + 1) / 2^d.  The
 // adjoint holds these subdivisions fixed.
 template <bool DIFF>
 __global__ void __launch_bounds__(256) k_flatten_emit(FrameDev f) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0 && f.counters->lines > f.line_cap) {  // the flattening scan's total against the capacity
+        atomicOr(&f.counters->status, kStatusLineCapacity);
+        f.counters->needed_lines = f.counters->lines;
+    }
     if (s >= f.seg_count || f.counters->lines > f.line_cap) return;
     const uint32_t sg = f.seg_begin + s;
     const SegRec sr = f.segs[sg];
@@ -483,7 +482,6 @@ void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     const uint32_t blocks = (f.seg_count + ft - 1) / ft;
     { count_launch(); k_flatten_count<<<blocks, ft, 0, s>>>(f); }
     launch_scan(f.seg_line_count, f.seg_line_base, nullptr, f.seg_count, f.seg_count, 0, &f.counters->lines, tmp, s);
-    { count_launch(); k_check_lines<<<1, 1, 0, s>>>(f); }
     count_launch();
     if (f.diff) k_flatten_emit<true><<<blocks, ft, 0, s>>>(f);
     else k_flatten_emit<false><<<blocks, ft, 0, s>>>(f);
@@ -575,6 +573,13 @@ struct EmitSinkF {
 
 template <int MODE>
 __global__ void __launch_bounds__(512) k_bin_emit(FrameDev f) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // the binning scans' totals against the capacities
+        if (f.counters->fills > f.fill_cap) {
+            atomicOr(&f.counters->status, kStatusFillCapacity);
+            f.counters->needed_fills = f.counters->fills;
+        }
+        if (f.counters->alpha_tiles > f.tile_cap) atomicOr(&f.counters->status, kStatusAlphaCapacity);
+    }
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     if (f.counters->fills > f.fill_cap) return;
     const uint32_t L = line_total(f);
@@ -604,16 +609,7 @@ void launch_bin_count(const FrameDev& f, cudaStream_t s) {
     else k_bin_count<kFillCpu><<<blocks, f.tune.bin_threads, 0, s>>>(f);
 }
 
-__global__ void k_check_fills(FrameDev f) {
-    if (f.counters->fills > f.fill_cap) {
-        atomicOr(&f.counters->status, kStatusFillCapacity);
-        f.counters->needed_fills = f.counters->fills;
-    }
-    if (f.counters->alpha_tiles > f.tile_cap) atomicOr(&f.counters->status, kStatusAlphaCapacity);
-}
-
 void launch_bin_emit(const FrameDev& f, cudaStream_t s) {
-    { count_launch(); k_check_fills<<<1, 1, 0, s>>>(f); }
     count_launch();
     const uint32_t blocks = 152 * f.tune.bin_blocks_per_sm;
     const int m = fill_mode(f);
