@@ -14,6 +14,7 @@
 // paths, segments and screen tiles of any contiguous range of scenes are
 // contiguous and one frame covers such a range.
 #include "pf_kernels.cuh"
+#include <cuda.h>
 #include "../../include/pathfinder_cuda.h"
 
 #include <algorithm>
@@ -1002,6 +1003,30 @@ int32_t PFCUDASceneUpload(PFCUDARendererRef r, const PFCUDASceneDesc* sc) {
     return PFCUDASceneUploadBatch(r, sc, nullptr, 1);
 }
 
+// Whether [p, p + bytes) lies inside one page-locked host allocation, asked
+// of the driver (cuPointerGetAttribute's range attributes, looked up through
+// the runtime so that nothing links the driver library). Any failure is a no.
+static bool inside_host_allocation(const void* p, size_t bytes) {
+    using GetAttr = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+    static GetAttr get = [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            fn = nullptr;
+        return (GetAttr)fn;
+    }();
+    if (!get) return false;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    const CUdeviceptr a = (CUdeviceptr)(uintptr_t)p;
+    if (get(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, a) != CUDA_SUCCESS ||
+        get(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, a) != CUDA_SUCCESS)
+        return false;
+    return start <= a && bytes <= size && a - start <= size - bytes;
+}
+
 static int32_t render_plain(PFCUDARendererRef r, const PFCUDABuildOptions* options, int32_t width, int32_t height,
                             void* out, int32_t out_memory, int32_t format) {
     if (!r || !out) return PF_CUDA_ERR_INVALID;
@@ -1020,8 +1045,10 @@ static int32_t render_plain(PFCUDARendererRef r, const PFCUDABuildOptions* optio
         // the composite writes the frame there itself (no device copy and no
         // separate device-to-host pass), and pixels outside the screen tiles
         // keep the caller's values. Pageable memory goes through a device copy.
+        // The whole image must lie in the one allocation: the GPU writes it.
         cudaPointerAttributes pa{};
-        if (cudaPointerGetAttributes(&pa, out) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+        if (cudaPointerGetAttributes(&pa, out) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+            inside_host_allocation(out, bytes))
             dst = pa.devicePointer;
         else
             staged = true;

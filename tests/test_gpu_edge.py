@@ -169,6 +169,12 @@ def test_pinned_host_output_matches_pageable(renderer):
     ref = renderer.render(s, out=np.full((200, 333, 4), 77, np.uint8))
     assert np.array_equal(img, ref)
     assert (img[:, :96] == 77).all()
+    # an image inside a larger page-locked allocation, rows around it untouched
+    big = torch.full((210, 333, 4), 5, dtype=torch.uint8).pin_memory()
+    view = big.numpy()[4:204]
+    img = renderer.render(s, out=view)
+    assert np.array_equal(img[:, 96:], ref[:, 96:]) and (img[:, :96] == 5).all()
+    assert (big.numpy()[:4] == 5).all() and (big.numpy()[204:] == 5).all()
 
 
 def _layout_scene(dx, seed=11):
