@@ -652,6 +652,7 @@ def main():
         run_strokes(args)
         return
 
+    import numpy as np
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -750,14 +751,14 @@ def main():
     # e2e through the public API with host buffers
     e2e_steps = args.e2e_steps or max(3, min(args.steps, 20))
     pinned = {}
-    for name in ("points", "flags", "contour_starts"):
+    for name in ("points", "flags", "contour_starts", "clip_paths", "draw_paths"):
         a = getattr(scene, name)
-        t = torch.from_numpy(a.copy()).pin_memory()
+        t = torch.from_numpy(a.view(np.uint8).reshape(-1).copy()).pin_memory()  # path records as bytes
         pinned[name] = t
-        setattr(scene, name, t.numpy())
+        setattr(scene, name, t.numpy().view(a.dtype).reshape(a.shape))
     host_out = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
     host_np = host_out.numpy()
-    h2d = scene.points.nbytes + scene.flags.nbytes + scene.contour_starts.nbytes
+    h2d = sum(getattr(scene, n).nbytes for n in ("points", "flags", "contour_starts", "clip_paths", "draw_paths"))
     d2h = host_np.nbytes
     r.set_profiling(False)
     for _ in range(2):

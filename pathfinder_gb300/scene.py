@@ -221,11 +221,27 @@ class Scene:
 
     # --- C ABI view -----------------------------------------------------------
     def desc(self) -> _abi.PFCUDASceneDesc:
-        """PFCUDASceneDesc pointing at this scene's host buffers."""
+        """PFCUDASceneDesc pointing at this scene's host buffers.  The same
+        epoch and buffers give the same descriptor, built once."""
         for name in ("points", "flags", "contour_starts", "clip_paths", "draw_paths"):
             a = getattr(self, name)
             if not a.flags["C_CONTIGUOUS"]:
                 setattr(self, name, np.ascontiguousarray(a))
+        vb = self.view_box
+        key = (self.epoch, vb.x0, vb.y0, vb.x1, vb.y1) + tuple(
+            (a.ctypes.data, a.shape[0]) for a in (self.points, self.flags, self.contour_starts, self.clip_paths,
+                                                  self.draw_paths))
+        cached = getattr(self, "_desc_cache", None)
+        if cached is not None and cached[0] == key:
+            return cached[1]
+        d = self._build_desc()
+        # gradients and patterns are converted when the descriptor is made:
+        # a scene with any is described afresh every time, so that edits of
+        # those objects are seen
+        self._desc_cache = (key, d) if not (self.gradients or self.patterns) else None
+        return d
+
+    def _build_desc(self) -> _abi.PFCUDASceneDesc:
         d = _abi.PFCUDASceneDesc()
         d.points = self.points.ctypes.data
         d.point_flags = self.flags.ctypes.data
