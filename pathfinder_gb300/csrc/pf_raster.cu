@@ -245,6 +245,21 @@ __device__ void warp_bitonic_sort(K* a, uint32_t n) {
     }
 }
 
+// Ascending bitonic sort of one key per lane over lanes [0, N), N a power of
+// two no larger than 32; lanes past the list hold the largest key.  Shuffles
+// only: no shared memory and no warp barriers.
+__device__ __forceinline__ unsigned long long warp_sort_lanes(unsigned long long v, uint32_t N) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t k = 2; k <= N; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            const unsigned long long o = __shfl_xor_sync(0xffffffffu, v, j);
+            const bool ascending = (lane & k) == 0, low = (lane & j) == 0;
+            v = (ascending == low) ? (o < v ? o : v) : (o > v ? o : v);
+        }
+    }
+    return v;
+}
+
 struct __align__(16) CovBuf { int acc[256]; int carry[256]; };  // cleared with int4 stores
 
 // Accumulate fills [b0, b1) (one alpha tile's) into `buf` (one warp).  DIFF
@@ -722,8 +737,11 @@ struct CompositeScratch {
     CovBuf b0, b1;
 };
 
+// Without paint effects the kernel is held to 80 registers (24 warps an SM):
+// fewer registers than it would take, a few spilled, and more warps to hide
+// the latency of each visible tile's dependent steps.
 template <int MODE, int WARPS, bool PAINT>
-__global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out, float4 bg) {
+__global__ void __launch_bounds__(WARPS * 32, PAINT ? 1 : 24 / WARPS) k_composite(FrameDev f, void* out, float4 bg) {
     extern __shared__ __align__(16) unsigned char comp_smem[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t st = blockIdx.x * WARPS + wid;  // frame screen tile
@@ -734,7 +752,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
     const int4 s = sc.screen;
     const int32_t sw = s.z - s.x;
     const uint32_t lst = f.screen_begin + st - sc.screen_offset;
-    const int32_t tx = s.x + (int32_t)(lst % (uint32_t)sw), ty = s.y + (int32_t)(lst / (uint32_t)sw);
+    const uint32_t row = lst / (uint32_t)sw;
+    const int32_t tx = s.x + (int32_t)(lst - row * (uint32_t)sw), ty = s.y + (int32_t)row;
     const int col = lane & 15, half = lane >> 4;
 
     const bool ok = frame_ok(f) && f.counters->fills <= f.fill_cap && f.counters->visible <= f.vis_cap;
@@ -742,14 +761,24 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
     if (ok) { base = f.screen_base[st]; n = f.screen_base[st + 1] - base; }
 
     // draw order = global tile order (paths in order)
-    const bool short_list = n <= kWarpListCap;
-    if (short_list) {
+    const bool short_list = n <= kWarpListCap, lane_list = n <= 32;  // up to 32: one key per lane
+    unsigned long long lane_key = ~0ull;
+    if (lane_list) {
+        if ((uint32_t)lane < n) {
+            lane_key = ((unsigned long long)f.vis[base + lane] << 32) | (uint32_t)lane;
+            ws.info[lane] = f.vis_info[base + lane];
+        }
+        uint32_t N = 1;
+        while (N < n) N <<= 1;
+        if (n > 1) lane_key = warp_sort_lanes(lane_key, N);
+        __syncwarp();
+    } else if (short_list) {
         for (uint32_t i = lane; i < n; i += 32) {
             ws.keys[i] = ((unsigned long long)f.vis[base + i] << 32) | i;
             ws.info[i] = f.vis_info[base + i];
         }
         __syncwarp();
-        if (n > 1) warp_bitonic_sort(ws.keys, n);
+        warp_bitonic_sort(ws.keys, n);
     } else {
         warp_bitonic_sort(f.vis + base, n);  // rare: long lists sort in place in global memory
     }
@@ -764,7 +793,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
         int4 info = make_int4(0, 0, 0, 0);
         uint32_t g;
         if (short_list) {
-            const unsigned long long key = ws.keys[i];
+            const unsigned long long key = lane_list ? __shfl_sync(0xffffffffu, lane_key, (int)i) : ws.keys[i];
             g = (uint32_t)(key >> 32);
             info = ws.info[(uint32_t)key];
             kind = ((uint32_t)info.w >> 9) & 3u;
@@ -816,12 +845,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite(FrameDev f, void* out,
     }
     const int X = tx * 16 + col;
     if (X < sc.clip.x || X >= sc.clip.z) return;
+    const int Y0 = ty * 16 + half * 8;
+    const bool rows_inside = Y0 >= sc.clip.y && Y0 + 8 <= sc.clip.w;
+    uint64_t o = sc.out_offset + (uint64_t)(int64_t)(Y0 - sc.origin_y) * (uint64_t)(int64_t)sc.pitch +
+                 (uint64_t)(int64_t)(X - sc.origin_x);
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const int Y = ty * 16 + half * 8 + k;
-        if (Y < sc.clip.y || Y >= sc.clip.w) continue;
-        const uint64_t o = sc.out_offset + (uint64_t)(int64_t)(Y - sc.origin_y) * (uint64_t)(int64_t)sc.pitch +
-                           (uint64_t)(int64_t)(X - sc.origin_x);
+    for (int k = 0; k < 8; k++, o += (uint64_t)(int64_t)sc.pitch) {
+        if (!rows_inside && (Y0 + k < sc.clip.y || Y0 + k >= sc.clip.w)) continue;
         if (MODE == 0) {
             auto q = [](float v) { return (uint32_t)__float2uint_rn(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f); };
             ((uint32_t*)out)[o] = q(d0[k]) | (q(d1[k]) << 8) | (q(d2[k]) << 16) | (q(d3[k]) << 24);
