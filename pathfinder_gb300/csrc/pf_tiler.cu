@@ -415,12 +415,15 @@ void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     { count_launch(); k_zero_tiles<<<152 * 8, 256, 0, s>>>(f); }
 }
 
+// Launch bounds of the flattening and binning passes: at most 42 registers a
+// thread (48 warps an SM at their block sizes), which they fit without spills;
+// the extra warps hide their gather and atomic latency.
 // ---------------------------------------------------------------------------
 // flattening: one thread per input segment (process_segment's recursion,
 // renderer/src/tiler.rs:166-184).  Lines are written in emission order: input
 // segments in path order, each segment's lines depth first.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_flatten_count(FrameDev f) {
+__global__ void __launch_bounds__(256, 6) k_flatten_count(FrameDev f) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= f.seg_count) return;
     uint32_t n = 0;
@@ -441,7 +444,7 @@ __global__ void __launch_bounds__(256) k_flatten_count(FrameDev f) {
 // at split path `addr` of depth d covers t in [addr, addr + 1) / 2^d.  The
 // adjoint holds these subdivisions fixed.
 template <bool DIFF>
-__global__ void __launch_bounds__(256) k_flatten_emit(FrameDev f) {
+__global__ void __launch_bounds__(256, 6) k_flatten_emit(FrameDev f) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s == 0 && f.counters->lines > f.line_cap) {  // the flattening scan's total against the capacity
         atomicOr(&f.counters->status, kStatusLineCapacity);
@@ -530,7 +533,7 @@ struct CountSink {
 };
 
 template <int MODE>
-__global__ void __launch_bounds__(512) k_bin_count(FrameDev f) {
+__global__ void __launch_bounds__(512, 3) k_bin_count(FrameDev f) {
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     const uint32_t L = line_total(f);
     for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
@@ -572,7 +575,7 @@ struct EmitSinkF {
 };
 
 template <int MODE>
-__global__ void __launch_bounds__(512) k_bin_emit(FrameDev f) {
+__global__ void __launch_bounds__(512, 3) k_bin_emit(FrameDev f) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {  // the binning scans' totals against the capacities
         if (f.counters->fills > f.fill_cap) {
             atomicOr(&f.counters->status, kStatusFillCapacity);
