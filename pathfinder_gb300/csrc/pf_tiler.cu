@@ -56,6 +56,22 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* t
     return r;
 }
 
+// Sum over the block (blockDim.x == NT), valid in thread 0.
+template <int NT>
+__device__ __forceinline__ uint32_t block_sum(uint32_t v) {
+    __shared__ uint32_t warp_part[NT / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) warp_part[wid] = v;
+    __syncthreads();
+    uint32_t t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < NT / 32; w++) t += warp_part[w];
+    __syncthreads();  // the next call reuses warp_part
+    return t;
+}
+
 // ---------------------------------------------------------------------------
 // generic exclusive scan (reduce, scan partials, down-sweep)
 // ---------------------------------------------------------------------------
@@ -83,8 +99,7 @@ __global__ void k_scan_reduce(const uint32_t* __restrict__ in, const uint64_t* d
     uint32_t s = 0;
 #pragma unroll
     for (int k = 0; k < kScanItems; k++) s += scan_in(in, base + k * kScanThreads + threadIdx.x, n, mode);
-    uint32_t total;
-    block_exclusive_scan<kScanThreads>(s, &total);
+    const uint32_t total = block_sum<kScanThreads>(s);
     if (threadIdx.x == 0) partials[blockIdx.x] = total;
 }
 
@@ -142,25 +157,30 @@ void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_
 // reduce / partials / down-sweep set (the per-tile fill offsets, alpha ids and
 // column backdrop prefixes share their length)
 // ---------------------------------------------------------------------------
+// NL lanes, indexed at compile time (a runtime lane index would copy the
+// lane table to local memory).
+template <int NL>
 __global__ void k_scanm_reduce(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, uint32_t* __restrict__ partials) {
     const uint32_t n = scan_count(d_n, n_cap);
     const uint32_t base = blockIdx.x * kScanChunk;
     if (base >= n) return;
     const uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
-    for (int l = 0; l < L.count; l++) {
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
         uint32_t s = 0;
 #pragma unroll
         for (int k = 0; k < kScanItems; k++) s += scan_in(L.in[l], base + k * kScanThreads + threadIdx.x, n, L.mode[l]);
-        uint32_t total;
-        block_exclusive_scan<kScanThreads>(s, &total);
+        const uint32_t total = block_sum<kScanThreads>(s);
         if (threadIdx.x == 0) partials[l * nb + blockIdx.x] = total;
     }
 }
 
+template <int NL>
 __global__ void k_scanm_partials(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, uint32_t* partials) {
     const uint32_t n = scan_count(d_n, n_cap);
     const uint32_t nb = (n + kScanChunk - 1) / kScanChunk, nbc = (n_cap + kScanChunk - 1) / kScanChunk;
-    for (int l = 0; l < L.count; l++) {
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
         uint32_t carry = 0;
         uint32_t* p = partials + l * nbc;
         for (uint32_t b0 = 0; b0 < nb; b0 += 1024) {
@@ -178,13 +198,15 @@ __global__ void k_scanm_partials(ScanLanes L, const uint64_t* d_n, uint32_t n_ca
     }
 }
 
+template <int NL>
 __global__ void k_scanm_down(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, const uint32_t* __restrict__ partials) {
     const uint32_t n = scan_count(d_n, n_cap);
     const uint32_t base = blockIdx.x * kScanChunk;
     if (base >= n) return;
     const uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
     const uint32_t first = base + threadIdx.x * kScanItems;
-    for (int l = 0; l < L.count; l++) {
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
         uint32_t v[kScanItems];
         uint32_t s = 0;
 #pragma unroll
@@ -199,12 +221,20 @@ __global__ void k_scanm_down(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, c
     }
 }
 
-void launch_scan_multi(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp, cudaStream_t s) {
+template <int NL>
+static void launch_scan_lanes(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp,
+                              cudaStream_t s) {
     uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
     if (nb == 0) nb = 1;
-    { count_launch(); k_scanm_reduce<<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
-    { count_launch(); k_scanm_partials<<<1, 1024, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
-    { count_launch(); k_scanm_down<<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+    { count_launch(); k_scanm_reduce<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+    { count_launch(); k_scanm_partials<NL><<<1, 1024, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+    { count_launch(); k_scanm_down<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+}
+
+void launch_scan_multi(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp, cudaStream_t s) {
+    if (lanes.count == 1) launch_scan_lanes<1>(lanes, d_n, n_cap, tmp, s);
+    else if (lanes.count == 2) launch_scan_lanes<2>(lanes, d_n, n_cap, tmp, s);
+    else launch_scan_lanes<3>(lanes, d_n, n_cap, tmp, s);
 }
 
 // ---------------------------------------------------------------------------
