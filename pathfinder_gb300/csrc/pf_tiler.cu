@@ -91,14 +91,45 @@ __device__ __forceinline__ uint32_t scan_in(const uint32_t* in, uint32_t i, uint
     return mode == 1 ? (v != 0u ? 1u : 0u) : v;
 }
 
+// A thread's kScanItems consecutive values from `first` (a multiple of
+// kScanItems): two 16-byte accesses when the run lies inside [0, n) and the
+// array is 16-byte aligned, else one value at a time.
+static_assert(kScanItems == 8, "load8 / store8 move eight values");
+__device__ __forceinline__ void load8(const uint32_t* in, uint32_t first, uint32_t n, int mode, uint32_t (&v)[8]) {
+    if (first + 8 <= n && ((uintptr_t)in & 15u) == 0) {
+        const uint4 a = *reinterpret_cast<const uint4*>(in + first);
+        const uint4 b = *reinterpret_cast<const uint4*>(in + first + 4);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        if (mode == 1) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) v[k] = v[k] != 0u ? 1u : 0u;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = scan_in(in, first + k, n, mode);
+    }
+}
+
+__device__ __forceinline__ void store8(uint32_t* out, uint32_t first, uint32_t n, const uint32_t (&e)[8]) {
+    if (first + 8 <= n && ((uintptr_t)out & 15u) == 0) {
+        *reinterpret_cast<uint4*>(out + first) = make_uint4(e[0], e[1], e[2], e[3]);
+        *reinterpret_cast<uint4*>(out + first + 4) = make_uint4(e[4], e[5], e[6], e[7]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (first + k < n) out[first + k] = e[k];
+    }
+}
+
 __global__ void k_scan_reduce(const uint32_t* __restrict__ in, const uint64_t* d_n, uint32_t n_host, int mode,
                               uint32_t* __restrict__ partials) {
     uint32_t n = scan_count(d_n, n_host);
     uint32_t base = blockIdx.x * kScanChunk;
     if (base >= n) return;
-    uint32_t s = 0;
+    uint32_t v[kScanItems], s = 0;
+    load8(in, base + threadIdx.x * kScanItems, n, mode, v);
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) s += scan_in(in, base + k * kScanThreads + threadIdx.x, n, mode);
+    for (int k = 0; k < kScanItems; k++) s += v[k];
     const uint32_t total = block_sum<kScanThreads>(s);
     if (threadIdx.x == 0) partials[blockIdx.x] = total;
 }
@@ -131,15 +162,18 @@ __global__ void k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restric
     uint32_t v[kScanItems];
     uint32_t s = 0;
     uint32_t first = base + threadIdx.x * kScanItems;
+    load8(in, first, n, mode, v);
 #pragma unroll
-    for (int k = 0; k < kScanItems; k++) { v[k] = scan_in(in, first + k, n, mode); s += v[k]; }
+    for (int k = 0; k < kScanItems; k++) s += v[k];
     uint32_t total;
     uint32_t ex = block_exclusive_scan<kScanThreads>(s, &total) + partials[blockIdx.x];
+    uint32_t e[kScanItems];
 #pragma unroll
     for (int k = 0; k < kScanItems; k++) {
-        if (first + k < n) out[first + k] = ex;
+        e[k] = ex;
         ex += v[k];
     }
+    store8(out, first, n, e);
 }
 
 void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_t n_host, uint32_t n_cap, int mode,
@@ -167,9 +201,10 @@ __global__ void k_scanm_reduce(ScanLanes L, const uint64_t* d_n, uint32_t n_cap,
     const uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
 #pragma unroll
     for (int l = 0; l < NL; l++) {
-        uint32_t s = 0;
+        uint32_t v[kScanItems], s = 0;
+        load8(L.in[l], base + threadIdx.x * kScanItems, n, L.mode[l], v);
 #pragma unroll
-        for (int k = 0; k < kScanItems; k++) s += scan_in(L.in[l], base + k * kScanThreads + threadIdx.x, n, L.mode[l]);
+        for (int k = 0; k < kScanItems; k++) s += v[k];
         const uint32_t total = block_sum<kScanThreads>(s);
         if (threadIdx.x == 0) partials[l * nb + blockIdx.x] = total;
     }
@@ -209,15 +244,18 @@ __global__ void k_scanm_down(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, c
     for (int l = 0; l < NL; l++) {
         uint32_t v[kScanItems];
         uint32_t s = 0;
+        load8(L.in[l], first, n, L.mode[l], v);
 #pragma unroll
-        for (int k = 0; k < kScanItems; k++) { v[k] = scan_in(L.in[l], first + k, n, L.mode[l]); s += v[k]; }
+        for (int k = 0; k < kScanItems; k++) s += v[k];
         uint32_t total;
         uint32_t ex = block_exclusive_scan<kScanThreads>(s, &total) + partials[l * nb + blockIdx.x];
+        uint32_t e[kScanItems];
 #pragma unroll
         for (int k = 0; k < kScanItems; k++) {
-            if (first + k < n) L.out[l][first + k] = ex;
+            e[k] = ex;
             ex += v[k];
         }
+        store8(L.out[l], first, n, e);
     }
 }
 
