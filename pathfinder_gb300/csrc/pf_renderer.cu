@@ -210,6 +210,10 @@ struct PFCUDARenderer {
     DevBuf<float> grad_mask, grad_alpha_tmp;
     bool diff_buffers = false;         // allocate the buffers above with the frame's
     bool last_diff = false;            // the last enqueued frame was differentiable
+    // Fill emission indices are written only by a frame that PFCUDAReadRecords
+    // runs for them (fill_order); last_opts is the options of the last frame.
+    bool fill_order = false, last_fill_order = false;
+    PFCUDABuildOptions last_opts{};
     bool diff_valid = false;           // PFCUDABackward may run on the last frame
     Range diff_range;
     bool diff_transformed = false;
@@ -310,7 +314,7 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.line_fill_base = r->line_fill_base.p;
     f.line_cap = r->line_cap;
     f.fills = r->fills.p;
-    f.fill_e = r->fill_e.p;
+    f.fill_e = r->fill_order ? r->fill_e.p : nullptr;
     f.tiles = r->tiles.p;
     f.clips = r->clips.p;
     f.alpha_owner = r->alpha_owner.p;
@@ -377,6 +381,8 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
         launch_transform(r->pts.p, r->pts_t.p, r->NP, m6, s);
     }
     r->last_diff = diff;
+    r->last_fill_order = r->fill_order;
+    if (opts != &r->last_opts) r->last_opts = opts ? *opts : PFCUDABuildOptions{};
     if (!diff) r->diff_valid = false;
     FrameDev f = frame_dev(r, transformed, g, diff);
     if (transformed) {  // gradients are evaluated at pixel centres mapped back to scene space
@@ -578,6 +584,8 @@ cudaError_t enqueue_plain(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
         }
     }
     r->last_diff = false;
+    r->last_fill_order = r->fill_order;  // part of the key
+    if (opts != &r->last_opts) r->last_opts = opts ? *opts : PFCUDABuildOptions{};
     r->diff_valid = false;
     return cudaGraphLaunch(r->replay_exec, r->stream);
 }
@@ -1256,6 +1264,16 @@ int32_t PFCUDAReadRecords(PFCUDARendererRef r, PFCUDAFill* fills, uint32_t* fill
     const Range& g = r->last;
     const uint64_t F = r->stats.fill_count, T = r->stats.tile_count, NPth = g.p1 - g.p0, NST = g.st1 - g.st0;
     if (fills && r->last_diff) return PF_CUDA_ERR_INVALID;  // differentiable frames keep FP32 fills only
+    if (fills && F && !r->last_fill_order) {
+        // the frame again, without composite, with each fill's emission index
+        r->fill_order = true;
+        const int32_t rc = run_frame(r, &r->last_opts, -1, nullptr, g);
+        r->fill_order = false;
+        // malformed input or a limit reached ends the frame as before; its
+        // records are still read
+        if (rc != PF_CUDA_OK && rc != PF_CUDA_ERR_INVALID && rc != PF_CUDA_ERR_LIMIT) return rc;
+        if (r->stats.fill_count != F) return PF_CUDA_ERR_LAUNCH;
+    }
     if ((fills || fill_tile) && fill_capacity < F) return PF_CUDA_ERR_CAPACITY;
     if ((tiles || clips) && tile_capacity < T) return PF_CUDA_ERR_CAPACITY;
     if ((path_tile_offsets || path_tile_rects) && path_capacity < NPth + 1) return PF_CUDA_ERR_CAPACITY;

@@ -613,6 +613,9 @@ __global__ void __launch_bounds__(512, 3) k_bin_count(FrameDev f) {
     }
 }
 
+// ORDER also writes each fill's emission index (only frames run for record
+// read-back do: the order of fills within a tile changes no output).
+template <bool ORDER>
 struct EmitSink {
     uint2* fills;
     uint32_t* fill_e;
@@ -621,10 +624,12 @@ struct EmitSink {
     uint32_t fill_cap;
     uint32_t e;
     __device__ __forceinline__ void fill(uint2 rec, uint32_t g) {
-        // the order of fills within a tile does not change any output
         const uint32_t slot = tile_fill_base[g] + atomicSub(&cursor[g], 1u) - 1u;
-        if (slot < fill_cap) { fills[slot] = rec; fill_e[slot] = e; }
-        e++;
+        if (slot < fill_cap) {
+            fills[slot] = rec;
+            if (ORDER) fill_e[slot] = e;
+        }
+        if (ORDER) e++;
     }
     __device__ __forceinline__ void backdrop(int32_t, int32_t, int32_t) {}
 };
@@ -642,7 +647,7 @@ struct EmitSinkF {
     __device__ __forceinline__ void backdrop(int32_t, int32_t, int32_t) {}
 };
 
-template <int MODE>
+template <int MODE, bool ORDER>
 __global__ void __launch_bounds__(512, 3) k_bin_emit(FrameDev f) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {  // the binning scans' totals against the capacities
         if (f.counters->fills > f.fill_cap) {
@@ -662,7 +667,8 @@ __global__ void __launch_bounds__(512, 3) k_bin_emit(FrameDev f) {
             EmitSinkF sink{f.fills_f, f.tile_fill_base, f.tile_fill_count, f.fill_cap};
             dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
         } else {
-            EmitSink sink{f.fills, f.fill_e, f.tile_fill_base, f.tile_fill_count, f.fill_cap, f.line_fill_base[l]};
+            EmitSink<ORDER> sink{f.fills, f.fill_e, f.tile_fill_base, f.tile_fill_count, f.fill_cap,
+                                 ORDER ? f.line_fill_base[l] : 0u};
             dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
         }
     }
@@ -684,9 +690,13 @@ void launch_bin_emit(const FrameDev& f, cudaStream_t s) {
     count_launch();
     const uint32_t blocks = 152 * f.tune.bin_blocks_per_sm;
     const int m = fill_mode(f);
-    if (m == kFillF32) k_bin_emit<kFillF32><<<blocks, f.tune.bin_threads, 0, s>>>(f);
-    else if (m == kFillD3D11) k_bin_emit<kFillD3D11><<<blocks, f.tune.bin_threads, 0, s>>>(f);
-    else k_bin_emit<kFillCpu><<<blocks, f.tune.bin_threads, 0, s>>>(f);
+    const int t = f.tune.bin_threads;
+    const bool order = f.fill_e != nullptr;
+    if (m == kFillF32) k_bin_emit<kFillF32, false><<<blocks, t, 0, s>>>(f);
+    else if (m == kFillD3D11 && order) k_bin_emit<kFillD3D11, true><<<blocks, t, 0, s>>>(f);
+    else if (m == kFillD3D11) k_bin_emit<kFillD3D11, false><<<blocks, t, 0, s>>>(f);
+    else if (order) k_bin_emit<kFillCpu, true><<<blocks, t, 0, s>>>(f);
+    else k_bin_emit<kFillCpu, false><<<blocks, t, 0, s>>>(f);
 }
 
 }  // namespace pf
