@@ -116,7 +116,7 @@ struct Range {
     uint32_t st0 = 0, st1 = 0;   // screen tiles
 };
 
-const TuneParams kDefaultTune{128, 256, 16, 4};
+const TuneParams kDefaultTune{128, 256, 32, 2};
 
 }  // namespace
 
