@@ -400,10 +400,18 @@ __global__ void k_bound(FrameDev f, const uint32_t* __restrict__ ord_contour, co
         uint32_t c = ord_contour[k];
         uint32_t a = starts[c], b = starts[c + 1];
         if (b > a) any = true;
-        for (uint32_t i = a + lane; i < b; i += 32) {
-            float2 p = f.pts[i];
-            mnx = smin(mnx, p.x); mny = smin(mny, p.y);
-            mxx = smax(mxx, p.x); mxy = smax(mxy, p.y);
+        // four loads in flight per lane; each lane still folds its points
+        // in the same order (i, i + 32, i + 64, ...)
+        for (uint32_t i = a + lane; i < b; i += 128) {
+            float2 p[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) p[u] = i + 32u * u < b ? f.pts[i + 32u * u] : make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (i + 32u * u >= b) break;
+                mnx = smin(mnx, p[u].x); mny = smin(mny, p[u].y);
+                mxx = smax(mxx, p[u].x); mxy = smax(mxy, p[u].y);
+            }
         }
     }
 #pragma unroll
