@@ -134,16 +134,30 @@ def stage_bytes(st, npts: int, nseg: int) -> dict:
     }
 
 
+def svg_config(scene, args, paints, world: int = 1) -> dict:
+    """The `config` of a 4K-scene line, the same in both arms."""
+    return {"workload": (WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}_scale{args.scale}")
+                        + ("_paints" if paints else ""),
+            **({"paints": paints} if paints else {}),
+            "paths": len(scene.draw_paths), "clip_paths": len(scene.clip_paths), "segments": scene.segment_count,
+            "points": len(scene.points), "width": W, "height": H, "seed": args.seed,
+            "l2": "GPU arm: flushed between steps (512 MiB write); CPU arm: frames far larger than the host caches",
+            "parallelism": f"replicas{world}",
+            "tiling": "d3d11 level (uniform dicing)" if args.d3d11 else "cpu tiler (bit-exact)"}
+
+
 def run_reference(args) -> None:
+    """The reference arm: the oracle's CPU restatement of the reference's
+    Rayon + SIMD CPU tiling path on all host threads.  It loads only the
+    oracle's library (which carries its own copy of the scene generator), not
+    the CUDA renderer."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     import pathfinder_gb300 as pf
     import oracle
-    from pathfinder_gb300 import build as pbuild
-    pbuild.build()
     oracle.build()
-    scene = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=args.seed)
+    scene = oracle.generate_scene(pf.PF_SCENE_SVG_4K, seed=args.seed, scale=args.scale)
     paints = add_paints(scene, args.seed) if args.paints else None
     nseg = scene.segment_count
     threads = os.cpu_count() or 1
@@ -159,9 +173,8 @@ def run_reference(args) -> None:
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": METRIC,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded, PF_SCENE_SVG_4K)",
-        "config": {"workload": WORKLOAD + ("_paints" if paints else ""), "paths": 20000, "segments": nseg,
-                   "width": W, "height": H, "seed": args.seed, **({"paints": paints} if paints else {})},
+        "data": "synthetic (seeded PF_SCENE_SVG_4K: 20,000 log-normal star paths, 40/30/30 line/quad/cubic)",
+        "config": svg_config(scene, args, paints),
         "cpu_baseline": {"value": round(value, 4), "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} full frames of the 4K scene (tiling + FP32 coverage + composite)"},
         "e2e": {"value": round(value, 4), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -235,18 +248,26 @@ def cpu_baseline(scene, nseg: int, budget_s: float = 12.0) -> dict:
 
 
 def run_atlas(args) -> None:
+    """The 16,384-glyph 4096x4096 R8 atlas as its own bench line."""
+    import torch
+    from pathfinder_gb300 import build as pbuild
+    pbuild.build()
+    torch.cuda.set_device(0)
+    line = atlas_measure(args.seed, args.scale, args.steps, args.warmup, args.autotune)
+    print(json.dumps(line), flush=True)
+
+
+def atlas_measure(seed: int, scale: float, steps: int, warmup: int, autotune: bool = False) -> dict:
     """The 16,384-glyph 4096x4096 R8 atlas: one batched frame (all glyph
     scenes in one set of launches, replayed from a CUDA graph) against plain
     per-glyph frames on the same GPU, with identical output."""
     import torch
-    from pathfinder_gb300 import build as pbuild
-    pbuild.build()
     import pathfinder_gb300 as pf
 
-    torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
+    prev_stream = torch.cuda.current_stream()
     torch.cuda.set_stream(stream)
-    atlas = pf.generate_scene(pf.PF_SCENE_GLYPH_ATLAS, seed=args.seed, scale=args.scale)
+    atlas = pf.generate_scene(pf.PF_SCENE_GLYPH_ATLAS, seed=seed, scale=scale)
     batch = pf.SceneBatch.glyphs_of(atlas)
     n, W_, H_ = len(batch), atlas.width, atlas.height
     nseg = atlas.segment_count
@@ -255,7 +276,7 @@ def run_atlas(args) -> None:
     batched = torch.zeros((H_, W_), dtype=torch.uint8, device="cuda")
     per_glyph = torch.zeros_like(batched)
     r.render_batch(batch, batched, pf.PF_CUDA_FORMAT_R8)
-    tuning = r.autotune(batch, batched, pf.PF_CUDA_FORMAT_R8, repeats=3) if args.autotune else r.get_tuning()
+    tuning = r.autotune(batch, batched, pf.PF_CUDA_FORMAT_R8, repeats=3) if autotune else r.get_tuning()
     st = r.stats()
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
 
@@ -269,13 +290,13 @@ def run_atlas(args) -> None:
         torch.cuda.synchronize()
         return sum(a.elapsed_time(b) for a, b in evs) / reps
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         r.render_batch(batch, batched, pf.PF_CUDA_FORMAT_R8, sync=False)
-    ms_batched = timed(lambda: r.render_batch(batch, batched, pf.PF_CUDA_FORMAT_R8, sync=False), args.steps)
+    ms_batched = timed(lambda: r.render_batch(batch, batched, pf.PF_CUDA_FORMAT_R8, sync=False), steps)
     r.graph_capture(batch, batched, pf.PF_CUDA_FORMAT_R8)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         r.graph_launch()
-    ms_graph = timed(r.graph_launch, args.steps)
+    ms_graph = timed(r.graph_launch, steps)
     r.graph_release()
     code, _ = r.render_status()
     assert code == 0, code
@@ -293,9 +314,9 @@ def run_atlas(args) -> None:
     identical = bool(torch.equal(batched, per_glyph))
     line = {
         "metric": "glyphs/s", "value": round(n / (ms_graph / 1e3), 1), "unit": "glyphs/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_graph, 4), "higher_is_better": True,
+        "steps": steps, "warmup": warmup, "ms_per_step": round(ms_graph, 4), "higher_is_better": True,
         "dtype": "f32", "data": "synthetic (seeded PF_SCENE_GLYPH_ATLAS: quadratic glyph outlines with holes)",
-        "config": {"workload": "glyph_atlas_16384" if args.scale == 1.0 else f"glyph_atlas_scale{args.scale}",
+        "config": {"workload": "glyph_atlas_16384" if scale == 1.0 else f"glyph_atlas_scale{scale}",
                    "glyphs": n, "segments": nseg, "width": W_, "height": H_, "format": "R8",
                    "l2": "flushed between steps (512 MiB write)"},
         "batched_graph_ms": round(ms_graph, 4), "batched_ms": round(ms_batched, 4),
@@ -305,8 +326,9 @@ def run_atlas(args) -> None:
                   "lines": st.line_count, "screen_tiles": st.screen_tile_count},
         "tuning": tuning, "gpu_launches_per_batched_frame": st.kernel_launches,
     }
-    print(json.dumps(line), flush=True)
     r.close()
+    torch.cuda.set_stream(prev_stream)
+    return line
 
 
 def stroke_workload(seed: int, scale: float = 1.0):
@@ -438,11 +460,8 @@ def _stroke_host(r, batch, npts, ncont):
     return pts, fl, cs, os_
 
 
-def _diff_common(args):
+def _diff_common():
     import torch
-    from pathfinder_gb300 import build as pbuild
-    pbuild.build()
-    torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
@@ -462,15 +481,26 @@ def _diff_common(args):
 
 
 def run_diff(args) -> None:
+    import torch
+    from pathfinder_gb300 import build as pbuild
+    pbuild.build()
+    torch.cuda.set_device(0)
+    line = diff_measure(args.seed, args.steps, args.warmup)
+    print(json.dumps(line), flush=True)
+
+
+def diff_measure(seed: int, steps: int, warmup: int) -> dict:
     """256 closed cubic paths (4,096 control points), 1024^2 single-channel
     FP32 coverage, L2 loss against the render of the points + N(0, 2 px):
     forward + adjoint (dL/dpoints, dL/dalpha) per step against the plain
     (non-differentiable) FP32 coverage frame of the same scene."""
-    torch, stream, timed = _diff_common(args)
+    import torch
+    prev_stream = torch.cuda.current_stream()
+    _, stream, timed = _diff_common()
     import pathfinder_gb300 as pf
     from pathfinder_gb300.diff import DiffRenderer
-    scene = pf.generate_scene(pf.PF_SCENE_CUBIC_1K, seed=args.seed)
-    tscene = pf.generate_scene(pf.PF_SCENE_CUBIC_1K, seed=args.seed, jitter_sigma=2.0, jitter_seed=args.seed + 1)
+    scene = pf.generate_scene(pf.PF_SCENE_CUBIC_1K, seed=seed)
+    tscene = pf.generate_scene(pf.PF_SCENE_CUBIC_1K, seed=seed, jitter_sigma=2.0, jitter_seed=seed + 1)
     Wd, Hd = scene.width, scene.height
     tdr = DiffRenderer(tscene)
     target = tdr.forward(tdr.points0, tdr.alpha0).clone()
@@ -493,22 +523,22 @@ def run_diff(args) -> None:
         gp, ga = dr.backward(2.0 * (img - target))
         grads["gp"], grads["ga"] = gp, ga
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         fwd_bwd()
         plain.render_batch(pbatch, pout, pf.PF_CUDA_FORMAT_F32, sync=False)
-    ms_plain = timed(lambda: plain.render_batch(pbatch, pout, pf.PF_CUDA_FORMAT_F32, sync=False), args.steps)
-    ms_fwd = timed(fwd, args.steps)
-    ms_fb = timed(fwd_bwd, args.steps)
+    ms_plain = timed(lambda: plain.render_batch(pbatch, pout, pf.PF_CUDA_FORMAT_F32, sync=False), steps)
+    ms_fwd = timed(fwd, steps)
+    ms_fb = timed(fwd_bwd, steps)
     code, _ = dr.renderer.render_status()
     assert code == 0, code
     st = dr.renderer.stats()
     loss = float(((grads["img"] - target) ** 2).sum()) if "img" in grads else None
     line = {
-        "metric": "fwd_bwd_ms", "value": round(ms_fb, 4), "unit": "ms", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms_fb, 4), "higher_is_better": False, "dtype": "f32",
+        "metric": "fwd_bwd_ms", "value": round(ms_fb, 4), "unit": "ms", "n_gpus": 1, "steps": steps,
+        "warmup": warmup, "ms_per_step": round(ms_fb, 4), "higher_is_better": False, "dtype": "f32",
         "data": "synthetic (seeded PF_SCENE_CUBIC_1K: 256 closed cubic paths; target = points + N(0, 2 px))",
         "config": {"workload": "diff_cubic_256_paths_1024", "paths": len(scene.draw_paths),
-                   "control_points": len(scene.points), "width": Wd, "height": Hd, "seed": args.seed,
+                   "control_points": len(scene.points), "width": Wd, "height": Hd, "seed": seed,
                    "l2": "flushed between steps (512 MiB write)"},
         "plain_forward_ms": round(ms_plain, 4), "diff_forward_ms": round(ms_fwd, 4),
         "fwd_bwd_over_plain_forward": round(ms_fb / ms_plain, 3),
@@ -517,7 +547,11 @@ def run_diff(args) -> None:
         "loss": loss, "grad_points_abs_max": float(grads["gp"].abs().max()),
         "grad_alpha_abs_max": float(grads["ga"].abs().max()),
     }
-    print(json.dumps(line), flush=True)
+    dr.renderer.close()
+    tdr.renderer.close()
+    plain.close()
+    torch.cuda.set_stream(prev_stream)
+    return line
 
 
 def run_fit(args) -> None:
@@ -525,7 +559,11 @@ def run_fit(args) -> None:
     256^2-1024^2, drawn from the seed) fitted jointly toward perturbed targets
     (points + N(0, 2 px)) with Adam (lr 0.5 px) on the control points: one
     batched differentiable frame and one batched adjoint per step."""
-    torch, stream, timed = _diff_common(args)
+    import torch
+    from pathfinder_gb300 import build as pbuild
+    pbuild.build()
+    torch.cuda.set_device(0)
+    _, stream, timed = _diff_common()
     import numpy as np
     import pathfinder_gb300 as pf
     from pathfinder_gb300.diff import DiffRenderer
@@ -612,6 +650,24 @@ def run_fit(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def side_workloads(args) -> dict:
+    """The other spec targets, measured in the same run: the batched
+    16,384-glyph atlas against per-glyph frames (speed-up and identical
+    output) and the differentiable frame's forward + adjoint against the
+    plain forward."""
+    a = atlas_measure(args.seed, 1.0, 20, 3)
+    d = diff_measure(args.seed, 20, 3)
+    return {
+        "glyph_atlas_16384": {k: a[k] for k in ("batched_graph_ms", "batched_ms", "per_glyph_ms",
+                                                "speedup_vs_per_glyph", "identical_output")}
+                             | {"glyphs": a["config"]["glyphs"], "segments": a["config"]["segments"],
+                                "format": "R8 4096x4096", "target": "speed-up >= 5x, identical output"},
+        "diff_cubic_256_paths_1024": {k: d[k] for k in ("value", "plain_forward_ms", "diff_forward_ms",
+                                                        "fwd_bwd_over_plain_forward")}
+                                     | {"unit": "ms (fwd+bwd)", "target": "fwd+bwd <= 3x plain forward"},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="svg4k", choices=["svg4k", "atlas", "diff", "fit", "strokes"],
@@ -630,6 +686,9 @@ def main():
     ap.add_argument("--impl", default="cuda", choices=["cuda", "reference"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-side", action="store_true", help="skip the atlas and differentiable side workloads")
+    ap.add_argument("--clock-soak", type=float, default=1.5,
+                    help="seconds of untimed replays sampled for clocks before the timed steps")
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--scale", type=float, default=1.0,
                     help="fraction of the 20,000 paths (small cases for profiling only)")
@@ -702,6 +761,17 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     sampler.start()
+    # The sampler reads every 100 ms, longer than the timed steps take: it runs
+    # over ~1.5 s of untimed replays of the same frame that lead straight into
+    # the timed steps, so the clocks are those of the GPU under this load.
+    soak_end, soak = time.perf_counter() + args.clock_soak, 0
+    while time.perf_counter() < soak_end:
+        flush.zero_()
+        r.graph_launch()
+        soak += 1
+        if soak % 32 == 0:
+            torch.cuda.synchronize()
+    torch.cuda.synchronize()
     for k in range(args.steps):
         flush.zero_()  # inputs are below L2 size: flush between steps
         evs[k][0].record(stream)
@@ -784,13 +854,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded PF_SCENE_SVG_4K: 20,000 log-normal star paths, 40/30/30 line/quad/cubic)",
-            "config": {"workload": (WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}_scale{args.scale}")
-                                   + ("_paints" if paints else ""),
-                       **({"paints": paints} if paints else {}),
-                       "paths": len(scene.draw_paths), "clip_paths": len(scene.clip_paths), "segments": nseg,
-                       "points": npts, "width": W, "height": H, "seed": args.seed,
-                       "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas{world}",
-                       "tiling": "d3d11 level (uniform dicing)" if args.d3d11 else "cpu tiler (bit-exact)"},
+            "config": svg_config(scene, args, paints, world),
             "mpx_per_s": round(world * W * H / (ms / 1e3) / 1e6, 3),
             "timing": "CUDA graph replay of the whole frame; ms_per_step_enqueued: the same frame enqueued "
                       "kernel by kernel with stage events",
@@ -807,12 +871,15 @@ def main():
             "e2e": {"value": round(e2e_value, 4), "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
             "gpu_launches": int(st.kernel_launches * args.steps),
-            "clocks": clocks,
+            "clocks": {**clocks, "window": f"{soak} untimed replays (~{args.clock_soak:.1f} s) then the timed steps"},
         }
         if world == 1 and not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(scene, nseg)
-        print(json.dumps(line), flush=True)
     r.close()
+    if rank == 0:
+        if world == 1 and not args.no_side and args.scale == 1.0 and not args.paints and not args.d3d11:
+            line["side_workloads"] = side_workloads(args)
+        print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
 

@@ -437,8 +437,12 @@ int32_t PFCUDAExclusiveScan(PFCUDARendererRef renderer, const uint32_t* in, uint
  * (`in` may be NULL when n == 0), out[0..n] is written, out[n] = total.
  * Asynchronous on `stream` (a cudaStream_t, NULL = legacy default stream).
  * The first call on a device looks up the array's device address, so make
- * that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race, so serialise them. */
+ * that first call before any stream capture; the address is kept for the
+ * life of the process, so the library must not be used across a reset of the
+ * device (cudaDeviceReset).  All calls share the array: calls that overlap on
+ * the GPU race, so serialise them.  The status covers this call's own
+ * launches only: the runtime's pending error from earlier work is neither
+ * read nor cleared. */
 int32_t PFCUDAExclusiveScanNoAlloc(const uint32_t* in, uint32_t* out, uint32_t n, void* stream);
 
 /* ---- differentiable rendering ----------------------------------------------

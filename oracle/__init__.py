@@ -21,10 +21,14 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "pf_oracle.cpp")
-SRCS = [SRC, os.path.join(HERE, "pf_oracle_stroke.cpp")]
+# The seeded scene generators (pathfinder_gb300/csrc/pf_scenes.cpp, host code)
+# are compiled in too, so that the CPU baseline can build its input scenes
+# without loading the CUDA library.
+SCENES_SRC = os.path.join(ROOT, "pathfinder_gb300", "csrc", "pf_scenes.cpp")
+SRCS = [SRC, os.path.join(HERE, "pf_oracle_stroke.cpp"), SCENES_SRC]
 LIB_PATH = os.path.join(HERE, "libpforacle.so")
 
-CXXFLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-Wall"]
+CXXFLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-Wall"]
 
 
 def build(force: bool = False) -> str:
@@ -55,8 +59,11 @@ def lib() -> C.CDLL:
         l.pfo_tiles.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         l.pfo_zbuffer.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         l.pfo_masks.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        l.pfo_mask_error.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         l.pfo_render.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                  C.c_int]
+        l.pfo_render_glyphs.restype = C.c_int32
+        l.pfo_render_glyphs.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int, C.c_int, C.c_void_p, C.c_int]
         l.pfo_cpu_frame.restype = C.c_double
         l.pfo_cpu_frame.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         l.pfo_area.restype = C.c_double
@@ -79,6 +86,15 @@ def lib() -> C.CDLL:
         l.pfo_diff_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib = l
     return _lib
+
+
+def generate_scene(workload: int, seed: int = 1, scale: float = 1.0, **kw):
+    """The seeded scene generator compiled into this library (the same source
+    as the package's libpfscenes.so), for CPU-only runs that must not load the
+    CUDA library."""
+    from pathfinder_gb300 import _abi
+    from pathfinder_gb300.scene import generate_scene as gen
+    return gen(workload, seed=seed, scale=scale, lib=_abi.bind_scene_generator(lib()), **kw)
 
 
 def _dtypes():
@@ -149,6 +165,24 @@ class OracleFrame:
         lib().pfo_masks(self._h, a.ctypes.data, t.ctypes.data, self.threads)
         return a, t
 
+    def mask_error(self, gpu_alpha=None, gpu_tile=None):
+        """Largest |gpu - oracle| of float32 raw alpha masks [A,16,16] and of
+        resolved tile coverage [T,16,16], computed tile by tile against the
+        FP64 values (no FP64 copy of the arrays).  Returns ((raw, tile),
+        (alpha tile, path tile) of the largest errors)."""
+        ga = None if gpu_alpha is None else np.ascontiguousarray(gpu_alpha, np.float32)
+        gt = None if gpu_tile is None else np.ascontiguousarray(gpu_tile, np.float32)
+        if ga is not None and ga.size != self.alpha_tile_count * 256:
+            raise ValueError("alpha mask count differs from the oracle's")
+        if gt is not None and gt.size != self.tile_count * 256:
+            raise ValueError("tile count differs from the oracle's")
+        err = np.zeros((2,), np.float64)
+        where = np.zeros((2,), np.uint64)
+        lib().pfo_mask_error(self._h, ga.ctypes.data if ga is not None else None,
+                             gt.ctypes.data if gt is not None else None, err.ctypes.data, where.ctypes.data,
+                             self.threads)
+        return (float(err[0]), float(err[1])), (int(where[0]), int(where[1]))
+
     def render(self, width: int, height: int, background=None, channels: int = 4):
         from pathfinder_gb300 import _abi
         bg = None
@@ -212,6 +246,22 @@ class DiffOracle:
         if lib().pfo_diff_grad(self._h, g.ctypes.data, dp.ctypes.data, da.ctypes.data) != 0:
             raise RuntimeError("render before grad")
         return dp, da
+
+
+def render_glyphs(atlas, threads: int = 0) -> np.ndarray:
+    """Every glyph of an atlas scene rendered as its own scene (its path alone,
+    view box = its cell) into its cell of one R8 image, FP64 coverage rounded
+    to u8: what a batch of glyph scenes writes."""
+    if atlas.cells is None:
+        raise ValueError("the scene has no glyph cells")
+    d = atlas.desc()
+    cells = np.ascontiguousarray(atlas.cells)
+    out = np.zeros((atlas.height, atlas.width), np.uint8)
+    rc = lib().pfo_render_glyphs(C.byref(d), cells.ctypes.data, len(cells), atlas.width, atlas.height,
+                                 out.ctypes.data, threads or (os.cpu_count() or 1))
+    if rc != 0:
+        raise ValueError("oracle rejected the atlas scene")
+    return out
 
 
 def cpu_frame(scene, width: int, height: int, threads: int = 0, build_options=None, want_image: bool = False):

@@ -33,6 +33,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -1223,7 +1224,8 @@ void o_blend(uint32_t mode, const T s[3], T a, T* dst, int channels) {
 // (shaders/d3d9/tile.vs.glsl:51-55).
 template <typename T>
 void composite(const Frame& fr, const std::vector<T>& masks, int w, int h, const T bg[4],
-               std::vector<T>& fb, int channels, int threads) {
+               std::vector<T>& fb, int channels, int threads, int ox = 0, int oy = 0) {
+    // The image covers pixels [ox, ox + w) x [oy, oy + h) of the scene.
     fb.assign((size_t)w * h * channels, (T)0);
     for (size_t k = 0; k < (size_t)w * h; k++)
         for (int c = 0; c < channels; c++) fb[k * channels + c] = bg[channels == 4 ? c : 3];
@@ -1255,15 +1257,15 @@ void composite(const Frame& fr, const std::vector<T>& masks, int w, int h, const
                     float tt[6];
                     if (g) o_frame_transform(fr, *g, tt);
                     for (int py = 0; py < 16; py++) {
-                        int Y = t.tile_y * 16 + py;
+                        int Y = t.tile_y * 16 + py - oy;
                         if (Y < 0 || Y >= h) continue;
                         for (int px = 0; px < 16; px++) {
-                            int X = t.tile_x * 16 + px;
+                            int X = t.tile_x * 16 + px - ox;
                             if (X < 0 || X >= w) continue;
                             T src[4] = {col[0], col[1], col[2], col[3]};
                             if (g) {  // combineColor0 SrcIn (shaders/tile_fragment.inc.glsl:81-89)
                                 T tex[4];
-                                o_gradient_color<T>(*g, tt, (T)X + (T)0.5, (T)Y + (T)0.5, tex);
+                                o_gradient_color<T>(*g, tt, (T)(X + ox) + (T)0.5, (T)(Y + oy) + (T)0.5, tex);
                                 src[0] = tex[0]; src[1] = tex[1]; src[2] = tex[2]; src[3] = tex[3] * col[3];
                             }
                             o_blend<T>(in.blend, src, src[3] * cov[py * 16 + px], &fb[((size_t)Y * w + X) * channels],
@@ -1273,10 +1275,10 @@ void composite(const Frame& fr, const std::vector<T>& masks, int w, int h, const
                     continue;
                 }
                 for (int py = 0; py < 16; py++) {
-                    int Y = t.tile_y * 16 + py;
+                    int Y = t.tile_y * 16 + py - oy;
                     if (Y < 0 || Y >= h) continue;
                     for (int px = 0; px < 16; px++) {
-                        int X = t.tile_x * 16 + px;
+                        int X = t.tile_x * 16 + px - ox;
                         if (X < 0 || X >= w) continue;
                         T a = col[3] * cov[py * 16 + px];
                         T* dst = &fb[((size_t)Y * w + X) * channels];
@@ -1850,6 +1852,52 @@ void pfo_masks(PFOFrame* f, double* alpha_masks, double* tile_cov, int threads) 
         });
 }
 
+// Largest |gpu - oracle| of the raw alpha masks [A][256] and of the resolved
+// coverage per path tile [T][256] against the FP64 values, computed tile by
+// tile, so that full-size scenes need no FP64 copy of either array.
+// out_err[0]: raw masks, out_err[1]: tile coverage; out_where[0..1]: the
+// first alpha tile / path tile with the largest error.
+void pfo_mask_error(PFOFrame* f, const float* gpu_alpha, const float* gpu_tile, double* out_err,
+                    uint64_t* out_where, int threads) {
+    Frame& fr = f->fr;
+    if (!f->masks_ready) { compute_raw_masks<double>(fr, f->masks64, threads); f->masks_ready = true; }
+    std::mutex m;
+    double ea = 0.0, et = 0.0;
+    uint64_t wa = 0, wt = 0;
+    const uint32_t A = (uint32_t)(f->masks64.size() / 256);
+    if (gpu_alpha)
+        parallel_for((A + 1023) / 1024, threads, [&](uint32_t blk) {
+            double e = 0.0;
+            uint64_t w = 0;
+            for (uint32_t a = blk * 1024; a < std::min(A, blk * 1024 + 1024); a++)
+                for (int k = 0; k < 256; k++) {
+                    const double d = std::fabs((double)gpu_alpha[(size_t)a * 256 + k] - f->masks64[(size_t)a * 256 + k]);
+                    if (d > e) { e = d; w = a; }
+                }
+            std::lock_guard<std::mutex> g(m);
+            if (e > ea || (e == ea && w < wa)) { ea = e; wa = w; }
+        });
+    if (gpu_tile)
+        parallel_for((uint32_t)fr.paths.size(), threads, [&](uint32_t p) {
+            double cov[256];
+            double e = 0.0;
+            uint64_t w = 0;
+            for (size_t i = 0; i < fr.built[p].tiles.size(); i++) {
+                tile_coverage<double>(fr, p, i, f->masks64, cov);
+                const size_t g = fr.tile_offset[p] + i;
+                for (int k = 0; k < 256; k++) {
+                    const double d = std::fabs((double)gpu_tile[g * 256 + k] - cov[k]);
+                    if (d > e) { e = d; w = g; }
+                }
+            }
+            std::lock_guard<std::mutex> g(m);
+            if (e > et || (e == et && w < wt)) { et = e; wt = w; }
+        });
+    out_err[0] = ea;
+    out_err[1] = et;
+    if (out_where) { out_where[0] = wa; out_where[1] = wt; }
+}
+
 // FP64 composite into premultiplied RGBA (channels=4, rounded to u8) or a
 // single FP64 channel (channels=1).
 void pfo_render(PFOFrame* f, int w, int h, const PFColorF* bg, int channels, uint8_t* out_rgba8,
@@ -1866,6 +1914,42 @@ void pfo_render(PFOFrame* f, int w, int h, const PFColorF* bg, int channels, uin
             double v = std::min(std::max(fb[k], 0.0), 1.0) * 255.0;
             out_rgba8[k] = (uint8_t)std::nearbyint(v);
         }
+}
+
+// Each glyph of an atlas scene rendered as its own scene, as a batch of glyph
+// scenes is: the glyph's draw path alone, view box = its cell, written into the
+// cell of a w x h R8 image (FP64 coverage and composite, rounded to u8).
+// Glyphs are independent: parallel over glyphs, each built on one thread.
+int32_t pfo_render_glyphs(const PFCUDASceneDesc* atlas, const PFRectI* cells, uint32_t n, int w, int h,
+                          uint8_t* out, int threads) {
+    if (!atlas || !cells || !out || n > atlas->draw_path_count) return 1;
+    std::atomic<int32_t> status{0};
+    parallel_for(n, threads, [&](uint32_t g) {
+        PFCUDASceneDesc d = *atlas;
+        d.clip_path_count = 0;
+        d.clip_paths = nullptr;
+        d.draw_paths = atlas->draw_paths + g;
+        d.draw_path_count = 1;
+        const PFRectI c = cells[g];
+        d.view_box = PFRectF{{(float)c.origin.x, (float)c.origin.y}, {(float)c.lower_right.x, (float)c.lower_right.y}};
+        Frame fr;
+        if (!make_frame(&d, nullptr, fr)) { status = 1; return; }
+        build_frame(fr, 1, 1ull << 24);
+        std::vector<double> masks, fb;
+        compute_raw_masks<double>(fr, masks, 1);
+        const double bg[4] = {0, 0, 0, 0};
+        const int cw = c.lower_right.x - c.origin.x, ch = c.lower_right.y - c.origin.y;
+        if (cw <= 0 || ch <= 0) return;
+        composite<double>(fr, masks, cw, ch, bg, fb, 1, 1, c.origin.x, c.origin.y);
+        for (int y = 0; y < ch; y++)
+            for (int x = 0; x < cw; x++) {
+                const int X = c.origin.x + x, Y = c.origin.y + y;
+                if (X < 0 || Y < 0 || X >= w || Y >= h) continue;
+                const double v = std::min(std::max(fb[(size_t)y * cw + x], 0.0), 1.0) * 255.0;
+                out[(size_t)Y * w + X] = (uint8_t)std::nearbyint(v);
+            }
+    });
+    return status.load();
 }
 
 // The CPU baseline: tiling + FP32 coverage + FP32 composite, all on `threads`

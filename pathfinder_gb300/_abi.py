@@ -253,12 +253,41 @@ _SIGS = {
                                           C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "PFCUDABackward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "PFCUDAStatusString": (C.c_char_p, [C.c_int32]),
+}
+
+# The seeded scene generators (include/pathfinder_cuda_scenes.h) live in their
+# own host-only library, libpfscenes.so: generating a test or benchmark scene
+# does not load the renderer.
+SCENES_LIB_PATH = os.path.join(HERE, "libpfscenes.so")
+_SCENE_SIGS = {
     "PFCUDASceneGenerate": (C.c_int32, [C.POINTER(PFCUDASceneParams), C.POINTER(C.c_void_p)]),
     "PFCUDASceneGetDesc": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDASceneDesc), C.POINTER(C.c_int32),
                                        C.POINTER(C.c_int32)]),
     "PFCUDASceneGetCells": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "PFCUDASceneDestroy": (C.c_int32, [C.c_void_p]),
 }
+
+
+def bind_scene_generator(l: C.CDLL) -> C.CDLL:
+    """Declare the scene generator's signatures on a library that exports them."""
+    for name, (res, args) in _SCENE_SIGS.items():
+        fn = getattr(l, name)
+        fn.restype = res
+        fn.argtypes = args
+    return l
+
+
+_scenes_lib = None
+
+
+def scenes_lib() -> C.CDLL:
+    """The loaded scene generator library (raises if it is missing)."""
+    global _scenes_lib
+    if _scenes_lib is None:
+        if not os.path.exists(SCENES_LIB_PATH):
+            raise ImportError(f"{SCENES_LIB_PATH} is missing: run pathfinder_gb300.build.build()")
+        _scenes_lib = bind_scene_generator(C.CDLL(SCENES_LIB_PATH))
+    return _scenes_lib
 
 _lib = None
 

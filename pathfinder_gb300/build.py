@@ -3,7 +3,8 @@
 Translation units compile in parallel into ``pathfinder_gb300/_build`` and
 link into ``pathfinder_gb300/libpathfinder_cuda.so``.  The tiler unit is built
 with ``-fmad=false`` so that its single-precision arithmetic matches the
-reference CPU tiler bit for bit.
+reference CPU tiler bit for bit.  The seeded scene generators (host code) are
+a separate library, ``pathfinder_gb300/libpfscenes.so``, built with g++.
 """
 from __future__ import annotations
 
@@ -18,6 +19,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpathfinder_cuda.so")
+SCENES_LIB = os.path.join(HERE, "libpfscenes.so")
+SCENES_SRC = os.path.join(CSRC, "pf_scenes.cpp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code: no multiply-add contraction (gcc contracts by default on aarch64),
@@ -32,7 +35,6 @@ UNITS = [
     ("pf_adjoint.cu", []),
     ("pf_renderer.cu", []),
     ("pf_noalloc.cu", []),
-    ("pf_scenes.cpp", []),
     ("pf_paint.cu", []),
     ("pf_stroke.cu", ["-fmad=false"]),
     ("pf_pack.cu", []),
@@ -76,13 +78,31 @@ def _compile(src: str, extra: list[str], verbose: bool) -> str:
     return obj
 
 
+def build_scenes(verbose: bool = False, force: bool = False) -> str:
+    """The scene generator library (host code only; no multiply-add contraction,
+    so that both host architectures generate the same bytes)."""
+    hdr = os.path.join(ROOT, "include", "pathfinder_cuda_scenes.h")
+    if not force and _newer(SCENES_LIB, [SCENES_SRC, hdr, os.path.join(ROOT, "include", "pathfinder_cuda.h")]):
+        return SCENES_LIB
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           "-I" + os.path.join(ROOT, "include"), "-o", SCENES_LIB, SCENES_SRC]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"scene generator build failed:\n{r.stderr}")
+    return SCENES_LIB
+
+
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     if force:
         for f in os.listdir(BUILD):
             os.remove(os.path.join(BUILD, f))
-    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+    with ThreadPoolExecutor(max_workers=len(UNITS) + 1) as ex:
+        scenes = ex.submit(build_scenes, verbose, force)
         objs = list(ex.map(lambda u: _compile(u[0], u[1], verbose), UNITS))
+        scenes.result()
     if force or not _newer(LIB, objs):
         cmd = [nvcc(), "-shared", "-o", LIB] + objs + ARCH + ["-Xcompiler", "-fPIC"]
         if verbose:

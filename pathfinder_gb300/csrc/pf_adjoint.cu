@@ -109,7 +109,7 @@ __global__ void k_zero_grad_mask(FrameDev f, float4* grad_mask) {
 void launch_composite_bwd(const FrameDev& f, const float* d_image, float* grad_mask, float* grad_alpha,
                           cudaStream_t s) {
     count_launch();
-    k_zero_grad_mask<<<152 * 4, 256, 0, s>>>(f, (float4*)grad_mask);
+    k_zero_grad_mask<<<f.sms * 4, 256, 0, s>>>(f, (float4*)grad_mask);
     if (f.screen_count == 0) return;
     count_launch();
     k_composite_bwd<4><<<(f.screen_count + 3) / 4, 128, 0, s>>>(f, d_image, grad_mask, grad_alpha);
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(256) k_line_grad(FrameDev f, const float* __re
 
 void launch_line_grad(const FrameDev& f, const float* grad_mask, float2* grad_points, cudaStream_t s) {
     count_launch();
-    k_line_grad<<<152 * 8, 256, 0, s>>>(f, grad_mask, grad_points);
+    k_line_grad<<<f.sms * 8, 256, 0, s>>>(f, grad_mask, grad_points);
 }
 
 // dL/dp = M^T dL/dp' for p' = M p + t (M = [m00 m01; m10 m11]).
@@ -267,7 +267,7 @@ __global__ void k_points_grad_transform(float2* g, uint32_t n, float m00, float 
 void launch_points_grad_transform(float2* grad_points, uint32_t n, const float* m4, cudaStream_t s) {
     if (n == 0) return;
     count_launch();
-    k_points_grad_transform<<<min((n + 255) / 256, 152u * 8u), 256, 0, s>>>(grad_points, n, m4[0], m4[1], m4[2], m4[3]);
+    k_points_grad_transform<<<min((n + 255) / 256, device_sm_count() * 8u), 256, 0, s>>>(grad_points, n, m4[0], m4[1], m4[2], m4[3]);
 }
 
 }  // namespace pf

@@ -32,6 +32,7 @@ struct FrameDev {
     uint32_t scene_begin, scene_count;
     uint32_t screen_begin;       // global index of the range's first screen tile
     TuneParams tune;
+    uint32_t sms;                // multiprocessors of the renderer's device (grid sizes)
     // tile arrays (capacity tile_cap; +1 for scan totals)
     uint32_t tile_cap, col_cap, fill_cap, vis_cap, screen_count;
     uint32_t* tile_fill_count;   // [tile_cap+1]
@@ -166,6 +167,9 @@ int32_t stroke_run(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, P
 // Number of kernels this library has launched (host counter).
 uint64_t launch_counter();
 void count_launch(uint32_t n = 1);
+// Multiprocessors of the current device (queried once per device; grid sizes
+// of the launches that do not carry a FrameDev).
+uint32_t device_sm_count();
 
 
 void launch_transform(const float2* in, float2* out, uint32_t n, const float* m6, cudaStream_t s);
@@ -240,6 +244,9 @@ void launch_bin_emit(const FrameDev& f, cudaStream_t s);
 // and, when total_out != NULL, the total as u64.
 void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_t n_host, uint32_t n_cap,
                  int mode, uint64_t* total_out, ScanTemp& tmp, cudaStream_t s);
+// The same scan of n host-counted values, each launch's status taken from its
+// own return value (the runtime's pending error state is not read).
+cudaError_t launch_scan_checked(const uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& tmp, cudaStream_t s);
 // Several exclusive scans over arrays of one length (device count at d_n,
 // clamped to n_cap); scratch needs count * (n_cap / 2048 + 1) partials.
 constexpr int kMaxScanLanes = 3;

@@ -17,7 +17,13 @@
 //     each other's results: serialise them;
 //   * nothing in the array needs to start at zero: each partial sum a call
 //     reads was written earlier by the same call, so the previous call's
-//     contents are never used.
+//     contents are never used;
+//   * the array's device address is looked up once per device and kept for
+//     the life of the process: a device reset (cudaDeviceReset) in the host
+//     process makes it stale, so the library must not outlive one;
+//   * the returned status is that of this call's own launches (taken from
+//     each launch's return value): an error that unrelated earlier work left
+//     pending in the runtime is neither reported nor cleared.
 #include "pf_kernels.cuh"
 #include "../../include/pathfinder_cuda.h"
 
@@ -65,6 +71,6 @@ extern "C" int32_t PFCUDAExclusiveScanNoAlloc(const uint32_t* in, uint32_t* out,
     cudaError_t e = scratch_for_current_device(&scratch);
     if (e != cudaSuccess) return e == cudaErrorNoDevice ? PF_CUDA_ERR_NO_DEVICE : PF_CUDA_ERR_LAUNCH;
     pf::ScanTemp tmp{scratch, kNoAllocPartials};
-    pf::launch_scan(in, out, nullptr, n, n, 0, nullptr, tmp, (cudaStream_t)stream);
-    return cudaGetLastError() == cudaSuccess ? PF_CUDA_OK : PF_CUDA_ERR_LAUNCH;
+    e = pf::launch_scan_checked(in, out, n, tmp, (cudaStream_t)stream);
+    return e == cudaSuccess ? PF_CUDA_OK : PF_CUDA_ERR_LAUNCH;
 }

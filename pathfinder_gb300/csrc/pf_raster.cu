@@ -19,6 +19,8 @@
 #include "pf_kernels.cuh"
 #include "pathfinder_cuda.h"
 
+#include <atomic>
+
 namespace pf {
 
 __device__ __forceinline__ int4 pack_tile(int32_t tx, int32_t ty, uint32_t alpha, uint32_t gp, uint16_t color,
@@ -165,7 +167,7 @@ __global__ void k_propagate(FrameDev f, int clip_pass) {
 
 void launch_propagate(const FrameDev& f, bool clip_pass, cudaStream_t s) {
     if (f.path_count == 0) return;
-    { count_launch(); k_propagate<<<152 * 16, 256, 0, s>>>(f, clip_pass ? 1 : 0); }
+    { count_launch(); k_propagate<<<f.sms * 16, 256, 0, s>>>(f, clip_pass ? 1 : 0); }
 }
 
 // ---------------------------------------------------------------------------
@@ -216,7 +218,7 @@ __global__ void k_visible(FrameDev f, int scatter) {
 }
 
 void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s) {
-    { count_launch(); k_visible<<<152 * 8, 256, 0, s>>>(f, scatter ? 1 : 0); }
+    { count_launch(); k_visible<<<f.sms * 8, 256, 0, s>>>(f, scatter ? 1 : 0); }
 }
 
 // ---------------------------------------------------------------------------
@@ -867,10 +869,15 @@ __global__ void __launch_bounds__(WARPS * 32, PAINT ? 1 : 24 / WARPS) k_composit
 template <int MODE, int WARPS, bool PAINT>
 void launch_composite_instance(const FrameDev& f, void* out, const float4& bg, cudaStream_t s) {
     constexpr size_t smem = WARPS * sizeof(CompositeScratch);
-    static bool configured = false;  // above 48 KiB needs the opt-in (once per instance)
-    if (!configured) {
-        cudaFuncSetAttribute(k_composite<MODE, WARPS, PAINT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        configured = true;
+    // Above 48 KiB needs the opt-in, once per instance and device (the
+    // attribute belongs to the device's context).  Setting it twice is
+    // harmless, so concurrent first calls need no lock.
+    static std::atomic<uint64_t> configured{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && !((configured.load() >> dev) & 1u)) {
+        if (cudaFuncSetAttribute(k_composite<MODE, WARPS, PAINT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) == cudaSuccess)
+            configured.fetch_or(1ull << dev);
     }
     count_launch();
     k_composite<MODE, WARPS, PAINT><<<(f.screen_count + WARPS - 1) / WARPS, WARPS * 32, smem, s>>>(f, out, bg);

@@ -122,6 +122,7 @@ const TuneParams kDefaultTune{128, 256, 32, 2};
 
 struct PFCUDARenderer {
     int device = 0;
+    uint32_t sms = 1;                  // multiprocessors of the device (grid sizes)
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
     // Uploads copy the points on their own stream, beside the packing
@@ -184,9 +185,17 @@ struct PFCUDARenderer {
     uint64_t launches = 0;
     TuneParams tune = kDefaultTune;
 
-    // captured frame
+    // captured frame, and the launch key it was captured with: every pointer,
+    // size and option its kernels read (a buffer regrown since makes the
+    // graph stale, and PFCUDAGraphLaunch refuses it)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
+    std::vector<uint8_t> graph_key;
+    PFCUDABuildOptions graph_opts{};
+    bool graph_has_opts = false;
+    int graph_format = 0;
+    void* graph_out = nullptr;
+    Range graph_range;
 
     // plain frames replayed from a graph while their key (every pointer, size
     // and option that a launch of the frame reads) repeats
@@ -233,6 +242,21 @@ int32_t cuda_status(cudaError_t e) {
         cudaError_t _e = (expr);                          \
         if (_e != cudaSuccess) return cuda_status(_e);    \
     } while (0)
+
+// Makes the renderer's device current for the duration of an entry point and
+// restores the caller's device afterwards.
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t status = cudaSuccess;
+    explicit DeviceGuard(int device) {
+        if ((status = cudaGetDevice(&prev)) != cudaSuccess) { prev = -1; return; }
+        if (prev != device) status = cudaSetDevice(device);
+        else prev = -1;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
 
 int4 screen_rect_of(PFRectF v) {
     // round_rect_out_to_tile_bounds (renderer/src/tiles.rs:64-66)
@@ -293,6 +317,7 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.scene_count = g.s1 - g.s0;
     f.screen_begin = g.st0;
     f.tune = r->tune;
+    f.sms = r->sms;
     f.tile_cap = r->tile_cap;
     f.col_cap = r->col_cap;
     f.fill_cap = r->fill_cap;
@@ -621,6 +646,7 @@ void release_graph(PFCUDARenderer* r) {
     if (r->graph) cudaGraphDestroy(r->graph);
     r->graph_exec = nullptr;
     r->graph = nullptr;
+    r->graph_key.clear();
 }
 
 // Single-image rendering: scenes uploaded without targets draw into the
@@ -663,8 +689,11 @@ int32_t PFCUDARendererCreate(int32_t device_ordinal, const PFCUDARendererOptions
     if (e != cudaSuccess || count == 0) return PF_CUDA_ERR_NO_DEVICE;
     if (device_ordinal < 0 || device_ordinal >= count) return PF_CUDA_ERR_INVALID;
     PF_TRY(cudaSetDevice(device_ordinal));
+    int sms = 0;
+    PF_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_ordinal));
     PFCUDARenderer* r = new PFCUDARenderer();
     r->device = device_ordinal;
+    r->sms = sms > 0 ? (uint32_t)sms : 1u;
     if (options) r->options = *options;
     if ((e = cudaStreamCreateWithFlags(&r->own_stream, cudaStreamNonBlocking)) ||
         (e = cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking)) ||
@@ -1097,6 +1126,8 @@ int32_t PFCUDARenderSceneAsync(PFCUDARendererRef r, const PFCUDABuildOptions* op
                                int32_t height, uint8_t* out_rgba8_device) {
     if (!r || !out_rgba8_device) return PF_CUDA_ERR_INVALID;
     if (!r->has_scene) return PF_CUDA_ERR_NO_SCENE;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     bool changed = false;
     int32_t rc = prepare_plain_targets(r, width, height, &changed);
     if (rc) return rc;
@@ -1119,6 +1150,8 @@ int32_t PFCUDARenderBatchAsync(PFCUDARendererRef r, const PFCUDABuildOptions* op
                                uint32_t count, int32_t format, void* out_device) {
     if (!r || !out_device || format < 0 || format > 2) return PF_CUDA_ERR_INVALID;
     if (!valid_range(r, first, count)) return r->has_scene ? PF_CUDA_ERR_INVALID : PF_CUDA_ERR_NO_SCENE;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     r->last = make_range(r, first, count);
     PF_TRY(ensure_frame_buffers(r));
     PF_TRY(enqueue_frame(r, options, format, out_device, r->last));
@@ -1127,6 +1160,8 @@ int32_t PFCUDARenderBatchAsync(PFCUDARendererRef r, const PFCUDABuildOptions* op
 
 int32_t PFCUDARenderStatus(PFCUDARendererRef r, uint64_t* out_needed) {
     if (!r) return PF_CUDA_ERR_INVALID;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     PF_TRY(cudaMemcpyAsync(r->h_counters, r->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, r->stream));
     PF_TRY(cudaStreamSynchronize(r->stream));
     Counters h = *r->h_counters;
@@ -1138,6 +1173,9 @@ int32_t PFCUDARenderStatus(PFCUDARendererRef r, uint64_t* out_needed) {
 
 int32_t PFCUDAGraphCapture(PFCUDARendererRef r, const PFCUDABuildOptions* options, uint32_t first, uint32_t count,
                            int32_t format, void* out_device) {
+    if (!r) return PF_CUDA_ERR_INVALID;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     int32_t rc = PFCUDARenderBatch(r, options, first, count, format, out_device);
     if (rc != PF_CUDA_OK) return rc;
     release_graph(r);
@@ -1154,11 +1192,25 @@ int32_t PFCUDAGraphCapture(PFCUDARendererRef r, const PFCUDABuildOptions* option
     }
     r->graph = g;
     PF_TRY(cudaGraphInstantiate(&r->graph_exec, g, 0));
+    r->graph_has_opts = options != nullptr;
+    r->graph_opts = options ? *options : PFCUDABuildOptions{};
+    r->graph_format = format;
+    r->graph_out = out_device;
+    r->graph_range = r->last;
+    r->graph_key = frame_key(r, options, format, out_device, r->last);
     return PF_CUDA_OK;
 }
 
 int32_t PFCUDAGraphLaunch(PFCUDARendererRef r) {
     if (!r || !r->graph_exec) return PF_CUDA_ERR_INVALID;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
+    // The graph holds the buffer pointers and sizes of its capture; a frame
+    // or upload since then that regrew a buffer or changed a size would make
+    // it launch on freed memory, so it is refused (capture it again).
+    if (frame_key(r, r->graph_has_opts ? &r->graph_opts : nullptr, r->graph_format, r->graph_out, r->graph_range) !=
+        r->graph_key)
+        return PF_CUDA_ERR_INVALID;
     PF_TRY(cudaGraphLaunch(r->graph_exec, r->stream));
     return PF_CUDA_OK;
 }

@@ -609,7 +609,8 @@ int32_t cuda_status_of(cudaError_t e) {
 #define PF_STROKE_TRY(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return cuda_status_of(e_); } while (0)
 uint32_t grid_for(uint64_t n) {
     const uint64_t b = (n + 255) / 256;
-    return (uint32_t)(b == 0 ? 1 : (b > 152 * 8 ? 152 * 8 : b));
+    const uint64_t cap = (uint64_t)device_sm_count() * 8;
+    return (uint32_t)(b == 0 ? 1 : (b > cap ? cap : b));
 }
 }  // namespace
 

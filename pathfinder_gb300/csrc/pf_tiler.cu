@@ -20,6 +20,19 @@ static std::atomic<uint64_t> g_launches{0};
 uint64_t launch_counter() { return g_launches.load(); }
 void count_launch(uint32_t n) { g_launches += n; }
 
+uint32_t device_sm_count() {
+    constexpr int kMaxDevices = 64;
+    static std::atomic<uint32_t> cache[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 1;
+    uint32_t v = cache[dev].load(std::memory_order_relaxed);
+    if (v) return v;
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 1;
+    cache[dev].store((uint32_t)n, std::memory_order_relaxed);
+    return (uint32_t)n;
+}
+
 // ---------------------------------------------------------------------------
 // warp / block scan helpers
 // ---------------------------------------------------------------------------
@@ -186,6 +199,23 @@ void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_
     { count_launch(); k_scan_down<<<nb, kScanThreads, 0, s>>>(in, out, d_n, n_host, mode, tmp.partials); }
 }
 
+cudaError_t launch_scan_checked(const uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& tmp, cudaStream_t s) {
+    uint32_t nb = (n + kScanChunk - 1) / kScanChunk;
+    if (nb == 0) nb = 1;
+    const uint64_t* d_n = nullptr;
+    uint64_t* total_out = nullptr;
+    int mode = 0;
+    uint32_t* partials = tmp.partials;
+    void* a_reduce[] = {(void*)&in, (void*)&d_n, (void*)&n, (void*)&mode, (void*)&partials};
+    void* a_part[] = {(void*)&partials, (void*)&d_n, (void*)&n, (void*)&out, (void*)&total_out};
+    void* a_down[] = {(void*)&in, (void*)&out, (void*)&d_n, (void*)&n, (void*)&mode, (void*)&partials};
+    cudaError_t e;
+    count_launch(3);
+    if ((e = cudaLaunchKernel((const void*)k_scan_reduce, dim3(nb), dim3(kScanThreads), a_reduce, 0, s))) return e;
+    if ((e = cudaLaunchKernel((const void*)k_scan_partials, dim3(1), dim3(1024), a_part, 0, s))) return e;
+    return cudaLaunchKernel((const void*)k_scan_down, dim3(nb), dim3(kScanThreads), a_down, 0, s);
+}
+
 // ---------------------------------------------------------------------------
 // fused scans: up to kMaxScanLanes arrays of the same length in one
 // reduce / partials / down-sweep set (the per-tile fill offsets, alpha ids and
@@ -291,7 +321,8 @@ __global__ void k_transform(const float2* __restrict__ in, float2* __restrict__ 
 void launch_transform(const float2* in, float2* out, uint32_t n, const float* m6, cudaStream_t s) {
     if (n == 0) return;
     uint32_t blocks = (n + 255) / 256;
-    if (blocks > 152 * 16) blocks = 152 * 16;
+    const uint32_t cap = device_sm_count() * 16;
+    if (blocks > cap) blocks = cap;
     { count_launch(); k_transform<<<blocks, 256, 0, s>>>(in, out, n, m6[0], m6[1], m6[2], m6[3], m6[4], m6[5]); }
 }
 
@@ -488,7 +519,7 @@ void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     lanes.in[1] = f.path_cols + f.path_begin; lanes.out[1] = f.path.col_offset + f.path_begin;
     lanes.total[1] = &f.counters->columns;
     launch_scan_multi(lanes, nullptr, f.path_count, tmp, s);
-    { count_launch(); k_zero_tiles<<<152 * 8, 256, 0, s>>>(f); }
+    { count_launch(); k_zero_tiles<<<f.sms * 8, 256, 0, s>>>(f); }
 }
 
 // Launch bounds of the flattening and binning passes: at most 42 registers a
@@ -687,7 +718,7 @@ static int fill_mode(const FrameDev& f) { return f.diff ? kFillF32 : (f.d3d11 ? 
 
 void launch_bin_count(const FrameDev& f, cudaStream_t s) {
     count_launch();
-    const uint32_t blocks = 152 * f.tune.bin_blocks_per_sm;
+    const uint32_t blocks = f.sms * f.tune.bin_blocks_per_sm;
     const int m = fill_mode(f);
     if (m == kFillF32) k_bin_count<kFillF32><<<blocks, f.tune.bin_threads, 0, s>>>(f);
     else if (m == kFillD3D11) k_bin_count<kFillD3D11><<<blocks, f.tune.bin_threads, 0, s>>>(f);
@@ -696,7 +727,7 @@ void launch_bin_count(const FrameDev& f, cudaStream_t s) {
 
 void launch_bin_emit(const FrameDev& f, cudaStream_t s) {
     count_launch();
-    const uint32_t blocks = 152 * f.tune.bin_blocks_per_sm;
+    const uint32_t blocks = f.sms * f.tune.bin_blocks_per_sm;
     const int m = fill_mode(f);
     const int t = f.tune.bin_threads;
     const bool order = f.fill_e != nullptr;

@@ -295,16 +295,22 @@ class Scene:
 
 
 def generate_scene(workload: int, seed: int = 1, scale: float = 1.0, jitter_sigma: float = 0.0,
-                   jitter_seed: int = 0, width: int = 0, height: int = 0) -> Scene:
-    """A seeded synthetic scene (include/pathfinder_cuda_scenes.h)."""
-    L = _abi.lib()
+                   jitter_seed: int = 0, width: int = 0, height: int = 0, lib=None) -> Scene:
+    """A seeded synthetic scene (include/pathfinder_cuda_scenes.h).  `lib`: a
+    loaded library exporting the generator (default: libpfscenes.so)."""
+    L = lib if lib is not None else _abi.scenes_lib()
+
+    def check(code, what):
+        if code != _abi.PF_CUDA_OK:
+            raise RuntimeError(f"{what} failed with status {code}")
+
     p = _abi.PFCUDASceneParams(workload, seed, scale, jitter_sigma, jitter_seed, width, height)
     h = C.c_void_p()
-    _abi.check(L.PFCUDASceneGenerate(C.byref(p), C.byref(h)), "PFCUDASceneGenerate")
+    check(L.PFCUDASceneGenerate(C.byref(p), C.byref(h)), "PFCUDASceneGenerate")
     try:
         d = _abi.PFCUDASceneDesc()
         w, hh = C.c_int32(), C.c_int32()
-        _abi.check(L.PFCUDASceneGetDesc(h, C.byref(d), C.byref(w), C.byref(hh)), "PFCUDASceneGetDesc")
+        check(L.PFCUDASceneGetDesc(h, C.byref(d), C.byref(w), C.byref(hh)), "PFCUDASceneGetDesc")
         s = Scene()
         npt, nc = d.point_count, d.contour_count
 

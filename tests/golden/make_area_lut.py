@@ -58,7 +58,10 @@ def decode_png_rgba8(data: bytes) -> np.ndarray:
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # the reference checkout: first argument, else $PATHFINDER_REFERENCE
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PATHFINDER_REFERENCE", "")
+    if not ref:
+        sys.exit("usage: make_area_lut.py <pathfinder checkout> (or set PATHFINDER_REFERENCE)")
     png = open(os.path.join(ref, "resources/textures/area-lut.png"), "rb").read()
     img = decode_png_rgba8(png)
     with open(os.path.join(HERE, "area_lut_rgba8.bin.zz"), "wb") as f:

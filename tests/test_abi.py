@@ -13,10 +13,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
 
 
-def declared_functions():
+def declared_functions(headers=None):
     names = []
     for h in sorted(os.listdir(INCLUDE)):
-        if h.endswith(".h"):
+        if h.endswith(".h") and (headers is None or h in headers):
             src = open(os.path.join(INCLUDE, h)).read()
             names += re.findall(r"^\s*(?:int32_t|const char\s*\*|void|uint8_t)\s+(PF\w+)\s*\(", src, re.M)
     return names
@@ -29,8 +29,13 @@ def test_headers_declare_entry_points():
 
 def test_library_exports_every_declared_symbol(built):
     lib = C.CDLL(_abi.LIB_PATH)
-    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    missing = [n for n in declared_functions(["pathfinder_cuda.h"]) if not hasattr(lib, n)]
     assert not missing, f"not exported: {missing}"
+    scenes = C.CDLL(_abi.SCENES_LIB_PATH)
+    missing = [n for n in declared_functions(["pathfinder_cuda_scenes.h"]) if not hasattr(scenes, n)]
+    assert not missing, f"scene generator library does not export: {missing}"
+    # the renderer does not carry the generators
+    assert not hasattr(lib, "PFCUDASceneGenerate")
 
 
 STRUCTS = ["PFVector2F", "PFRectF", "PFRectI", "PFColorU", "PFColorF", "PFTransform2F", "PFCUDAPath",
@@ -68,7 +73,7 @@ def test_invalid_arguments_are_rejected_without_a_device(built):
     assert L.PFCUDARendererCreate(0, None, None) == _abi.PF_CUDA_ERR_INVALID
     p = _abi.PFCUDASceneParams(99, 1, 1.0, 0.0, 0, 0, 0)
     h = C.c_void_p()
-    assert L.PFCUDASceneGenerate(C.byref(p), C.byref(h)) == _abi.PF_CUDA_ERR_INVALID
+    assert _abi.scenes_lib().PFCUDASceneGenerate(C.byref(p), C.byref(h)) == _abi.PF_CUDA_ERR_INVALID
     assert L.PFCUDARenderScene(None, None, 16, 16, None, 0) == _abi.PF_CUDA_ERR_INVALID
 
 

@@ -82,3 +82,31 @@ def test_autotune_changes_speed_not_pixels(renderer):
         renderer.render_batch(batch, out, pf.PF_CUDA_FORMAT_RGBA8)
         assert torch.equal(out, ref)
     renderer.set_tuning(**best)
+
+
+def test_graph_refused_after_buffers_regrow(built):
+    """A captured graph holds the buffers of its capture: once a larger frame
+    has regrown them, launching it is refused (it is never replayed on freed
+    memory), and a new capture works again."""
+    torch = pytest.importorskip("torch")
+    from pathfinder_gb300 import _abi
+    small = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=12, scale=0.002)
+    big = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=13, scale=0.05)
+    batch = pf.SceneBatch.packed([small, big])
+    out = torch.zeros((batch.total_pixels,), dtype=torch.int32, device="cuda")
+    with pf.Renderer(0) as r:
+        r.graph_capture(batch, out, pf.PF_CUDA_FORMAT_RGBA8, first=0, count=1)
+        r.graph_launch()
+        r.render_batch(batch, out, pf.PF_CUDA_FORMAT_RGBA8, first=0, count=2)  # regrows the frame buffers
+        with pytest.raises(_abi.PFCUDAError) as e:
+            r.graph_launch()
+        assert e.value.code == _abi.PF_CUDA_ERR_INVALID
+        ref = torch.zeros_like(out)
+        r.render_batch(batch, ref, pf.PF_CUDA_FORMAT_RGBA8, first=0, count=1)
+        out.zero_()
+        r.graph_capture(batch, out, pf.PF_CUDA_FORMAT_RGBA8, first=0, count=1)
+        out.zero_()
+        r.graph_launch()
+        code, _ = r.render_status()
+        assert code == 0
+        assert torch.equal(out, ref)

@@ -11,7 +11,9 @@ from pathfinder_gb300.stroke import StrokeBatch, outlines_from_buffers
 from pathfinder_gb300.svg import load_svg, parse_color, parse_path_data, parse_transform
 from tests import svgdocs
 
-TIGER = "/root/reference/resources/svg/Ghostscript_Tiger.svg"
+# The reference's tiger asset, from the checkout named by $PATHFINDER_REFERENCE
+# (the test that draws it is skipped when the variable or the file is absent).
+TIGER = os.path.join(os.environ.get("PATHFINDER_REFERENCE", ""), "resources/svg/Ghostscript_Tiger.svg")
 
 
 class OracleStroker:
