@@ -91,7 +91,16 @@ def test_graph_refused_after_buffers_regrow(built):
     torch = pytest.importorskip("torch")
     from pathfinder_gb300 import _abi
     small = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=12, scale=0.002)
-    big = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=13, scale=0.05)
+    # 60 translucent full-canvas rectangles: 15 path tiles per screen tile,
+    # far above the tile capacity an upload reserves (4 per screen tile)
+    big = pf.Scene()
+    big.set_view_box(pf.RectF(0, 0, 1024, 1024))
+    for k in range(60):
+        c = pf.Contour()
+        for x, y in ((1.5 + k, 2.5), (1020.5, 1.5 + k), (1019.5 - k, 1021.5), (3.5, 1020.5 - k)):
+            c.push_endpoint(x, y)
+        c.close()
+        big.push_draw_path(pf.DrawPath(pf.Outline([c]), pf.ColorU(k * 4, 255 - k * 4, 90, 40)))
     batch = pf.SceneBatch.packed([small, big])
     out = torch.zeros((batch.total_pixels,), dtype=torch.int32, device="cuda")
     with pf.Renderer(0) as r:
