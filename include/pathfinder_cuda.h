@@ -397,11 +397,12 @@ typedef struct PFCUDATuning {
     int32_t bin_threads;         /* 128, 256 or 512 */
     int32_t bin_blocks_per_sm;   /* 4 .. 64 */
     int32_t composite_warps;     /* 2, 4 or 8 */
+    int32_t composite_batch;     /* screen tiles per work item of the persistent composite: 1, 2, 4 or 8 */
 } PFCUDATuning;
 int32_t PFCUDASetTuning(PFCUDARendererRef renderer, const PFCUDATuning* tuning);
 int32_t PFCUDAGetTuning(PFCUDARendererRef renderer, PFCUDATuning* out_tuning);
 /* Autotuner: times `repeats` frames of the given range per candidate shape
- * (coordinate descent over the four parameters), keeps the fastest and
+ * (coordinate descent over the five parameters), keeps the fastest and
  * returns it.  Synchronises. */
 int32_t PFCUDAAutotune(PFCUDARendererRef renderer, const PFCUDABuildOptions* options,
                        uint32_t first_scene, uint32_t scene_count, int32_t format, void* out_device,

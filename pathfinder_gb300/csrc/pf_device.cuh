@@ -33,6 +33,9 @@ constexpr uint32_t kStatusMalformed      = 1u << 5;
 constexpr uint32_t kStatusColumnCapacity = 1u << 6;
 constexpr uint32_t kStatusAlphaCapacity  = 1u << 7;
 constexpr uint32_t kStatusLineCapacity   = 1u << 8;
+// A bounded wait for a bulk copy gave up (the tile was computed from global
+// memory instead); reported as a launch error.
+constexpr uint32_t kStatusCopyStall      = 1u << 9;
 
 // ---------------------------------------------------------------------------
 // Records in HBM
@@ -137,6 +140,8 @@ struct Counters {
     uint64_t lines;        // flattened lines
     uint64_t visible;      // composited tiles
     uint64_t needed_fills, needed_tiles, needed_visible, needed_lines;
+    uint32_t composite_next;   // work counter of the persistent composite (screen tiles handed out)
+    uint32_t mask_items;       // visible tiles with a mask (k_mask's work list)
 };
 
 // ---------------------------------------------------------------------------
@@ -367,25 +372,47 @@ __device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink
 constexpr uint32_t kMaxSegmentLines = 1u << 20;
 __host__ __device__ __forceinline__ bool finite2(float2 p) { return isfinite(p.x) && isfinite(p.y); }
 
-template <class Emit>
-__device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Emit&& emit, uint32_t* status) {
-    float2 p0 = pts[sr.x];
-    float2 pe = pts[sr.y];
-    if (!finite2(p0) || !finite2(pe)) { atomicOr(status, kStatusMalformed); return; }
-    if (sr.z == (int)kSegLine) {
-        emit(Line{p0.x, p0.y, pe.x, pe.y}, 0u, 0);
-        return;
-    }
-    Cubic c;
+// The root of a segment's subdivision: a curve as a cubic (a quadratic
+// elevated by Segment::to_cubic), a line as its base.  Returns 0 for a segment
+// with a non-finite point (flagged malformed), 1 for a line, 2 for a curve.
+enum : int { kRootInvalid = 0, kRootLine = 1, kRootCurve = 2 };
+__device__ __forceinline__ int segment_root(const float2* pts, SegRec sr, Cubic& c, uint32_t* status) {
+    const float2 p0 = pts[sr.x], pe = pts[sr.y];
+    if (!finite2(p0) || !finite2(pe)) { atomicOr(status, kStatusMalformed); return kRootInvalid; }
+    c.base = Line{p0.x, p0.y, pe.x, pe.y};
+    c.ctrl = c.base;
+    if (sr.z == (int)kSegLine) return kRootLine;
     if (sr.z == (int)kSegQuad) {
-        float2 q = pts[sr.x + 1];
-        if (!finite2(q)) { atomicOr(status, kStatusMalformed); return; }
+        const float2 q = pts[sr.x + 1];
+        if (!finite2(q)) { atomicOr(status, kStatusMalformed); return kRootInvalid; }
         c = quad_to_cubic(p0.x, p0.y, q.x, q.y, pe.x, pe.y);
     } else {
-        float2 c0 = pts[sr.x + 1], c1 = pts[sr.x + 2];
-        if (!finite2(c0) || !finite2(c1)) { atomicOr(status, kStatusMalformed); return; }
-        c.base = Line{p0.x, p0.y, pe.x, pe.y};
+        const float2 c0 = pts[sr.x + 1], c1 = pts[sr.x + 2];
+        if (!finite2(c0) || !finite2(c1)) { atomicOr(status, kStatusMalformed); return kRootInvalid; }
         c.ctrl = Line{c0.x, c0.y, c1.x, c1.y};
+    }
+    return kRootCurve;
+}
+
+// The node of a subdivision at split path `addr` (d bits, first split most
+// significant) of the root: exactly the splits the recursion performs.
+__device__ __forceinline__ Cubic subdivision_node(Cubic c, uint32_t addr, int d) {
+    for (int i = d - 1; i >= 0; i--) {
+        Cubic a, b;
+        cubic_split_half(c, a, b);
+        c = ((addr >> i) & 1u) ? b : a;
+    }
+    return c;
+}
+
+template <class Emit>
+__device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Emit&& emit, uint32_t* status) {
+    Cubic c;
+    const int kind = segment_root(pts, sr, c, status);
+    if (kind == kRootInvalid) return;
+    if (kind == kRootLine) {
+        emit(c.base, 0u, 0);
+        return;
     }
     uint32_t emitted = 0;
     // Depth-first without a stack: the current node is named by its split
@@ -413,12 +440,7 @@ __device__ __forceinline__ void flatten_segment(const float2* pts, SegRec sr, Em
         while (d > 0 && (addr & 1u)) { addr >>= 1; d--; }  // climb past right children
         if (d == 0) break;
         addr |= 1u;  // the right sibling
-        c = root;
-        for (int i = d - 1; i >= 0; i--) {
-            Cubic a, b;
-            cubic_split_half(c, a, b);
-            c = ((addr >> i) & 1u) ? b : a;
-        }
+        c = subdivision_node(root, addr, d);
     }
 }
 
@@ -537,17 +559,19 @@ __device__ __forceinline__ void accumulate_fill_column(float x0, float y0, float
         if (r + 1 < 16) atomicAdd(&carry[(r + 1) * 16 + px], __float2int_rn(w * kCovScale));
         return;
     }
-    const float inv_h = __fdividef(1.0f, yhi - ylo);
+    // Row r of the piece gets the trapezoid below the piece in its own cell
+    // plus the x-extent of the part of the piece above the row,
+    // w (max(ylo, r) - ylo) / (yhi - ylo); the rows below the piece get its
+    // whole extent w through the column carry.  One atomic per row.
+    const float ws = w * __fdividef(1.0f, yhi - ylo);  // extent per unit of height
     const int r0 = (int)floorf(ylo), r1 = min((int)floorf(yhi), 15);
     for (int r = r0; r <= r1; r++) {
         const float yt = fmaxf(ylo, (float)r), yb2 = fminf(yhi, (float)(r + 1));
-        const float h = yb2 - yt;
-        if (h <= 0.0f) continue;
-        const float wr = w * (h * inv_h);
-        const float a = wr * ((float)(r + 1) - 0.5f * (yt + yb2));
+        const float h = fmaxf(yb2 - yt, 0.0f);
+        const float a = ws * (h * ((float)(r + 1) - 0.5f * (yt + yb2)) + (yt - ylo));
         atomicAdd(&acc[r * 16 + px], __float2int_rn(a * kCovScale));
-        if (r + 1 < 16) atomicAdd(&carry[(r + 1) * 16 + px], __float2int_rn(wr * kCovScale));
     }
+    if (r1 + 1 < 16) atomicAdd(&carry[(r1 + 1) * 16 + px], __float2int_rn(w * kCovScale));
 }
 
 // sampleMask resolve (shaders/tile_fragment.inc.glsl:539-556).

@@ -15,6 +15,7 @@ struct TuneParams {
     int bin_threads;       // threads per block of the binning passes
     int bin_blocks_per_sm; // grid of the binning passes = SMs x this
     int comp_warps;        // warps per block of the composite (2, 4 or 8)
+    int comp_batch;        // screen tiles per work item of the persistent composite (1, 2, 4 or 8)
 };
 
 // One frame covers a contiguous range of the uploaded scenes; paths,
@@ -45,6 +46,7 @@ struct FrameDev {
     int32_t*  col_backdrop;      // [col_cap] above-rect column sums
     uint32_t* seg_line_count;    // [seg_count+1] flattened lines per input segment
     uint32_t* seg_line_base;     // [seg_count+1] exclusive scan
+    unsigned long long* seg_leaves;  // [seg_count] leaf start slots of each segment's subdivision (0: walked)
     float4*   lines;             // [line_cap] flattened lines in emission order
     uint32_t* line_path;         // [line_cap] global path of each line
     uint32_t* line_fill_count;   // [line_cap+1] kept fills per line
@@ -60,6 +62,10 @@ struct FrameDev {
     uint32_t* screen_base;       // [screen_count+1]
     uint32_t* vis;               // [vis_cap] global tile indices
     int4*     vis_info;          // [vis_cap] per visible tile: see VisInfo
+    unsigned long long* vis_key; // [vis_cap] global tile << 32 | slot: draw order within a screen tile
+    uint4*    vis_mask;          // [vis_cap * 32] resolved coverage of each visible entry with a mask:
+                                 //   16-bit unorm, lane l's 8 pixels (column l & 15, rows (l >> 4) * 8 ..) at 32 * slot + l
+    int4*     mask_items;        // [vis_cap] visible entries with a mask: first fill, fill count, meta, slot
     Counters* counters;
     uint32_t dda_limit;
     uint32_t clip_chain_max;     // bound of clip-chain walks (longest chain in the batch)
@@ -262,6 +268,8 @@ void launch_scan_multi(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_c
 void launch_propagate(const FrameDev& f, bool clip_pass, cudaStream_t s);
 void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s);
 // mode 0: RGBA8, 1: R8 single channel, 2: FP32 single channel
+// The fill pass (resolved coverage of every visible tile with a mask), then
+// the composite.
 void launch_composite(const FrameDev& f, int mode, void* out, const float4& background, cudaStream_t s);
 void launch_masks(const FrameDev& f, float* alpha_masks, float* tile_cov, cudaStream_t s);
 

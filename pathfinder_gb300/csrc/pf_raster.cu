@@ -19,6 +19,7 @@
 #include "pf_kernels.cuh"
 #include "pathfinder_cuda.h"
 
+#include <algorithm>
 #include <atomic>
 
 namespace pf {
@@ -196,6 +197,7 @@ __global__ void k_visible(FrameDev f, int scatter) {
             uint32_t slot = f.screen_base[st] + atomicSub(&f.screen_cnt[st], 1u) - 1u;
             if (slot < f.vis_cap) {
                 f.vis[slot] = g;
+                f.vis_key[slot] = ((unsigned long long)g << 32) | slot;
                 uint32_t kind = (uint32_t)rec.y == kInvalid ? kVisSolid : kVisMask;
                 if (tile_ctrl(rec) & kCtrlClipChain) kind = kVisChain;
                 else if (kind == kVisMask && f.path.clip_gpath[gp] >= 0) {
@@ -208,10 +210,19 @@ __global__ void k_visible(FrameDev f, int scatter) {
                     b0 = f.tile_fill_base[owner];
                     nf = f.tile_fill_base[owner + 1] - b0;
                 }
-                f.vis_info[slot] = make_int4((int)b0, (int)nf, (int)f.path.paint[gp],
-                                             vis_meta(tile_backdrop(rec), (tile_ctrl(rec) & 0x2u) != 0, kind,
-                                                      f.paint_effects ? paint_fx_bits(f.path.blend[gp], f.path.overlay[gp])
-                                                                      : 0u));
+                const int32_t meta = vis_meta(tile_backdrop(rec), (tile_ctrl(rec) & 0x2u) != 0, kind,
+                                              f.paint_effects ? paint_fx_bits(f.path.blend[gp], f.path.overlay[gp])
+                                                              : 0u);
+                f.vis_info[slot] = make_int4((int)b0, (int)nf, (int)f.path.paint[gp], meta);
+                if (kind != kVisSolid) {
+                    // the mask kernel's work list, one slot reservation per warp
+                    const uint32_t m = __activemask();
+                    const int leader = __ffs(m) - 1, lane = threadIdx.x & 31;
+                    uint32_t at = 0;
+                    if (lane == leader) at = atomicAdd(&f.counters->mask_items, (uint32_t)__popc(m));
+                    at = __shfl_sync(m, at, leader) + (uint32_t)__popc(m & ((1u << lane) - 1u));
+                    if (at < f.vis_cap) f.mask_items[at] = make_int4((int)b0, (int)nf, meta, (int)slot);
+                }
             }
         }
     }
@@ -264,10 +275,10 @@ __device__ __forceinline__ unsigned long long warp_sort_lanes(unsigned long long
 
 struct __align__(16) CovBuf { int acc[256]; int carry[256]; };  // cleared with int4 stores
 
-// Accumulate fills [b0, b1) (one alpha tile's) into `buf` (one warp).  DIFF
-// reads the FP32 fills of differentiable frames.
-template <bool DIFF = false>
-__device__ __forceinline__ void warp_accumulate_fills(const FrameDev& f, uint32_t b0, uint32_t b1, CovBuf& buf) {
+// Accumulate `count` fills into `buf` (one warp); fetch(i, x0, y0, x1, y1)
+// gives fill i in tile pixels.
+template <class Fetch>
+__device__ __forceinline__ void warp_accumulate(uint32_t count, Fetch&& fetch, CovBuf& buf) {
     const int lane = threadIdx.x & 31;
     int4* z = reinterpret_cast<int4*>(&buf);  // acc and carry: 512 ints
 #pragma unroll
@@ -276,20 +287,13 @@ __device__ __forceinline__ void warp_accumulate_fills(const FrameDev& f, uint32_
     // Work items are (fill, pixel column) pairs, spread over the lanes: a
     // warp scan of the column counts of 32 fills, then each lane finds the
     // fill of its item with a 5-step search over the scanned counts.
-    for (uint32_t base = b0; base < b1; base += 32) {
+    for (uint32_t base = 0; base < count; base += 32) {
         const uint32_t i = base + lane;
         float x0 = 0.0f, y0 = 0.0f, x1 = 0.0f, slope = 0.0f;
         int c0 = 0, ncol = 0;
-        if (i < b1) {
+        if (i < count) {
             float y1;
-            if constexpr (DIFF) {
-                const float4 rec = f.fills_f[i];
-                x0 = rec.x; y0 = rec.y; x1 = rec.z; y1 = rec.w;
-            } else {
-                const uint2 rec = f.fills[i];
-                x0 = (float)(rec.x & 0xffffu) * (1.0f / 256.0f); y0 = (float)(rec.x >> 16) * (1.0f / 256.0f);
-                x1 = (float)(rec.y & 0xffffu) * (1.0f / 256.0f); y1 = (float)(rec.y >> 16) * (1.0f / 256.0f);
-            }
+            fetch(i, x0, y0, x1, y1);
             if (x0 != x1) {
                 slope = __fdividef(y1 - y0, x1 - x0);
                 c0 = max((int)floorf(fminf(x0, x1)), 0);
@@ -322,6 +326,29 @@ __device__ __forceinline__ void warp_accumulate_fills(const FrameDev& f, uint32_
     __syncwarp();
 }
 
+// `count` packed LineSegmentU16 fills at `src` (global or shared memory).
+__device__ __forceinline__ void warp_accumulate_packed(const uint2* src, uint32_t count, CovBuf& buf) {
+    warp_accumulate(count, [&](uint32_t i, float& x0, float& y0, float& x1, float& y1) {
+        const uint2 rec = src[i];
+        x0 = (float)(rec.x & 0xffffu) * (1.0f / 256.0f); y0 = (float)(rec.x >> 16) * (1.0f / 256.0f);
+        x1 = (float)(rec.y & 0xffffu) * (1.0f / 256.0f); y1 = (float)(rec.y >> 16) * (1.0f / 256.0f);
+    }, buf);
+}
+
+// Fills [b0, b1) (one alpha tile's).  DIFF reads the FP32 fills of
+// differentiable frames.
+template <bool DIFF = false>
+__device__ __forceinline__ void warp_accumulate_fills(const FrameDev& f, uint32_t b0, uint32_t b1, CovBuf& buf) {
+    if constexpr (DIFF) {
+        warp_accumulate(b1 - b0, [&](uint32_t i, float& x0, float& y0, float& x1, float& y1) {
+            const float4 rec = f.fills_f[b0 + i];
+            x0 = rec.x; y0 = rec.y; x1 = rec.z; y1 = rec.w;
+        }, buf);
+    } else {
+        warp_accumulate_packed(f.fills + b0, b1 - b0, buf);
+    }
+}
+
 // The same for alpha tile `alpha`, its fill range found through its owner.
 template <bool DIFF = false>
 __device__ __forceinline__ void warp_accumulate_tile(const FrameDev& f, uint32_t alpha, CovBuf& buf) {
@@ -348,7 +375,8 @@ __device__ __forceinline__ void warp_column_values(const CovBuf& buf, int out[8]
     }
 }
 
-struct WarpScratch { uint32_t keys[128]; CovBuf b0, b1; };
+constexpr uint32_t kWarpListCap = 128;
+struct WarpScratch { uint32_t keys[kWarpListCap]; CovBuf b0, b1; };
 
 // Per-pixel coverage of one path tile for this lane's 8 pixels.
 // |mask + backdrop| of one tile for this lane's 8 pixels (the backdrop alone
@@ -727,120 +755,262 @@ __device__ __forceinline__ void composite_paint_tile(const FrameDev& f, uint32_t
 }
 
 // ---------------------------------------------------------------------------
-// fused fill + composite: one warp per screen tile, no block barriers
+// Fill + composite in two kernels.  k_mask: one warp per visible tile with a
+// mask (the fill pass, shaders/d3d11/fill.cs.glsl:61-88, with the resolve and
+// clip combine of the tile pass) writes its resolved coverage as 16-bit
+// unorms; visible entries are independent, so every warp works on its own
+// tile.  k_composite: a persistent kernel whose warps pull batches of screen
+// tiles from a work counter and composite each screen tile's visible list in
+// draw order (tile.cs.glsl:91-159) from those coverages.
 // ---------------------------------------------------------------------------
-constexpr uint32_t kWarpListCap = 128;
+__device__ __forceinline__ uint4 pack_cov16(const float cov[8]) {
+    auto q = [](float c) { return (uint32_t)__float2uint_rn(__saturatef(c) * 65535.0f); };
+    return make_uint4(q(cov[0]) | (q(cov[1]) << 16), q(cov[2]) | (q(cov[3]) << 16), q(cov[4]) | (q(cov[5]) << 16),
+                      q(cov[6]) | (q(cov[7]) << 16));
+}
+__device__ __forceinline__ void unpack_cov16(uint4 m, float cov[8]) {
+    const float s = 1.0f / 65535.0f;
+    cov[0] = (float)(m.x & 0xffffu) * s; cov[1] = (float)(m.x >> 16) * s;
+    cov[2] = (float)(m.y & 0xffffu) * s; cov[3] = (float)(m.y >> 16) * s;
+    cov[4] = (float)(m.z & 0xffffu) * s; cov[5] = (float)(m.z >> 16) * s;
+    cov[6] = (float)(m.w & 0xffffu) * s; cov[7] = (float)(m.w >> 16) * s;
+}
 
-// Per warp: the screen tile's list as (tile << 32 | position) keys, the
-// visible-tile records by position, and two coverage buffers.
-struct CompositeScratch {
-    unsigned long long keys[kWarpListCap];
-    int4 info[kWarpListCap];
+// Occupancy of a kernel instance on the current device, queried once per
+// instance and device (persistent grids are the multiprocessors times this).
+template <typename K>
+int resident_blocks(K kernel, int threads) {
+    static std::atomic<int> cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    int v = cache[dev].load(std::memory_order_relaxed);
+    if (v) return v;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, 0) != cudaSuccess || v <= 0) v = 1;
+    cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
+
+// ---- bulk copies (cp.async.bulk) into shared memory, completed on an mbarrier
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+// orders this thread's earlier shared-memory accesses before later bulk copies into the same memory
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bulk_copy_to_smem(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Bounded wait for phase `parity` of `bar` to complete (false: gave up).
+constexpr uint32_t kCopyWaitLimit = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+    for (uint32_t it = 0; it < kCopyWaitLimit; it++)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+
+// k_mask: each warp takes every (total warps)-th entry of the mask work list.
+// An entry's fill range is copied into the warp's shared memory by one bulk
+// copy (rounded out to 16-byte boundaries) one entry ahead of its use, and
+// the work list itself is read two entries ahead, so a warp waits on neither.
+// Ranges larger than a staging buffer, and clip-combined or clip-chain tiles
+// (which read tile and clip records), are read from global memory.
+constexpr int kMaskKernelWarps = 4;
+constexpr uint32_t kStageFills = 128;  // per staging buffer (1 KiB)
+struct MaskScratch {
     CovBuf b0, b1;
+    uint2 stage[2][kStageFills];
+    unsigned long long bar[2];
 };
 
-// Without paint effects the kernel is held to 80 registers (24 warps an SM):
-// fewer registers than it would take, a few spilled, and more warps to hide
-// the latency of each visible tile's dependent steps.
-template <int MODE, int WARPS, bool PAINT>
-__global__ void __launch_bounds__(WARPS * 32, PAINT ? 1 : 24 / WARPS) k_composite(FrameDev f, void* out, float4 bg) {
-    extern __shared__ __align__(16) unsigned char comp_smem[];
-    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t st = blockIdx.x * WARPS + wid;  // frame screen tile
-    if (st >= f.screen_count) return;
-    CompositeScratch& ws = reinterpret_cast<CompositeScratch*>(comp_smem)[wid];
+// Issue the bulk copy of entry `e`'s fills into staging buffer `buf` (lane 0;
+// every lane gets the same answer: whether it was issued).
+__device__ __forceinline__ bool stage_fills(const FrameDev& f, int4 e, MaskScratch& ws, int buf) {
+    const uint32_t kind = ((uint32_t)e.z >> 9) & 3u;
+    if (kind != kVisMask || e.y == 0) return false;
+    const uint32_t first = (uint32_t)e.x & ~1u, end = ((uint32_t)e.x + (uint32_t)e.y + 1u) & ~1u;
+    if (end - first > kStageFills) return false;
+    if ((threadIdx.x & 31) == 0) {
+        fence_proxy_async_smem();  // the buffer's previous contents were read through the generic proxy
+        bulk_copy_to_smem(ws.stage[buf], f.fills + first, (end - first) * 8u, &ws.bar[buf]);
+    }
+    return true;
+}
 
+__global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask(FrameDev f) {
+    __shared__ MaskScratch scratch[kMaskKernelWarps];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    MaskScratch& ws = scratch[wid];
+    if (!frame_ok(f) || f.counters->fills > f.fill_cap || f.counters->visible > f.vis_cap) return;
+    const uint32_t M = (uint32_t)min((unsigned long long)f.counters->mask_items, (unsigned long long)f.vis_cap);
+    const uint32_t stride = gridDim.x * kMaskKernelWarps;
+    uint32_t k = blockIdx.x * kMaskKernelWarps + wid;
+    if (k >= M) return;
+    if (lane == 0) {
+        mbar_init(&ws.bar[0], 1);
+        mbar_init(&ws.bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    const int4 none = make_int4(0, 0, 0, 0);  // a solid entry: no work
+    int4 cur = f.mask_items[k];
+    int4 nxt = k + stride < M ? f.mask_items[k + stride] : none;
+    uint32_t phase = 0;  // bit b: parity of the next completion of buffer b
+    int buf = 0;
+    bool cur_staged = stage_fills(f, cur, ws, buf);
+    bool stalled = false;
+    int stall_buf = 0;
+    uint32_t stall_parity = 0;
+    for (; k < M; k += stride) {
+        const int4 later = k + 2 * stride < M ? f.mask_items[k + 2 * stride] : none;
+        const bool nxt_staged = !stalled && stage_fills(f, nxt, ws, buf ^ 1);
+        const uint32_t kind = ((uint32_t)cur.z >> 9) & 3u, slot = (uint32_t)cur.w;
+        float cov[8];
+        if (kind == kVisMask) {
+            const uint2* src = f.fills + (uint32_t)cur.x;
+            if (cur_staged) {
+                const uint32_t parity = (phase >> buf) & 1u;
+                const bool arrived = mbar_wait(&ws.bar[buf], parity);
+                phase ^= 1u << buf;
+                if (arrived) {
+                    src = ws.stage[buf] + ((uint32_t)cur.x & 1u);
+                } else if (!stalled) {
+                    stalled = true;  // no more copies: read global memory from here on
+                    stall_buf = buf;
+                    stall_parity = parity;
+                    if (lane == 0) atomicOr(&f.counters->status, kStatusCopyStall);
+                }
+            }
+            int v[8];
+            warp_accumulate_packed(src, (uint32_t)cur.y, ws.b0);
+            warp_column_values(ws.b0, v);
+            __syncwarp();  // the buffer is cleared by the next tile
+            const bool even_odd = ((uint32_t)cur.z >> 8) & 1u;
+            const float bd = (float)(int8_t)(cur.z & 0xff);
+#pragma unroll
+            for (int q = 0; q < 8; q++) cov[q] = resolve_coverage((float)v[q] * kCovInvScale + bd, even_odd);
+        } else {  // clip-combined or behind a clip chain: from the tile and clip records
+            const uint32_t g = (uint32_t)(f.vis_key[slot] >> 32);
+            tile_coverage8(f, f.tiles[g], g, ws.b0, ws.b1, cov);
+        }
+        f.vis_mask[(size_t)slot * 32u + (uint32_t)lane] = pack_cov16(cov);
+        cur = nxt;
+        nxt = later;
+        cur_staged = nxt_staged;
+        buf ^= 1;
+    }
+    // the copy a wait gave up on may still be in flight: wait for it again,
+    // with the same bound, before the warp leaves its shared memory
+    if (stalled) mbar_wait(&ws.bar[stall_buf], stall_parity);
+}
+
+void launch_mask(const FrameDev& f, cudaStream_t s) {
+    const int blocks = (int)f.sms * resident_blocks(k_mask, kMaskKernelWarps * 32);
+    count_launch();
+    k_mask<<<blocks, kMaskKernelWarps * 32, 0, s>>>(f);
+}
+
+// Composite screen tile st (frame index) into this lane's 8 pixels: n
+// visible entries from `base`; for n <= 32, lane_key is the lane's entry key
+// (read ahead by the caller).
+template <int MODE, bool PAINT>
+__device__ __forceinline__ void composite_screen_tile(const FrameDev& f, uint32_t st, uint32_t base, uint32_t n,
+                                                      unsigned long long lane_key, void* out, float4 bg) {
+    const int lane = threadIdx.x & 31, col = lane & 15, half = lane >> 4;
     const SceneDev& sc = f.scenes[scene_of_screen_tile(f, f.screen_begin + st)];
     const int4 s = sc.screen;
     const int32_t sw = s.z - s.x;
     const uint32_t lst = f.screen_begin + st - sc.screen_offset;
     const uint32_t row = lst / (uint32_t)sw;
     const int32_t tx = s.x + (int32_t)(lst - row * (uint32_t)sw), ty = s.y + (int32_t)row;
-    const int col = lane & 15, half = lane >> 4;
 
-    const bool ok = frame_ok(f) && f.counters->fills <= f.fill_cap && f.counters->visible <= f.vis_cap;
-    uint32_t n = 0, base = 0;
-    if (ok) { base = f.screen_base[st]; n = f.screen_base[st + 1] - base; }
-
-    // draw order = global tile order (paths in order)
-    const bool short_list = n <= kWarpListCap, lane_list = n <= 32;  // up to 32: one key per lane
-    unsigned long long lane_key = ~0ull;
+    // draw order = global tile order (paths in order): sort the (tile, slot) keys
+    const bool lane_list = n <= 32;  // one key per lane; longer lists sort in place in global memory
+    int2 lane_info = make_int2(0, 0);  // paint, meta of the lane's entry in draw order
     if (lane_list) {
-        if ((uint32_t)lane < n) {
-            lane_key = ((unsigned long long)f.vis[base + lane] << 32) | (uint32_t)lane;
-            ws.info[lane] = f.vis_info[base + lane];
-        }
         uint32_t N = 1;
         while (N < n) N <<= 1;
         if (n > 1) lane_key = warp_sort_lanes(lane_key, N);
-        __syncwarp();
-    } else if (short_list) {
-        for (uint32_t i = lane; i < n; i += 32) {
-            ws.keys[i] = ((unsigned long long)f.vis[base + i] << 32) | i;
-            ws.info[i] = f.vis_info[base + i];
+        if ((uint32_t)lane < n) {
+            const int4 info = f.vis_info[(uint32_t)lane_key];
+            lane_info = make_int2(info.z, info.w);
         }
-        __syncwarp();
-        warp_bitonic_sort(ws.keys, n);
     } else {
-        warp_bitonic_sort(f.vis + base, n);  // rare: long lists sort in place in global memory
+        warp_bitonic_sort(f.vis_key + base, n);
     }
+    // entry i of the draw order: slot, paint, meta; its coverage is fetched
+    // one entry ahead
+    auto entry = [&](uint32_t i, uint32_t& slot, uint32_t& paint, uint32_t& meta) {
+        if (lane_list) {
+            slot = __shfl_sync(0xffffffffu, (uint32_t)lane_key, (int)i);
+            paint = (uint32_t)__shfl_sync(0xffffffffu, lane_info.x, (int)i);
+            meta = (uint32_t)__shfl_sync(0xffffffffu, lane_info.y, (int)i);
+        } else {
+            slot = (uint32_t)f.vis_key[base + i];
+            const int4 info = f.vis_info[slot];
+            paint = (uint32_t)info.z;
+            meta = (uint32_t)info.w;
+        }
+    };
+    // (read whatever the kind: a solid entry's slot holds no coverage, and its
+    // value is not used; the read starts before the entry's kind is known)
+    auto fetch = [&](uint32_t slot) { return f.vis_mask[(size_t)slot * 32u + (uint32_t)lane]; };
 
     float d0[8], d1[8], d2[8], d3[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) { d0[k] = bg.x; d1[k] = bg.y; d2[k] = bg.z; d3[k] = bg.w; }
+    uint32_t n_slot = 0, n_paint = 0, n_meta = 0;
+    uint4 n_mask = make_uint4(0u, 0u, 0u, 0u);
+    if (n) {
+        entry(0, n_slot, n_paint, n_meta);
+        n_mask = fetch(n_slot);
+    }
     for (uint32_t i = 0; i < n; i++) {
-        float cov[8];
-        uint32_t paint, fx = 0;
-        uint32_t kind = kVisCombine;
-        int4 info = make_int4(0, 0, 0, 0);
-        uint32_t g;
-        if (short_list) {
-            const unsigned long long key = lane_list ? __shfl_sync(0xffffffffu, lane_key, (int)i) : ws.keys[i];
-            g = (uint32_t)(key >> 32);
-            info = ws.info[(uint32_t)key];
-            kind = ((uint32_t)info.w >> 9) & 3u;
-            paint = (uint32_t)info.z;
-            if (PAINT) fx = (uint32_t)info.w >> 11;
-        } else {
-            g = f.vis[base + i];
+        const uint32_t paint = n_paint, meta = n_meta;
+        const uint4 m = n_mask;
+        if (i + 1 < n) {
+            entry(i + 1, n_slot, n_paint, n_meta);
+            n_mask = fetch(n_slot);
         }
-        if (kind == kVisMask) {
-            const bool even_odd = ((uint32_t)info.w >> 8) & 1u;
-            const float bd = (float)(int8_t)(info.w & 0xff);
-            int v[8];
-            warp_accumulate_fills(f, (uint32_t)info.x, (uint32_t)info.x + (uint32_t)info.y, ws.b0);
-            warp_column_values(ws.b0, v);
-            __syncwarp();  // the buffer is cleared by the next tile
-#pragma unroll
-            for (int k = 0; k < 8; k++) cov[k] = resolve_coverage((float)v[k] * kCovInvScale + bd, even_odd);
-        } else if (kind == kVisSolid) {
-            const float c = resolve_coverage((float)(int8_t)(info.w & 0xff), ((uint32_t)info.w >> 8) & 1u);
+        float cov[8];
+        if (((meta >> 9) & 3u) == kVisSolid) {
+            const float c = resolve_coverage((float)(int8_t)(meta & 0xffu), (meta >> 8) & 1u);
 #pragma unroll
             for (int k = 0; k < 8; k++) cov[k] = c;
-        } else {  // clip-combined tile, or a long list: from the tile records
-            const int4 rec = f.tiles[g];
-            tile_coverage8(f, rec, g, ws.b0, ws.b1, cov);
-            const uint32_t gp = (uint32_t)rec.z;
-            paint = f.path.paint[gp];
-            if (PAINT) fx = paint_fx_bits(f.path.blend[gp], f.path.overlay[gp]);
+        } else {
+            unpack_cov16(m, cov);
         }
-        float pa = (float)(paint >> 24) * (1.0f / 255.0f);
+        const uint32_t fx = PAINT ? (meta >> 11) : 0u;
+        const float pa = (float)(paint >> 24) * (1.0f / 255.0f);
         if (PAINT && fx != 0) {
             composite_paint_tile(f, fx, paint, cov, tx, ty, col, half, d0, d1, d2, d3);
         } else if (MODE == 0) {
-            float pr = (float)(paint & 0xffu) * (1.0f / 255.0f);
-            float pg = (float)((paint >> 8) & 0xffu) * (1.0f / 255.0f);
-            float pb = (float)((paint >> 16) & 0xffu) * (1.0f / 255.0f);
+            const float pr = (float)(paint & 0xffu) * (1.0f / 255.0f);
+            const float pg = (float)((paint >> 8) & 0xffu) * (1.0f / 255.0f);
+            const float pb = (float)((paint >> 16) & 0xffu) * (1.0f / 255.0f);
 #pragma unroll
             for (int k = 0; k < 8; k++) {
-                float a = pa * cov[k], ia = 1.0f - a;
+                const float a = pa * cov[k], ia = 1.0f - a;
                 d0[k] = pr * a + d0[k] * ia; d1[k] = pg * a + d1[k] * ia;
                 d2[k] = pb * a + d2[k] * ia; d3[k] = a + d3[k] * ia;
             }
         } else {
 #pragma unroll
             for (int k = 0; k < 8; k++) {
-                float a = pa * cov[k];
+                const float a = pa * cov[k];
                 d3[k] = a + d3[k] * (1.0f - a);
             }
         }
@@ -855,32 +1025,60 @@ __global__ void __launch_bounds__(WARPS * 32, PAINT ? 1 : 24 / WARPS) k_composit
     for (int k = 0; k < 8; k++, o += (uint64_t)(int64_t)sc.pitch) {
         if (!rows_inside && (Y0 + k < sc.clip.y || Y0 + k >= sc.clip.w)) continue;
         if (MODE == 0) {
-            auto q = [](float v) { return (uint32_t)__float2uint_rn(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f); };
+            auto q = [](float v) { return (uint32_t)__float2uint_rn(__saturatef(v) * 255.0f); };
             ((uint32_t*)out)[o] = q(d0[k]) | (q(d1[k]) << 8) | (q(d2[k]) << 16) | (q(d3[k]) << 24);
         } else if (MODE == 1) {
-            ((uint8_t*)out)[o] = (uint8_t)__float2uint_rn(fminf(fmaxf(d3[k], 0.0f), 1.0f) * 255.0f);
+            ((uint8_t*)out)[o] = (uint8_t)__float2uint_rn(__saturatef(d3[k]) * 255.0f);
         } else {
             ((float*)out)[o] = d3[k];
         }
     }
 }
 
-// Solid SrcOver batches run the instance without the paint-effect path.
+// Persistent: each warp pulls batches of `comp_batch` screen tiles from the
+// frame's work counter until none are left, so long lists do not hold up a
+// fixed share of the grid.
+template <int MODE, int WARPS, bool PAINT>
+__global__ void __launch_bounds__(WARPS * 32, PAINT ? 1 : 32 / WARPS) k_composite(FrameDev f, void* out, float4 bg) {
+    const int lane = threadIdx.x & 31;
+    const bool ok = frame_ok(f) && f.counters->fills <= f.fill_cap && f.counters->visible <= f.vis_cap;
+    const uint32_t batch = (uint32_t)f.tune.comp_batch;
+    for (uint32_t it = 0; it <= f.screen_count; it++) {  // bounded: each step takes at least one tile
+        uint32_t st0 = 0;
+        if (lane == 0) st0 = atomicAdd(&f.counters->composite_next, batch);
+        st0 = __shfl_sync(0xffffffffu, st0, 0);
+        if (st0 >= f.screen_count) break;
+        const uint32_t nb = min(st0 + batch, f.screen_count) - st0;
+        // the batch's list bounds (lane t: screen_base[st0 + t]); each tile's
+        // keys are read while the previous tile composites
+        const uint32_t lb = (ok && (uint32_t)lane <= nb) ? f.screen_base[st0 + lane] : 0u;
+        auto keys = [&](uint32_t t, uint32_t& base, uint32_t& n) {
+            base = __shfl_sync(0xffffffffu, lb, (int)t);
+            n = __shfl_sync(0xffffffffu, lb, (int)t + 1) - base;
+            return (n <= 32 && (uint32_t)lane < n) ? f.vis_key[base + lane] : ~0ull;
+        };
+        uint32_t base, n;
+        unsigned long long key = keys(0, base, n);
+        for (uint32_t t = 0; t < nb; t++) {
+            uint32_t base_n = 0, n_n = 0;
+            unsigned long long key_n = ~0ull;
+            if (t + 1 < nb) key_n = keys(t + 1, base_n, n_n);
+            composite_screen_tile<MODE, PAINT>(f, st0 + t, base, n, key, out, bg);
+            base = base_n;
+            n = n_n;
+            key = key_n;
+        }
+    }
+}
+
 template <int MODE, int WARPS, bool PAINT>
 void launch_composite_instance(const FrameDev& f, void* out, const float4& bg, cudaStream_t s) {
-    constexpr size_t smem = WARPS * sizeof(CompositeScratch);
-    // Above 48 KiB needs the opt-in, once per instance and device (the
-    // attribute belongs to the device's context).  Setting it twice is
-    // harmless, so concurrent first calls need no lock.
-    static std::atomic<uint64_t> configured{0};
-    int dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && !((configured.load() >> dev) & 1u)) {
-        if (cudaFuncSetAttribute(k_composite<MODE, WARPS, PAINT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) == cudaSuccess)
-            configured.fetch_or(1ull << dev);
-    }
+    const int threads = WARPS * 32;
+    const uint32_t per_block = (uint32_t)f.tune.comp_batch * WARPS;
+    const uint32_t needed = (f.screen_count + per_block - 1) / per_block;
+    const uint32_t resident = f.sms * (uint32_t)resident_blocks(k_composite<MODE, WARPS, PAINT>, threads);
     count_launch();
-    k_composite<MODE, WARPS, PAINT><<<(f.screen_count + WARPS - 1) / WARPS, WARPS * 32, smem, s>>>(f, out, bg);
+    k_composite<MODE, WARPS, PAINT><<<std::max(1u, std::min(needed, resident)), threads, 0, s>>>(f, out, bg);
 }
 
 template <int MODE, int WARPS>
@@ -899,6 +1097,7 @@ void launch_composite_mode(const FrameDev& f, void* out, const float4& bg, cudaS
 
 void launch_composite(const FrameDev& f, int mode, void* out, const float4& bg, cudaStream_t s) {
     if (f.screen_count == 0) return;
+    launch_mask(f, s);
     if (mode == 0) launch_composite_mode<0>(f, out, bg, s);
     else if (mode == 1) launch_composite_mode<1>(f, out, bg, s);
     else launch_composite_mode<2>(f, out, bg, s);

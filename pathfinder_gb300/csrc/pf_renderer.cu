@@ -116,7 +116,7 @@ struct Range {
     uint32_t st0 = 0, st1 = 0;   // screen tiles
 };
 
-const TuneParams kDefaultTune{128, 256, 32, 2};
+const TuneParams kDefaultTune{128, 256, 32, 4, 2};
 
 }  // namespace
 
@@ -130,6 +130,12 @@ struct PFCUDARenderer {
     // points_done before anything that reads points.
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t points_done = nullptr, prior_done = nullptr;
+    // A frame runs two pairs of independent stages side by side: flattening
+    // beside the bounds and path scans, and the fill emission beside
+    // propagation and visibility.  The second branch of each pair runs on
+    // branch_stream, forked from and joined back to the frame's stream.
+    cudaStream_t branch_stream = nullptr;
+    cudaEvent_t fork_ev[2] = {}, join_ev[2] = {};
     PFCUDARendererOptions options{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -161,6 +167,7 @@ struct PFCUDARenderer {
     DevBuf<int4> tile_rect;
     DevBuf<uint32_t> tile_offset, col_offset;
     DevBuf<uint32_t> seg_line_count, seg_line_base;
+    DevBuf<unsigned long long> seg_leaves;
     DevBuf<float4> lines;
     DevBuf<uint32_t> line_path, line_fill_count, line_fill_base;
     DevBuf<uint32_t> tile_fill_count, tile_fill_base, tile_alpha, alpha_owner;
@@ -171,7 +178,10 @@ struct PFCUDARenderer {
     DevBuf<int4> tiles, clips;
     DevBuf<uint32_t> screen_cnt, screen_base, vis;
     DevBuf<int4> vis_info;
-    DevBuf<uint32_t> scan_partials;
+    DevBuf<unsigned long long> vis_key;
+    DevBuf<uint4> vis_mask;
+    DevBuf<int4> mask_items;
+    DevBuf<uint32_t> scan_partials, scan_partials_branch;
     DevBuf<Counters> counters;
     DevBuf<uint8_t> out_tmp;
     Counters* h_counters = nullptr;  // pinned
@@ -333,6 +343,7 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.col_backdrop = r->col_backdrop.p;
     f.seg_line_count = r->seg_line_count.p;
     f.seg_line_base = r->seg_line_base.p;
+    f.seg_leaves = r->seg_leaves.p;
     f.lines = r->lines.p;
     f.line_path = r->line_path.p;
     f.line_fill_count = r->line_fill_count.p;
@@ -348,6 +359,9 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.screen_base = r->screen_base.p;
     f.vis = r->vis.p;
     f.vis_info = r->vis_info.p;
+    f.vis_key = r->vis_key.p;
+    f.vis_mask = r->vis_mask.p;
+    f.mask_items = r->mask_items.p;
     f.counters = r->counters.p;
     f.dda_limit = 1u << 24;
     f.clip_chain_max = r->clip_chain_max;
@@ -364,7 +378,9 @@ cudaError_t ensure_frame_buffers(PFCUDARenderer* r) {
         (e = r->tiles.ensure(T)) || (e = r->clips.ensure(T)) || (e = r->col_backdrop.ensure((size_t)r->col_cap + 1)) ||
         (e = r->fills.ensure(F)) || (e = r->fill_e.ensure(F)) || (e = r->lines.ensure(L)) ||
         (e = r->line_path.ensure(L)) || (e = r->line_fill_count.ensure(L)) || (e = r->line_fill_base.ensure(L)) ||
-        (e = r->vis.ensure((size_t)r->vis_cap + 1)) || (e = r->vis_info.ensure((size_t)r->vis_cap + 1)) || (e = r->zbuf.ensure(ST)) || (e = r->screen_cnt.ensure(ST)) ||
+        (e = r->vis.ensure((size_t)r->vis_cap + 1)) || (e = r->vis_info.ensure((size_t)r->vis_cap + 1)) ||
+        (e = r->vis_key.ensure((size_t)r->vis_cap + 1)) || (e = r->vis_mask.ensure(((size_t)r->vis_cap + 1) * 32)) ||
+        (e = r->mask_items.ensure((size_t)r->vis_cap + 1)) || (e = r->zbuf.ensure(ST)) || (e = r->screen_cnt.ensure(ST)) ||
         (e = r->screen_base.ensure(ST)) || (e = r->path_tiles.ensure(P)) || (e = r->path_cols.ensure(P)))
         return e;
     if (r->diff_buffers) {
@@ -375,6 +391,8 @@ cudaError_t ensure_frame_buffers(PFCUDARenderer* r) {
     }
     size_t nmax = std::max<size_t>({(size_t)r->tile_cap, (size_t)r->S, (size_t)r->screen_total, (size_t)r->nord,
                                     (size_t)r->line_cap, (size_t)r->P}) + 1;
+    if ((e = r->scan_partials_branch.ensure(kMaxScanLanes * ((size_t)r->S + 1) / 2048 + 2 * kMaxScanLanes)))
+        return e;
     return r->scan_partials.ensure(kMaxScanLanes * (nmax / 2048 + 2));
 }
 
@@ -421,18 +439,35 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
         }
     }
     ScanTemp tmp{r->scan_partials.p, (uint32_t)r->scan_partials.cap};
+    ScanTemp tmp_branch{r->scan_partials_branch.p, (uint32_t)r->scan_partials_branch.cap};
     Counters* c = r->counters.p;
     auto mark = [&](int stage) {
         if (r->profiling) cudaEventRecord(r->stage_ev[stage], s);
+    };
+    // Stage-timed frames run every kernel on the frame's stream, in order.
+    const bool branches = !r->profiling;
+    cudaStream_t b = branches ? r->branch_stream : s;
+    auto fork = [&](int k) -> cudaError_t {
+        if (!branches) return cudaSuccess;
+        cudaError_t e1 = cudaEventRecord(r->fork_ev[k], s);
+        return e1 ? e1 : cudaStreamWaitEvent(b, r->fork_ev[k], 0);
+    };
+    auto join = [&](int k) -> cudaError_t {
+        if (!branches) return cudaSuccess;
+        cudaError_t e1 = cudaEventRecord(r->join_ev[k], b);
+        return e1 ? e1 : cudaStreamWaitEvent(s, r->join_ev[k], 0);
     };
     const size_t nst = (size_t)(g.st1 - g.st0) + 1;
     uint64_t before = launch_counter();
     if ((e = cudaMemsetAsync(c, 0, sizeof(Counters), s))) return e;
     mark(0);
+    // flattening needs no tile rects: it runs beside the bounds and path scans
+    if ((e = fork(0))) return e;
     launch_bound(f, r->ord_contour.p, r->starts.p, s);
     launch_path_scan(f, tmp, s);
     mark(1);
-    launch_flatten(f, tmp, s);
+    launch_flatten(f, branches ? tmp_branch : tmp, b);
+    if ((e = join(0))) return e;
     mark(2);
     launch_bin_count(f, s);
     mark(3);
@@ -448,7 +483,10 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
         launch_scan_multi(lanes, &c->tiles, r->tile_cap, tmp, s);
     }
     mark(4);
-    launch_bin_emit(f, s);
+    // propagation and visibility read the tile scans, not the fills: the fill
+    // emission runs beside them
+    if ((e = fork(1))) return e;
+    launch_bin_emit(f, b);
     mark(5);
     // clip paths first: draw tiles of clipped paths read their clip's finished tiles
     launch_propagate(f, true, s);
@@ -458,6 +496,7 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     launch_scan(r->screen_cnt.p, r->screen_base.p, nullptr, (uint32_t)(nst - 1), (uint32_t)(nst - 1), 0, &c->visible,
                 tmp, s);
     launch_visible(f, true, s);
+    if ((e = join(1))) return e;
     mark(7);
     if (mode >= 0 || diff) {
         const float4 bg = background_of(r);
@@ -699,6 +738,11 @@ int32_t PFCUDARendererCreate(int32_t device_ordinal, const PFCUDARendererOptions
         (e = cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking)) ||
         (e = cudaEventCreateWithFlags(&r->points_done, cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&r->prior_done, cudaEventDisableTiming)) ||
+        (e = cudaStreamCreateWithFlags(&r->branch_stream, cudaStreamNonBlocking)) ||
+        (e = cudaEventCreateWithFlags(&r->fork_ev[0], cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&r->fork_ev[1], cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&r->join_ev[0], cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&r->join_ev[1], cudaEventDisableTiming)) ||
         (e = cudaEventCreate(&r->ev0)) || (e = cudaEventCreate(&r->ev1)) ||
         (e = cudaMallocHost((void**)&r->h_counters, sizeof(Counters))) || (e = r->counters.ensure(1))) {
         PFCUDARendererDestroy(r);
@@ -720,12 +764,14 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->scene_of.release(); r->clip_gpath.release(); r->rule.release(); r->is_clip.release();
     r->scenes_dev.release(); r->tile_rect.release(); r->tile_offset.release(); r->col_offset.release();
     r->seg_line_count.release(); r->seg_line_base.release(); r->lines.release(); r->line_path.release();
+    r->seg_leaves.release();
     r->line_fill_count.release(); r->line_fill_base.release(); r->tile_fill_count.release();
     r->tile_fill_base.release(); r->tile_alpha.release(); r->alpha_owner.release(); r->tile_delta.release();
     r->tile_delta_scan.release(); r->path_tiles.release(); r->path_cols.release();
     r->col_backdrop.release(); r->zbuf.release(); r->fills.release(); r->fill_e.release(); r->tiles.release();
     r->clips.release(); r->screen_cnt.release(); r->screen_base.release(); r->vis.release(); r->vis_info.release();
-    r->scan_partials.release(); r->counters.release(); r->out_tmp.release();
+    r->vis_key.release(); r->vis_mask.release(); r->mask_items.release();
+    r->scan_partials.release(); r->scan_partials_branch.release(); r->counters.release(); r->out_tmp.release();
     r->draw_index.release(); r->blend.release(); r->occludes.release(); r->overlay.release();
     r->starts_raw.release(); r->path_ncont.release(); r->scene_ranges.release(); r->path_in.release();
     r->scene_pack.release(); r->pack_info.release(); r->overlay_opaque.release(); r->alpha_default.release();
@@ -746,6 +792,14 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     }
     if (r->points_done) cudaEventDestroy(r->points_done);
     if (r->prior_done) cudaEventDestroy(r->prior_done);
+    if (r->branch_stream) {
+        cudaStreamSynchronize(r->branch_stream);
+        cudaStreamDestroy(r->branch_stream);
+    }
+    for (int k = 0; k < 2; k++) {
+        if (r->fork_ev[k]) cudaEventDestroy(r->fork_ev[k]);
+        if (r->join_ev[k]) cudaEventDestroy(r->join_ev[k]);
+    }
     stroke_work_destroy(r->stroke);
     delete r;
     return PF_CUDA_OK;
@@ -949,7 +1003,7 @@ static int32_t upload_tables(PFCUDARendererRef r, const PFCUDASceneDesc* scenes,
     if (hinfo->segs >= 0x7fffffffull) return PF_CUDA_ERR_INVALID;
     const uint32_t S = (uint32_t)hinfo->segs;
     if ((e = r->segs.ensure((size_t)S + 1)) || (e = r->seg_line_count.ensure((size_t)S + 1)) ||
-        (e = r->seg_line_base.ensure((size_t)S + 1)))
+        (e = r->seg_line_base.ensure((size_t)S + 1)) || (e = r->seg_leaves.ensure((size_t)S + 1)))
         return cuda_status(e);
     launch_contour_segemit(r->ord_contour.p, r->ord_path.p, &info->nord, cap, r->starts.p, nb, r->flags.p,
                            r->contour_seg_base.p, r->segs.p, s);
@@ -1225,16 +1279,19 @@ int32_t PFCUDASetTuning(PFCUDARendererRef r, const PFCUDATuning* t) {
     if (!r || !t) return PF_CUDA_ERR_INVALID;
     auto in = [](int v, std::initializer_list<int> ok) { return std::find(ok.begin(), ok.end(), v) != ok.end(); };
     if (!in(t->flatten_threads, {64, 128, 256}) || !in(t->bin_threads, {128, 256, 512}) ||
-        t->bin_blocks_per_sm < 4 || t->bin_blocks_per_sm > 64 || !in(t->composite_warps, {2, 4, 8}))
+        t->bin_blocks_per_sm < 4 || t->bin_blocks_per_sm > 64 || !in(t->composite_warps, {2, 4, 8}) ||
+        !in(t->composite_batch, {1, 2, 4, 8}))
         return PF_CUDA_ERR_INVALID;
-    r->tune = TuneParams{t->flatten_threads, t->bin_threads, t->bin_blocks_per_sm, t->composite_warps};
+    r->tune = TuneParams{t->flatten_threads, t->bin_threads, t->bin_blocks_per_sm, t->composite_warps,
+                         t->composite_batch};
     release_graph(r);
     return PF_CUDA_OK;
 }
 
 int32_t PFCUDAGetTuning(PFCUDARendererRef r, PFCUDATuning* t) {
     if (!r || !t) return PF_CUDA_ERR_INVALID;
-    *t = PFCUDATuning{r->tune.flatten_threads, r->tune.bin_threads, r->tune.bin_blocks_per_sm, r->tune.comp_warps};
+    *t = PFCUDATuning{r->tune.flatten_threads, r->tune.bin_threads, r->tune.bin_blocks_per_sm, r->tune.comp_warps,
+                      r->tune.comp_batch};
     return PF_CUDA_OK;
 }
 
@@ -1263,16 +1320,18 @@ int32_t PFCUDAAutotune(PFCUDARendererRef r, const PFCUDABuildOptions* options, u
     TuneParams best = r->tune;
     float best_ms = 0;
     if ((rc = time_it(best, &best_ms))) return rc;
-    const int flat[] = {64, 128, 256}, bin[] = {128, 256, 512}, bps[] = {4, 8, 16, 32}, cw[] = {2, 4, 8};
-    for (int dim = 0; dim < 4; dim++) {
-        const int* cand = dim == 0 ? flat : dim == 1 ? bin : dim == 2 ? bps : cw;
-        const int nc = dim == 2 ? 4 : 3;
+    const int flat[] = {64, 128, 256}, bin[] = {128, 256, 512}, bps[] = {4, 8, 16, 32}, cw[] = {2, 4, 8},
+              cb[] = {1, 2, 4, 8};
+    for (int dim = 0; dim < 5; dim++) {
+        const int* cand = dim == 0 ? flat : dim == 1 ? bin : dim == 2 ? bps : dim == 3 ? cw : cb;
+        const int nc = (dim == 2 || dim == 4) ? 4 : 3;
         for (int i = 0; i < nc; i++) {
             TuneParams tp = best;
             if (dim == 0) tp.flatten_threads = cand[i];
             if (dim == 1) tp.bin_threads = cand[i];
             if (dim == 2) tp.bin_blocks_per_sm = cand[i];
             if (dim == 3) tp.comp_warps = cand[i];
+            if (dim == 4) tp.comp_batch = cand[i];
             float ms = 0;
             if ((rc = time_it(tp, &ms))) return rc;
             if (ms < best_ms) { best_ms = ms; best = tp; }

@@ -523,28 +523,119 @@ void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
 }
 
 // Launch bounds of the flattening and binning passes: at most 42 registers a
-// thread (48 warps an SM at their block sizes), which they fit without spills;
-// the extra warps hide their gather and atomic latency.
+// thread (48 warps an SM at their block sizes); the extra warps hide their
+// gather and atomic latency.
 // ---------------------------------------------------------------------------
-// flattening: one thread per input segment (process_segment's recursion,
-// renderer/src/tiler.rs:166-184).  Lines are written in emission order: input
-// segments in path order, each segment's lines depth first.
+// flattening (process_segment's recursion, renderer/src/tiler.rs:166-184).
+// Lines are written in emission order: input segments in path order, each
+// segment's lines depth first.
+//
+// A warp takes 32 segments and tests their subdivision level by level: at
+// level d the nodes still to test (children of nodes that were not flat) of
+// all 32 segments are spread over the lanes, each lane computing its node
+// from the root with exactly the splits the recursion performs.  A flat node
+// is a leaf: leaf masks record, on a grid of 2^kLeafLevels parameter slots,
+// where each leaf starts, so the count is the mask's population and the
+// depth-first order is the order of the slots.  The emit pass spreads the
+// leaves of 32 segments over the lanes the same way.  A segment with a node
+// still not flat at depth kLeafLevels is flattened by the depth-first walk
+// (flatten_segment) instead, by its own lane.
 // ---------------------------------------------------------------------------
+constexpr int kLeafLevels = 6;
+constexpr uint32_t kFlattenMaxWarps = 8;  // flatten_threads <= 256
+
+// Lane owning item i of a warp's items: the first lane whose inclusive count
+// exceeds i (incl: the lane's inclusive count).
+__device__ __forceinline__ uint32_t warp_owner(uint32_t incl, uint32_t i) {
+    uint32_t j = 0;
+#pragma unroll
+    for (uint32_t step = 16; step > 0; step >>= 1) {
+        const uint32_t v = __shfl_sync(0xffffffffu, incl, j + step - 1);
+        if (v <= i) j += step;
+    }
+    return j;
+}
+
+// Position of the k-th (from 0) set bit of m; m has more than k set bits.
+__device__ __forceinline__ uint32_t nth_set_bit64(unsigned long long m, uint32_t k) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (int w = 32; w >= 1; w >>= 1) {
+        const unsigned long long low = m & ((1ull << w) - 1ull);
+        const uint32_t c = (uint32_t)__popcll(low);
+        if (k >= c) {
+            k -= c;
+            m >>= w;
+            pos += (uint32_t)w;
+        } else {
+            m = low;
+        }
+    }
+    return pos;
+}
+
+struct FlattenWarp {
+    Cubic root[32];                    // each lane's segment as a cubic (a line as its base)
+    unsigned long long leaves[32];     // leaf start slots of each segment
+    unsigned long long next[32];       // nodes of the next level to test
+    uint32_t deep;                     // segments deeper than kLeafLevels
+};
+
 __global__ void __launch_bounds__(256, 6) k_flatten_count(FrameDev f) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ FlattenWarp smw[kFlattenMaxWarps];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    FlattenWarp& w = smw[wib];
+    const uint32_t s0 = (blockIdx.x * (blockDim.x >> 5) + wib) * 32u;
+    if (s0 >= f.seg_count) return;  // whole warps
+    const uint32_t s = s0 + lane;
+    unsigned long long active = 0;  // nodes of the current level to test
+    unsigned long long leaves = 0;
+    if (s < f.seg_count) {
+        Cubic c;
+        const int kind = segment_root(f.pts, f.segs[f.seg_begin + s], c, &f.counters->status);
+        if (kind == kRootLine) leaves = 1;  // one leaf: the line itself
+        else if (kind == kRootCurve) { w.root[lane] = c; active = 1; }
+    }
+    w.leaves[lane] = leaves;
+    w.next[lane] = 0;
+    if (lane == 0) w.deep = 0;
+    __syncwarp();
+    for (int d = 0; d <= kLeafLevels; d++) {
+        const uint32_t cnt = (uint32_t)__popcll(active);
+        const uint32_t incl = warp_inclusive_scan(cnt);
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total == 0) break;
+        for (uint32_t i0 = 0; i0 < total; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const uint32_t j = warp_owner(incl, i);
+            const uint32_t first = __shfl_sync(0xffffffffu, incl - cnt, j);
+            const unsigned long long aj = __shfl_sync(0xffffffffu, active, j);
+            if (i < total) {
+                const uint32_t a = nth_set_bit64(aj, i - first);
+                const Cubic c = subdivision_node(w.root[j], a, d);
+                if (cubic_is_flat(c)) atomicOr(&w.leaves[j], 1ull << (a << (kLeafLevels - d)));
+                else if (d < kLeafLevels) atomicOr(&w.next[j], 3ull << (2u * a));
+                else atomicOr(&w.deep, 1u << j);
+            }
+        }
+        __syncwarp();
+        active = w.next[lane];
+        w.next[lane] = 0;
+        __syncwarp();
+    }
     if (s >= f.seg_count) return;
-    uint32_t n = 0;
-    if (f.d3d11) {
-        bool limited = false;
-        const DiceSeg dsg = dice_seg(f.pts, f.segs[f.seg_begin + s]);
-        if (dice_finite(dsg)) n = dice_count(dsg, &limited);
-        else atomicOr(&f.counters->status, kStatusMalformed);  // no pieces for non-finite input
-        if (limited) atomicOr(&f.counters->status, kStatusDepthLimit);
-    } else {
+    leaves = w.leaves[lane];
+    uint32_t n;
+    if ((w.deep >> lane) & 1u) {
+        n = 0;
         flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&, uint32_t, int) { n++; },
                         &f.counters->status);
+        leaves = 0;  // no mask: the emit pass walks the segment
+    } else {
+        n = (uint32_t)__popcll(leaves);
     }
     f.seg_line_count[s] = n;
+    f.seg_leaves[s] = leaves;
 }
 
 // DIFF also records each line's segment and curve-parameter interval: the leaf
@@ -552,31 +643,64 @@ __global__ void __launch_bounds__(256, 6) k_flatten_count(FrameDev f) {
 // adjoint holds these subdivisions fixed.
 template <bool DIFF>
 __global__ void __launch_bounds__(256, 6) k_flatten_emit(FrameDev f) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s == 0 && f.counters->lines > f.line_cap) {  // the flattening scan's total against the capacity
+    __shared__ Cubic roots[kFlattenMaxWarps][32];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t s0 = (blockIdx.x * (blockDim.x >> 5) + wib) * 32u;
+    if (s0 == 0 && lane == 0 && f.counters->lines > f.line_cap) {  // the flattening scan's total
         atomicOr(&f.counters->status, kStatusLineCapacity);
         f.counters->needed_lines = f.counters->lines;
     }
-    if (s >= f.seg_count || f.counters->lines > f.line_cap) return;
-    const uint32_t sg = f.seg_begin + s;
-    const SegRec sr = f.segs[sg];
-    uint32_t l = f.seg_line_base[s];
-    if (!DIFF && f.d3d11) {  // uniform pieces, ends rounded to 1/256 px
-        const DiceSeg d = dice_seg(f.pts, sr);
-        bool limited = false;
-        const uint32_t n = dice_finite(d) ? dice_count(d, &limited) : 0u;
-        float2 a = make_float2(dice_q(d.p0.x), dice_q(d.p0.y));
-        for (uint32_t k = 1; k <= n; k++, l++) {
-            const float2 b = dice_point(d, k, n);
-            f.lines[l] = make_float4(a.x, a.y, b.x, b.y);
-            f.line_path[l] = (uint32_t)sr.w;
-            a = b;
+    if (s0 >= f.seg_count || f.counters->lines > f.line_cap) return;  // whole warps
+    const uint32_t s = s0 + lane;
+    uint32_t n = 0, base = 0, path = 0;
+    unsigned long long leaves = 0;
+    if (s < f.seg_count) {
+        const SegRec sr = f.segs[f.seg_begin + s];
+        n = f.seg_line_count[s];
+        if (n) {
+            Cubic c;
+            segment_root(f.pts, sr, c, &f.counters->status);
+            roots[wib][lane] = c;
+            leaves = f.seg_leaves[s];
+            base = f.seg_line_base[s];
+            path = (uint32_t)sr.w;
         }
-        return;
     }
-    flatten_segment(f.pts, sr, [&](const Line& ln, uint32_t addr, int d) {
+    const bool walk = n != 0 && leaves == 0;
+    const uint32_t nl = walk ? 0u : n;
+    const uint32_t incl = warp_inclusive_scan(nl);
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    __syncwarp();
+    for (uint32_t i0 = 0; i0 < total; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const uint32_t j = warp_owner(incl, i);
+        const uint32_t k = i - __shfl_sync(0xffffffffu, incl - nl, j);
+        const unsigned long long lj = __shfl_sync(0xffffffffu, leaves, j);
+        const uint32_t bj = __shfl_sync(0xffffffffu, base, j), pj = __shfl_sync(0xffffffffu, path, j);
+        if (i < total) {
+            // leaf k: from its start slot to the next leaf's (or the end)
+            const uint32_t start = nth_set_bit64(lj, k);
+            const unsigned long long above = start >= 63u ? 0ull : (lj >> (start + 1u));
+            const uint32_t next = above ? start + (uint32_t)__ffsll((long long)above) : 64u;
+            const int d = kLeafLevels - (31 - __clz((int)(next - start)));
+            const uint32_t addr = start >> (kLeafLevels - d);
+            const Cubic c = subdivision_node(roots[wib][j], addr, d);
+            const uint32_t l = bj + k;
+            f.lines[l] = make_float4(c.base.fx, c.base.fy, c.base.tx, c.base.ty);
+            f.line_path[l] = pj;
+            if constexpr (DIFF) {
+                const float step = ldexpf(1.0f, -d), t0 = (float)addr * step;
+                f.line_seg[l] = f.seg_begin + s0 + j;
+                f.line_t[l] = make_float2(t0, t0 + step);
+            }
+        }
+    }
+    if (!walk) return;
+    const uint32_t sg = f.seg_begin + s;
+    uint32_t l = base;
+    flatten_segment(f.pts, f.segs[sg], [&](const Line& ln, uint32_t addr, int d) {
         f.lines[l] = make_float4(ln.fx, ln.fy, ln.tx, ln.ty);
-        f.line_path[l] = (uint32_t)sr.w;
+        f.line_path[l] = path;
         if constexpr (DIFF) {
             const float step = ldexpf(1.0f, -d), t0 = (float)addr * step;
             f.line_seg[l] = sg;
@@ -586,14 +710,55 @@ __global__ void __launch_bounds__(256, 6) k_flatten_emit(FrameDev f) {
     }, &f.counters->status);
 }
 
+// The D3D11 level's uniform dicing: one thread per input segment.
+__global__ void __launch_bounds__(256, 6) k_dice_count(FrameDev f) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= f.seg_count) return;
+    uint32_t n = 0;
+    bool limited = false;
+    const DiceSeg dsg = dice_seg(f.pts, f.segs[f.seg_begin + s]);
+    if (dice_finite(dsg)) n = dice_count(dsg, &limited);
+    else atomicOr(&f.counters->status, kStatusMalformed);  // no pieces for non-finite input
+    if (limited) atomicOr(&f.counters->status, kStatusDepthLimit);
+    f.seg_line_count[s] = n;
+}
+
+__global__ void __launch_bounds__(256, 6) k_dice_emit(FrameDev f) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0 && f.counters->lines > f.line_cap) {  // the dicing scan's total against the capacity
+        atomicOr(&f.counters->status, kStatusLineCapacity);
+        f.counters->needed_lines = f.counters->lines;
+    }
+    if (s >= f.seg_count || f.counters->lines > f.line_cap) return;
+    const SegRec sr = f.segs[f.seg_begin + s];
+    uint32_t l = f.seg_line_base[s];
+    // uniform pieces, ends rounded to 1/256 px
+    const DiceSeg d = dice_seg(f.pts, sr);
+    bool limited = false;
+    const uint32_t n = dice_finite(d) ? dice_count(d, &limited) : 0u;
+    float2 a = make_float2(dice_q(d.p0.x), dice_q(d.p0.y));
+    for (uint32_t k = 1; k <= n; k++, l++) {
+        const float2 b = dice_point(d, k, n);
+        f.lines[l] = make_float4(a.x, a.y, b.x, b.y);
+        f.line_path[l] = (uint32_t)sr.w;
+        a = b;
+    }
+}
+
 void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     if (f.seg_count == 0) return;
     const int ft = f.tune.flatten_threads;
-    const uint32_t blocks = (f.seg_count + ft - 1) / ft;
-    { count_launch(); k_flatten_count<<<blocks, ft, 0, s>>>(f); }
+    const bool dice = f.d3d11 && !f.diff;
+    // dicing: a thread per segment; flattening: a warp per 32 segments
+    const uint32_t blocks = dice ? (f.seg_count + ft - 1) / ft
+                                 : (uint32_t)(((uint64_t)f.seg_count + 31) / 32 * 32 + ft - 1) / ft;
+    count_launch();
+    if (dice) k_dice_count<<<blocks, ft, 0, s>>>(f);
+    else k_flatten_count<<<blocks, ft, 0, s>>>(f);
     launch_scan(f.seg_line_count, f.seg_line_base, nullptr, f.seg_count, f.seg_count, 0, &f.counters->lines, tmp, s);
     count_launch();
-    if (f.diff) k_flatten_emit<true><<<blocks, ft, 0, s>>>(f);
+    if (dice) k_dice_emit<<<blocks, ft, 0, s>>>(f);
+    else if (f.diff) k_flatten_emit<true><<<blocks, ft, 0, s>>>(f);
     else k_flatten_emit<false><<<blocks, ft, 0, s>>>(f);
 }
 
@@ -654,21 +819,36 @@ __global__ void __launch_bounds__(512, 3) k_bin_count(FrameDev f) {
 
 // ORDER also writes each fill's emission index (only frames run for record
 // read-back do: the order of fills within a tile changes no output).
+// A fill's slot is its tile's fill base plus a decrementing cursor (the
+// tile's count).  The store of each fill waits one fill: the cursor's value
+// comes back from L2 while the DDA computes the next fill (flush() stores the
+// last one).
+// The sink reads the frame's pointers from the kernel parameter itself.
 template <bool ORDER>
 struct EmitSink {
-    uint2* fills;
-    uint32_t* fill_e;
-    const uint32_t* tile_fill_base;
-    uint32_t* cursor;
-    uint32_t fill_cap;
+    const FrameDev* f;
     uint32_t e;
-    __device__ __forceinline__ void fill(uint2 rec, uint32_t g) {
-        const uint32_t slot = tile_fill_base[g] + atomicSub(&cursor[g], 1u) - 1u;
-        if (slot < fill_cap) {
-            fills[slot] = rec;
-            if (ORDER) fill_e[slot] = e;
+    bool pending = false;
+    uint32_t p_base = 0, p_old = 0, p_e = 0;
+    uint2 p_rec = make_uint2(0u, 0u);
+    __device__ __forceinline__ void store_pending() {
+        const uint32_t slot = p_base + p_old - 1u;
+        if (slot < f->fill_cap) {
+            f->fills[slot] = p_rec;
+            if (ORDER) f->fill_e[slot] = p_e;
         }
+    }
+    __device__ __forceinline__ void fill(uint2 rec, uint32_t g) {
+        const uint32_t base = f->tile_fill_base[g];
+        const uint32_t old = atomicSub(&f->tile_fill_count[g], 1u);
+        if (pending) store_pending();
+        pending = true;
+        p_base = base; p_old = old; p_rec = rec; p_e = e;
         if (ORDER) e++;
+    }
+    __device__ __forceinline__ void flush() {
+        if (pending) store_pending();
+        pending = false;
     }
     __device__ __forceinline__ void backdrop(int32_t, int32_t, int32_t) {}
 };
@@ -683,11 +863,12 @@ struct EmitSinkF {
         const uint32_t slot = tile_fill_base[g] + atomicSub(&cursor[g], 1u) - 1u;
         if (slot < fill_cap) fills[slot] = rec;
     }
+    __device__ __forceinline__ void flush() {}
     __device__ __forceinline__ void backdrop(int32_t, int32_t, int32_t) {}
 };
 
 template <int MODE, bool ORDER>
-__global__ void __launch_bounds__(512, 3) k_bin_emit(FrameDev f) {
+__global__ void __launch_bounds__(512, 3) k_bin_emit(const __grid_constant__ FrameDev f) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {  // the binning scans' totals against the capacities
         if (f.counters->fills > f.fill_cap) {
             atomicOr(&f.counters->status, kStatusFillCapacity);
@@ -706,9 +887,9 @@ __global__ void __launch_bounds__(512, 3) k_bin_emit(FrameDev f) {
             EmitSinkF sink{f.fills_f, f.tile_fill_base, f.tile_fill_count, f.fill_cap};
             dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
         } else {
-            EmitSink<ORDER> sink{f.fills, f.fill_e, f.tile_fill_base, f.tile_fill_count, f.fill_cap,
-                                 ORDER ? f.line_fill_base[l] : 0u};
+            EmitSink<ORDER> sink{&f, ORDER ? f.line_fill_base[l] : 0u};
             dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+            sink.flush();
         }
     }
 }

@@ -76,8 +76,10 @@ def test_autotune_changes_speed_not_pixels(renderer):
     out = torch.zeros_like(ref)
     best = renderer.autotune(batch, out, pf.PF_CUDA_FORMAT_RGBA8, repeats=2)
     assert best["composite_warps"] in (2, 4, 8) and best["bin_threads"] in (128, 256, 512)
-    for warps in (2, 8):
-        renderer.set_tuning(composite_warps=warps, flatten_threads=64, bin_threads=512, bin_blocks_per_sm=4)
+    assert best["composite_batch"] in (1, 2, 4, 8)
+    for warps, per_item in ((2, 1), (8, 8), (4, 2)):
+        renderer.set_tuning(composite_warps=warps, composite_batch=per_item, flatten_threads=64, bin_threads=512,
+                            bin_blocks_per_sm=4)
         out.zero_()
         renderer.render_batch(batch, out, pf.PF_CUDA_FORMAT_RGBA8)
         assert torch.equal(out, ref)
