@@ -98,38 +98,51 @@ class ClockSampler:
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# Stages that are one kernel each (the roofline names one kernel).
+STAGE_KERNELS = {"bound": "k_bound", "bin_count": "k_bin_count", "bin_emit": "k_bin_emit", "fill": "k_mask",
+                 "composite": "k_composite"}
+
+
 def measured_traffic(kernel_stage: str, full_size: bool):
     """DRAM bytes per launch of the dominant kernel from its committed ncu
-    capture (profiles/), for the full-size workload only."""
-    if kernel_stage != "fill_composite" or not full_size:
+    capture (profiles/svg4k_<stage>_dram_full.md), for the full-size workload
+    only."""
+    if not full_size:
         return None, None
-    path = os.path.join(ROOT, "profiles", "svg4k_composite_dram_full.md")
+    rel = os.path.join("profiles", f"svg4k_{kernel_stage}_dram_full.md")
     try:
-        with open(path) as f:
+        with open(os.path.join(ROOT, rel)) as f:
             for line in f:
                 if line.startswith("traffic_bytes_per_launch:"):
-                    return int(line.split(":")[1]), "profiles/svg4k_composite_dram_full.md"
+                    return int(line.split(":")[1]), rel
     except OSError:
         pass
     return None, None
 
 
 def stage_bytes(st, npts: int, nseg: int) -> dict:
-    """Algorithmic bytes per stage from the per-unit figures: 8 B per point,
-    8 B per segment record, 12 B per fill, 16 B per path tile, 1 B per mask
-    pixel (256 per alpha tile), 4 B per output pixel; the flattened lines are
-    an intermediate of this design (16 B + 4 B path index, written once and
-    read by both binning passes)."""
+    """Bytes each stage must move in this design, from per-unit figures:
+    8 B per point and per segment record, 20 B per flattened line (an
+    intermediate: written once, read by both binning passes), 8 B per fill
+    (LineSegmentU16) written by the emit pass, 16 B per path tile record;
+    the fill pass reads the 8 B fills of the visible mask tiles and writes
+    their coverage (512 B: 256 pixels of 16-bit unorm) and reads a 16 B work
+    item each; the composite reads that coverage and a 24 B record and key
+    per visible tile and writes 4 B per pixel.  `frame` is the path's own
+    formula, 8P + 8S + 12F + 16T + 256A + 4WH (12 B Fill records and 1 B mask
+    pixels, as the reference stores them)."""
     P, S, F, T, A, L = npts, nseg, st.fill_count, st.tile_count, st.alpha_tile_count, st.line_count
+    V, Am, Fm = st.visible_tile_count, st.mask_tile_count, st.mask_fill_count
     return {
         "bound": 8 * P,
         "flatten": 8 * P + 8 * S + 20 * L,
         "bin_count": 20 * L + 4 * L,
         "scans": 4 * L + 8 * T,
-        "bin_emit": 20 * L + 12 * F,
+        "bin_emit": 20 * L + 8 * F,
         "propagate": 16 * T,
         "visibility": 16 * T,
-        "fill_composite": 12 * F + 256 * A + 4 * W * H,
+        "fill": 8 * Fm + 528 * Am,
+        "composite": 512 * Am + 24 * V + 4 * W * H,
         "frame": 8 * P + 8 * S + 12 * F + 16 * T + 256 * A + 4 * W * H,
     }
 
@@ -812,7 +825,7 @@ def main():
     # roofline of the dominant stage
     stage_ms = {n: v / args.steps for n, v in stage_sum.items()}
     sb = stage_bytes(st, npts, nseg)
-    dom = max(stage_ms, key=stage_ms.get)
+    dom = max((n for n in stage_ms if n in STAGE_KERNELS), key=stage_ms.get)
     peak, peak_kind = _peaks()
     achieved = sb[dom] / (stage_ms[dom] / 1e3) / 1e9
     frame_gbs = sb["frame"] / (ms / 1e3) / 1e9
@@ -864,7 +877,8 @@ def main():
                       "algorithmic_bytes": sb["frame"], "achieved_gbs": round(frame_gbs, 1),
                       "frac_of_" + peak_kind: round(frame_gbs / peak, 4)},
             "stages_ms": {n: round(v, 4) for n, v in stage_ms.items()},
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": STAGE_KERNELS[dom], "stage": dom, "achieved": round(achieved, 1),
+                         "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": sb[dom], "traffic": traffic,
                          "traffic_source": traffic_src},

@@ -232,6 +232,8 @@ typedef struct PFCUDARenderStats {
     uint64_t status;            /* device status bits of the last frame            */
     double   gpu_time_ms;       /* CUDA-event time of the last frame               */
     uint64_t kernel_launches;   /* kernels this library launched for the frame     */
+    uint64_t mask_tile_count;   /* visible tiles whose coverage the fill pass computed */
+    uint64_t mask_fill_count;   /* fills those tiles hold (the fills the fill pass reads) */
 } PFCUDARenderStats;
 
 /* Record layouts read back for parity checks. */
@@ -411,8 +413,10 @@ int32_t PFCUDAAutotune(PFCUDARendererRef renderer, const PFCUDABuildOptions* opt
 /* Per-stage CUDA-event timing of subsequent frames (Renderer timer queries,
  * renderer/src/gpu/perf.rs:96-186, bucketed like RenderTime :223-240).
  * Stages: 0 bound, 1 flatten, 2 bin count, 3 scans, 4 bin emit,
- * 5 propagate, 6 visibility, 7 fill+composite. */
-#define PF_CUDA_STAGE_COUNT 8
+ * 5 propagate, 6 visibility, 7 fill (coverage of the visible mask tiles),
+ * 8 composite.  Stage-timed frames run every kernel in order on the
+ * renderer's stream (other frames run independent stages side by side). */
+#define PF_CUDA_STAGE_COUNT 9
 int32_t PFCUDASetProfiling(PFCUDARendererRef renderer, int32_t enable);
 /* Milliseconds per stage of the last profiled frame; synchronises. */
 int32_t PFCUDAGetStageTimes(PFCUDARendererRef renderer, float* out_ms, int32_t capacity);

@@ -59,8 +59,8 @@ PF_SCENE_GLYPH_ATLAS = 3
 PF_SCENE_CUBIC_1K = 4
 PF_SCENE_EDGE_CASES = 5
 
-PF_CUDA_STAGE_COUNT = 8
-STAGE_NAMES = ["bound", "flatten", "bin_count", "scans", "bin_emit", "propagate", "visibility", "fill_composite"]
+PF_CUDA_STAGE_COUNT = 9
+STAGE_NAMES = ["bound", "flatten", "bin_count", "scans", "bin_emit", "propagate", "visibility", "fill", "composite"]
 
 
 class PFVector2F(C.Structure):
@@ -155,7 +155,8 @@ class PFCUDARenderStats(C.Structure):
     _fields_ = [("path_count", C.c_uint64), ("segment_count", C.c_uint64), ("line_count", C.c_uint64),
                 ("fill_count", C.c_uint64), ("tile_count", C.c_uint64), ("alpha_tile_count", C.c_uint64),
                 ("visible_tile_count", C.c_uint64), ("screen_tile_count", C.c_uint64),
-                ("status", C.c_uint64), ("gpu_time_ms", C.c_double), ("kernel_launches", C.c_uint64)]
+                ("status", C.c_uint64), ("gpu_time_ms", C.c_double), ("kernel_launches", C.c_uint64),
+                ("mask_tile_count", C.c_uint64), ("mask_fill_count", C.c_uint64)]
 
 
 class PFCUDAFill(C.Structure):

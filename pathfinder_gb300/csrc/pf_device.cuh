@@ -142,6 +142,7 @@ struct Counters {
     uint64_t needed_fills, needed_tiles, needed_visible, needed_lines;
     uint32_t composite_next;   // work counter of the persistent composite (screen tiles handed out)
     uint32_t mask_items;       // visible tiles with a mask (k_mask's work list)
+    uint64_t mask_fills;       // fills of those tiles
 };
 
 // ---------------------------------------------------------------------------

@@ -268,8 +268,9 @@ void launch_scan_multi(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_c
 void launch_propagate(const FrameDev& f, bool clip_pass, cudaStream_t s);
 void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s);
 // mode 0: RGBA8, 1: R8 single channel, 2: FP32 single channel
-// The fill pass (resolved coverage of every visible tile with a mask), then
-// the composite.
+// The fill pass: resolved coverage of every visible tile with a mask.
+void launch_mask(const FrameDev& f, cudaStream_t s);
+// The composite (after the fill pass).
 void launch_composite(const FrameDev& f, int mode, void* out, const float4& background, cudaStream_t s);
 void launch_masks(const FrameDev& f, float* alpha_masks, float* tile_cov, cudaStream_t s);
 

@@ -874,10 +874,12 @@ __global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask(FrameDev f) {
     bool stalled = false;
     int stall_buf = 0;
     uint32_t stall_parity = 0;
+    unsigned long long fills_read = 0;  // the fills of this warp's tiles (frame statistics)
     for (; k < M; k += stride) {
         const int4 later = k + 2 * stride < M ? f.mask_items[k + 2 * stride] : none;
         const bool nxt_staged = !stalled && stage_fills(f, nxt, ws, buf ^ 1);
         const uint32_t kind = ((uint32_t)cur.z >> 9) & 3u, slot = (uint32_t)cur.w;
+        fills_read += (uint32_t)cur.y;
         float cov[8];
         if (kind == kVisMask) {
             const uint2* src = f.fills + (uint32_t)cur.x;
@@ -912,12 +914,14 @@ __global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask(FrameDev f) {
         cur_staged = nxt_staged;
         buf ^= 1;
     }
+    if (lane == 0) atomicAdd((unsigned long long*)&f.counters->mask_fills, fills_read);
     // the copy a wait gave up on may still be in flight: wait for it again,
     // with the same bound, before the warp leaves its shared memory
     if (stalled) mbar_wait(&ws.bar[stall_buf], stall_parity);
 }
 
 void launch_mask(const FrameDev& f, cudaStream_t s) {
+    if (f.screen_count == 0) return;
     const int blocks = (int)f.sms * resident_blocks(k_mask, kMaskKernelWarps * 32);
     count_launch();
     k_mask<<<blocks, kMaskKernelWarps * 32, 0, s>>>(f);
@@ -953,38 +957,32 @@ __device__ __forceinline__ void composite_screen_tile(const FrameDev& f, uint32_
     }
     // entry i of the draw order: slot, paint, meta; its coverage is fetched
     // one entry ahead
-    auto entry = [&](uint32_t i, uint32_t& slot, uint32_t& paint, uint32_t& meta) {
+    // Entry i: its slot, then (read whatever the entry's kind: a solid entry's
+    // slot holds no coverage, and the value is not used) its coverage, then
+    // its record; the coverage read starts before the record is waited for.
+    auto entry = [&](uint32_t i, uint32_t& slot, uint4& mask, uint32_t& paint, uint32_t& meta) {
+        slot = lane_list ? __shfl_sync(0xffffffffu, (uint32_t)lane_key, (int)i) : (uint32_t)f.vis_key[base + i];
+        mask = f.vis_mask[(size_t)slot * 32u + (uint32_t)lane];
         if (lane_list) {
-            slot = __shfl_sync(0xffffffffu, (uint32_t)lane_key, (int)i);
             paint = (uint32_t)__shfl_sync(0xffffffffu, lane_info.x, (int)i);
             meta = (uint32_t)__shfl_sync(0xffffffffu, lane_info.y, (int)i);
         } else {
-            slot = (uint32_t)f.vis_key[base + i];
             const int4 info = f.vis_info[slot];
             paint = (uint32_t)info.z;
             meta = (uint32_t)info.w;
         }
     };
-    // (read whatever the kind: a solid entry's slot holds no coverage, and its
-    // value is not used; the read starts before the entry's kind is known)
-    auto fetch = [&](uint32_t slot) { return f.vis_mask[(size_t)slot * 32u + (uint32_t)lane]; };
 
     float d0[8], d1[8], d2[8], d3[8];
 #pragma unroll
     for (int k = 0; k < 8; k++) { d0[k] = bg.x; d1[k] = bg.y; d2[k] = bg.z; d3[k] = bg.w; }
     uint32_t n_slot = 0, n_paint = 0, n_meta = 0;
     uint4 n_mask = make_uint4(0u, 0u, 0u, 0u);
-    if (n) {
-        entry(0, n_slot, n_paint, n_meta);
-        n_mask = fetch(n_slot);
-    }
+    if (n) entry(0, n_slot, n_mask, n_paint, n_meta);
     for (uint32_t i = 0; i < n; i++) {
         const uint32_t paint = n_paint, meta = n_meta;
         const uint4 m = n_mask;
-        if (i + 1 < n) {
-            entry(i + 1, n_slot, n_paint, n_meta);
-            n_mask = fetch(n_slot);
-        }
+        if (i + 1 < n) entry(i + 1, n_slot, n_mask, n_paint, n_meta);
         float cov[8];
         if (((meta >> 9) & 3u) == kVisSolid) {
             const float c = resolve_coverage((float)(int8_t)(meta & 0xffu), (meta >> 8) & 1u);
@@ -1097,7 +1095,6 @@ void launch_composite_mode(const FrameDev& f, void* out, const float4& bg, cudaS
 
 void launch_composite(const FrameDev& f, int mode, void* out, const float4& bg, cudaStream_t s) {
     if (f.screen_count == 0) return;
-    launch_mask(f, s);
     if (mode == 0) launch_composite_mode<0>(f, out, bg, s);
     else if (mode == 1) launch_composite_mode<1>(f, out, bg, s);
     else launch_composite_mode<2>(f, out, bg, s);

@@ -498,12 +498,14 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     launch_visible(f, true, s);
     if ((e = join(1))) return e;
     mark(7);
+    if (mode >= 0 && !diff) launch_mask(f, s);
+    mark(8);
     if (mode >= 0 || diff) {
         const float4 bg = background_of(r);
         if (diff) launch_composite_diff(f, (float*)out_dev, bg, s);
         else launch_composite(f, mode, out_dev, bg, s);
     }
-    mark(8);
+    mark(9);
     r->launches = launch_counter() - before;
     return cudaGetLastError();
 }
@@ -543,6 +545,8 @@ void record_stats(PFCUDARenderer* r, const Counters& h, float ms) {
     r->stats.status = h.status;
     r->stats.gpu_time_ms = ms;
     r->stats.kernel_launches = r->launches;
+    r->stats.mask_tile_count = h.mask_items;
+    r->stats.mask_fill_count = h.mask_fills;
 }
 
 cudaError_t upload_scene_records(PFCUDARenderer* r) {

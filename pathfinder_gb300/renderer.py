@@ -81,6 +81,8 @@ class RenderStats:
     status: int = 0
     gpu_time_ms: float = 0.0
     kernel_launches: int = 0
+    mask_tile_count: int = 0
+    mask_fill_count: int = 0
 
 
 def _ptr(x):
