@@ -36,6 +36,9 @@ constexpr uint32_t kStatusLineCapacity   = 1u << 8;
 // A bounded wait for a bulk copy gave up (the tile was computed from global
 // memory instead); reported as a launch error.
 constexpr uint32_t kStatusCopyStall      = 1u << 9;
+// A bounded wait of a single-pass scan gave up: the offsets it produced are
+// not valid (reported as a launch error).
+constexpr uint32_t kStatusScanStall      = 1u << 10;
 
 // ---------------------------------------------------------------------------
 // Records in HBM

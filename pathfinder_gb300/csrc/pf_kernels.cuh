@@ -147,8 +147,19 @@ __device__ __forceinline__ uint32_t scene_of_screen_tile(const FrameDev& f, uint
 __host__ __device__ __forceinline__ uint32_t enc_d(float d) { return d > 0.0f ? 1u : (d < 0.0f ? 2u : 0u); }
 __host__ __device__ __forceinline__ float dec_d(uint32_t c) { return c == 1u ? 1.0f : (c == 2u ? -1.0f : 0.0f); }
 
-// scan scratch
-struct ScanTemp { uint32_t* partials; uint32_t cap; };
+// Scan scratch.  `partials` serves the three-pass scans (reduce, partials,
+// down-sweep).  With `lookback` set, scans run in one pass instead: each call
+// takes a ticket word and one word per 2,048-value tile and lane from the
+// region (which must be zero before the first call: frames clear it once),
+// and reports a look-back that gave up in *status.
+struct ScanTemp {
+    uint32_t* partials;
+    uint32_t cap;
+    unsigned long long* lookback = nullptr;
+    uint32_t lookback_cap = 0;   // words in the region
+    uint32_t lookback_used = 0;  // words taken by earlier calls
+    uint32_t* status = nullptr;
+};
 
 }  // namespace pf
 struct PFCUDAGradient;
@@ -176,6 +187,12 @@ void count_launch(uint32_t n = 1);
 // Multiprocessors of the current device (queried once per device; grid sizes
 // of the launches that do not carry a FrameDev).
 uint32_t device_sm_count();
+// Blocks of `threads` threads of `kernel` resident on one multiprocessor of
+// the current device (persistent grids are the multiprocessors times this);
+// queried once per kernel, block size and device.
+int resident_blocks_of(const void* kernel, int threads);
+template <typename K>
+int resident_blocks(K kernel, int threads) { return resident_blocks_of((const void*)kernel, threads); }
 
 
 void launch_transform(const float2* in, float2* out, uint32_t n, const float* m6, cudaStream_t s);

@@ -776,20 +776,6 @@ __device__ __forceinline__ void unpack_cov16(uint4 m, float cov[8]) {
     cov[6] = (float)(m.w & 0xffffu) * s; cov[7] = (float)(m.w >> 16) * s;
 }
 
-// Occupancy of a kernel instance on the current device, queried once per
-// instance and device (persistent grids are the multiprocessors times this).
-template <typename K>
-int resident_blocks(K kernel, int threads) {
-    static std::atomic<int> cache[64] = {};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
-    int v = cache[dev].load(std::memory_order_relaxed);
-    if (v) return v;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, 0) != cudaSuccess || v <= 0) v = 1;
-    cache[dev].store(v, std::memory_order_relaxed);
-    return v;
-}
-
 // ---- bulk copies (cp.async.bulk) into shared memory, completed on an mbarrier
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {

@@ -182,6 +182,9 @@ struct PFCUDARenderer {
     DevBuf<uint4> vis_mask;
     DevBuf<int4> mask_items;
     DevBuf<uint32_t> scan_partials, scan_partials_branch;
+    // look-back words of the frame's single-pass scans: one half for the
+    // frame's stream, one for its branch stream; cleared at the frame's start
+    DevBuf<unsigned long long> scan_lookback;
     DevBuf<Counters> counters;
     DevBuf<uint8_t> out_tmp;
     Counters* h_counters = nullptr;  // pinned
@@ -393,6 +396,8 @@ cudaError_t ensure_frame_buffers(PFCUDARenderer* r) {
                                     (size_t)r->line_cap, (size_t)r->P}) + 1;
     if ((e = r->scan_partials_branch.ensure(kMaxScanLanes * ((size_t)r->S + 1) / 2048 + 2 * kMaxScanLanes)))
         return e;
+    // per half: a ticket and one word per tile and lane for each of the frame's scans
+    if ((e = r->scan_lookback.ensure(2 * (16 + 3 * kMaxScanLanes * (nmax / 2048 + 2))))) return e;
     return r->scan_partials.ensure(kMaxScanLanes * (nmax / 2048 + 2));
 }
 
@@ -438,9 +443,11 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
             f.inv_m[3] = c; f.inv_m[4] = d; f.inv_m[5] = -(c * t.vector.x + d * t.vector.y);
         }
     }
-    ScanTemp tmp{r->scan_partials.p, (uint32_t)r->scan_partials.cap};
-    ScanTemp tmp_branch{r->scan_partials_branch.p, (uint32_t)r->scan_partials_branch.cap};
     Counters* c = r->counters.p;
+    const uint32_t half = (uint32_t)(r->scan_lookback.cap / 2);
+    ScanTemp tmp{r->scan_partials.p, (uint32_t)r->scan_partials.cap, r->scan_lookback.p, half, 0, &c->status};
+    ScanTemp tmp_branch{r->scan_partials_branch.p, (uint32_t)r->scan_partials_branch.cap, r->scan_lookback.p + half,
+                        half, 0, &c->status};
     auto mark = [&](int stage) {
         if (r->profiling) cudaEventRecord(r->stage_ev[stage], s);
     };
@@ -460,6 +467,7 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     const size_t nst = (size_t)(g.st1 - g.st0) + 1;
     uint64_t before = launch_counter();
     if ((e = cudaMemsetAsync(c, 0, sizeof(Counters), s))) return e;
+    if ((e = cudaMemsetAsync(r->scan_lookback.p, 0, r->scan_lookback.cap * sizeof(unsigned long long), s))) return e;
     mark(0);
     // flattening needs no tile rects: it runs beside the bounds and path scans
     if ((e = fork(0))) return e;
@@ -530,6 +538,7 @@ int32_t status_to_code(uint32_t st) {
     if (st & kCapacityBits) return PF_CUDA_ERR_CAPACITY;
     if (st & (kStatusDdaLimit | kStatusDepthLimit)) return PF_CUDA_ERR_LIMIT;
     if (st & kStatusMalformed) return PF_CUDA_ERR_INVALID;
+    if (st & kStatusScanStall) return PF_CUDA_ERR_LAUNCH;
     return PF_CUDA_OK;
 }
 
@@ -600,9 +609,11 @@ std::vector<uint8_t> frame_key(PFCUDARenderer* r, const PFCUDABuildOptions* opts
     std::vector<uint8_t> k;
     auto put = [&k](const void* p, size_t n) { k.insert(k.end(), (const uint8_t*)p, (const uint8_t*)p + n); };
     put(&f, sizeof f);
-    const void* ptrs[] = {r->pts.p, r->ord_contour.p, r->starts.p, r->scan_partials.p, out_dev};
+    const void* ptrs[] = {r->pts.p, r->ord_contour.p, r->starts.p, r->scan_partials.p, r->scan_partials_branch.p,
+                          r->scan_lookback.p, out_dev};
     put(ptrs, sizeof ptrs);
-    const uint64_t vals[] = {r->scan_partials.cap, r->NP, (uint64_t)(int64_t)mode, transformed ? 1u : 0u};
+    const uint64_t vals[] = {r->scan_partials.cap, r->scan_partials_branch.cap, r->scan_lookback.cap, r->NP,
+                             (uint64_t)(int64_t)mode, transformed ? 1u : 0u};
     put(vals, sizeof vals);
     const float4 bg = background_of(r);
     put(&bg, sizeof bg);
@@ -775,7 +786,8 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->col_backdrop.release(); r->zbuf.release(); r->fills.release(); r->fill_e.release(); r->tiles.release();
     r->clips.release(); r->screen_cnt.release(); r->screen_base.release(); r->vis.release(); r->vis_info.release();
     r->vis_key.release(); r->vis_mask.release(); r->mask_items.release();
-    r->scan_partials.release(); r->scan_partials_branch.release(); r->counters.release(); r->out_tmp.release();
+    r->scan_partials.release(); r->scan_partials_branch.release(); r->scan_lookback.release(); r->counters.release();
+    r->out_tmp.release();
     r->draw_index.release(); r->blend.release(); r->occludes.release(); r->overlay.release();
     r->starts_raw.release(); r->path_ncont.release(); r->scene_ranges.release(); r->path_in.release();
     r->scene_pack.release(); r->pack_info.release(); r->overlay_opaque.release(); r->alpha_default.release();

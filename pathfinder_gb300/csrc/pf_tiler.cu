@@ -13,12 +13,29 @@
 #include "pf_kernels.cuh"
 
 #include <atomic>
+#include <mutex>
+#include <vector>
 
 namespace pf {
 
 static std::atomic<uint64_t> g_launches{0};
 uint64_t launch_counter() { return g_launches.load(); }
 void count_launch(uint32_t n) { g_launches += n; }
+
+int resident_blocks_of(const void* kernel, int threads) {
+    struct Entry { int dev; const void* kernel; int threads, blocks; };
+    static std::mutex m;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    std::lock_guard<std::mutex> g(m);
+    for (const Entry& e : cache)
+        if (e.dev == dev && e.kernel == kernel && e.threads == threads) return e.blocks;
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, threads, 0) != cudaSuccess || v <= 0) v = 1;
+    cache.push_back(Entry{dev, kernel, threads, v});
+    return v;
+}
 
 uint32_t device_sm_count() {
     constexpr int kMaxDevices = 64;
@@ -189,11 +206,133 @@ __global__ void k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restric
     store8(out, first, n, e);
 }
 
+// ---------------------------------------------------------------------------
+// single-pass scans (decoupled look-back): a block scans its 2,048-value tile,
+// publishes the tile's sum (kTileAggregate), takes the sum of everything
+// before it from its predecessors' words back to the nearest running total
+// (kTileInclusive), publishes its own running total and writes its outputs.
+// Blocks take their tile from a ticket in the order they start, so every
+// predecessor has started and publishes its sum before it looks back itself:
+// the waits end.  They are bounded all the same (kStatusScanStall).
+// ---------------------------------------------------------------------------
+constexpr unsigned long long kTileAggregate = 1ull << 62, kTileInclusive = 2ull << 62;
+constexpr unsigned long long kTileValue = (1ull << 62) - 1ull;
+constexpr uint32_t kLookBackLimit = 1u << 22;
+
+__device__ __forceinline__ unsigned long long load_tile_word(const unsigned long long* p) {
+    return *reinterpret_cast<const volatile unsigned long long*>(p);
+}
+__device__ __forceinline__ void store_tile_word(unsigned long long* p, unsigned long long v) {
+    *reinterpret_cast<volatile unsigned long long*>(p) = v;
+}
+
+// Exclusive prefix of tile t whose sum is `sum` (one warp; every lane gets it).
+__device__ __forceinline__ unsigned long long look_back(unsigned long long* words, uint32_t t, unsigned long long sum,
+                                                        uint32_t* status) {
+    const uint32_t lane = threadIdx.x & 31;
+    if (lane == 0) store_tile_word(&words[t], kTileAggregate | sum);
+    unsigned long long prefix = 0;
+    uint32_t j = t;  // tiles [0, j) are still to add
+    uint32_t polls = 0;
+    while (j > 0) {
+        const unsigned long long w = lane < j ? load_tile_word(&words[j - 1 - lane]) : kTileInclusive;
+        const uint32_t incl = __ballot_sync(0xffffffffu, (w & ~kTileValue) == kTileInclusive);
+        const uint32_t none = __ballot_sync(0xffffffffu, (w & ~kTileValue) == 0ull);
+        const int first = incl ? __ffs(incl) - 1 : 32;  // the nearest running total
+        const uint32_t span = first < 31 ? (2u << first) - 1u : 0xffffffffu;
+        if (none & span) {  // a predecessor has not published yet
+            if (++polls >= kLookBackLimit) {
+                if (lane == 0 && status) atomicOr(status, kStatusScanStall);
+                break;
+            }
+            continue;
+        }
+        unsigned long long v = ((span >> lane) & 1u) ? (w & kTileValue) : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        prefix += v;
+        if (first < 32) break;
+        j -= 32;
+    }
+    if (lane == 0) store_tile_word(&words[t], kTileInclusive | ((prefix + sum) & kTileValue));
+    return prefix;
+}
+
+// NL lanes of the same length; lb[0] is the ticket, lane l's tile words
+// start at lb + 1 + l * nb.
+template <int NL>
+__global__ void __launch_bounds__(kScanThreads) k_scan_onepass(ScanLanes L, const uint64_t* d_n, uint32_t n_cap,
+                                                               unsigned long long* lb, uint32_t nb, uint32_t* status) {
+    __shared__ uint32_t tile_sh;
+    __shared__ unsigned long long prefix_sh;
+    if (threadIdx.x == 0) tile_sh = atomicAdd(reinterpret_cast<unsigned int*>(lb), 1u);
+    __syncthreads();
+    const uint32_t t = tile_sh;
+    const uint32_t n = scan_count(d_n, n_cap);
+    const uint32_t tiles = (n + kScanChunk - 1) / kScanChunk;
+    if (t >= (tiles ? tiles : 1u)) return;  // (n == 0: tile 0 writes the zero totals)
+    const uint32_t first = t * kScanChunk + threadIdx.x * kScanItems;
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+        uint32_t v[kScanItems], s = 0;
+        load8(L.in[l], first, n, L.mode[l], v);
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) s += v[k];
+        uint32_t total;
+        uint32_t ex = block_exclusive_scan<kScanThreads>(s, &total);
+        if (threadIdx.x < 32) {
+            const unsigned long long p = look_back(lb + 1 + (size_t)l * nb, t, total, status);
+            if (threadIdx.x == 0) prefix_sh = p;
+        }
+        __syncthreads();
+        const unsigned long long p = prefix_sh;
+        ex += (uint32_t)p;
+        uint32_t e[kScanItems];
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            e[k] = ex;
+            ex += v[k];
+        }
+        store8(L.out[l], first, n, e);
+        if (threadIdx.x == 0 && t + 1 >= tiles) {  // the last tile: the total
+            L.out[l][n] = (uint32_t)(p + total);
+            if (L.total[l]) *L.total[l] = p + total;
+        }
+        __syncthreads();  // prefix_sh is reused by the next lane
+    }
+}
+
+// The single-pass form when the scratch has a look-back region with room and
+// the scan has at most kOnePassTiles tiles: on longer scans every block is
+// resident at once, and each walks back over many predecessors whose running
+// totals are not known yet (the three-pass form is faster there).
+constexpr uint32_t kOnePassTiles = 64;
+template <int NL>
+static bool launch_scan_onepass(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp,
+                                cudaStream_t s) {
+    uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
+    if (nb == 0) nb = 1;
+    if (nb > kOnePassTiles) return false;
+    const uint64_t words = 1 + (uint64_t)NL * nb;
+    if (!tmp.lookback || tmp.lookback_used + words > tmp.lookback_cap) return false;
+    unsigned long long* lb = tmp.lookback + tmp.lookback_used;
+    tmp.lookback_used += (uint32_t)words;
+    count_launch();
+    k_scan_onepass<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, lb, nb, tmp.status);
+    return true;
+}
+
 void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_t n_host, uint32_t n_cap, int mode,
                  uint64_t* total_out, ScanTemp& tmp, cudaStream_t s) {
     uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
     if (nb == 0) nb = 1;
     if (d_n) n_host = n_cap;  // device count is clamped to the capacity
+    {
+        ScanLanes one{};
+        one.count = 1;
+        one.in[0] = in; one.out[0] = out; one.total[0] = total_out; one.mode[0] = mode;
+        if (launch_scan_onepass<1>(one, d_n, n_host, tmp, s)) return;
+    }
     { count_launch(); k_scan_reduce<<<nb, kScanThreads, 0, s>>>(in, d_n, n_host, mode, tmp.partials); }
     { count_launch(); k_scan_partials<<<1, 1024, 0, s>>>(tmp.partials, d_n, n_host, out, total_out); }
     { count_launch(); k_scan_down<<<nb, kScanThreads, 0, s>>>(in, out, d_n, n_host, mode, tmp.partials); }
@@ -300,6 +439,9 @@ static void launch_scan_lanes(const ScanLanes& lanes, const uint64_t* d_n, uint3
 }
 
 void launch_scan_multi(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp, cudaStream_t s) {
+    if (lanes.count == 1 && launch_scan_onepass<1>(lanes, d_n, n_cap, tmp, s)) return;
+    if (lanes.count == 2 && launch_scan_onepass<2>(lanes, d_n, n_cap, tmp, s)) return;
+    if (lanes.count == 3 && launch_scan_onepass<3>(lanes, d_n, n_cap, tmp, s)) return;
     if (lanes.count == 1) launch_scan_lanes<1>(lanes, d_n, n_cap, tmp, s);
     else if (lanes.count == 2) launch_scan_lanes<2>(lanes, d_n, n_cap, tmp, s);
     else launch_scan_lanes<3>(lanes, d_n, n_cap, tmp, s);
