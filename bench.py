@@ -104,16 +104,17 @@ STAGE_KERNELS = {"bound": "k_bound", "bin_count": "k_bin_count", "bin_emit": "k_
 
 
 def measured_traffic(kernel_stage: str, full_size: bool):
-    """DRAM bytes per launch of the dominant kernel from its committed ncu
-    capture (profiles/svg4k_<stage>_dram_full.md), for the full-size workload
-    only."""
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    capture of the full-size frame (profiles/svg4k_dram_full.md), for the
+    full-size workload only."""
     if not full_size:
         return None, None
-    rel = os.path.join("profiles", f"svg4k_{kernel_stage}_dram_full.md")
+    rel = os.path.join("profiles", "svg4k_dram_full.md")
+    key = f"traffic_bytes_per_launch {kernel_stage}:"
     try:
         with open(os.path.join(ROOT, rel)) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_launch:"):
+                if line.startswith(key):
                     return int(line.split(":")[1]), rel
     except OSError:
         pass
@@ -829,7 +830,8 @@ def main():
     peak, peak_kind = _peaks()
     achieved = sb[dom] / (stage_ms[dom] / 1e3) / 1e9
     frame_gbs = sb["frame"] / (ms / 1e3) / 1e9
-    traffic, traffic_src = measured_traffic(dom, args.scale == 1.0)
+    # the committed capture is of the plain full-size frame only
+    traffic, traffic_src = measured_traffic(dom, args.scale == 1.0 and not args.paints and not args.d3d11)
 
     # e2e through the public API with host buffers
     e2e_steps = args.e2e_steps or max(3, min(args.steps, 20))

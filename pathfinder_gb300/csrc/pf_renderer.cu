@@ -479,12 +479,17 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     mark(2);
     launch_bin_count(f, s);
     mark(3);
-    launch_scan(r->line_fill_count.p, r->line_fill_base.p, &c->lines, 0, r->line_cap, 0, &c->fills, tmp, s);
+    // the first fill of each line in emission order: only frames run for
+    // record read-back write emission indices
+    if (r->fill_order)
+        launch_scan(r->line_fill_count.p, r->line_fill_base.p, &c->lines, 0, r->line_cap, 0, &c->fills, tmp, s);
     {
-        // per tile: fill offsets, alpha-tile ids, column backdrop prefixes
+        // per tile: fill offsets (their total is the frame's fill count),
+        // alpha-tile ids, column backdrop prefixes
         ScanLanes lanes{};
         lanes.count = 3;
         lanes.in[0] = r->tile_fill_count.p; lanes.out[0] = r->tile_fill_base.p; lanes.mode[0] = 0;
+        lanes.total[0] = &c->fills;
         lanes.in[1] = r->tile_fill_count.p; lanes.out[1] = r->tile_alpha.p; lanes.mode[1] = 1;
         lanes.total[1] = &c->alpha_tiles;
         lanes.in[2] = (const uint32_t*)r->tile_delta.p; lanes.out[2] = r->tile_delta_scan.p; lanes.mode[2] = 0;
@@ -742,7 +747,8 @@ int32_t PFCUDARendererCreate(int32_t device_ordinal, const PFCUDARendererOptions
     cudaError_t e = cudaGetDeviceCount(&count);
     if (e != cudaSuccess || count == 0) return PF_CUDA_ERR_NO_DEVICE;
     if (device_ordinal < 0 || device_ordinal >= count) return PF_CUDA_ERR_INVALID;
-    PF_TRY(cudaSetDevice(device_ordinal));
+    DeviceGuard dg(device_ordinal);
+    PF_TRY(dg.status);
     int sms = 0;
     PF_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_ordinal));
     PFCUDARenderer* r = new PFCUDARenderer();
@@ -770,7 +776,7 @@ int32_t PFCUDARendererCreate(int32_t device_ordinal, const PFCUDARendererOptions
 
 int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     if (!r) return PF_CUDA_OK;
-    cudaSetDevice(r->device);
+    DeviceGuard dg(r->device);
     if (r->stream) cudaStreamSynchronize(r->stream);
     release_graph(r);
     r->pts.release(); r->pts_t.release(); r->flags.release(); r->starts.release();
@@ -1054,7 +1060,8 @@ static int32_t upload_tables(PFCUDARendererRef r, const PFCUDASceneDesc* scenes,
 int32_t PFCUDASceneUploadBatch(PFCUDARendererRef r, const PFCUDASceneDesc* scenes, const PFCUDASceneTarget* targets,
                                uint32_t scene_count) {
     if (!r || !scenes || scene_count == 0) return PF_CUDA_ERR_INVALID;
-    PF_TRY(cudaSetDevice(r->device));
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     cudaStream_t s = r->stream;
     release_graph(r);
     r->has_scene = false;
@@ -1138,7 +1145,8 @@ static int32_t render_plain(PFCUDARendererRef r, const PFCUDABuildOptions* optio
                             void* out, int32_t out_memory, int32_t format) {
     if (!r || !out) return PF_CUDA_ERR_INVALID;
     if (!r->has_scene) return PF_CUDA_ERR_NO_SCENE;
-    PF_TRY(cudaSetDevice(r->device));
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     bool changed = false;
     int32_t rc = prepare_plain_targets(r, width, height, &changed);
     if (rc) return rc;
@@ -1212,7 +1220,8 @@ int32_t PFCUDARenderBatch(PFCUDARendererRef r, const PFCUDABuildOptions* options
                           int32_t format, void* out_device) {
     if (!r || !out_device || format < 0 || format > 2) return PF_CUDA_ERR_INVALID;
     if (!valid_range(r, first, count)) return r->has_scene ? PF_CUDA_ERR_INVALID : PF_CUDA_ERR_NO_SCENE;
-    PF_TRY(cudaSetDevice(r->device));
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     return run_frame(r, options, format, out_device, make_range(r, first, count));
 }
 
@@ -1314,6 +1323,8 @@ int32_t PFCUDAGetTuning(PFCUDARendererRef r, PFCUDATuning* t) {
 int32_t PFCUDAAutotune(PFCUDARendererRef r, const PFCUDABuildOptions* options, uint32_t first, uint32_t count,
                        int32_t format, void* out_device, int32_t repeats, PFCUDATuning* out_best) {
     if (!r || repeats <= 0) return PF_CUDA_ERR_INVALID;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     int32_t rc = PFCUDARenderBatch(r, options, first, count, format, out_device);  // sizes the buffers
     if (rc != PF_CUDA_OK) return rc;
     const Range g = r->last;
@@ -1364,7 +1375,8 @@ int32_t PFCUDAAutotune(PFCUDARendererRef r, const PFCUDABuildOptions* options, u
 int32_t PFCUDAReadMasks(PFCUDARendererRef r, float* out_alpha, uint64_t alpha_cap, float* out_tile,
                         uint64_t tile_cap) {
     if (!r || !r->has_scene) return PF_CUDA_ERR_NO_SCENE;
-    PF_TRY(cudaSetDevice(r->device));
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     uint64_t A = r->stats.alpha_tile_count, T = r->stats.tile_count;
     if ((out_alpha && alpha_cap < A) || (out_tile && tile_cap < T)) return PF_CUDA_ERR_CAPACITY;
     FrameDev f = frame_dev(r, false, r->last, r->last_diff);
@@ -1386,7 +1398,8 @@ int32_t PFCUDAReadRecords(PFCUDARendererRef r, PFCUDAFill* fills, uint32_t* fill
                           PFRectI* path_tile_rects, uint64_t path_capacity, PFCUDAClip* clips, int32_t* z_buffer,
                           uint64_t z_capacity) {
     if (!r || !r->has_scene) return PF_CUDA_ERR_NO_SCENE;
-    PF_TRY(cudaSetDevice(r->device));
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     cudaStream_t s = r->stream;
     const Range& g = r->last;
     const uint64_t F = r->stats.fill_count, T = r->stats.tile_count, NPth = g.p1 - g.p0, NST = g.st1 - g.st0;
@@ -1454,7 +1467,8 @@ int32_t PFCUDAReadRecords(PFCUDARendererRef r, PFCUDAFill* fills, uint32_t* fill
 
 int32_t PFCUDASetProfiling(PFCUDARendererRef r, int32_t enable) {
     if (!r) return PF_CUDA_ERR_INVALID;
-    PF_TRY(cudaSetDevice(r->device));
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     if (enable && !r->stage_ev[0])
         for (int i = 0; i <= PF_CUDA_STAGE_COUNT; i++) PF_TRY(cudaEventCreate(&r->stage_ev[i]));
     r->profiling = enable != 0;
@@ -1464,6 +1478,8 @@ int32_t PFCUDASetProfiling(PFCUDARendererRef r, int32_t enable) {
 int32_t PFCUDAGetStageTimes(PFCUDARendererRef r, float* out_ms, int32_t capacity) {
     if (!r || !out_ms || capacity < PF_CUDA_STAGE_COUNT) return PF_CUDA_ERR_INVALID;
     if (!r->profiling) return PF_CUDA_ERR_INVALID;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     PF_TRY(cudaEventSynchronize(r->stage_ev[PF_CUDA_STAGE_COUNT]));
     for (int i = 0; i < PF_CUDA_STAGE_COUNT; i++) {
         float ms = 0;
@@ -1475,14 +1491,16 @@ int32_t PFCUDAGetStageTimes(PFCUDARendererRef r, float* out_ms, int32_t capacity
 
 int32_t PFCUDAStrokeToFill(PFCUDARendererRef r, const PFCUDAStrokeInput* input, PFCUDAStrokeOutput* output) {
     if (!r || !input || !output) return PF_CUDA_ERR_INVALID;
-    PF_TRY(cudaSetDevice(r->device));
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     if (!r->stroke) r->stroke = stroke_work_create();
     return stroke_run(r->stroke, r->stream, input, output);
 }
 
 int32_t PFCUDAExclusiveScan(PFCUDARendererRef r, const uint32_t* in, uint32_t* out, uint32_t n) {
     if (!r || !out || (!in && n) || n >= 0x80000000u) return PF_CUDA_ERR_INVALID;
-    PF_TRY(cudaSetDevice(r->device));
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     PF_TRY(r->scan_partials.ensure((size_t)n / 2048 + 2));
     ScanTemp tmp{r->scan_partials.p, (uint32_t)r->scan_partials.cap};
     launch_scan(in, out, nullptr, n, n, 0, nullptr, tmp, r->stream);
@@ -1496,7 +1514,8 @@ int32_t PFCUDASetPoints(PFCUDARendererRef r, const PFVector2F* points, uint64_t 
     if (!r->has_scene) return PF_CUDA_ERR_NO_SCENE;
     if (count != r->NP || (count && !points)) return PF_CUDA_ERR_INVALID;
     if (memory != PF_MEMORY_HOST && memory != PF_MEMORY_DEVICE) return PF_CUDA_ERR_INVALID;
-    PF_TRY(cudaSetDevice(r->device));
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     r->diff_valid = false;
     if (count)
         PF_TRY(cudaMemcpyAsync(r->pts.p, points, sizeof(float2) * count,
@@ -1513,7 +1532,6 @@ static int32_t diff_prologue(PFCUDARendererRef r, uint32_t first, uint32_t count
     if (r->nested_clips) return PF_CUDA_ERR_INVALID;  // the adjoint covers single-level clips
     if (r->paint_effects) return PF_CUDA_ERR_INVALID;  // and solid paint with SrcOver
     if (r->options.flags & PF_CUDA_RENDERER_D3D11_SEMANTICS) return PF_CUDA_ERR_INVALID;  // pieces rounded to 1/256 px
-    PF_TRY(cudaSetDevice(r->device));
     if (width > 0 || height > 0) {
         bool changed = false;
         int32_t rc = prepare_plain_targets(r, width, height, &changed);
@@ -1545,6 +1563,9 @@ static void diff_epilogue(PFCUDARendererRef r, const PFCUDABuildOptions* options
 
 int32_t PFCUDARenderDiff(PFCUDARendererRef r, const PFCUDABuildOptions* options, uint32_t first, uint32_t count,
                          int32_t width, int32_t height, const float* draw_alpha, float* out_device) {
+    if (!r) return PF_CUDA_ERR_INVALID;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     int32_t rc = diff_prologue(r, first, count, width, height, draw_alpha, out_device);
     if (rc != PF_CUDA_OK) return rc;
     const Range g = make_range(r, first, count);
@@ -1557,6 +1578,9 @@ int32_t PFCUDARenderDiff(PFCUDARendererRef r, const PFCUDABuildOptions* options,
 int32_t PFCUDARenderDiffAsync(PFCUDARendererRef r, const PFCUDABuildOptions* options, uint32_t first,
                               uint32_t count, int32_t width, int32_t height, const float* draw_alpha,
                               float* out_device) {
+    if (!r) return PF_CUDA_ERR_INVALID;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     int32_t rc = diff_prologue(r, first, count, width, height, draw_alpha, out_device);
     if (rc != PF_CUDA_OK) return rc;
     const Range g = make_range(r, first, count);
@@ -1570,7 +1594,8 @@ int32_t PFCUDARenderDiffAsync(PFCUDARendererRef r, const PFCUDABuildOptions* opt
 int32_t PFCUDABackward(PFCUDARendererRef r, const float* d_image, PFVector2F* d_points, float* d_alpha) {
     if (!r || !d_image || !d_points) return PF_CUDA_ERR_INVALID;
     if (!r->diff_valid) return PF_CUDA_ERR_INVALID;
-    PF_TRY(cudaSetDevice(r->device));
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
     cudaStream_t s = r->stream;
     const uint64_t before = launch_counter();
     PF_TRY(r->grad_mask.ensure(((size_t)r->tile_cap + 1) * 256));  // alpha ids < tiles <= tile_cap
