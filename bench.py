@@ -704,6 +704,7 @@ def main():
     ap.add_argument("--clock-soak", type=float, default=1.5,
                     help="seconds of untimed replays sampled for clocks before the timed steps")
     ap.add_argument("--e2e-steps", type=int, default=0)
+    ap.add_argument("--e2e-depth", type=int, default=2, help="frames in flight in the end-to-end leg")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="fraction of the 20,000 paths (small cases for profiling only)")
     args = ap.parse_args()
@@ -834,7 +835,8 @@ def main():
     traffic, traffic_src = measured_traffic(dom, args.scale == 1.0 and not args.paints and not args.d3d11)
 
     # e2e through the public API with host buffers
-    e2e_steps = args.e2e_steps or max(3, min(args.steps, 20))
+    e2e_steps = args.e2e_steps or max(3, min(2 * args.steps, 40))
+    depth = max(1, args.e2e_depth)
     pinned = {}
     for name in ("points", "flags", "contour_starts", "clip_paths", "draw_paths"):
         a = getattr(scene, name)
@@ -856,11 +858,33 @@ def main():
         r.upload_scene(scene, force=True)
         r.render(scene, out=host_np)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_ms = 1e3 * sum(e2e_times) / len(e2e_times)
+    serial_ms = 1e3 * sum(e2e_times) / len(e2e_times)
+    # The same steps with `depth` frames in flight (RenderPipeline: one
+    # renderer, stream and host thread per frame in flight), so one frame's
+    # upload and image write-back overlap another's kernels.  Step i is
+    # submitted once step i - depth is done, into that step's host buffer;
+    # every step uploads its scene and writes its image to host memory.
+    pipe = pf.RenderPipeline(local, depth=depth, options=pf.RendererOptions(d3d11_semantics=args.d3d11))
+    pouts = [torch.empty((H, W, 4), dtype=torch.uint8).pin_memory().numpy() for _ in range(depth)]
+    for f in [pipe.submit(scene, pouts[i % depth], force=True) for i in range(3 * depth)]:
+        f.result()
+    for o in pouts:
+        if not np.array_equal(o, host_np):
+            raise RuntimeError("pipelined frame differs from the serial frame")
+    futs = []
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        if i >= depth:
+            futs[i - depth].result()
+        futs.append(pipe.submit(scene, pouts[i % depth], force=True))
+    for f in futs[-depth:]:
+        f.result()
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / e2e_steps
+    pipe.close()
     if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
+        t = torch.tensor([e2e_ms, serial_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+        e2e_ms, serial_ms = (float(v) for v in t.tolist())
     e2e_value = world * nseg / (e2e_ms / 1e3) / 1e6
 
     if rank == 0:
@@ -885,7 +909,13 @@ def main():
                          "algorithmic_bytes_per_launch": sb[dom], "traffic": traffic,
                          "traffic_source": traffic_src},
             "e2e": {"value": round(e2e_value, 4), "unit": METRIC, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3), "steps": e2e_steps,
+                    "frames_in_flight": depth,
+                    "mode": f"RenderPipeline, {depth} renderers on their own streams and host threads; every "
+                            "step uploads the scene from pinned host memory and writes its RGBA8 image to "
+                            "pinned host memory",
+                    "serial_ms_per_step": round(serial_ms, 3),
+                    "serial_value": round(world * nseg / (serial_ms / 1e3) / 1e6, 4)},
             "gpu_launches": int(st.kernel_launches * args.steps),
             "clocks": {**clocks, "window": f"{soak} untimed replays (~{args.clock_soak:.1f} s) then the timed steps"},
         }

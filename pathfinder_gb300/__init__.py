@@ -12,6 +12,7 @@ from .stroke import LineCap, LineJoin, StrokeStyle
 from .renderer import (BuildOptions, Renderer, RendererLevel, RendererOptions, RenderStats, Transform2F)
 from . import _abi
 from .batch import SceneBatch, target
+from .pipeline import RenderPipeline
 
 PF_CUDA_FORMAT_RGBA8 = _abi.PF_CUDA_FORMAT_RGBA8
 PF_CUDA_FORMAT_R8 = _abi.PF_CUDA_FORMAT_R8
@@ -28,5 +29,5 @@ __all__ = [
     "generate_scene", "BuildOptions", "Renderer", "RendererLevel", "RendererOptions", "RenderStats",
     "Transform2F", "PF_SCENE_STARS_512", "PF_SCENE_SVG_4K", "PF_SCENE_GLYPH_ATLAS", "PF_SCENE_CUBIC_1K",
     "PF_SCENE_EDGE_CASES", "BlendMode", "ColorStop", "Gradient", "GradientKind", "GradientWrap", "Pattern", "PatternFilterKind", "LineCap",
-    "LineJoin", "StrokeStyle",
+    "LineJoin", "StrokeStyle", "SceneBatch", "RenderPipeline",
 ]
