@@ -1,5 +1,6 @@
 """Full-size parity: the 20,000-path 4K scene the benchmark renders (seed 1,
-scale 1.0) and the whole 16,384-glyph atlas against the oracle, and scenes
+scale 1.0; also in the D3D11 semantics and with the paint workload) and the
+whole 16,384-glyph atlas against the oracle, and scenes
 built to reach the composite's long screen-tile lists (33-128 entries, sorted
 in shared memory; over 128, sorted in place in global memory), an i8 backdrop
 that wraps, and one alpha tile holding hundreds of fills."""
@@ -38,6 +39,42 @@ def test_svg_4k_full_size_seed1(renderer):
     assert not fr.limit_hit
     st = _check_full(renderer, s, fr)
     assert st.fill_count > 5_000_000 and st.path_count == 20_000 + len(s.clip_paths)
+
+
+def test_svg_4k_full_size_d3d11_semantics(built):
+    """The same frame in the D3D11 level's tiling semantics (uniform dicing,
+    unclipped truncating bins): 3.5M microlines, 5.7M fills."""
+    import oracle
+    s = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=1, scale=1.0)
+    fr = oracle.OracleFrame(s, d3d11=True)
+    assert not fr.limit_hit
+    with pf.Renderer(0, pf.RendererOptions(d3d11_semantics=True)) as r:
+        st = _check_full(r, s, fr)
+        assert st.line_count == fr.line_count
+
+
+def test_svg_4k_full_size_with_paints(renderer):
+    """The bench's paint workload at full size (gradients, image patterns with
+    filters, blend modes; destructive modes tile the view box, 15M path
+    tiles): records bit-exact, and the image against the oracle's FP64
+    composite (masks are not read back at this tile count).  The GPU samples
+    gradients and blends in FP32 over coverage accumulated in 2^-22 steps,
+    and stacks of blend modes with divisions (dodge, burn, the non-separable
+    modes' division by the spread of the destination's channels) can amplify
+    those differences; so at 33M channel values a few may differ by 3-4/255:
+    at most one in a million above 2/255, none above 4/255."""
+    import bench
+    import oracle
+    s = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=1, scale=1.0)
+    bench.add_paints(s, 1)
+    img = renderer.render(s)
+    fr = oracle.OracleFrame(s)
+    assert renderer.stats().tile_count == fr.tile_count
+    compare_records(s, renderer.read_records(s), fr)
+    ora, _ = fr.render(s.width, s.height)
+    d = np.abs(img.astype(np.int16) - ora.astype(np.int16))
+    assert int((d > 2).sum()) <= d.size // 1_000_000, f"{int((d > 2).sum())} channel values differ by more than 2/255"
+    compare_images(img, ora, max_diff=4, frac_exact=0.95)
 
 
 def test_glyph_atlas_full_size():
