@@ -207,11 +207,14 @@ __device__ __forceinline__ void cubic_split_half(const Cubic& s, Cubic& a, Cubic
 }
 
 // Per-path context for the DDA.
-struct PathCtx {
+// A path's binning context, one 48-byte record per path written once per
+// frame, so a line's path costs one dependent read of three 16-byte words.
+struct __align__(16) PathCtx {
     int32_t minx, miny, maxx, maxy;  // tile rect
     uint32_t tile_base;              // global tile index of (minx, miny)
     uint32_t col_base;               // first above-rect column backdrop
     float vminx, vmaxx, vmaxy;       // clip box x range and max y (view box)
+    uint32_t pad[3];
 };
 
 __device__ __forceinline__ uint32_t outcode(float x, float y, float minx, float maxx, float maxy) {

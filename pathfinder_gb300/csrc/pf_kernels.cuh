@@ -43,6 +43,7 @@ struct FrameDev {
     uint32_t* tile_delta_scan;   // [tile_cap+1] exclusive scan of tile_delta
     uint32_t* path_tiles;        // [P+1] tiles per path (scan input)
     uint32_t* path_cols;         // [P+1] tile columns per path (scan input)
+    PathCtx*  path_bin;          // [P+1] binning context per global path (written after the path scan)
     int32_t*  col_backdrop;      // [col_cap] above-rect column sums
     uint32_t* seg_line_count;    // [seg_count+1] flattened lines per input segment
     uint32_t* seg_line_base;     // [seg_count+1] exclusive scan

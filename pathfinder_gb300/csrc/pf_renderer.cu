@@ -165,6 +165,7 @@ struct PFCUDARenderer {
 
     // per-frame buffers
     DevBuf<int4> tile_rect;
+    DevBuf<PathCtx> path_bin;
     DevBuf<uint32_t> tile_offset, col_offset;
     DevBuf<uint32_t> seg_line_count, seg_line_base;
     DevBuf<unsigned long long> seg_leaves;
@@ -321,6 +322,7 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.path.local_index = r->local_index.p;
     f.path.scene = r->scene_of.p;
     f.path.tile_rect = r->tile_rect.p;
+    f.path_bin = r->path_bin.p;
     f.path.tile_offset = r->tile_offset.p;
     f.path.col_offset = r->col_offset.p;
     f.scenes = r->scenes_dev.p;
@@ -785,7 +787,7 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->scene_of.release(); r->clip_gpath.release(); r->rule.release(); r->is_clip.release();
     r->scenes_dev.release(); r->tile_rect.release(); r->tile_offset.release(); r->col_offset.release();
     r->seg_line_count.release(); r->seg_line_base.release(); r->lines.release(); r->line_path.release();
-    r->seg_leaves.release();
+    r->seg_leaves.release(); r->path_bin.release();
     r->line_fill_count.release(); r->line_fill_base.release(); r->tile_fill_count.release();
     r->tile_fill_base.release(); r->tile_alpha.release(); r->alpha_owner.release(); r->tile_delta.release();
     r->tile_delta_scan.release(); r->path_tiles.release(); r->path_cols.release();
@@ -922,7 +924,7 @@ static int32_t upload_tables(PFCUDARendererRef r, const PFCUDASceneDesc* scenes,
         (e = r->path_in.ensure(Pz + 1)) || (e = r->scene_pack.ensure(scene_count)) ||
         (e = r->path_ncont.ensure(Pz + 1)) || (e = r->first_ord.ensure(Pz + 1)) || (e = r->paint.ensure(Pz + 1)) ||
         (e = r->local_index.ensure(Pz + 1)) || (e = r->scene_of.ensure(Pz + 1)) || (e = r->clip_gpath.ensure(Pz + 1)) ||
-        (e = r->rule.ensure(Pz + 1)) || (e = r->is_clip.ensure(Pz + 1)) || (e = r->tile_rect.ensure(Pz + 1)) ||
+        (e = r->rule.ensure(Pz + 1)) || (e = r->is_clip.ensure(Pz + 1)) || (e = r->tile_rect.ensure(Pz + 1)) || (e = r->path_bin.ensure(Pz + 1)) ||
         (e = r->draw_index.ensure(Pz + 1)) || (e = r->alpha_default.ensure((size_t)draw_base + 1)) ||
         (e = r->blend.ensure(Pz + 1)) || (e = r->occludes.ensure(Pz + 1)) || (e = r->overlay.ensure(Pz + 1)) ||
         (e = r->overlays.ensure(overlays.size() + 1)) || (e = r->overlay_opaque.ensure(overlays.size() + 1)) ||

@@ -629,10 +629,27 @@ void launch_bound(const FrameDev& f, const uint32_t* ord_contour, const uint32_t
     { count_launch(); k_bound<<<blocks, 256, 0, s>>>(f, ord_contour, starts); }
 }
 
+// A path's binning context from its tile rect, its scanned offsets and its
+// scene's view box.
+__device__ __forceinline__ PathCtx path_ctx(const FrameDev& f, uint32_t gp) {
+    PathCtx pc;
+    int4 r = f.path.tile_rect[gp];
+    pc.minx = r.x; pc.miny = r.y; pc.maxx = r.z; pc.maxy = r.w;
+    pc.tile_base = f.path.tile_offset[gp];
+    pc.col_base = f.path.col_offset[gp];
+    float4 v = f.scenes[f.path.scene[gp]].view_box;
+    pc.vminx = v.x; pc.vmaxx = v.z; pc.vmaxy = v.w;
+    pc.pad[0] = pc.pad[1] = pc.pad[2] = 0u;
+    return pc;
+}
+
 // Zero the per-tile accumulators and the per-screen-tile z-buffer and counts
-// of this frame; block 0 also checks the path scans' totals against the
-// capacities (one kernel instead of a check kernel and two memsets).
+// of this frame, and write each path's binning context; block 0 also checks
+// the path scans' totals against the capacities (one kernel instead of a
+// check kernel and two memsets).
 __global__ void k_zero_tiles(FrameDev f) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < f.path_count; i += gridDim.x * blockDim.x)
+        f.path_bin[f.path_begin + i] = path_ctx(f, f.path_begin + i);
     uint64_t T = f.counters->tiles, C = f.counters->columns;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (T > f.tile_cap) {
@@ -733,16 +750,18 @@ __global__ void __launch_bounds__(256, 6) k_flatten_count(FrameDev f) {
     unsigned long long active = 0;  // nodes of the current level to test
     unsigned long long leaves = 0;
     if (s < f.seg_count) {
+        // level 0 by the segment's own lane: a line, or a curve flat as a
+        // whole, is one leaf; otherwise both halves are tested at level 1
         Cubic c;
         const int kind = segment_root(f.pts, f.segs[f.seg_begin + s], c, &f.counters->status);
-        if (kind == kRootLine) leaves = 1;  // one leaf: the line itself
-        else if (kind == kRootCurve) { w.root[lane] = c; active = 1; }
+        if (kind == kRootLine || (kind == kRootCurve && cubic_is_flat(c))) leaves = 1;
+        else if (kind == kRootCurve) { w.root[lane] = c; active = 3; }
     }
     w.leaves[lane] = leaves;
     w.next[lane] = 0;
     if (lane == 0) w.deep = 0;
     __syncwarp();
-    for (int d = 0; d <= kLeafLevels; d++) {
+    for (int d = 1; d <= kLeafLevels; d++) {
         const uint32_t cnt = (uint32_t)__popcll(active);
         const uint32_t incl = warp_inclusive_scan(cnt);
         const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
@@ -796,20 +815,28 @@ __global__ void __launch_bounds__(256, 6) k_flatten_emit(FrameDev f) {
     const uint32_t s = s0 + lane;
     uint32_t n = 0, base = 0, path = 0;
     unsigned long long leaves = 0;
+    Cubic c{};
     if (s < f.seg_count) {
         const SegRec sr = f.segs[f.seg_begin + s];
         n = f.seg_line_count[s];
         if (n) {
-            Cubic c;
             segment_root(f.pts, sr, c, &f.counters->status);
-            roots[wib][lane] = c;
             leaves = f.seg_leaves[s];
             base = f.seg_line_base[s];
             path = (uint32_t)sr.w;
         }
     }
     const bool walk = n != 0 && leaves == 0;
-    const uint32_t nl = walk ? 0u : n;
+    if (n != 0 && leaves > 1ull) roots[wib][lane] = c;  // leaves spread over the warp below
+    if (n != 0 && leaves == 1ull) {  // one leaf at level 0: the root's base line, by its own lane
+        f.lines[base] = make_float4(c.base.fx, c.base.fy, c.base.tx, c.base.ty);
+        f.line_path[base] = path;
+        if constexpr (DIFF) {
+            f.line_seg[base] = f.seg_begin + s;
+            f.line_t[base] = make_float2(0.0f, 1.0f);
+        }
+    }
+    const uint32_t nl = walk || leaves == 1ull ? 0u : n;
     const uint32_t incl = warp_inclusive_scan(nl);
     const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
     __syncwarp();
@@ -909,17 +936,6 @@ void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
 // adjust_alpha_tile_backdrop: renderer/src/tiler.rs:191-308,
 // renderer/src/builder.rs:509-616)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ PathCtx path_ctx(const FrameDev& f, uint32_t gp) {
-    PathCtx pc;
-    int4 r = f.path.tile_rect[gp];
-    pc.minx = r.x; pc.miny = r.y; pc.maxx = r.z; pc.maxy = r.w;
-    pc.tile_base = f.path.tile_offset[gp];
-    pc.col_base = f.path.col_offset[gp];
-    float4 v = f.scenes[f.path.scene[gp]].view_box;
-    pc.vminx = v.x; pc.vmaxx = v.z; pc.vmaxy = v.w;
-    return pc;
-}
-
 __device__ __forceinline__ uint32_t line_total(const FrameDev& f) {
     uint64_t L = f.counters->lines;
     return L <= f.line_cap ? (uint32_t)L : 0u;
@@ -952,7 +968,7 @@ __global__ void __launch_bounds__(512, 3) k_bin_count(FrameDev f) {
     const uint32_t L = line_total(f);
     for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
         const float4 ln = f.lines[l];
-        const PathCtx pc = path_ctx(f, f.line_path[l]);
+        const PathCtx pc = f.path_bin[f.line_path[l]];
         CountSink sink{&pc, f.tile_fill_count, f.tile_delta, f.col_backdrop, 0};
         dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
         f.line_fill_count[l] = sink.n;
@@ -1022,9 +1038,12 @@ __global__ void __launch_bounds__(512, 3) k_bin_emit(const __grid_constant__ Fra
     if (f.counters->fills > f.fill_cap) return;
     const uint32_t L = line_total(f);
     for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
-        if (f.line_fill_count[l] == 0) continue;
+        // the line's reads issued together, its fill count tested after
+        const uint32_t nfill = f.line_fill_count[l];
         const float4 ln = f.lines[l];
-        const PathCtx pc = path_ctx(f, f.line_path[l]);
+        const uint32_t gp = f.line_path[l];
+        if (nfill == 0) continue;
+        const PathCtx pc = f.path_bin[gp];
         if constexpr (MODE == kFillF32) {
             EmitSinkF sink{f.fills_f, f.tile_fill_base, f.tile_fill_count, f.fill_cap};
             dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
