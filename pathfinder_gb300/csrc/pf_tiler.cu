@@ -817,12 +817,15 @@ __global__ void __launch_bounds__(256, 6) k_flatten_emit(FrameDev f) {
     unsigned long long leaves = 0;
     Cubic c{};
     if (s < f.seg_count) {
+        // the segment's four reads issued together
         const SegRec sr = f.segs[f.seg_begin + s];
         n = f.seg_line_count[s];
+        const unsigned long long lv = f.seg_leaves[s];
+        const uint32_t b = f.seg_line_base[s];
         if (n) {
             segment_root(f.pts, sr, c, &f.counters->status);
-            leaves = f.seg_leaves[s];
-            base = f.seg_line_base[s];
+            leaves = lv;
+            base = b;
             path = (uint32_t)sr.w;
         }
     }
