@@ -681,9 +681,10 @@ void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     { count_launch(); k_zero_tiles<<<f.sms * 8, 256, 0, s>>>(f); }
 }
 
-// Launch bounds of the flattening and binning passes: at most 42 registers a
-// thread (48 warps an SM at their block sizes); the extra warps hide their
-// gather and atomic latency.
+// Launch bounds: the flattening passes run at 32 registers a thread (64 warps
+// an SM, a few spilled values), the binning passes at 40 (48 warps); the
+// extra warps hide their gather and atomic latency (measured: 36 or 32
+// registers spill the binning passes' walk state and slow them).
 // ---------------------------------------------------------------------------
 // flattening (process_segment's recursion, renderer/src/tiler.rs:166-184).
 // Lines are written in emission order: input segments in path order, each
@@ -740,7 +741,7 @@ struct FlattenWarp {
     uint32_t deep;                     // segments deeper than kLeafLevels
 };
 
-__global__ void __launch_bounds__(256, 6) k_flatten_count(FrameDev f) {
+__global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
     __shared__ FlattenWarp smw[kFlattenMaxWarps];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     FlattenWarp& w = smw[wib];
@@ -803,7 +804,7 @@ __global__ void __launch_bounds__(256, 6) k_flatten_count(FrameDev f) {
 // at split path `addr` of depth d covers t in [addr, addr + 1) / 2^d.  The
 // adjoint holds these subdivisions fixed.
 template <bool DIFF>
-__global__ void __launch_bounds__(256, 6) k_flatten_emit(FrameDev f) {
+__global__ void __launch_bounds__(256, 8) k_flatten_emit(FrameDev f) {
     __shared__ Cubic roots[kFlattenMaxWarps][32];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t s0 = (blockIdx.x * (blockDim.x >> 5) + wib) * 32u;
