@@ -704,7 +704,7 @@ def main():
     ap.add_argument("--clock-soak", type=float, default=1.5,
                     help="seconds of untimed replays sampled for clocks before the timed steps")
     ap.add_argument("--e2e-steps", type=int, default=0)
-    ap.add_argument("--e2e-depth", type=int, default=2, help="frames in flight in the end-to-end leg")
+    ap.add_argument("--e2e-depth", type=int, default=3, help="frames in flight in the end-to-end leg")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="fraction of the 20,000 paths (small cases for profiling only)")
     args = ap.parse_args()
@@ -835,7 +835,7 @@ def main():
     traffic, traffic_src = measured_traffic(dom, args.scale == 1.0 and not args.paints and not args.d3d11)
 
     # e2e through the public API with host buffers
-    e2e_steps = args.e2e_steps or max(3, min(2 * args.steps, 40))
+    e2e_steps = args.e2e_steps or max(3, min(10 * args.steps, 200))
     depth = max(1, args.e2e_depth)
     pinned = {}
     for name in ("points", "flags", "contour_starts", "clip_paths", "draw_paths"):
@@ -861,9 +861,9 @@ def main():
     serial_ms = 1e3 * sum(e2e_times) / len(e2e_times)
     # The same steps with `depth` frames in flight (RenderPipeline: one
     # renderer, stream and host thread per frame in flight), so one frame's
-    # upload and image write-back overlap another's kernels.  Step i is
-    # submitted once step i - depth is done, into that step's host buffer;
-    # every step uploads its scene and writes its image to host memory.
+    # upload and image copy overlap another's kernels.  Step i is submitted
+    # once step i - depth is done, into that step's host buffer; every step
+    # uploads its scene and copies its image to host memory.
     pipe = pf.RenderPipeline(local, depth=depth, options=pf.RendererOptions(d3d11_semantics=args.d3d11))
     pouts = [torch.empty((H, W, 4), dtype=torch.uint8).pin_memory().numpy() for _ in range(depth)]
     for f in [pipe.submit(scene, pouts[i % depth], force=True) for i in range(3 * depth)]:
@@ -912,8 +912,8 @@ def main():
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3), "steps": e2e_steps,
                     "frames_in_flight": depth,
                     "mode": f"RenderPipeline, {depth} renderers on their own streams and host threads; every "
-                            "step uploads the scene from pinned host memory and writes its RGBA8 image to "
-                            "pinned host memory",
+                            "step uploads the scene from pinned host memory and copies its RGBA8 image to "
+                            "pinned host memory (one device-to-host copy after the composite)",
                     "serial_ms_per_step": round(serial_ms, 3),
                     "serial_value": round(world * nseg / (serial_ms / 1e3) / 1e6, 4)},
             "gpu_launches": int(st.kernel_launches * args.steps),

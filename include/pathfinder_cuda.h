@@ -156,6 +156,12 @@ typedef struct PFCUDAPattern {
 
 #define PF_MEMORY_HOST   0
 #define PF_MEMORY_DEVICE 1
+/* Frame outputs only (PFCUDARenderScene, PFCUDARenderCoverage): host memory
+ * written by one device-to-host copy of the frame's image, which the copy
+ * engine makes after the composite, instead of by the composite itself.  On
+ * page-locked memory the copy leaves the SMs free for other streams' work
+ * (frames in flight on other renderers). */
+#define PF_MEMORY_HOST_COPY 2
 
 /* One path of the scene: a range of contours of the shared outline buffers.
  * Mirrors DrawPath / ClipPath (renderer/src/scene.rs:441-472): outline,
@@ -295,7 +301,8 @@ int32_t PFCUDASceneUpload(PFCUDARendererRef renderer, const PFCUDASceneDesc* sce
  * (renderer/src/gpu/renderer.rs:350-460) with the seven D3D11 dispatches
  * (renderer/src/gpu/d3d11/renderer.rs:427-782) replaced by this library's
  * kernels.  Writes premultiplied RGBA8, row 0 = top, into `out_rgba8`
- * (width*height*4 bytes; host or device memory per out_memory): every pixel
+ * (width*height*4 bytes; host or device memory, or host memory written by a
+ * copy, per out_memory): every pixel
  * of the view box's 16x16 screen tiles; pixels outside them keep the
  * buffer's contents.  Synchronises the stream before returning. */
 int32_t PFCUDARenderScene(PFCUDARendererRef renderer,

@@ -23,6 +23,7 @@ PF_CUDA_ERR_NO_SCENE = 6
 
 PF_MEMORY_HOST = 0
 PF_MEMORY_DEVICE = 1
+PF_MEMORY_HOST_COPY = 2  # frame outputs: host memory written by one device-to-host copy
 
 PF_CUDA_RENDERER_D3D11_SEMANTICS = 0x1
 

@@ -676,9 +676,17 @@ cudaError_t enqueue_plain(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     return cudaGraphLaunch(r->replay_exec, r->stream);
 }
 
-// Run one frame synchronously with regrow-and-retry.
+// A device-to-host copy enqueued after a frame and before its status read.
+struct ImageCopy {
+    void* dst;
+    const void* src;
+    size_t bytes;
+};
+
+// Run one frame synchronously with regrow-and-retry; `copy` (optional) is
+// enqueued behind each attempt, so the one synchronisation covers it.
 int32_t run_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, void* out_dev, const Range& g,
-                  bool diff = false) {
+                  bool diff = false, const ImageCopy* copy = nullptr) {
     if (!r->has_scene) return PF_CUDA_ERR_NO_SCENE;
     r->last = g;
     for (int attempt = 0; attempt < 4; attempt++) {
@@ -687,6 +695,7 @@ int32_t run_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int mode, v
         if (diff || r->profiling) PF_TRY(enqueue_frame(r, opts, mode, out_dev, g, diff));
         else PF_TRY(enqueue_plain(r, opts, mode, out_dev, g));
         PF_TRY(cudaEventRecord(r->ev1, r->stream));
+        if (copy) PF_TRY(cudaMemcpyAsync(copy->dst, copy->src, copy->bytes, cudaMemcpyDeviceToHost, r->stream));
         PF_TRY(cudaMemcpyAsync(r->h_counters, r->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, r->stream));
         PF_TRY(cudaStreamSynchronize(r->stream));
         float ms = 0;
@@ -1156,7 +1165,7 @@ static int32_t render_plain(PFCUDARendererRef r, const PFCUDABuildOptions* optio
     const size_t elem = format == PF_CUDA_FORMAT_RGBA8 ? 4 : (format == PF_CUDA_FORMAT_R8 ? 1 : 4);
     const size_t bytes = (size_t)width * (size_t)height * elem;
     void* dst = out;
-    bool staged = false;
+    bool staged = out_memory == PF_MEMORY_HOST_COPY;
     if (out_memory == PF_MEMORY_HOST) {
         // Page-locked host memory is mapped into the device's address space:
         // the composite writes the frame there itself (no device copy and no
@@ -1170,7 +1179,7 @@ static int32_t render_plain(PFCUDARendererRef r, const PFCUDABuildOptions* optio
         else
             staged = true;
         (void)cudaGetLastError();
-    } else if (out_memory != PF_MEMORY_DEVICE) {
+    } else if (out_memory != PF_MEMORY_DEVICE && out_memory != PF_MEMORY_HOST_COPY) {
         return PF_CUDA_ERR_INVALID;
     }
     if (staged) {
@@ -1184,12 +1193,9 @@ static int32_t render_plain(PFCUDARendererRef r, const PFCUDABuildOptions* optio
                                   (int64_t)si.screen.z * 16 >= width && (int64_t)si.screen.w * 16 >= height);
         if (!covered) PF_TRY(cudaMemcpyAsync(dst, out, bytes, cudaMemcpyHostToDevice, r->stream));
     }
-    rc = run_frame(r, options, format, dst, make_range(r, 0, (uint32_t)r->scenes.size()));
-    if (rc == PF_CUDA_OK && staged) {
-        PF_TRY(cudaMemcpyAsync(out, dst, bytes, cudaMemcpyDeviceToHost, r->stream));
-        PF_TRY(cudaStreamSynchronize(r->stream));
-    }
-    return rc;
+    const ImageCopy copy{out, dst, bytes};
+    return run_frame(r, options, format, dst, make_range(r, 0, (uint32_t)r->scenes.size()), false,
+                     staged ? &copy : nullptr);
 }
 
 int32_t PFCUDARenderScene(PFCUDARendererRef r, const PFCUDABuildOptions* options, int32_t width, int32_t height,

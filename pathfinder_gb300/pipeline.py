@@ -25,14 +25,18 @@ class RenderPipeline:
     ``submit(scene, out)`` uploads the scene to the next free renderer (when
     that renderer does not hold it yet, or always with ``force``) and renders
     it into ``out``; the returned future's result is ``out`` once the frame is
-    written.  A frame writes only its own ``out``: do not reuse that buffer
-    before its future is done.  Errors of a frame are raised by its future.
+    written.  With ``copy_image`` (the default) a host ``out`` is written by a
+    device-to-host copy after each composite, which the copy engine makes
+    while the SMs run the other frames in flight.  A frame writes only its
+    own ``out``: do not reuse that buffer before its future is done.  Errors
+    of a frame are raised by its future.
     """
 
-    def __init__(self, device: int = 0, depth: int = 2, options: RendererOptions | None = None,
-                 renderer_factory=None):
+    def __init__(self, device: int = 0, depth: int = 3, options: RendererOptions | None = None,
+                 renderer_factory=None, copy_image: bool = True):
         if depth < 1:
             raise ValueError("depth must be at least 1")
+        self.copy_image = copy_image
         make = renderer_factory or (lambda: Renderer(device, options))
         self.depth = depth
         self._renderers = []
@@ -57,7 +61,7 @@ class RenderPipeline:
         r = self._free.get()
         try:
             r.upload_scene(scene, force=force)
-            return r.render(scene, options, out=out)
+            return r.render(scene, options, out=out, copy_image=self.copy_image)
         finally:
             self._free.put(r)
 

@@ -159,14 +159,19 @@ class Renderer:
         self._uploaded = key
 
     def render(self, scene: Scene, options: BuildOptions | None = None, out=None,
-               width: int | None = None, height: int | None = None):
+               width: int | None = None, height: int | None = None, copy_image: bool = False):
         """Scene::build_and_render for the CUDA level: premultiplied RGBA8,
-        row 0 at the top.  ``out`` may be a host numpy array or a CUDA tensor."""
+        row 0 at the top.  ``out`` may be a host numpy array or a CUDA tensor.
+        ``copy_image``: a host ``out`` is written by one device-to-host copy
+        after the composite (PF_MEMORY_HOST_COPY) instead of by the composite
+        itself, which leaves the SMs to frames on other renderers."""
         self.upload_scene(scene)
         w, h = width or scene.width, height or scene.height
         if out is None:
             out = np.zeros((h, w, 4), np.uint8)
         p, mem = _ptr(out)
+        if copy_image and mem == _abi.PF_MEMORY_HOST:
+            mem = _abi.PF_MEMORY_HOST_COPY
         bo = (options or BuildOptions()).to_c()
         _abi.check(self._lib.PFCUDARenderScene(self._h, C.byref(bo), w, h, C.c_void_p(p), mem), "PFCUDARenderScene")
         return out

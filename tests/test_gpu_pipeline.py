@@ -30,3 +30,25 @@ def test_pipeline_frames_equal_serial_frames(renderer, depth):
             f.result()
         for d in dev:
             assert np.array_equal(d.cpu().numpy(), refs[0])
+
+
+def test_image_copy_equals_direct_host_writes(renderer):
+    """PF_MEMORY_HOST_COPY (one device-to-host copy after the composite) and
+    the composite's own writes into page-locked memory, and pageable memory,
+    give the same image; pixels outside the screen tiles keep the buffer's
+    contents either way."""
+    torch = pytest.importorskip("torch")
+    s = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=31, scale=0.05)
+    ref = renderer.render(s)
+    for pinned in (True, False):
+        out = torch.full((s.height, s.width, 4), 7, dtype=torch.uint8)
+        out = (out.pin_memory() if pinned else out).numpy()
+        renderer.render(s, out=out, copy_image=True)
+        assert np.array_equal(out, ref)
+    # a target larger than the view box's screen tiles: the margin is kept
+    big = torch.full((s.height + 16, s.width + 16, 4), 9, dtype=torch.uint8).pin_memory().numpy()
+    direct = big.copy()
+    renderer.render(s, out=big, width=s.width + 16, height=s.height + 16, copy_image=True)
+    renderer.render(s, out=direct, width=s.width + 16, height=s.height + 16)
+    assert np.array_equal(big, direct)
+    assert (big[s.height + 8:, :, :] == 9).all()

@@ -32,7 +32,7 @@ class FakeRenderer:
             self.uploads += 1
             self.held = (scene.id, scene.epoch)
 
-    def render(self, scene, options=None, out=None):
+    def render(self, scene, options=None, out=None, copy_image=False):
         assert not self.busy, "renderer used by two threads at once"
         self.busy = True
         with FakeRenderer.lock:
