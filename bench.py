@@ -866,7 +866,7 @@ def main():
     # uploads its scene and copies its image to host memory.
     pipe = pf.RenderPipeline(local, depth=depth, options=pf.RendererOptions(d3d11_semantics=args.d3d11))
     pouts = [torch.empty((H, W, 4), dtype=torch.uint8).pin_memory().numpy() for _ in range(depth)]
-    for f in [pipe.submit(scene, pouts[i % depth], force=True) for i in range(3 * depth)]:
+    for f in [pipe.submit(scene, pouts[i % depth]) for i in range(3 * depth)]:
         f.result()
     for o in pouts:
         if not np.array_equal(o, host_np):
@@ -876,7 +876,7 @@ def main():
     for i in range(e2e_steps):
         if i >= depth:
             futs[i - depth].result()
-        futs.append(pipe.submit(scene, pouts[i % depth], force=True))
+        futs.append(pipe.submit(scene, pouts[i % depth]))
     for f in futs[-depth:]:
         f.result()
     e2e_ms = 1e3 * (time.perf_counter() - t0) / e2e_steps
@@ -911,7 +911,8 @@ def main():
             "e2e": {"value": round(e2e_value, 4), "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3), "steps": e2e_steps,
                     "frames_in_flight": depth,
-                    "mode": f"RenderPipeline, {depth} renderers on their own streams and host threads; every "
+                    "mode": f"RenderPipeline (PFCUDAPipeline), {depth} renderers on their own streams and "
+                            "worker threads; every "
                             "step uploads the scene from pinned host memory and copies its RGBA8 image to "
                             "pinned host memory (one device-to-host copy after the composite)",
                     "serial_ms_per_step": round(serial_ms, 3),

@@ -561,6 +561,38 @@ int32_t PFCUDAStrokeToFill(PFCUDARendererRef renderer, const PFCUDAStrokeInput* 
 /* Human-readable text for a status code (static storage). */
 const char* PFCUDAStatusString(int32_t status);
 
+/* ---- frames in flight (no reference counterpart in this form) --------------
+ * The CUDA level's SceneProxy (renderer/src/concurrent/scene_proxy.rs:11-20,
+ * :86-121 builds scenes on a worker thread and keeps a bounded number of
+ * render commands in flight): `depth` renderers on one device, each with its
+ * own stream, buffers and worker thread, render the submitted frames in
+ * submission order, at most `depth` at once, so one frame's upload and image
+ * copy overlap the other frames' kernels. */
+typedef struct PFCUDAPipeline* PFCUDAPipelineRef;
+int32_t PFCUDAPipelineCreate(int32_t device_ordinal, int32_t depth,
+                             const PFCUDARendererOptions* options,
+                             PFCUDAPipelineRef* out_pipeline);
+/* Waits for every submitted frame, then frees the renderers and threads. */
+int32_t PFCUDAPipelineDestroy(PFCUDAPipelineRef pipeline);
+/* Queues one frame: PFCUDASceneUpload of `scene` on the next free renderer,
+ * then PFCUDARenderScene(options, width, height, out_rgba8, out_memory)
+ * (options may be NULL: identity).  Returns at once with the frame's ticket
+ * (1, 2, ...).  The scene's buffers, `out_rgba8` and `options` must stay
+ * valid and unchanged until the frame is done.  For host outputs,
+ * PF_MEMORY_HOST_COPY into page-locked memory keeps the SMs for the other
+ * frames. */
+int32_t PFCUDAPipelineSubmit(PFCUDAPipelineRef pipeline, const PFCUDASceneDesc* scene,
+                             const PFCUDABuildOptions* options, int32_t width, int32_t height,
+                             uint8_t* out_rgba8, int32_t out_memory, uint64_t* out_ticket);
+/* *out_done = 1 when frame `ticket` is done (its status then waits for
+ * PFCUDAPipelineWait), else 0.  PF_CUDA_ERR_INVALID for a ticket that was
+ * never submitted or was already waited for. */
+int32_t PFCUDAPipelinePoll(PFCUDAPipelineRef pipeline, uint64_t ticket, int32_t* out_done);
+/* Waits for frame `ticket` and returns its status: the upload's or the
+ * frame's error, else PF_CUDA_OK.  A ticket is waited for once;
+ * PF_CUDA_ERR_INVALID for one never submitted or already waited for. */
+int32_t PFCUDAPipelineWait(PFCUDAPipelineRef pipeline, uint64_t ticket);
+
 #ifdef __cplusplus
 }
 #endif

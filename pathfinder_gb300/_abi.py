@@ -255,6 +255,13 @@ _SIGS = {
                                           C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
     "PFCUDABackward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "PFCUDAStatusString": (C.c_char_p, [C.c_int32]),
+    "PFCUDAPipelineCreate": (C.c_int32, [C.c_int32, C.c_int32, C.POINTER(PFCUDARendererOptions),
+                                         C.POINTER(C.c_void_p)]),
+    "PFCUDAPipelineDestroy": (C.c_int32, [C.c_void_p]),
+    "PFCUDAPipelineSubmit": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDASceneDesc), C.POINTER(PFCUDABuildOptions),
+                                         C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.POINTER(C.c_uint64)]),
+    "PFCUDAPipelinePoll": (C.c_int32, [C.c_void_p, C.c_uint64, C.POINTER(C.c_int32)]),
+    "PFCUDAPipelineWait": (C.c_int32, [C.c_void_p, C.c_uint64]),
 }
 
 # The seeded scene generators (include/pathfinder_cuda_scenes.h) live in their

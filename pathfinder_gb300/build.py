@@ -38,6 +38,7 @@ UNITS = [
     ("pf_paint.cu", []),
     ("pf_stroke.cu", ["-fmad=false"]),
     ("pf_pack.cu", []),
+    ("pf_pipeline.cu", []),
 ]
 
 

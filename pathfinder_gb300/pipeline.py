@@ -1,82 +1,106 @@
 """Frames in flight: a stream of scenes rendered by several renderers at once,
-each on its own CUDA stream and host thread, so that one frame's upload and
-image write-back overlap the kernels of another.
+each on its own CUDA stream and worker thread, so that one frame's upload and
+image copy overlap the kernels of the others.
 
-This is the CUDA level's counterpart of SceneProxy
-(renderer/src/concurrent/scene_proxy.rs:11-20, :86-121).  SceneProxy moves
-scene building off the thread that drives the GPU and keeps a bounded number
-of render commands in flight.  Here every stage of a frame is GPU work, so
-what overlaps is whole frames, at most `depth` of them.  Each renderer is used
-by one thread at a time (renderers are not thread-safe, as the reference's
-`&mut Renderer` is not), and the C ABI selects each renderer's device for the
-duration of every call.
+This is the host mirror of PFCUDAPipeline (include/pathfinder_cuda.h), the
+CUDA level's counterpart of SceneProxy
+(renderer/src/concurrent/scene_proxy.rs:11-20, :86-121).  SceneProxy builds
+scenes on a worker thread and keeps a bounded number of render commands in
+flight; here every stage of a frame is GPU work, so what is kept in flight is
+whole frames, at most `depth` of them.  The workers are native threads of the
+library: submitting returns at once, and waiting for a frame releases the
+interpreter.
 """
 from __future__ import annotations
 
-import queue
-from concurrent.futures import Future, ThreadPoolExecutor
+import ctypes as C
 
-from .renderer import BuildOptions, Renderer, RendererOptions
+from . import _abi
+from .renderer import BuildOptions, RendererOptions, _ptr
+
+
+class Frame:
+    """One submitted frame: ``result()`` waits for it and returns its output
+    buffer (raising the frame's error), ``done()`` asks without waiting."""
+
+    def __init__(self, pipeline: "RenderPipeline", ticket: int, out):
+        self._pipeline = pipeline
+        self.ticket = ticket
+        self._out = out
+        self._code = None
+
+    def done(self) -> bool:
+        if self._code is not None:
+            return True
+        flag = C.c_int32()
+        _abi.check(self._pipeline._lib.PFCUDAPipelinePoll(self._pipeline._h, self.ticket, C.byref(flag)),
+                   "PFCUDAPipelinePoll")
+        return bool(flag.value)
+
+    def result(self):
+        if self._code is None:
+            self._code = self._pipeline._wait(self.ticket)
+        _abi.check(self._code, "pipelined frame")
+        return self._out
 
 
 class RenderPipeline:
-    """`depth` renderers on one device behind a pool of `depth` host threads.
+    """`depth` renderers on one device behind the library's worker threads.
 
-    ``submit(scene, out)`` uploads the scene to the next free renderer (when
-    that renderer does not hold it yet, or always with ``force``) and renders
-    it into ``out``; the returned future's result is ``out`` once the frame is
-    written.  With ``copy_image`` (the default) a host ``out`` is written by a
-    device-to-host copy after each composite, which the copy engine makes
-    while the SMs run the other frames in flight.  A frame writes only its
-    own ``out``: do not reuse that buffer before its future is done.  Errors
-    of a frame are raised by its future.
+    ``submit(scene, out)`` uploads the scene to the next free renderer and
+    renders it (premultiplied RGBA8) into ``out``, a host numpy array or a
+    CUDA tensor; the returned Frame's ``result()`` is ``out`` once written.
+    With ``copy_image`` (the default) a host ``out`` is written by one
+    device-to-host copy after the composite (PF_MEMORY_HOST_COPY), which the
+    copy engine makes while the SMs run the other frames; use page-locked
+    memory for it.  The scene and ``out`` are kept alive until their frame
+    is waited for or the pipeline is closed; do not change them before.
     """
 
     def __init__(self, device: int = 0, depth: int = 3, options: RendererOptions | None = None,
-                 renderer_factory=None, copy_image: bool = True):
-        if depth < 1:
-            raise ValueError("depth must be at least 1")
-        self.copy_image = copy_image
-        make = renderer_factory or (lambda: Renderer(device, options))
+                 copy_image: bool = True):
+        self._lib = _abi.lib()
         self.depth = depth
-        self._renderers = []
-        try:
-            for _ in range(depth):
-                self._renderers.append(make())
-        except Exception:
-            for r in self._renderers:
-                r.close()
-            raise
-        self._free: queue.SimpleQueue = queue.SimpleQueue()
-        for r in self._renderers:
-            self._free.put(r)
-        self._pool = ThreadPoolExecutor(max_workers=depth, thread_name_prefix="pf-frame")
+        self.copy_image = copy_image
+        self._h = C.c_void_p()
+        self._held = {}  # ticket -> what the frame reads or writes
+        o = (options or RendererOptions()).to_c()
+        _abi.check(self._lib.PFCUDAPipelineCreate(device, depth, C.byref(o), C.byref(self._h)),
+                   "PFCUDAPipelineCreate")
 
-    @property
-    def renderers(self) -> list:
-        return list(self._renderers)
-
-    def _frame(self, scene, out, options, force):
-        # a task starts only on one of `depth` workers, so a renderer is free
-        r = self._free.get()
-        try:
-            r.upload_scene(scene, force=force)
-            return r.render(scene, options, out=out, copy_image=self.copy_image)
-        finally:
-            self._free.put(r)
-
-    def submit(self, scene, out, options: BuildOptions | None = None, force: bool = False) -> Future:
-        if self._pool is None:
+    def submit(self, scene, out, options: BuildOptions | None = None, width: int | None = None,
+               height: int | None = None) -> Frame:
+        if not self._h:
             raise RuntimeError("pipeline is closed")
-        return self._pool.submit(self._frame, scene, out, options, force)
+        w, h = width or scene.width, height or scene.height
+        p, mem = _ptr(out)
+        if self.copy_image and mem == _abi.PF_MEMORY_HOST:
+            mem = _abi.PF_MEMORY_HOST_COPY
+        desc = scene.desc()
+        bo = (options or BuildOptions()).to_c()
+        ticket = C.c_uint64()
+        _abi.check(self._lib.PFCUDAPipelineSubmit(self._h, C.byref(desc), C.byref(bo), w, h, C.c_void_p(p), mem,
+                                                  C.byref(ticket)), "PFCUDAPipelineSubmit")
+        self._held[ticket.value] = (scene, desc, bo, out)
+        return Frame(self, ticket.value, out)
+
+    def _wait(self, ticket: int) -> int:
+        code = self._lib.PFCUDAPipelineWait(self._h, ticket)
+        self._held.pop(ticket, None)
+        return code
 
     def close(self) -> None:
-        if self._pool is not None:
-            self._pool.shutdown(wait=True)
-            self._pool = None
-        for r in self._renderers:
-            r.close()
-        self._renderers = []
+        """Waits for every submitted frame and frees the renderers."""
+        if self._h:
+            self._lib.PFCUDAPipelineDestroy(self._h)
+            self._h = C.c_void_p()
+        self._held.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
     def __enter__(self):
         return self

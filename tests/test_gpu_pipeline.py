@@ -1,35 +1,75 @@
-"""Frames in flight on several renderers give exactly the images of one
-renderer rendering the same scenes one after another."""
+"""Frames in flight (PFCUDAPipeline) give exactly the images of one renderer
+rendering the same scenes one after another; a frame's error is its own."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
 import pathfinder_gb300 as pf
+from pathfinder_gb300 import _abi
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("depth", [2, 3])
-def test_pipeline_frames_equal_serial_frames(renderer, depth):
-    torch = pytest.importorskip("torch")
+def _scenes():
     scenes = [pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=s, scale=0.05) for s in (21, 22, 23)]
     scenes.append(pf.generate_scene(pf.PF_SCENE_STARS_512, seed=4))
     scenes.append(pf.generate_scene(pf.PF_SCENE_EDGE_CASES))
+    return scenes
+
+
+@pytest.mark.parametrize("depth,copy_image", [(1, True), (2, False), (3, True)])
+def test_pipeline_frames_equal_serial_frames(renderer, depth, copy_image):
+    torch = pytest.importorskip("torch")
+    scenes = _scenes()
     refs = [renderer.render(s) for s in scenes]
     order = [0, 1, 2, 3, 4, 0, 2, 4, 1, 3, 0, 0]
-    with pf.RenderPipeline(0, depth=depth) as p:
+    with pf.RenderPipeline(0, depth=depth, copy_image=copy_image) as p:
         outs = [torch.empty((scenes[k].height, scenes[k].width, 4), dtype=torch.uint8).pin_memory().numpy()
                 for k in order]
-        futs = [p.submit(scenes[k], out) for k, out in zip(order, outs)]
-        for k, f in zip(order, futs):
+        frames = [p.submit(scenes[k], out) for k, out in zip(order, outs)]
+        for k, f in zip(order, frames):
             assert np.array_equal(f.result(), refs[k])
-        # forced uploads of one scene, frames into device memory
+            assert f.done()
+        # frames into device memory
         dev = [torch.zeros((scenes[0].height, scenes[0].width, 4), dtype=torch.uint8, device="cuda")
                for _ in range(2 * depth)]
-        futs = [p.submit(scenes[0], d, force=True) for d in dev]
-        for f in futs:
+        frames = [p.submit(scenes[0], d) for d in dev]
+        for f in frames:
             f.result()
         for d in dev:
             assert np.array_equal(d.cpu().numpy(), refs[0])
+
+
+def test_pipeline_frame_errors_are_their_own(renderer):
+    """A scene the upload refuses fails its frame only; tickets are waited for
+    once, and unknown tickets are refused."""
+    good = pf.generate_scene(pf.PF_SCENE_STARS_512, seed=5)
+    ref = renderer.render(good)
+    bad = pf.generate_scene(pf.PF_SCENE_STARS_512, seed=5)
+    bad.draw_paths["contour_count"][0] = 1 << 20  # past the scene's contours
+    bad.epoch += 1
+    with pf.RenderPipeline(0, depth=2) as p:
+        outs = [np.zeros((good.height, good.width, 4), np.uint8) for _ in range(4)]
+        frames = [p.submit(s, o) for s, o in zip((good, bad, good, bad), outs)]
+        for i, f in enumerate(frames):
+            if i % 2:
+                with pytest.raises(_abi.PFCUDAError) as e:
+                    f.result()
+                assert e.value.code == _abi.PF_CUDA_ERR_INVALID
+            else:
+                assert np.array_equal(f.result(), ref)
+        L = _abi.lib()
+        t = C.c_uint64()
+        desc = good.desc()
+        out = outs[0]
+        assert L.PFCUDAPipelineSubmit(p._h, C.byref(desc), None, good.width, good.height,
+                                      C.c_void_p(out.ctypes.data), _abi.PF_MEMORY_HOST, C.byref(t)) == 0
+        assert L.PFCUDAPipelineWait(p._h, t.value) == _abi.PF_CUDA_OK
+        assert L.PFCUDAPipelineWait(p._h, t.value) == _abi.PF_CUDA_ERR_INVALID
+        done = C.c_int32()
+        assert L.PFCUDAPipelinePoll(p._h, t.value + 100, C.byref(done)) == _abi.PF_CUDA_ERR_INVALID
+        assert np.array_equal(out, ref)
 
 
 def test_image_copy_equals_direct_host_writes(renderer):
@@ -51,4 +91,4 @@ def test_image_copy_equals_direct_host_writes(renderer):
     renderer.render(s, out=big, width=s.width + 16, height=s.height + 16, copy_image=True)
     renderer.render(s, out=direct, width=s.width + 16, height=s.height + 16)
     assert np.array_equal(big, direct)
-    assert (big[s.height + 8:, :, :] == 9).all()
+    assert (big[s.height:, :, :] == 9).all()
