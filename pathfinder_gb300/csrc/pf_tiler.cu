@@ -102,6 +102,18 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v) {
     return t;
 }
 
+// The sum of v over the block, in every thread.
+template <int NT>
+__device__ __forceinline__ uint32_t block_sum_all(uint32_t v) {
+    __shared__ uint32_t sum;
+    const uint32_t t = block_sum<NT>(v);
+    if (threadIdx.x == 0) sum = t;
+    __syncthreads();
+    const uint32_t r = sum;
+    __syncthreads();  // the next call rewrites `sum`
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // generic exclusive scan (reduce, scan partials, down-sweep)
 // ---------------------------------------------------------------------------
@@ -322,6 +334,13 @@ static bool launch_scan_onepass(const ScanLanes& lanes, const uint64_t* d_n, uin
     return true;
 }
 
+template <int NL>
+__global__ void k_scanm_reduce(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, uint32_t* __restrict__ partials);
+template <int NL>
+__global__ void k_scanm_down_fused(ScanLanes L, const uint64_t* d_n, uint32_t n_cap,
+                                   const uint32_t* __restrict__ partials);
+constexpr uint32_t kFusedScanBlocks = 2048;  // the most blocks a two-launch scan takes
+
 void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_t n_host, uint32_t n_cap, int mode,
                  uint64_t* total_out, ScanTemp& tmp, cudaStream_t s) {
     uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
@@ -332,6 +351,14 @@ void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_
         one.count = 1;
         one.in[0] = in; one.out[0] = out; one.total[0] = total_out; one.mode[0] = mode;
         if (launch_scan_onepass<1>(one, d_n, n_host, tmp, s)) return;
+    }
+    if (nb <= kFusedScanBlocks) {  // reduce, then down-sweeps that sum their own prefixes
+        ScanLanes one{};
+        one.count = 1;
+        one.in[0] = in; one.out[0] = out; one.total[0] = total_out; one.mode[0] = mode;
+        { count_launch(); k_scanm_reduce<1><<<nb, kScanThreads, 0, s>>>(one, d_n, n_host, tmp.partials); }
+        { count_launch(); k_scanm_down_fused<1><<<nb, kScanThreads, 0, s>>>(one, d_n, n_host, tmp.partials); }
+        return;
     }
     { count_launch(); k_scan_reduce<<<nb, kScanThreads, 0, s>>>(in, d_n, n_host, mode, tmp.partials); }
     { count_launch(); k_scan_partials<<<1, 1024, 0, s>>>(tmp.partials, d_n, n_host, out, total_out); }
@@ -428,11 +455,64 @@ __global__ void k_scanm_down(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, c
     }
 }
 
+// Down-sweep that sums its block's prefix from the blocks' partial sums
+// itself (each block reads fewer than kFusedScanBlocks of them, from L2), so a
+// scan of that many blocks needs no launch that scans the partials.  The
+// last block with values writes the totals; with no values, block 0 does.
+template <int NL>
+__global__ void k_scanm_down_fused(ScanLanes L, const uint64_t* d_n, uint32_t n_cap,
+                                   const uint32_t* __restrict__ partials) {
+    const uint32_t n = scan_count(d_n, n_cap);
+    const uint32_t base = blockIdx.x * kScanChunk;
+    const uint32_t nbc = (n_cap + kScanChunk - 1) / kScanChunk, nb = (n + kScanChunk - 1) / kScanChunk;
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+#pragma unroll
+            for (int l = 0; l < NL; l++) {
+                L.out[l][0] = 0;
+                if (L.total[l]) *L.total[l] = 0;
+            }
+        }
+        return;
+    }
+    if (base >= n) return;
+    const uint32_t first = base + threadIdx.x * kScanItems;
+#pragma unroll
+    for (int l = 0; l < NL; l++) {
+        uint32_t ps = 0;
+        for (uint32_t j = threadIdx.x; j < blockIdx.x; j += kScanThreads) ps += partials[l * nbc + j];
+        const uint32_t prefix = block_sum_all<kScanThreads>(ps);
+        uint32_t v[kScanItems];
+        uint32_t sv = 0;
+        load8(L.in[l], first, n, L.mode[l], v);
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) sv += v[k];
+        uint32_t total;
+        uint32_t ex = block_exclusive_scan<kScanThreads>(sv, &total) + prefix;
+        uint32_t e[kScanItems];
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            e[k] = ex;
+            ex += v[k];
+        }
+        store8(L.out[l], first, n, e);
+        if (blockIdx.x == nb - 1 && threadIdx.x == 0) {
+            L.out[l][n] = prefix + total;
+            if (L.total[l]) *L.total[l] = prefix + total;
+        }
+    }
+}
+
 template <int NL>
 static void launch_scan_lanes(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp,
                               cudaStream_t s) {
     uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
     if (nb == 0) nb = 1;
+    if (nb <= kFusedScanBlocks) {
+        { count_launch(); k_scanm_reduce<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+        { count_launch(); k_scanm_down_fused<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+        return;
+    }
     { count_launch(); k_scanm_reduce<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
     { count_launch(); k_scanm_partials<NL><<<1, 1024, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
     { count_launch(); k_scanm_down<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
