@@ -46,7 +46,9 @@ struct FrameDev {
     PathCtx*  path_bin;          // [P+1] binning context per global path (written after the path scan)
     int32_t*  col_backdrop;      // [col_cap] above-rect column sums
     uint32_t* seg_line_count;    // [seg_count+1] flattened lines per input segment
-    uint32_t* seg_line_base;     // [seg_count+1] exclusive scan
+    uint32_t* seg_line_base;     // [seg_count+1] exclusive scan (uniform dicing)
+    uint32_t* seg_warp_lines;    // [seg_count/32+1] flattened lines per warp of 32 segments
+    uint32_t* seg_warp_base;     // [seg_count/32+2] exclusive scan
     unsigned long long* seg_leaves;  // [seg_count] leaf start slots of each segment's subdivision (0: walked)
     float4*   lines;             // [line_cap] flattened lines in emission order
     uint32_t* line_path;         // [line_cap] global path of each line

@@ -167,7 +167,7 @@ struct PFCUDARenderer {
     DevBuf<int4> tile_rect;
     DevBuf<PathCtx> path_bin;
     DevBuf<uint32_t> tile_offset, col_offset;
-    DevBuf<uint32_t> seg_line_count, seg_line_base;
+    DevBuf<uint32_t> seg_line_count, seg_line_base, seg_warp;
     DevBuf<unsigned long long> seg_leaves;
     DevBuf<float4> lines;
     DevBuf<uint32_t> line_path, line_fill_count, line_fill_base;
@@ -348,6 +348,9 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.col_backdrop = r->col_backdrop.p;
     f.seg_line_count = r->seg_line_count.p;
     f.seg_line_base = r->seg_line_base.p;
+    // two arrays of one value per warp of 32 segments (+ the scan total)
+    f.seg_warp_lines = r->seg_warp.p;
+    f.seg_warp_base = r->seg_warp.p ? r->seg_warp.p + ((size_t)r->S + 31) / 32 + 2 : nullptr;
     f.seg_leaves = r->seg_leaves.p;
     f.lines = r->lines.p;
     f.line_path = r->line_path.p;
@@ -795,7 +798,7 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->segs.release(); r->first_ord.release(); r->paint.release(); r->local_index.release();
     r->scene_of.release(); r->clip_gpath.release(); r->rule.release(); r->is_clip.release();
     r->scenes_dev.release(); r->tile_rect.release(); r->tile_offset.release(); r->col_offset.release();
-    r->seg_line_count.release(); r->seg_line_base.release(); r->lines.release(); r->line_path.release();
+    r->seg_line_count.release(); r->seg_line_base.release(); r->seg_warp.release(); r->lines.release(); r->line_path.release();
     r->seg_leaves.release(); r->path_bin.release();
     r->line_fill_count.release(); r->line_fill_base.release(); r->tile_fill_count.release();
     r->tile_fill_base.release(); r->tile_alpha.release(); r->alpha_owner.release(); r->tile_delta.release();
@@ -1036,7 +1039,8 @@ static int32_t upload_tables(PFCUDARendererRef r, const PFCUDASceneDesc* scenes,
     if (hinfo->segs >= 0x7fffffffull) return PF_CUDA_ERR_INVALID;
     const uint32_t S = (uint32_t)hinfo->segs;
     if ((e = r->segs.ensure((size_t)S + 1)) || (e = r->seg_line_count.ensure((size_t)S + 1)) ||
-        (e = r->seg_line_base.ensure((size_t)S + 1)) || (e = r->seg_leaves.ensure((size_t)S + 1)))
+        (e = r->seg_line_base.ensure((size_t)S + 1)) || (e = r->seg_leaves.ensure((size_t)S + 1)) ||
+        (e = r->seg_warp.ensure(2 * (((size_t)S + 31) / 32 + 2))))
         return cuda_status(e);
     launch_contour_segemit(r->ord_contour.p, r->ord_path.p, &info->nord, cap, r->starts.p, nb, r->flags.p,
                            r->contour_seg_base.p, r->segs.p, s);

@@ -865,19 +865,23 @@ __global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
         w.next[lane] = 0;
         __syncwarp();
     }
-    if (s >= f.seg_count) return;
-    leaves = w.leaves[lane];
-    uint32_t n;
-    if ((w.deep >> lane) & 1u) {
-        n = 0;
-        flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&, uint32_t, int) { n++; },
-                        &f.counters->status);
-        leaves = 0;  // no mask: the emit pass walks the segment
-    } else {
-        n = (uint32_t)__popcll(leaves);
+    uint32_t n = 0;
+    if (s < f.seg_count) {
+        leaves = w.leaves[lane];
+        if ((w.deep >> lane) & 1u) {
+            flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&, uint32_t, int) { n++; },
+                            &f.counters->status);
+            leaves = 0;  // no mask: the emit pass walks the segment
+        } else {
+            n = (uint32_t)__popcll(leaves);
+        }
+        f.seg_line_count[s] = n;
+        f.seg_leaves[s] = leaves;
     }
-    f.seg_line_count[s] = n;
-    f.seg_leaves[s] = leaves;
+    // the warp's lines: the emit pass places the warp's lines after those of
+    // the warps before it (a scan of one value per warp)
+    const uint32_t warp_lines = __reduce_add_sync(0xffffffffu, n);
+    if (lane == 0) f.seg_warp_lines[s0 / 32u] = warp_lines;
 }
 
 // DIFF also records each line's segment and curve-parameter interval: the leaf
@@ -894,22 +898,23 @@ __global__ void __launch_bounds__(256, 8) k_flatten_emit(FrameDev f) {
     }
     if (s0 >= f.seg_count || f.counters->lines > f.line_cap) return;  // whole warps
     const uint32_t s = s0 + lane;
-    uint32_t n = 0, base = 0, path = 0;
+    uint32_t n = 0, path = 0;
     unsigned long long leaves = 0;
     Cubic c{};
+    const uint32_t warp_base = f.seg_warp_base[s0 / 32u];
     if (s < f.seg_count) {
-        // the segment's four reads issued together
+        // the segment's reads issued together
         const SegRec sr = f.segs[f.seg_begin + s];
         n = f.seg_line_count[s];
         const unsigned long long lv = f.seg_leaves[s];
-        const uint32_t b = f.seg_line_base[s];
         if (n) {
             segment_root(f.pts, sr, c, &f.counters->status);
             leaves = lv;
-            base = b;
             path = (uint32_t)sr.w;
         }
     }
+    // the segment's first line: the warp's base plus the lines of its lanes before it
+    const uint32_t base = warp_base + warp_inclusive_scan(n) - n;
     const bool walk = n != 0 && leaves == 0;
     if (n != 0 && leaves > 1ull) roots[wib][lane] = c;  // leaves spread over the warp below
     if (n != 0 && leaves == 1ull) {  // one leaf at level 0: the root's base line, by its own lane
@@ -1008,7 +1013,13 @@ void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     count_launch();
     if (dice) k_dice_count<<<blocks, ft, 0, s>>>(f);
     else k_flatten_count<<<blocks, ft, 0, s>>>(f);
-    launch_scan(f.seg_line_count, f.seg_line_base, nullptr, f.seg_count, f.seg_count, 0, &f.counters->lines, tmp, s);
+    if (dice) {
+        launch_scan(f.seg_line_count, f.seg_line_base, nullptr, f.seg_count, f.seg_count, 0, &f.counters->lines, tmp,
+                    s);
+    } else {  // one value per warp of 32 segments
+        const uint32_t warps = (f.seg_count + 31) / 32;
+        launch_scan(f.seg_warp_lines, f.seg_warp_base, nullptr, warps, warps, 0, &f.counters->lines, tmp, s);
+    }
     count_launch();
     if (dice) k_dice_emit<<<blocks, ft, 0, s>>>(f);
     else if (f.diff) k_flatten_emit<true><<<blocks, ft, 0, s>>>(f);
