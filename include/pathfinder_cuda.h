@@ -404,7 +404,8 @@ int32_t PFCUDAGraphRelease(PFCUDARendererRef renderer);
 typedef struct PFCUDATuning {
     int32_t flatten_threads;     /* 64, 128 or 256 */
     int32_t bin_threads;         /* 128, 256 or 512 */
-    int32_t bin_blocks_per_sm;   /* 4 .. 64 */
+    int32_t bin_blocks_per_sm;   /* 4 .. 64: the count pass's grid (the emit pass runs two waves of
+                                    resident blocks beside propagation and visibility) */
     int32_t composite_warps;     /* 2, 4 or 8 */
     int32_t composite_batch;     /* screen tiles per work item of the persistent composite: 1, 2, 4 or 8 */
 } PFCUDATuning;

@@ -12,6 +12,7 @@
 //   (tiler.rs:191-308, builder.rs:509-616)                 -> k_bin_count, k_bin_emit
 #include "pf_kernels.cuh"
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <vector>
@@ -1132,6 +1133,9 @@ __global__ void __launch_bounds__(512, 3) k_bin_emit(const __grid_constant__ Fra
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     if (f.counters->fills > f.fill_cap) return;
     const uint32_t L = line_total(f);
+    // one sink for all of the thread's lines: a fill's store waits for the
+    // thread's next fill, whichever line it comes from
+    EmitSink<ORDER> sink{&f, 0u};
     for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
         // the line's reads issued together, its fill count tested after
         const uint32_t nfill = f.line_fill_count[l];
@@ -1140,14 +1144,14 @@ __global__ void __launch_bounds__(512, 3) k_bin_emit(const __grid_constant__ Fra
         if (nfill == 0) continue;
         const PathCtx pc = f.path_bin[gp];
         if constexpr (MODE == kFillF32) {
-            EmitSinkF sink{f.fills_f, f.tile_fill_base, f.tile_fill_count, f.fill_cap};
-            dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+            EmitSinkF sinkf{f.fills_f, f.tile_fill_base, f.tile_fill_count, f.fill_cap};
+            dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sinkf, f.dda_limit, &f.counters->status);
         } else {
-            EmitSink<ORDER> sink{&f, ORDER ? f.line_fill_base[l] : 0u};
+            if (ORDER) sink.e = f.line_fill_base[l];
             dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
-            sink.flush();
         }
     }
+    if constexpr (MODE != kFillF32) sink.flush();
 }
 
 // The binning pass's fill conversion for the frame.
@@ -1162,17 +1166,27 @@ void launch_bin_count(const FrameDev& f, cudaStream_t s) {
     else k_bin_count<kFillCpu><<<blocks, f.tune.bin_threads, 0, s>>>(f);
 }
 
+// The emit pass runs beside propagation and visibility: two waves of
+// resident blocks leave those kernels room on the SMs (measured on the 4K
+// frame: 12-16 blocks an SM make the frame 0.006 ms shorter than 32, 4-6
+// longer).
+template <class K>
+static uint32_t emit_blocks(const FrameDev& f, K kernel, int threads) {
+    return f.sms * 2u * (uint32_t)std::max(resident_blocks(kernel, threads), 1);
+}
+
 void launch_bin_emit(const FrameDev& f, cudaStream_t s) {
     count_launch();
-    const uint32_t blocks = f.sms * f.tune.bin_blocks_per_sm;
     const int m = fill_mode(f);
     const int t = f.tune.bin_threads;
     const bool order = f.fill_e != nullptr;
-    if (m == kFillF32) k_bin_emit<kFillF32, false><<<blocks, t, 0, s>>>(f);
-    else if (m == kFillD3D11 && order) k_bin_emit<kFillD3D11, true><<<blocks, t, 0, s>>>(f);
-    else if (m == kFillD3D11) k_bin_emit<kFillD3D11, false><<<blocks, t, 0, s>>>(f);
-    else if (order) k_bin_emit<kFillCpu, true><<<blocks, t, 0, s>>>(f);
-    else k_bin_emit<kFillCpu, false><<<blocks, t, 0, s>>>(f);
+    if (m == kFillF32) k_bin_emit<kFillF32, false><<<emit_blocks(f, k_bin_emit<kFillF32, false>, t), t, 0, s>>>(f);
+    else if (m == kFillD3D11 && order)
+        k_bin_emit<kFillD3D11, true><<<emit_blocks(f, k_bin_emit<kFillD3D11, true>, t), t, 0, s>>>(f);
+    else if (m == kFillD3D11)
+        k_bin_emit<kFillD3D11, false><<<emit_blocks(f, k_bin_emit<kFillD3D11, false>, t), t, 0, s>>>(f);
+    else if (order) k_bin_emit<kFillCpu, true><<<emit_blocks(f, k_bin_emit<kFillCpu, true>, t), t, 0, s>>>(f);
+    else k_bin_emit<kFillCpu, false><<<emit_blocks(f, k_bin_emit<kFillCpu, false>, t), t, 0, s>>>(f);
 }
 
 }  // namespace pf
