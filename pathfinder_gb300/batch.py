@@ -27,7 +27,10 @@ class SceneBatch:
         self.scenes = list(scenes)
         self.targets = targets
         n = len(self.scenes)
-        self._descs = (_abi.PFCUDASceneDesc * n)(*[s.desc() for s in self.scenes])
+        # the array holds copies of the descriptors: the descriptors themselves
+        # stay alive with the batch, with the buffers they point into
+        self._desc_objs = [s.desc() for s in self.scenes]
+        self._descs = (_abi.PFCUDASceneDesc * n)(*self._desc_objs)
         self._targets = None
         if targets is not None:
             if len(targets) != n:

@@ -141,7 +141,6 @@ class Scene:
         self.gradients: list = []  # paint.Gradient: overlays 1..len(gradients)
         self.patterns: list = []   # paint.Pattern: the overlays after the gradients
         self._pending: list = []
-        self._keep: list = []
 
     # --- the reference's mutators -----------------------------------------
     def set_view_box(self, rect: RectF) -> None:
@@ -279,7 +278,9 @@ class Scene:
             dp["overlay"][pat] = ov[pat] - self.PATTERN_OVERLAY_BASE + len(self.gradients) + 1
             keep.append(dp)
             d.draw_paths = dp.ctypes.data
-        self._keep = keep  # the descriptor points into these
+        # the descriptor points into these: it holds them itself, so a
+        # descriptor still in use (a frame in flight) outlives a newer one
+        d._keep = keep
         return d
 
     @property

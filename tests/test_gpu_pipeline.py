@@ -92,3 +92,19 @@ def test_image_copy_equals_direct_host_writes(renderer):
     renderer.render(s, out=direct, width=s.width + 16, height=s.height + 16)
     assert np.array_equal(big, direct)
     assert (big[s.height:, :, :] == 9).all()
+
+
+def test_pipeline_frames_of_scenes_with_paints(renderer):
+    """A scene with gradients and image patterns gets a new descriptor (and
+    new gradient and texel buffers) at every submission: each frame in flight
+    keeps its own alive until it is done."""
+    torch = pytest.importorskip("torch")
+    import bench
+    s = pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=41, scale=0.05)
+    bench.add_paints(s, 41)
+    ref = renderer.render(s)
+    with pf.RenderPipeline(0, depth=3) as p:
+        outs = [torch.empty((s.height, s.width, 4), dtype=torch.uint8).pin_memory().numpy() for _ in range(9)]
+        frames = [p.submit(s, o) for o in outs]
+        for f in frames:
+            assert np.array_equal(f.result(), ref)
