@@ -11,13 +11,16 @@
 //      content/src/outline.rs:1020-1065);
 //   2. a thread per (contour, pass, segment) walks its segment's offset
 //      recursion depth first and counts its points: pieces exactly, the join
-//      before each piece exactly (the previous piece of the first leaf is the
-//      rightmost leaf of the previous segment, found by descending it);
-//      a closing join exactly; a cap as an upper bound (16);
-//   3. the same threads write their points at the scanned offsets;
+//      before each piece after the first exactly, a closing join exactly, a
+//      cap as an upper bound (16); it records the recursion's leaves and its
+//      first and last pieces' points, and the join before each first piece
+//      is counted from those records (the previous item's last piece);
+//   3. the same threads write their points at the scanned offsets,
+//      recomputing only the recorded leaves;
 //   4. a thread per open contour writes its caps, which look back through
 //      the points written so far (add_cap's search for a distinct point);
-//   5. the points are compacted over the unused cap slots.
+//   5. the points are compacted over the unused cap slots (a warp per 32
+//      items, whose output is one contiguous range).
 // The unit is compiled with -fmad=false: single-precision ops round as the
 // reference's SSE lanes do, so the points are bit-identical to the
 // reference's op order (IEEE division and square root).
@@ -346,6 +349,10 @@ struct StrokeDev {
     float2* res_pts;                  // reserved layout
     uint8_t* res_flags;
     uint32_t* status;                 // bit 0: recursion depth bound reached
+    unsigned long long* item_leaves;  // [I] the count pass's leaf slots of the item's recursion (0: not recorded)
+    float4* item_last;                // [I] the last two points of the item's last piece
+    float4* item_first;               // [I] the first piece's next_tangent (its to and from points)
+    float2* item_first_at;            // [I] the first leaf's from point (the join point)
 };
 
 __device__ __forceinline__ bool is_end(const uint8_t* fl, uint32_t i) {
@@ -433,8 +440,22 @@ __device__ __forceinline__ Seg pass_segment(const StrokeDev& d, const ItemRef& r
     return r.backward ? seg_reversed(sg[r.n - 1 - i]) : sg[i];
 }
 
-// One work item: count (sink without storage) or write its points.
-__device__ void stroke_item(const StrokeDev& d, const ItemRef& r, Sink& k, bool* limited) {
+// The count pass records each segment's recursion as leaf start slots on a
+// grid of 2^kStrokeLeafLevels parameter slots (as the flattening does), when
+// every leaf lies at most that deep, the last two points of its last piece
+// and what the join before its first piece needs of it.  The join before an
+// item's first piece needs the previous item's last piece: k_stroke_joins
+// counts it from the records once every item is walked, and the emit pass
+// takes it from the previous item's record; no item descends the previous
+// segment's recursion.  The emit pass recomputes only the recorded leaves
+// (the splits from the root along each leaf's path, then one offset_once)
+// instead of testing every node against the tolerance again.
+constexpr int kStrokeLeafLevels = 6;
+
+// One work item: count (sink without storage; records the item's leaves) or
+// write its points (replaying recorded leaves).
+__device__ void stroke_item(const StrokeDev& d, const ItemRef& r, uint32_t g, Sink& k, bool* limited) {
+    const bool counting = k.pts == nullptr;
     const PFCUDAStrokeStyle st = d.styles[d.contour_outline[r.c]];
     const float radius = st.line_width * 0.5f;
     const bool closed = d.closed[r.c] != 0;
@@ -454,33 +475,83 @@ __device__ void stroke_item(const StrokeDev& d, const ItemRef& r, Sink& k, bool*
     // the first segment of a pass joins with Bevel (offset_forward/backward, :208-230)
     const int join = r.i == 0 ? PF_LINE_JOIN_BEVEL : st.line_join;
     const bool joins = join == PF_LINE_JOIN_MITER || join == PF_LINE_JOIN_ROUND;
+    const unsigned long long replay = counting ? 0ull : d.item_leaves[g];
     V p0{0.0f, 0.0f}, p1{0.0f, 0.0f};
-    if (joins) last_two(edge_leaf(pass_segment(d, r, r.i - 1), -radius, true, limited), &p0, &p1);
+    if (joins && !counting) {
+        // the previous piece: the last piece of the previous item (same pass, segment i - 1)
+        const float4 q = d.item_last[g - 1];
+        p0 = V{q.x, q.y};
+        p1 = V{q.z, q.w};
+    }
+    // Offset::add_to_contour (:256-279) for one leaf `s` with its piece; the
+    // count pass leaves the first join to k_stroke_joins
+    bool first = true;
+    auto add = [&](const Seg& s, const Seg& piece) {
+        const V q3 = piece.base.f, q4 = piece.kind == kKindLine ? piece.base.t : piece.ctrl.f;
+        if (counting && first) {
+            d.item_first[g] = make_float4(q4.x, q4.y, q3.x, q3.y);
+            d.item_first_at[g] = make_float2(s.base.f.x, s.base.f.y);
+        } else if (joins) {
+            add_join(k, p0, p1, -radius, join, st.miter_limit, s.base.f, L{q4, q3});
+        }
+        first = false;
+        k.push_segment(piece);
+        last_two(piece, &p0, &p1);
+    };
+    if (replay) {
+        // the recorded leaves in depth-first order: each recomputed from the root
+        const Seg root = pass_segment(d, r, r.i);
+        for (unsigned long long m = replay; m;) {
+            const uint32_t start = (uint32_t)__ffsll((long long)m) - 1u;
+            m &= m - 1ull;
+            const uint32_t next = m ? (uint32_t)__ffsll((long long)m) - 1u : 64u;
+            const int depth = kStrokeLeafLevels - (31 - __clz((int)(next - start)));
+            const uint32_t addr = start >> (kStrokeLeafLevels - depth);
+            Seg s = root;
+            for (int lv = depth - 1; lv >= 0; lv--) {
+                Seg a, b;
+                seg_split(s, 0.5f, &a, &b);
+                s = ((addr >> lv) & 1u) ? b : a;
+            }
+            // offset_leaf's piece for a leaf above the depth bound: the segment
+            // itself when tiny, else its offset (which the count pass found
+            // within the tolerance)
+            const Seg piece = vsqlen(lvec(s.base)) < kStrokeTolerance * kStrokeTolerance ? s : offset_once(s, -radius);
+            add(s, piece);
+        }
+        return;
+    }
     // depth-first walk of the offset recursion (Offset::offset, :238-254)
     Seg stack[kStrokeMaxDepth + 2];
     int depth_of[kStrokeMaxDepth + 2];
+    uint32_t addr_of[kStrokeMaxDepth + 2];
     int sp = 0;
     stack[sp] = pass_segment(d, r, r.i);
-    depth_of[sp++] = 0;
+    depth_of[sp] = 0;
+    addr_of[sp++] = 0;
     uint32_t pieces = 0;  // at most kMaxStrokePieces per segment, then the walk stops
+    unsigned long long leaves = 0;
+    bool recordable = true;
     while (sp > 0) {
         const Seg s = stack[--sp];
         const int depth = depth_of[sp];
+        const uint32_t addr = addr_of[sp];
         Seg piece;
         if (!offset_leaf(s, -radius, depth, &piece, limited)) {
             Seg a, b;
             seg_split(s, 0.5f, &a, &b);
-            stack[sp] = b; depth_of[sp++] = depth + 1;
-            stack[sp] = a; depth_of[sp++] = depth + 1;
+            stack[sp] = b; depth_of[sp] = depth + 1; addr_of[sp++] = 2u * addr + 1u;
+            stack[sp] = a; depth_of[sp] = depth + 1; addr_of[sp++] = 2u * addr;
             continue;
         }
-        if (joins) {  // Offset::add_to_contour (:256-279)
-            const V q3 = piece.base.f, q4 = piece.kind == kKindLine ? piece.base.t : piece.ctrl.f;
-            add_join(k, p0, p1, -radius, join, st.miter_limit, s.base.f, L{q4, q3});
-        }
-        k.push_segment(piece);
-        last_two(piece, &p0, &p1);
-        if (++pieces >= kMaxStrokePieces) { *limited = true; break; }
+        if (depth <= kStrokeLeafLevels) leaves |= 1ull << (addr << (kStrokeLeafLevels - depth));
+        else recordable = false;
+        add(s, piece);
+        if (++pieces >= kMaxStrokePieces) { *limited = true; recordable = false; break; }
+    }
+    if (counting) {
+        d.item_leaves[g] = recordable ? leaves : 0ull;
+        d.item_last[g] = make_float4(p0.x, p0.y, p1.x, p1.y);
     }
 }
 
@@ -488,9 +559,26 @@ __global__ void k_stroke_count(StrokeDev d, uint32_t items) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < items; g += gridDim.x * blockDim.x) {
         bool limited = false;
         Sink k{nullptr, nullptr, 0};
-        stroke_item(d, item_ref(d, g), k, &limited);
+        stroke_item(d, item_ref(d, g), g, k, &limited);
         d.item_cnt[g] = k.n;
         if (limited) atomicOr(d.status, 1u);
+    }
+}
+
+// The join before each item's first piece (count pass): from the previous
+// item's last piece and the item's first, as recorded.
+__global__ void k_stroke_joins(StrokeDev d, uint32_t items) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < items; g += gridDim.x * blockDim.x) {
+        const ItemRef r = item_ref(d, g);
+        if (r.tail || r.i == 0) continue;  // tails count their own joins; a pass's first segment joins with Bevel
+        const PFCUDAStrokeStyle st = d.styles[d.contour_outline[r.c]];
+        if (st.line_join != PF_LINE_JOIN_MITER && st.line_join != PF_LINE_JOIN_ROUND) continue;
+        const float4 last = d.item_last[g - 1], nt = d.item_first[g];
+        const float2 at = d.item_first_at[g];
+        Sink k{nullptr, nullptr, 0};
+        add_join(k, V{last.x, last.y}, V{last.z, last.w}, -(st.line_width * 0.5f), st.line_join, st.miter_limit,
+                 V{at.x, at.y}, L{V{nt.x, nt.y}, V{nt.z, nt.w}});
+        d.item_cnt[g] += k.n;
     }
 }
 
@@ -501,7 +589,7 @@ __global__ void k_stroke_emit(StrokeDev d, uint32_t items) {
         if (r.tail && d.closed[r.c] == 0) continue;  // caps: k_stroke_caps
         bool limited = false;
         Sink k{d.res_pts + off, d.res_flags + off, 0};
-        stroke_item(d, r, k, &limited);
+        stroke_item(d, r, g, k, &limited);
         d.actual[g] = reserved;
     }
 }
@@ -558,12 +646,31 @@ __global__ void k_stroke_caps(StrokeDev d) {
 }
 
 // Gather every item's written points to their final places.
+// A warp per 32 items: their output points are one contiguous range, which
+// the lanes copy in order (each point's item found among the warp's 32 by a
+// search over their output offsets), so the stores coalesce.
 __global__ void k_stroke_compact(StrokeDev d, uint32_t items, float2* out_pts, uint8_t* out_flags) {
-    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < items; g += gridDim.x * blockDim.x) {
-        const uint32_t src = d.item_off[g], dst = d.final_off[g], n = d.final_off[g + 1] - dst;
-        for (uint32_t i = 0; i < n; i++) {
-            out_pts[dst + i] = d.res_pts[src + i];
-            out_flags[dst + i] = d.res_flags[src + i];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t g0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; g0 < items; g0 += warps * 32u) {
+        const uint32_t g = g0 + lane;
+        const uint32_t last = min(g0 + 32u, items);  // the range ends at the first item past the warp's
+        const uint32_t dst = g < items ? d.final_off[g] : d.final_off[last];
+        const uint32_t src = g < items ? d.item_off[g] : 0u;
+        const uint32_t begin = __shfl_sync(0xffffffffu, dst, 0), end = d.final_off[last];
+        for (uint32_t o0 = begin; o0 < end; o0 += 32u) {  // warp-uniform: every lane shuffles
+            const uint32_t o = o0 + lane;
+            uint32_t j = 0;  // the last lane whose output starts at or before o
+#pragma unroll
+            for (uint32_t step = 16; step > 0; step >>= 1) {
+                const uint32_t v = __shfl_sync(0xffffffffu, dst, (int)(j + step));
+                if (v <= o) j += step;
+            }
+            const uint32_t from = __shfl_sync(0xffffffffu, src, (int)j) + (o - __shfl_sync(0xffffffffu, dst, (int)j));
+            if (o < end) {
+                out_pts[o] = d.res_pts[from];
+                out_flags[o] = d.res_flags[from];
+            }
         }
     }
 }
@@ -621,6 +728,9 @@ struct StrokeWork {
         out_cstarts, status, partials;
     SBuf<PFCUDAStrokeStyle> styles;
     SBuf<Seg> segs;
+    SBuf<unsigned long long> item_leaves;
+    SBuf<float4> item_last, item_first;
+    SBuf<float2> item_first_at;
 };
 
 StrokeWork* stroke_work_create() { return new StrokeWork(); }
@@ -632,6 +742,7 @@ void stroke_work_destroy(StrokeWork* w) {
     w->cnt.release(); w->nseg.release(); w->item_base.release(); w->item_cnt.release(); w->item_off.release();
     w->actual.release(); w->final_off.release(); w->cbase.release(); w->out_cstarts.release();
     w->status.release(); w->partials.release(); w->styles.release(); w->segs.release();
+    w->item_leaves.release(); w->item_last.release(); w->item_first.release(); w->item_first_at.release();
     delete w;
 }
 
@@ -730,13 +841,22 @@ int32_t stroke_run(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, P
     PF_STROKE_TRY(w->item_off.ensure(I + 1));
     PF_STROKE_TRY(w->actual.ensure(I + 1));
     PF_STROKE_TRY(w->final_off.ensure(I + 1));
+    PF_STROKE_TRY(w->item_leaves.ensure(I + 1));
+    PF_STROKE_TRY(w->item_last.ensure(I + 1));
+    PF_STROKE_TRY(w->item_first.ensure(I + 1));
+    PF_STROKE_TRY(w->item_first_at.ensure(I + 1));
     PF_STROKE_TRY(w->partials.ensure((size_t)(I > C ? I : C) / 2048 + 2));
     tmp = ScanTemp{w->partials.p, (uint32_t)w->partials.cap};
     d.item_cnt = w->item_cnt.p;
     d.item_off = w->item_off.p;
     d.actual = w->actual.p;
     d.final_off = w->final_off.p;
+    d.item_leaves = w->item_leaves.p;
+    d.item_last = w->item_last.p;
+    d.item_first = w->item_first.p;
+    d.item_first_at = w->item_first_at.p;
     if (I) { count_launch(); k_stroke_count<<<grid_for(I), 256, 0, s>>>(d, I); }
+    if (I) { count_launch(); k_stroke_joins<<<grid_for(I), 256, 0, s>>>(d, I); }
     launch_scan(w->item_cnt.p, w->item_off.p, nullptr, I, I, 0, nullptr, tmp, s);
     uint32_t R = 0;
     PF_STROKE_TRY(cudaMemcpyAsync(&R, w->item_off.p + I, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
