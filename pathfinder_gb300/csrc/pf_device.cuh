@@ -311,7 +311,10 @@ enum FillMode : int {
 // sink.fill(rec, g) for every kept fill in emission order and
 // sink.backdrop(tx, ty, delta) for every backdrop adjustment.  kFillF32
 // fills reach sink.fill as float4, the others as packed LineSegmentU16.
-template <int MODE = kFillCpu, class Sink>
+// ONE_TILE: a line within one tile takes a short path without the walk's
+// divisions (the count pass gains from it; in the emit pass the two paths'
+// divergence costs more than the divisions).
+template <int MODE = kFillCpu, bool ONE_TILE = false, class Sink>
 __device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink, uint32_t dda_limit,
                                          uint32_t* status) {
     if (MODE != kFillD3D11 && !clip_to_view(seg, pc.vminx, pc.vmaxx, pc.vmaxy)) return;
@@ -319,6 +322,25 @@ __device__ __forceinline__ void dda_line(const PathCtx& pc, Line seg, Sink& sink
     int32_t ftx = cvt_rne(floorf(fmul(seg.fx, r))), fty = cvt_rne(floorf(fmul(seg.fy, r)));
     int32_t ttx = cvt_rne(floorf(fmul(seg.tx, r))), tty = cvt_rne(floorf(fmul(seg.ty, r)));
     float vx = fsub(seg.tx, seg.fx), vy = fsub(seg.ty, seg.fy);
+    if (ONE_TILE && ftx == ttx && fty == tty && dda_limit > 0) {
+        // One tile: the walk's single step.  Its next_t is min(t_max, 1) = 1
+        // (the line ends before the next tile boundary in x and in y, so both
+        // t_max are at least 1), it stops there (dir 0) with no y piece and no
+        // backdrop: one fill from the start to start + v.
+        const Line l{seg.fx, seg.fy, fadd(seg.fx, fmul(vx, 1.0f)), fadd(seg.fy, fmul(vy, 1.0f))};
+        uint32_t g;
+        if constexpr (MODE == kFillF32) {
+            float4 rec;
+            if (make_fill_f(pc, l, ftx, fty, rec, g)) sink.fill(rec, g);
+        } else if constexpr (MODE == kFillD3D11) {
+            uint2 rec;
+            if (make_fill_d3d11(pc, l, ftx, fty, rec, g)) sink.fill(rec, g);
+        } else {
+            uint2 rec;
+            if (make_fill(pc, l, ftx, fty, rec, g)) sink.fill(rec, g);
+        }
+        return;
+    }
     bool negx = vx < 0.0f, negy = vy < 0.0f;
     int32_t stepx = negx ? -1 : 1, stepy = negy ? -1 : 1;
     float fcx = fmul(i2f(ftx + (negx ? 0 : 1)), 16.0f), fcy = fmul(i2f(fty + (negy ? 0 : 1)), 16.0f);

@@ -1066,7 +1066,7 @@ __global__ void __launch_bounds__(512, 3) k_bin_count(FrameDev f) {
         const float4 ln = f.lines[l];
         const PathCtx pc = f.path_bin[f.line_path[l]];
         CountSink sink{&pc, f.tile_fill_count, f.tile_delta, f.col_backdrop, 0};
-        dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
+        dda_line<MODE, true>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
         f.line_fill_count[l] = sink.n;
     }
 }
