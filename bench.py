@@ -665,7 +665,7 @@ def run_fit(args) -> None:
 
 
 def side_workloads(args) -> dict:
-    """The other spec targets, measured in the same run: the batched
+    """The path's other targets, measured in the same run: the batched
     16,384-glyph atlas against per-glyph frames (speed-up and identical
     output) and the differentiable frame's forward + adjoint against the
     plain forward."""
