@@ -573,7 +573,9 @@ typedef struct PFCUDAPipeline* PFCUDAPipelineRef;
 int32_t PFCUDAPipelineCreate(int32_t device_ordinal, int32_t depth,
                              const PFCUDARendererOptions* options,
                              PFCUDAPipelineRef* out_pipeline);
-/* Waits for every submitted frame, then frees the renderers and threads. */
+/* Waits for every submitted frame, then frees the renderers and threads.  No
+ * other call on the pipeline may be in progress or follow; statuses not yet
+ * waited for are dropped. */
 int32_t PFCUDAPipelineDestroy(PFCUDAPipelineRef pipeline);
 /* Queues one frame: PFCUDASceneUpload of `scene` on the next free renderer,
  * then PFCUDARenderScene(options, width, height, out_rgba8, out_memory)
