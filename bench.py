@@ -148,6 +148,22 @@ def stage_bytes(st, npts: int, nseg: int) -> dict:
     }
 
 
+def job_totals(dist, segments: float, times_ms):
+    """Whole-job figures of replica ranks: the input segments summed over the
+    ranks (each renders its own scene) and each time the maximum over the
+    ranks (the job ends with its slowest rank).  With no process group, this
+    rank's own figures."""
+    if dist is None:
+        return float(segments), [float(t) for t in times_ms]
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    s = torch.tensor([float(segments)], dtype=torch.float64, device=dev)
+    t = torch.tensor([float(v) for v in times_ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(s, op=dist.ReduceOp.SUM)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(s.item()), [float(v) for v in t.tolist()]
+
+
 def svg_config(scene, args, paints, world: int = 1) -> dict:
     """The `config` of a 4K-scene line, the same in both arms."""
     return {"workload": (WORKLOAD if args.scale == 1.0 else f"{WORKLOAD}_scale{args.scale}")
@@ -166,6 +182,7 @@ def run_reference(args) -> None:
     oracle's library (which carries its own copy of the scene generator), not
     the CUDA renderer."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
     import pathfinder_gb300 as pf
@@ -188,7 +205,7 @@ def run_reference(args) -> None:
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded PF_SCENE_SVG_4K: 20,000 log-normal star paths, 40/30/30 line/quad/cubic)",
-        "config": svg_config(scene, args, paints),
+        "config": svg_config(scene, args, paints, world),
         "cpu_baseline": {"value": round(value, 4), "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} full frames of the 4K scene (tiling + FP32 coverage + composite)"},
         "e2e": {"value": round(value, 4), "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -818,11 +835,8 @@ def main():
         raise RuntimeError(f"render failed with status {code}")
     st = r.stats()
     ms_enqueued = sum(a.elapsed_time(b) for a, b in evs2) / args.steps
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * nseg / (ms / 1e3) / 1e6
+    job_seg, (ms,) = job_totals(dist, nseg, [ms])
+    value = job_seg / (ms / 1e3) / 1e6
 
     # roofline of the dominant stage
     stage_ms = {n: v / args.steps for n, v in stage_sum.items()}
@@ -881,11 +895,8 @@ def main():
         f.result()
     e2e_ms = 1e3 * (time.perf_counter() - t0) / e2e_steps
     pipe.close()
-    if dist:
-        t = torch.tensor([e2e_ms, serial_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms, serial_ms = (float(v) for v in t.tolist())
-    e2e_value = world * nseg / (e2e_ms / 1e3) / 1e6
+    _, (e2e_ms, serial_ms) = job_totals(dist, nseg, [e2e_ms, serial_ms])
+    e2e_value = job_seg / (e2e_ms / 1e3) / 1e6
 
     if rank == 0:
         line = {
@@ -916,7 +927,7 @@ def main():
                             "step uploads the scene from pinned host memory and copies its RGBA8 image to "
                             "pinned host memory (one device-to-host copy after the composite)",
                     "serial_ms_per_step": round(serial_ms, 3),
-                    "serial_value": round(world * nseg / (serial_ms / 1e3) / 1e6, 4)},
+                    "serial_value": round(job_seg / (serial_ms / 1e3) / 1e6, 4)},
             "gpu_launches": int(st.kernel_launches * args.steps),
             "clocks": {**clocks, "window": f"{soak} untimed replays (~{args.clock_soak:.1f} s) then the timed steps"},
         }
