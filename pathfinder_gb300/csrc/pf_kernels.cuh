@@ -29,6 +29,7 @@ struct FrameDev {
     uint32_t seg_begin, seg_count;
     PathDev path;
     const SceneDev* scenes;
+    const uint32_t* scene_st;    // [scenes] each scene's first global screen tile
     uint32_t path_begin, path_count;
     uint32_t scene_begin, scene_count;
     uint32_t screen_begin;       // global index of the range's first screen tile
@@ -140,7 +141,7 @@ __device__ __forceinline__ uint32_t scene_of_screen_tile(const FrameDev& f, uint
     uint32_t lo = f.scene_begin, hi = f.scene_begin + f.scene_count;
     while (hi - lo > 1) {
         uint32_t mid = (lo + hi) >> 1;
-        if (f.scenes[mid].screen_offset <= st_global) lo = mid; else hi = mid;
+        if (f.scene_st[mid] <= st_global) lo = mid; else hi = mid;
     }
     return lo;
 }

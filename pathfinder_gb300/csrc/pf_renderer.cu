@@ -162,6 +162,8 @@ struct PFCUDARenderer {
     DevBuf<OverlayDev> overlays;
     DevBuf<SceneDev> scenes_dev;
     std::vector<SceneDev> scenes_host;
+    DevBuf<uint32_t> scene_st;             // each scene's first global screen tile
+    std::vector<uint32_t> scene_st_host;
 
     // per-frame buffers
     DevBuf<int4> tile_rect;
@@ -326,6 +328,7 @@ FrameDev frame_dev(PFCUDARenderer* r, bool transformed, const Range& g, bool dif
     f.path.tile_offset = r->tile_offset.p;
     f.path.col_offset = r->col_offset.p;
     f.scenes = r->scenes_dev.p;
+    f.scene_st = r->scene_st.p;
     f.path_begin = g.p0;
     f.path_count = g.p1 - g.p0;
     f.scene_begin = g.s0;
@@ -569,7 +572,15 @@ void record_stats(PFCUDARenderer* r, const Counters& h, float ms) {
 }
 
 cudaError_t upload_scene_records(PFCUDARenderer* r) {
-    return cudaMemcpyAsync(r->scenes_dev.p, r->scenes_host.data(), sizeof(SceneDev) * r->scenes_host.size(),
+    cudaError_t e = cudaMemcpyAsync(r->scenes_dev.p, r->scenes_host.data(), sizeof(SceneDev) * r->scenes_host.size(),
+                                    cudaMemcpyHostToDevice, r->stream);
+    if (e) return e;
+    // each scene's first screen tile, packed: the composite's screen-tile ->
+    // scene search reads these 4-byte words instead of the scene records
+    r->scene_st_host.resize(r->scenes_host.size());
+    for (size_t k = 0; k < r->scenes_host.size(); k++) r->scene_st_host[k] = r->scenes_host[k].screen_offset;
+    if ((e = r->scene_st.ensure(r->scene_st_host.size() + 1))) return e;
+    return cudaMemcpyAsync(r->scene_st.p, r->scene_st_host.data(), sizeof(uint32_t) * r->scene_st_host.size(),
                            cudaMemcpyHostToDevice, r->stream);
 }
 
@@ -797,7 +808,7 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
     r->ord_contour.release(); r->ord_path.release(); r->contour_segs.release(); r->contour_seg_base.release();
     r->segs.release(); r->first_ord.release(); r->paint.release(); r->local_index.release();
     r->scene_of.release(); r->clip_gpath.release(); r->rule.release(); r->is_clip.release();
-    r->scenes_dev.release(); r->tile_rect.release(); r->tile_offset.release(); r->col_offset.release();
+    r->scenes_dev.release(); r->scene_st.release(); r->tile_rect.release(); r->tile_offset.release(); r->col_offset.release();
     r->seg_line_count.release(); r->seg_line_base.release(); r->seg_warp.release(); r->lines.release(); r->line_path.release();
     r->seg_leaves.release(); r->path_bin.release();
     r->line_fill_count.release(); r->line_fill_base.release(); r->tile_fill_count.release();
