@@ -559,6 +559,59 @@ typedef struct PFCUDAStrokeOutput {
 /* Synchronous on the renderer's stream. */
 int32_t PFCUDAStrokeToFill(PFCUDARendererRef renderer, const PFCUDAStrokeInput* input, PFCUDAStrokeOutput* output);
 
+/* ---- dashes: OutlineDash (content/src/dash.rs:18-152) ------------------------
+ * Outline o is dashed with the pattern dashes[dash_starts[o] .. dash_starts[o+1])
+ * (alternating "on" and "off" lengths, used as given: the canvas front-end's
+ * doubling of an odd-length pattern, canvas/src/lib.rs:253-262, is the
+ * caller's) and the phase offsets[o].  The reference's walk, op for op: the
+ * offset is reduced modulo the pattern's sum and the whole dashes it covers
+ * are skipped (DashState::new), then each segment of each contour (closing
+ * segments included) is cut where the distance left in the current dash runs
+ * out, distances being chord lengths (Segment::arc_length /
+ * time_for_distance, content/src/segment.rs:246-254); the pieces of an "on"
+ * dash form one open contour, which continues across the outline's contours.
+ * An outline with an empty pattern is passed through unchanged (the
+ * front-ends only dash a non-empty pattern, canvas/src/lib.rs:340,
+ * svg/src/lib.rs:159).  A pattern must hold finite non-negative lengths with a
+ * positive finite sum, and its offset must be finite (PF_CUDA_ERR_INVALID
+ * otherwise).  An outline whose walk takes more than 2^20 steps (a cut or a
+ * whole segment each) is cut short there and the call returns
+ * PF_CUDA_ERR_LIMIT with the output complete up to that point.  One GPU thread
+ * walks one outline: the distance left carries from segment to segment in
+ * single precision, so the outlines are the parallel unit.  Arrays in the
+ * stroke input's memory. */
+typedef struct PFCUDADashInput {
+    const float*    dashes;             /* dash_starts[outline_count] lengths */
+    const uint32_t* dash_starts;        /* outline_count + 1 */
+    const float*    offsets;            /* outline_count */
+} PFCUDADashInput;
+
+/* Outlines as flat buffers (in `memory`) with each contour's closed flag: the
+ * layout of PFCUDAStrokeInput, so a dashed result can be stroked as it is.
+ * Sizes and capacity as in PFCUDAStrokeOutput. */
+typedef struct PFCUDAOutlineOutput {
+    PFVector2F* points;
+    uint8_t*    point_flags;
+    uint32_t*   contour_starts;         /* contour_capacity + 1 */
+    uint8_t*    contour_closed;         /* contour_capacity */
+    uint32_t*   outline_starts;         /* outline_count + 1 */
+    uint64_t    point_capacity, contour_capacity;
+    uint64_t    point_count, contour_count;
+    int32_t     memory;
+} PFCUDAOutlineOutput;
+
+/* OutlineDash::dash + into_outline for every outline of `input` (its styles
+ * are not read and may be NULL).  Synchronous on the renderer's stream. */
+int32_t PFCUDADashOutlines(PFCUDARendererRef renderer, const PFCUDAStrokeInput* input, const PFCUDADashInput* dash,
+                           PFCUDAOutlineOutput* output);
+
+/* The front-ends' stroke of a dashed outline (svg/src/lib.rs:159-167,
+ * canvas/src/lib.rs:340-350): dashes, then OutlineStrokeToFill of the dashed
+ * outlines with input->styles, both on the device with no copy between them.
+ * Output as PFCUDAStrokeToFill's; PF_CUDA_ERR_LIMIT from either stage. */
+int32_t PFCUDAStrokeToFillDashed(PFCUDARendererRef renderer, const PFCUDAStrokeInput* input,
+                                 const PFCUDADashInput* dash, PFCUDAStrokeOutput* output);
+
 /* Human-readable text for a status code (static storage). */
 const char* PFCUDAStatusString(int32_t status);
 

@@ -289,6 +289,34 @@ def fill_coverage(seg) -> np.ndarray:
     return m
 
 
+def dash(stroke_input, dash_input):
+    """The oracle's OutlineDash of a host-memory PFCUDAStrokeInput with a
+    host-memory PFCUDADashInput: (points (N, 2) float32, flags (N,) uint8,
+    contour_starts, contour_closed, outline_starts, step_limit_hit)."""
+    L = lib()
+    L.pfo_dash.restype = C.c_void_p
+    L.pfo_dash.argtypes = [C.c_void_p, C.c_void_p]
+    L.pfo_dash_counts.argtypes = [C.c_void_p, C.c_void_p]
+    L.pfo_dash_read.argtypes = [C.c_void_p] * 6
+    L.pfo_dash_free.argtypes = [C.c_void_p]
+    h = L.pfo_dash(C.byref(stroke_input), C.byref(dash_input))
+    if not h:
+        raise ValueError("oracle rejected the dash input")
+    try:
+        n = np.zeros((3,), np.uint64)
+        L.pfo_dash_counts(h, n.ctypes.data)
+        npts, nc = int(n[0]), int(n[1])
+        pts = np.zeros((npts, 2), np.float32)
+        flags = np.zeros((npts,), np.uint8)
+        cs = np.zeros((nc + 1,), np.uint32)
+        closed = np.zeros((nc,), np.uint8)
+        os_ = np.zeros((stroke_input.outline_count + 1,), np.uint32)
+        L.pfo_dash_read(h, pts.ctypes.data, flags.ctypes.data, cs.ctypes.data, closed.ctypes.data, os_.ctypes.data)
+        return pts, flags, cs, closed, os_, bool(n[2])
+    finally:
+        L.pfo_dash_free(h)
+
+
 def area_lut_value(u: int, v: int, k: int) -> int:
     """The reference LUT texel (u, v) channel k, computed in f32 by the oracle."""
     return int(lib().pfo_area_lut_value(u, v, k))

@@ -8,8 +8,10 @@
 // UnitVector rotations (geometry/src/unit_vector.rs), Transform2F products
 // (geometry/src/transform2d.rs), Contour::push_segment and
 // push_arc_from_unit_chord (content/src/outline.rs:560-669) and ContourIter
-// (outline.rs:1020-1065).  Single precision in the reference's op order,
-// built with -ffp-contract=off; the checker of the CUDA stroker.
+// (outline.rs:1020-1065); and the dashing pass before it, OutlineDash
+// (content/src/dash.rs:18-152).  Single precision in the reference's op
+// order, built with -ffp-contract=off; the checker of the CUDA stroker and
+// dasher.
 #include "../include/pathfinder_cuda.h"
 
 #include <cmath>
@@ -433,9 +435,160 @@ void stroke_contour(StrokeResult& r, const Style& st, const PFVector2F* pts, con
     push_stroked_contour(r, k, closed, first);
 }
 
+// ---- OutlineDash (content/src/dash.rs:18-152) --------------------------------
+constexpr float kDashEpsilon = 0.0001f;       // dash.rs:16
+constexpr uint32_t kMaxDashSteps = 1u << 20;  // the CUDA library's step bound per outline
+
+struct DashResult {
+    std::vector<PFVector2F> pts;
+    std::vector<uint8_t> flags;
+    std::vector<uint32_t> contour_starts{0};
+    std::vector<uint8_t> closed;
+    std::vector<uint32_t> outline_starts{0};
+    bool limited = false;
+};
+
+// Contour::push_segment (content/src/outline.rs:576-600) onto the open dash contour
+void push_dash_segment(std::vector<PFVector2F>& c, std::vector<uint8_t>& f, const Seg& s) {
+    c.push_back(PFVector2F{s.base.f.x, s.base.f.y});
+    f.push_back(0);
+    if (s.kind != kLine) {
+        c.push_back(PFVector2F{s.ctrl.f.x, s.ctrl.f.y});
+        f.push_back(PF_POINT_FLAG_CONTROL_POINT_0);
+        if (s.kind != kQuad) {
+            c.push_back(PFVector2F{s.ctrl.t.x, s.ctrl.t.y});
+            f.push_back(PF_POINT_FLAG_CONTROL_POINT_1);
+        }
+    }
+    c.push_back(PFVector2F{s.base.t.x, s.base.t.y});
+    f.push_back(0);
+}
+
+// OutlineDash::new + dash + into_outline for one outline: DashState::new
+// (:124-145), ContourDash::dash (:73-113), is_on (:147-150), into_outline
+// (:52-57); arc_length and time_for_distance are the chord's
+// (content/src/segment.rs:246-254).
+void dash_outline(DashResult& r, const PFCUDAStrokeInput* in, uint32_t o, const float* dashes, uint32_t nd,
+                  float offset0) {
+    std::vector<PFVector2F> cur_pts;
+    std::vector<uint8_t> cur_flags;
+    auto push_contour = [&]() {  // Outline::push_contour drops an empty contour (outline.rs:180-192)
+        if (cur_pts.empty()) return;
+        r.pts.insert(r.pts.end(), cur_pts.begin(), cur_pts.end());
+        r.flags.insert(r.flags.end(), cur_flags.begin(), cur_flags.end());
+        r.contour_starts.push_back((uint32_t)r.pts.size());
+        r.closed.push_back(0);
+        cur_pts.clear();
+        cur_flags.clear();
+    };
+    float total = 0.0f;
+    for (uint32_t i = 0; i < nd; i++) total += dashes[i];
+    float offset = std::fmod(offset0, total);
+    uint32_t idx = 0;
+    while (idx < nd) {
+        if (offset < dashes[idx]) break;
+        offset -= dashes[idx];
+        idx++;
+    }
+    float left = offset;
+    uint32_t steps = 0;
+    bool limited = false;
+    for (uint32_t c = in->outline_starts[o]; c < in->outline_starts[o + 1] && !limited; c++) {
+        const uint32_t a = in->contour_starts[c], b = in->contour_starts[c + 1];
+        const std::vector<Seg> segs = contour_segments(in->points + a, in->point_flags + a, b - a,
+                                                       in->contour_closed[c] != 0);
+        size_t next = 0;
+        Seg queued{};
+        bool have = false;
+        for (;;) {
+            if (!have) {
+                if (next == segs.size()) break;
+                queued = segs[next++];
+            }
+            if (steps++ == kMaxDashSteps) { limited = true; break; }
+            Seg cur = queued;
+            have = false;
+            float distance = left;
+            const float t = distance / std::sqrt(vsqlen(lvec(cur.base)));
+            if (t < 1.0f) {
+                Seg a0, b0;
+                seg_split(cur, t, &a0, &b0);
+                cur = a0;
+                queued = b0;
+                have = true;
+            } else {
+                distance = std::sqrt(vsqlen(lvec(cur.base)));
+            }
+            const bool on = idx % 2 == 0;
+            if (on) push_dash_segment(cur_pts, cur_flags, cur);
+            left -= distance;
+            if (left < kDashEpsilon) {
+                if (on) push_contour();
+                idx++;
+                if (idx >= nd) idx = 0;  // the reference compares with ==; >= also wraps an offset past the end
+                left = dashes[idx];
+            }
+        }
+    }
+    if (idx % 2 == 0) push_contour();
+    r.limited = r.limited || limited;
+}
+
 }  // namespace
 
 extern "C" {
+
+// Dashes every outline of `in` (host memory) with the patterns of `dash`
+// (an outline with an empty pattern is copied); returns a handle, or NULL for
+// invalid input.
+void* pfo_dash(const PFCUDAStrokeInput* in, const PFCUDADashInput* dash) {
+    if (!in || !dash || in->memory != PF_MEMORY_HOST || !dash->dash_starts) return nullptr;
+    if (in->outline_count && (!in->outline_starts || !dash->offsets)) return nullptr;
+    if (in->contour_count && (!in->contour_starts || !in->contour_closed)) return nullptr;
+    if (in->point_count && (!in->points || !in->point_flags)) return nullptr;
+    DashResult* r = new DashResult();
+    for (uint32_t o = 0; o < in->outline_count; o++) {
+        const uint32_t c0 = in->outline_starts[o], c1 = in->outline_starts[o + 1];
+        const uint32_t d0 = dash->dash_starts[o], d1 = dash->dash_starts[o + 1];
+        if (c0 > c1 || c1 > in->contour_count || d0 > d1) { delete r; return nullptr; }
+        for (uint32_t c = c0; c < c1; c++) {
+            const uint32_t a = in->contour_starts[c], b = in->contour_starts[c + 1];
+            if (a > b || b > in->point_count) { delete r; return nullptr; }
+        }
+        if (d0 == d1) {
+            for (uint32_t c = c0; c < c1; c++) {
+                const uint32_t a = in->contour_starts[c], b = in->contour_starts[c + 1];
+                r->pts.insert(r->pts.end(), in->points + a, in->points + b);
+                r->flags.insert(r->flags.end(), in->point_flags + a, in->point_flags + b);
+                r->contour_starts.push_back((uint32_t)r->pts.size());
+                r->closed.push_back(in->contour_closed[c] != 0 ? 1 : 0);
+            }
+        } else {
+            dash_outline(*r, in, o, dash->dashes + d0, d1 - d0, dash->offsets[o]);
+        }
+        r->outline_starts.push_back((uint32_t)(r->contour_starts.size() - 1));
+    }
+    return r;
+}
+
+void pfo_dash_counts(void* h, uint64_t* out3) {
+    const DashResult* r = (const DashResult*)h;
+    out3[0] = r->pts.size();
+    out3[1] = r->contour_starts.size() - 1;
+    out3[2] = r->limited ? 1 : 0;
+}
+
+void pfo_dash_read(void* h, PFVector2F* pts, uint8_t* flags, uint32_t* contour_starts, uint8_t* closed,
+                   uint32_t* outline_starts) {
+    const DashResult* r = (const DashResult*)h;
+    if (pts && !r->pts.empty()) std::memcpy(pts, r->pts.data(), r->pts.size() * sizeof(PFVector2F));
+    if (flags && !r->flags.empty()) std::memcpy(flags, r->flags.data(), r->flags.size());
+    if (contour_starts) std::memcpy(contour_starts, r->contour_starts.data(), r->contour_starts.size() * 4);
+    if (closed && !r->closed.empty()) std::memcpy(closed, r->closed.data(), r->closed.size());
+    if (outline_starts) std::memcpy(outline_starts, r->outline_starts.data(), r->outline_starts.size() * 4);
+}
+
+void pfo_dash_free(void* h) { delete (DashResult*)h; }
 
 // Strokes every outline of `in` (host memory); returns a handle, or NULL for
 // invalid input.

@@ -144,6 +144,17 @@ class PFCUDAStrokeOutput(C.Structure):
                 ("memory", C.c_int32)]
 
 
+class PFCUDADashInput(C.Structure):
+    _fields_ = [("dashes", C.c_void_p), ("dash_starts", C.c_void_p), ("offsets", C.c_void_p)]
+
+
+class PFCUDAOutlineOutput(C.Structure):
+    _fields_ = [("points", C.c_void_p), ("point_flags", C.c_void_p), ("contour_starts", C.c_void_p),
+                ("contour_closed", C.c_void_p), ("outline_starts", C.c_void_p), ("point_capacity", C.c_uint64),
+                ("contour_capacity", C.c_uint64), ("point_count", C.c_uint64), ("contour_count", C.c_uint64),
+                ("memory", C.c_int32)]
+
+
 class PFCUDABuildOptions(C.Structure):
     _fields_ = [("transform", PFTransform2F), ("has_transform", C.c_int32)]
 
@@ -213,6 +224,10 @@ def record_dtypes():
 
 _SIGS = {
     "PFCUDAStrokeToFill": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDAStrokeInput), C.POINTER(PFCUDAStrokeOutput)]),
+    "PFCUDADashOutlines": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDAStrokeInput), C.POINTER(PFCUDADashInput),
+                                       C.POINTER(PFCUDAOutlineOutput)]),
+    "PFCUDAStrokeToFillDashed": (C.c_int32, [C.c_void_p, C.POINTER(PFCUDAStrokeInput), C.POINTER(PFCUDADashInput),
+                                             C.POINTER(PFCUDAStrokeOutput)]),
     "PFCUDAGradientSample": (C.c_int32, [C.POINTER(PFCUDAGradient), C.c_float, C.POINTER(PFColorU)]),
     "PFCUDAGradientRamp": (C.c_int32, [C.POINTER(PFCUDAGradient), C.c_void_p]),
     "PFCUDARendererCreate": (C.c_int32, [C.c_int32, C.POINTER(PFCUDARendererOptions), C.POINTER(C.c_void_p)]),

@@ -170,6 +170,8 @@ struct PFCUDAGradient;
 struct PFCUDAPattern;
 struct PFCUDAStrokeInput;
 struct PFCUDAStrokeOutput;
+struct PFCUDADashInput;
+struct PFCUDAOutlineOutput;
 struct PFCUDAColorStop;
 namespace pf {
 // Paint overlays (host): the record of one gradient with its 256-texel ramp,
@@ -184,6 +186,10 @@ struct StrokeWork;
 StrokeWork* stroke_work_create();
 void stroke_work_destroy(StrokeWork* w);
 int32_t stroke_run(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, PFCUDAStrokeOutput* out);
+int32_t dash_outlines(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, const PFCUDADashInput* dash,
+                      PFCUDAOutlineOutput* out);
+int32_t stroke_dashed(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, const PFCUDADashInput* dash,
+                      PFCUDAStrokeOutput* out);
 
 // Number of kernels this library has launched (host counter).
 uint64_t launch_counter();

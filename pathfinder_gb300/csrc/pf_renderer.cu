@@ -1520,6 +1520,24 @@ int32_t PFCUDAStrokeToFill(PFCUDARendererRef r, const PFCUDAStrokeInput* input, 
     return stroke_run(r->stroke, r->stream, input, output);
 }
 
+int32_t PFCUDADashOutlines(PFCUDARendererRef r, const PFCUDAStrokeInput* input, const PFCUDADashInput* dash,
+                           PFCUDAOutlineOutput* output) {
+    if (!r || !input || !dash || !output) return PF_CUDA_ERR_INVALID;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
+    if (!r->stroke) r->stroke = stroke_work_create();
+    return dash_outlines(r->stroke, r->stream, input, dash, output);
+}
+
+int32_t PFCUDAStrokeToFillDashed(PFCUDARendererRef r, const PFCUDAStrokeInput* input, const PFCUDADashInput* dash,
+                                 PFCUDAStrokeOutput* output) {
+    if (!r || !input || !dash || !output) return PF_CUDA_ERR_INVALID;
+    DeviceGuard dg(r->device);
+    PF_TRY(dg.status);
+    if (!r->stroke) r->stroke = stroke_work_create();
+    return stroke_dashed(r->stroke, r->stream, input, dash, output);
+}
+
 int32_t PFCUDAExclusiveScan(PFCUDARendererRef r, const uint32_t* in, uint32_t* out, uint32_t n) {
     if (!r || !out || (!in && n) || n >= 0x80000000u) return PF_CUDA_ERR_INVALID;
     DeviceGuard dg(r->device);

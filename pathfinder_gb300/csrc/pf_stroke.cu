@@ -691,6 +691,201 @@ __global__ void k_stroke_contours(StrokeDev d, const uint32_t* cbase, uint32_t* 
     if (c == 0) out_cstarts[cbase[d.C]] = total_points;
 }
 
+// ---- dashes: OutlineDash (content/src/dash.rs:18-152) -----------------------
+// The distance left in the current dash is carried from segment to segment in
+// single precision, and each cut's remainder is the next step's segment, so an
+// outline is one sequential walk; a thread walks one outline, twice (count,
+// then write at the scanned offsets).  Outlines without a pattern are copied
+// by a thread per point and a thread per contour.
+constexpr float kDashEpsilon = 0.0001f;       // content/src/dash.rs:16
+constexpr uint32_t kMaxDashSteps = 1u << 20;  // steps per outline (a cut or a whole segment each)
+
+struct DashDev {
+    const float2* pts;
+    const uint8_t* pflags;
+    const uint32_t* cstarts;   // [C + 1]
+    const uint8_t* closed;     // [C]
+    const uint32_t* ostarts;   // [O + 1] contours of each outline
+    const uint32_t* opstarts;  // [O + 1] points of each outline (cstarts[ostarts[o]])
+    const float* dashes;
+    const uint32_t* dstarts;   // [O + 1] each outline's pattern
+    const float* offsets;      // [O]
+    uint32_t O, C;
+    uint32_t* cnt_pts;         // [O] output points per outline, then scanned into pbase
+    uint32_t* cnt_cont;        // [O] output contours per outline, then scanned into cbase
+    const uint32_t* pbase;     // [O + 1]
+    const uint32_t* cbase;     // [O + 1]
+    float2* out_pts;
+    uint8_t* out_flags;
+    uint32_t* out_cstarts;
+    uint8_t* out_closed;
+    uint32_t* status;          // bit 0: an outline reached the step bound
+};
+
+// ContourIter (content/src/outline.rs:1020-1065) as a cursor, closing segment
+// included; indices past the end clamp to the last point, as contour_segments.
+struct SegCursor {
+    const float2* p;
+    const uint8_t* fl;
+    uint32_t n, index;
+    bool closed;
+    __device__ V P(uint32_t i) const { const uint32_t j = i < n ? i : n - 1; return V{p[j].x, p[j].y}; }
+    __device__ bool next(Seg* sg) {
+        if (n == 0 || index > n || (index == n && !closed)) return false;
+        const V p0 = P(index - 1);
+        if (index == n) { index++; *sg = mk_line(L{p0, P(0)}); return true; }
+        const uint32_t i1 = index++;
+        if (is_end(fl, i1)) { *sg = mk_line(L{p0, P(i1)}); return true; }
+        const uint32_t i2 = index++;
+        if (i2 >= n || is_end(fl, i2)) { *sg = mk_quad(L{p0, P(i2)}, P(i1)); return true; }
+        const uint32_t i3 = index++;
+        *sg = mk_cubic(L{p0, P(i3)}, L{P(i1), P(i2)});
+        return true;
+    }
+};
+
+// The dashes' output of one outline: counts when pts is NULL, else writes
+// from the outline's scanned bases.
+struct DashSink {
+    float2* pts;
+    uint8_t* flags;
+    uint32_t* cstarts;
+    uint8_t* closed;
+    uint32_t pbase, cbase;
+    uint32_t n, nc, start;  // points, finished contours, first point of the open contour
+    __device__ void push(V q, uint8_t f) {
+        if (pts) { pts[pbase + n] = make_float2(q.x, q.y); flags[pbase + n] = f; }
+        n++;
+    }
+    // Contour::push_segment (content/src/outline.rs:576-600): the from point always
+    __device__ void push_segment(const Seg& s) {
+        push(s.base.f, 0);
+        if (s.kind != kKindLine) {
+            push(s.ctrl.f, PF_POINT_FLAG_CONTROL_POINT_0);
+            if (s.kind != kKindQuad) push(s.ctrl.t, PF_POINT_FLAG_CONTROL_POINT_1);
+        }
+        push(s.base.t, 0);
+    }
+    // Outline::push_contour of the dash's open contour (outline.rs:180-192):
+    // an empty one is dropped
+    __device__ void end_contour() {
+        if (n == start) return;
+        if (pts) { cstarts[cbase + nc] = pbase + start; closed[cbase + nc] = 0; }
+        nc++;
+        start = n;
+    }
+};
+
+// Segment::arc_length (content/src/segment.rs:246-249): the chord's length
+__device__ __forceinline__ float chord_length(const Seg& s) { return sqrtf(vsqlen(lvec(s.base))); }
+
+// OutlineDash::dash + into_outline (dash.rs:46-57) for outline o with a
+// non-empty pattern; returns true when the step bound cut it short.
+__device__ bool dash_outline(const DashDev& d, uint32_t o, DashSink& k) {
+    const float* dashes = d.dashes + d.dstarts[o];
+    const uint32_t nd = d.dstarts[o + 1] - d.dstarts[o];
+    // DashState::new (:124-145): the offset modulo the pattern's sum (a fold
+    // from zero), then the whole dashes it covers are skipped; the distance
+    // left starts at what remains of the offset
+    float total = 0.0f;
+    for (uint32_t i = 0; i < nd; i++) total = total + dashes[i];
+    float offset = fmodf(d.offsets[o], total);
+    uint32_t idx = 0;
+    while (idx < nd) {
+        if (offset < dashes[idx]) break;
+        offset = offset - dashes[idx];
+        idx++;
+    }
+    float left = offset;
+    uint32_t steps = 0;
+    bool limited = false;
+    // ContourDash::dash (:73-113) over every contour; the open dash contour
+    // carries from one contour to the next
+    for (uint32_t c = d.ostarts[o]; c < d.ostarts[o + 1] && !limited; c++) {
+        const uint32_t a = d.cstarts[c];
+        SegCursor it{d.pts + a, d.pflags + a, d.cstarts[c + 1] - a, 1u, d.closed[c] != 0};
+        Seg queued;
+        bool have = false;
+        for (;;) {
+            if (!have && !it.next(&queued)) break;
+            if (steps++ == kMaxDashSteps) { limited = true; break; }
+            Seg cur = queued;
+            have = false;
+            float distance = left;
+            const float t = distance / chord_length(cur);  // time_for_distance (segment.rs:251-254)
+            if (t < 1.0f) {
+                Seg a0, b0;
+                seg_split(cur, t, &a0, &b0);
+                cur = a0;
+                queued = b0;
+                have = true;
+            } else {
+                distance = chord_length(cur);
+            }
+            const bool on = (idx & 1u) == 0u;  // DashState::is_on (:147-150)
+            if (on) k.push_segment(cur);
+            left = left - distance;
+            if (left < kDashEpsilon) {
+                if (on) k.end_contour();
+                // the next dash, wrapping (an offset rounding onto the pattern's
+                // end wraps here too; the reference would index past it)
+                idx++;
+                if (idx >= nd) idx = 0;
+                left = dashes[idx];
+            }
+        }
+    }
+    if ((idx & 1u) == 0u) k.end_contour();
+    return limited;
+}
+
+__global__ void k_dash_count(DashDev d) {
+    for (uint32_t o = blockIdx.x * blockDim.x + threadIdx.x; o < d.O; o += gridDim.x * blockDim.x) {
+        if (d.dstarts[o + 1] == d.dstarts[o]) {
+            d.cnt_pts[o] = d.opstarts[o + 1] - d.opstarts[o];
+            d.cnt_cont[o] = d.ostarts[o + 1] - d.ostarts[o];
+            continue;
+        }
+        DashSink k{nullptr, nullptr, nullptr, nullptr, 0u, 0u, 0u, 0u, 0u};
+        if (dash_outline(d, o, k)) atomicOr(d.status, 1u);
+        d.cnt_pts[o] = k.n;
+        d.cnt_cont[o] = k.nc;
+    }
+}
+
+__global__ void k_dash_emit(DashDev d) {
+    for (uint32_t o = blockIdx.x * blockDim.x + threadIdx.x; o < d.O; o += gridDim.x * blockDim.x) {
+        if (d.dstarts[o + 1] == d.dstarts[o]) continue;
+        DashSink k{d.out_pts, d.out_flags, d.out_cstarts, d.out_closed, d.pbase[o], d.cbase[o], 0u, 0u, 0u};
+        dash_outline(d, o, k);
+    }
+}
+
+// Points of outlines without a pattern, unchanged: a thread per input point.
+__global__ void k_dash_copy_points(DashDev d) {
+    const uint32_t end = d.opstarts[d.O];
+    for (uint32_t p = d.opstarts[0] + blockIdx.x * blockDim.x + threadIdx.x; p < end; p += gridDim.x * blockDim.x) {
+        const uint32_t o = upper_bound_items(d.opstarts, d.O + 1, p) - 1;
+        if (d.dstarts[o + 1] != d.dstarts[o]) continue;
+        const uint32_t q = d.pbase[o] + (p - d.opstarts[o]);
+        d.out_pts[q] = d.pts[p];
+        d.out_flags[q] = d.pflags[p];
+    }
+}
+
+// Contours of outlines without a pattern, with their closed flags; thread 0
+// also ends the contour list.
+__global__ void k_dash_copy_contours(DashDev d, uint32_t total_points) {
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < d.C; c += gridDim.x * blockDim.x) {
+        const uint32_t o = upper_bound_items(d.ostarts, d.O + 1, c) - 1;
+        if (o >= d.O || d.dstarts[o + 1] != d.dstarts[o]) continue;
+        const uint32_t q = d.cbase[o] + (c - d.ostarts[o]);
+        d.out_cstarts[q] = d.pbase[o] + (d.cstarts[c] - d.opstarts[o]);
+        d.out_closed[q] = d.closed[c];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.out_cstarts[d.cbase[d.O]] = total_points;
+}
+
 }  // namespace
 }  // namespace pf
 
@@ -731,6 +926,14 @@ struct StrokeWork {
     SBuf<unsigned long long> item_leaves;
     SBuf<float4> item_last, item_first;
     SBuf<float2> item_first_at;
+    // dashes: the input's index arrays, the patterns, counts and their scans,
+    // and the dashed outlines (the stroke's input when both run)
+    SBuf<uint32_t> d_cstarts, d_ostarts, d_opstarts, d_dstarts, d_cnt_p, d_cnt_c, d_pbase, d_cbase, dash_cstarts,
+        dash_ostarts;
+    SBuf<float> d_dashes, d_offsets;
+    SBuf<float2> dash_pts;
+    SBuf<uint8_t> dash_flags, dash_closed;
+    SBuf<PFCUDAStrokeStyle> dash_styles;
 };
 
 StrokeWork* stroke_work_create() { return new StrokeWork(); }
@@ -743,34 +946,51 @@ void stroke_work_destroy(StrokeWork* w) {
     w->actual.release(); w->final_off.release(); w->cbase.release(); w->out_cstarts.release();
     w->status.release(); w->partials.release(); w->styles.release(); w->segs.release();
     w->item_leaves.release(); w->item_last.release(); w->item_first.release(); w->item_first_at.release();
+    w->d_cstarts.release(); w->d_ostarts.release(); w->d_opstarts.release(); w->d_dstarts.release();
+    w->d_cnt_p.release(); w->d_cnt_c.release(); w->d_pbase.release(); w->d_cbase.release();
+    w->dash_cstarts.release(); w->dash_ostarts.release(); w->d_dashes.release(); w->d_offsets.release();
+    w->dash_pts.release(); w->dash_flags.release(); w->dash_closed.release(); w->dash_styles.release();
     delete w;
+}
+
+// Host copies of an outline set's index arrays, checked before any kernel
+// reads them: contour starts in order and within the points, outline starts
+// in order from 0 to the contour count.
+int32_t read_index_arrays(const PFCUDAStrokeInput* in, std::vector<uint32_t>& hc, std::vector<uint32_t>& ho) {
+    if (in->memory != PF_MEMORY_HOST && in->memory != PF_MEMORY_DEVICE) return PF_CUDA_ERR_INVALID;
+    const uint32_t NP = in->point_count, C = in->contour_count, O = in->outline_count;
+    if (NP >= 0x40000000u || C >= 0x20000000u || O >= 0x20000000u) return PF_CUDA_ERR_INVALID;
+    if ((NP && (!in->points || !in->point_flags)) || !in->contour_starts || (C && !in->contour_closed) ||
+        !in->outline_starts)
+        return PF_CUDA_ERR_INVALID;
+    const cudaMemcpyKind down = in->memory == PF_MEMORY_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+    hc.assign(C + 1, 0u);
+    ho.assign(O + 1, 0u);
+    PF_STROKE_TRY(cudaMemcpy(hc.data(), in->contour_starts, sizeof(uint32_t) * (C + 1), down));
+    PF_STROKE_TRY(cudaMemcpy(ho.data(), in->outline_starts, sizeof(uint32_t) * (O + 1), down));
+    for (uint32_t c = 0; c < C; c++)
+        if (hc[c] > hc[c + 1]) return PF_CUDA_ERR_INVALID;
+    if (hc[C] > NP || ho[0] != 0 || ho[O] != C) return PF_CUDA_ERR_INVALID;
+    for (uint32_t o = 0; o < O; o++)
+        if (ho[o] > ho[o + 1]) return PF_CUDA_ERR_INVALID;
+    return PF_CUDA_OK;
 }
 
 int32_t stroke_run(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, PFCUDAStrokeOutput* out) {
     if (!w || !in || !out) return PF_CUDA_ERR_INVALID;
-    if ((in->memory != PF_MEMORY_HOST && in->memory != PF_MEMORY_DEVICE) ||
-        (out->memory != PF_MEMORY_HOST && out->memory != PF_MEMORY_DEVICE))
-        return PF_CUDA_ERR_INVALID;
+    if (out->memory != PF_MEMORY_HOST && out->memory != PF_MEMORY_DEVICE) return PF_CUDA_ERR_INVALID;
+    std::vector<uint32_t> hc, ho;
+    const int32_t irc = read_index_arrays(in, hc, ho);
+    if (irc != PF_CUDA_OK) return irc;
     const uint32_t NP = in->point_count, C = in->contour_count, O = in->outline_count;
-    if (NP >= 0x40000000u || C >= 0x20000000u || O > C + 1u) return PF_CUDA_ERR_INVALID;
-    if ((NP && (!in->points || !in->point_flags)) || !in->contour_starts || (C && !in->contour_closed) ||
-        !in->outline_starts || (O && !in->styles))
-        return PF_CUDA_ERR_INVALID;
+    if (O && !in->styles) return PF_CUDA_ERR_INVALID;
     const bool dev_in = in->memory == PF_MEMORY_DEVICE;
     const cudaMemcpyKind up = dev_in ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    // host copies of the small index arrays, validated before any kernel reads them
-    std::vector<uint32_t> hc(C + 1), ho(O + 1);
     std::vector<PFCUDAStrokeStyle> hs(O);
     const cudaMemcpyKind down = dev_in ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
-    PF_STROKE_TRY(cudaMemcpy(hc.data(), in->contour_starts, sizeof(uint32_t) * (C + 1), down));
-    PF_STROKE_TRY(cudaMemcpy(ho.data(), in->outline_starts, sizeof(uint32_t) * (O + 1), down));
     if (O) PF_STROKE_TRY(cudaMemcpy(hs.data(), in->styles, sizeof(PFCUDAStrokeStyle) * O, down));
-    for (uint32_t c = 0; c < C; c++)
-        if (hc[c] > hc[c + 1]) return PF_CUDA_ERR_INVALID;
-    if (hc[C] > NP || ho[0] != 0 || ho[O] != C) return PF_CUDA_ERR_INVALID;
     std::vector<uint32_t> outline_of(C > 0 ? C : 1);
     for (uint32_t o = 0; o < O; o++) {
-        if (ho[o] > ho[o + 1]) return PF_CUDA_ERR_INVALID;
         const PFCUDAStrokeStyle& st = hs[o];
         if (!(st.line_width >= 0.0f && st.line_width < 1e30f) || st.line_cap < 0 || st.line_cap > 2 ||
             st.line_join < 0 || st.line_join > 2 || !(std::fabs(st.miter_limit) < 1e30f))
@@ -916,6 +1136,205 @@ int32_t stroke_run(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, P
     PF_STROKE_TRY(cudaStreamSynchronize(s));
     PF_STROKE_TRY(cudaGetLastError());
     return (status & 1u) ? PF_CUDA_ERR_LIMIT : PF_CUDA_OK;
+}
+
+namespace {
+// Blocks of 64 threads for the walks (a thread per outline), so that a few
+// hundred outlines still spread over the SMs.
+uint32_t walk_grid(uint64_t n) {
+    const uint64_t b = (n + 63) / 64;
+    const uint64_t cap = (uint64_t)device_sm_count() * 32;
+    return (uint32_t)(b == 0 ? 1 : (b > cap ? cap : b));
+}
+
+// The dashed outlines, in the work's dash buffers on the device.
+struct DashResult {
+    uint32_t P = 0, OC = 0;
+    std::vector<uint32_t> ostarts;  // host copy of the output outline starts
+    bool limited = false;
+};
+
+int32_t dash_run(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, const PFCUDADashInput* dash,
+                 DashResult* r) {
+    if (!w || !in || !dash) return PF_CUDA_ERR_INVALID;
+    std::vector<uint32_t> hc, ho;
+    const int32_t irc = read_index_arrays(in, hc, ho);
+    if (irc != PF_CUDA_OK) return irc;
+    const uint32_t NP = in->point_count, C = in->contour_count, O = in->outline_count;
+    if (!dash->dash_starts || (O && !dash->offsets)) return PF_CUDA_ERR_INVALID;
+    const bool dev_in = in->memory == PF_MEMORY_DEVICE;
+    const cudaMemcpyKind down = dev_in ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+    std::vector<uint32_t> hd(O + 1);
+    PF_STROKE_TRY(cudaMemcpy(hd.data(), dash->dash_starts, sizeof(uint32_t) * (O + 1), down));
+    if (hd[0] != 0) return PF_CUDA_ERR_INVALID;
+    for (uint32_t o = 0; o < O; o++)
+        if (hd[o] > hd[o + 1]) return PF_CUDA_ERR_INVALID;
+    const uint32_t ND = hd[O];
+    if (ND >= 0x40000000u || (ND && !dash->dashes)) return PF_CUDA_ERR_INVALID;
+    std::vector<float> hv(ND), hoff(O);
+    if (ND) PF_STROKE_TRY(cudaMemcpy(hv.data(), dash->dashes, sizeof(float) * ND, down));
+    if (O) PF_STROKE_TRY(cudaMemcpy(hoff.data(), dash->offsets, sizeof(float) * O, down));
+    for (uint32_t o = 0; o < O; o++) {
+        if (hd[o + 1] == hd[o]) continue;
+        float total = 0.0f;
+        for (uint32_t i = hd[o]; i < hd[o + 1]; i++) {
+            if (!(hv[i] >= 0.0f) || !std::isfinite(hv[i])) return PF_CUDA_ERR_INVALID;
+            total = total + hv[i];
+        }
+        if (!(total > 0.0f) || !std::isfinite(total) || !std::isfinite(hoff[o])) return PF_CUDA_ERR_INVALID;
+    }
+    std::vector<uint32_t> hop(O + 1);
+    for (uint32_t o = 0; o <= O; o++) hop[o] = hc[ho[o]];
+
+    PF_STROKE_TRY(w->d_cstarts.ensure(C + 1));
+    PF_STROKE_TRY(w->d_ostarts.ensure(O + 1));
+    PF_STROKE_TRY(w->d_opstarts.ensure(O + 1));
+    PF_STROKE_TRY(w->d_dstarts.ensure(O + 1));
+    PF_STROKE_TRY(w->d_dashes.ensure((size_t)ND + 1));
+    PF_STROKE_TRY(w->d_offsets.ensure(O + 1));
+    PF_STROKE_TRY(w->d_cnt_p.ensure(O + 1));
+    PF_STROKE_TRY(w->d_cnt_c.ensure(O + 1));
+    PF_STROKE_TRY(w->d_pbase.ensure(O + 1));
+    PF_STROKE_TRY(w->d_cbase.ensure(O + 1));
+    PF_STROKE_TRY(w->status.ensure(1));
+    PF_STROKE_TRY(w->partials.ensure(2 * ((size_t)O / 2048 + 2)));  // two scan lanes
+    DashDev d{};
+    if (dev_in) {
+        d.pts = (const float2*)in->points;
+        d.pflags = in->point_flags;
+        d.closed = in->contour_closed;
+    } else {
+        const cudaMemcpyKind up = cudaMemcpyHostToDevice;
+        PF_STROKE_TRY(w->pts.ensure(NP + 1));
+        PF_STROKE_TRY(w->pflags.ensure(NP + 1));
+        PF_STROKE_TRY(w->closed.ensure(C + 1));
+        if (NP) {
+            PF_STROKE_TRY(cudaMemcpyAsync(w->pts.p, in->points, sizeof(float2) * NP, up, s));
+            PF_STROKE_TRY(cudaMemcpyAsync(w->pflags.p, in->point_flags, NP, up, s));
+        }
+        if (C) PF_STROKE_TRY(cudaMemcpyAsync(w->closed.p, in->contour_closed, C, up, s));
+        d.pts = w->pts.p;
+        d.pflags = w->pflags.p;
+        d.closed = w->closed.p;
+    }
+    PF_STROKE_TRY(cudaMemcpyAsync(w->d_cstarts.p, hc.data(), sizeof(uint32_t) * (C + 1), cudaMemcpyHostToDevice, s));
+    PF_STROKE_TRY(cudaMemcpyAsync(w->d_ostarts.p, ho.data(), sizeof(uint32_t) * (O + 1), cudaMemcpyHostToDevice, s));
+    PF_STROKE_TRY(cudaMemcpyAsync(w->d_opstarts.p, hop.data(), sizeof(uint32_t) * (O + 1), cudaMemcpyHostToDevice, s));
+    PF_STROKE_TRY(cudaMemcpyAsync(w->d_dstarts.p, hd.data(), sizeof(uint32_t) * (O + 1), cudaMemcpyHostToDevice, s));
+    if (ND) PF_STROKE_TRY(cudaMemcpyAsync(w->d_dashes.p, hv.data(), sizeof(float) * ND, cudaMemcpyHostToDevice, s));
+    if (O) PF_STROKE_TRY(cudaMemcpyAsync(w->d_offsets.p, hoff.data(), sizeof(float) * O, cudaMemcpyHostToDevice, s));
+    PF_STROKE_TRY(cudaMemsetAsync(w->status.p, 0, sizeof(uint32_t), s));
+    d.cstarts = w->d_cstarts.p;
+    d.ostarts = w->d_ostarts.p;
+    d.opstarts = w->d_opstarts.p;
+    d.dashes = w->d_dashes.p;
+    d.dstarts = w->d_dstarts.p;
+    d.offsets = w->d_offsets.p;
+    d.O = O;
+    d.C = C;
+    d.cnt_pts = w->d_cnt_p.p;
+    d.cnt_cont = w->d_cnt_c.p;
+    d.pbase = w->d_pbase.p;
+    d.cbase = w->d_cbase.p;
+    d.status = w->status.p;
+    ScanTemp tmp{w->partials.p, (uint32_t)w->partials.cap};
+
+    if (O) { count_launch(); k_dash_count<<<walk_grid(O), 64, 0, s>>>(d); }
+    ScanLanes lanes{};
+    lanes.count = 2;
+    lanes.in[0] = w->d_cnt_p.p; lanes.out[0] = w->d_pbase.p;
+    lanes.in[1] = w->d_cnt_c.p; lanes.out[1] = w->d_cbase.p;
+    launch_scan_multi(lanes, nullptr, O, tmp, s);
+    uint32_t status = 0;
+    r->ostarts.assign(O + 1, 0u);
+    PF_STROKE_TRY(cudaMemcpyAsync(r->ostarts.data(), w->d_cbase.p, sizeof(uint32_t) * (O + 1),
+                                  cudaMemcpyDeviceToHost, s));
+    PF_STROKE_TRY(cudaMemcpyAsync(&r->P, w->d_pbase.p + O, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    PF_STROKE_TRY(cudaMemcpyAsync(&status, w->status.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    PF_STROKE_TRY(cudaStreamSynchronize(s));
+    PF_STROKE_TRY(cudaGetLastError());
+    r->OC = r->ostarts[O];
+    r->limited = (status & 1u) != 0;
+    if (r->P >= 0x40000000u || r->OC >= 0x20000000u) return PF_CUDA_ERR_CAPACITY;
+    PF_STROKE_TRY(w->dash_pts.ensure((size_t)r->P + 1));
+    PF_STROKE_TRY(w->dash_flags.ensure((size_t)r->P + 1));
+    PF_STROKE_TRY(w->dash_cstarts.ensure((size_t)r->OC + 1));
+    PF_STROKE_TRY(w->dash_closed.ensure((size_t)r->OC + 1));
+    d.out_pts = w->dash_pts.p;
+    d.out_flags = w->dash_flags.p;
+    d.out_cstarts = w->dash_cstarts.p;
+    d.out_closed = w->dash_closed.p;
+    if (O) { count_launch(); k_dash_emit<<<walk_grid(O), 64, 0, s>>>(d); }
+    if (hop[O] > hop[0]) { count_launch(); k_dash_copy_points<<<grid_for(hop[O] - hop[0]), 256, 0, s>>>(d); }
+    { count_launch(); k_dash_copy_contours<<<grid_for(C), 256, 0, s>>>(d, r->P); }
+    PF_STROKE_TRY(cudaGetLastError());
+    return PF_CUDA_OK;
+}
+}  // namespace
+
+int32_t dash_outlines(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, const PFCUDADashInput* dash,
+                      PFCUDAOutlineOutput* out) {
+    if (!out || (out->memory != PF_MEMORY_HOST && out->memory != PF_MEMORY_DEVICE)) return PF_CUDA_ERR_INVALID;
+    DashResult r;
+    const int32_t rc = dash_run(w, s, in, dash, &r);
+    if (rc != PF_CUDA_OK) return rc;
+    const uint32_t O = in->outline_count;
+    out->point_count = r.P;
+    out->contour_count = r.OC;
+    if (out->point_capacity < r.P || out->contour_capacity < r.OC) {
+        PF_STROKE_TRY(cudaStreamSynchronize(s));
+        return PF_CUDA_ERR_CAPACITY;
+    }
+    if ((r.P && (!out->points || !out->point_flags)) || !out->contour_starts || (r.OC && !out->contour_closed) ||
+        !out->outline_starts) {
+        PF_STROKE_TRY(cudaStreamSynchronize(s));
+        return PF_CUDA_ERR_INVALID;
+    }
+    const cudaMemcpyKind k = out->memory == PF_MEMORY_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (r.P) {
+        PF_STROKE_TRY(cudaMemcpyAsync(out->points, w->dash_pts.p, sizeof(float2) * r.P, k, s));
+        PF_STROKE_TRY(cudaMemcpyAsync(out->point_flags, w->dash_flags.p, r.P, k, s));
+    }
+    PF_STROKE_TRY(cudaMemcpyAsync(out->contour_starts, w->dash_cstarts.p, sizeof(uint32_t) * (r.OC + 1), k, s));
+    if (r.OC) PF_STROKE_TRY(cudaMemcpyAsync(out->contour_closed, w->dash_closed.p, r.OC, k, s));
+    if (out->memory == PF_MEMORY_DEVICE)
+        PF_STROKE_TRY(cudaMemcpyAsync(out->outline_starts, r.ostarts.data(), sizeof(uint32_t) * (O + 1),
+                                      cudaMemcpyHostToDevice, s));
+    else
+        std::memcpy(out->outline_starts, r.ostarts.data(), sizeof(uint32_t) * (O + 1));
+    PF_STROKE_TRY(cudaStreamSynchronize(s));
+    PF_STROKE_TRY(cudaGetLastError());
+    return r.limited ? PF_CUDA_ERR_LIMIT : PF_CUDA_OK;
+}
+
+int32_t stroke_dashed(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, const PFCUDADashInput* dash,
+                      PFCUDAStrokeOutput* out) {
+    if (!w || !in || !out || (in->outline_count && !in->styles)) return PF_CUDA_ERR_INVALID;
+    DashResult r;
+    const int32_t rc = dash_run(w, s, in, dash, &r);
+    if (rc != PF_CUDA_OK) return rc;
+    const uint32_t O = in->outline_count;
+    PF_STROKE_TRY(w->dash_styles.ensure(O + 1));
+    PF_STROKE_TRY(w->dash_ostarts.ensure(O + 1));
+    const cudaMemcpyKind up = in->memory == PF_MEMORY_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (O) PF_STROKE_TRY(cudaMemcpyAsync(w->dash_styles.p, in->styles, sizeof(PFCUDAStrokeStyle) * O, up, s));
+    PF_STROKE_TRY(cudaMemcpyAsync(w->dash_ostarts.p, r.ostarts.data(), sizeof(uint32_t) * (O + 1),
+                                  cudaMemcpyHostToDevice, s));
+    PF_STROKE_TRY(cudaStreamSynchronize(s));
+    PFCUDAStrokeInput dashed{};
+    dashed.points = (const PFVector2F*)w->dash_pts.p;
+    dashed.point_flags = w->dash_flags.p;
+    dashed.contour_starts = w->dash_cstarts.p;
+    dashed.contour_closed = w->dash_closed.p;
+    dashed.outline_starts = w->dash_ostarts.p;
+    dashed.styles = w->dash_styles.p;
+    dashed.point_count = r.P;
+    dashed.contour_count = r.OC;
+    dashed.outline_count = O;
+    dashed.memory = PF_MEMORY_DEVICE;
+    const int32_t src = stroke_run(w, s, &dashed, out);
+    if (src != PF_CUDA_OK) return src;
+    return r.limited ? PF_CUDA_ERR_LIMIT : PF_CUDA_OK;
 }
 
 }  // namespace pf

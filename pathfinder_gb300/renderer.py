@@ -327,11 +327,14 @@ class Renderer:
                    "PFCUDABackward")
 
     def stroke_to_fill_buffers(self, items):
-        """PFCUDAStrokeToFill over [(Outline, StrokeStyle)]: the stroked outlines as
-        (points (N, 2) float32, flags (N,) uint8, contour_starts, outline_starts)."""
+        """PFCUDAStrokeToFill over [(Outline, StrokeStyle)] (PFCUDAStrokeToFillDashed
+        when an item is (Outline, StrokeStyle, dashes, dash_offset) with a
+        non-empty pattern): the stroked outlines as (points (N, 2) float32,
+        flags (N,) uint8, contour_starts, outline_starts)."""
         from .stroke import StrokeBatch
         b = StrokeBatch(items)
         d = b.desc()
+        dd = b.dash_desc() if b.dashed else None
         cap_p = max(64, 8 * len(b.points) + 64 * b.contour_count)
         cap_c = 2 * b.contour_count
         for _ in range(2):
@@ -344,7 +347,10 @@ class Renderer:
             o.contour_starts, o.outline_starts = cs.ctypes.data, os_.ctypes.data
             o.point_capacity, o.contour_capacity = cap_p, cap_c
             o.memory = _abi.PF_MEMORY_HOST
-            rc = self._lib.PFCUDAStrokeToFill(self._h, C.byref(d), C.byref(o))
+            if dd is None:
+                rc = self._lib.PFCUDAStrokeToFill(self._h, C.byref(d), C.byref(o))
+            else:
+                rc = self._lib.PFCUDAStrokeToFillDashed(self._h, C.byref(d), C.byref(dd), C.byref(o))
             if rc == _abi.PF_CUDA_ERR_CAPACITY and (o.point_count > cap_p or o.contour_count > cap_c):
                 cap_p, cap_c = int(o.point_count), int(o.contour_count)
                 continue
@@ -352,6 +358,43 @@ class Renderer:
             n, nc = int(o.point_count), int(o.contour_count)
             return pts[:n], flags[:n], cs[:nc + 1], os_
         raise RuntimeError("PFCUDAStrokeToFill: capacity did not converge")
+
+    def dash_buffers(self, items):
+        """PFCUDADashOutlines over [(Outline, dashes, dash_offset)]: the dashed
+        outlines as (points (N, 2) float32, flags (N,) uint8, contour_starts,
+        contour_closed, outline_starts)."""
+        from .stroke import StrokeBatch
+        b = StrokeBatch([(ol, None, dashes, offset) for ol, dashes, offset in items])
+        d, dd = b.desc(), b.dash_desc()
+        cap_p = max(64, 4 * len(b.points))
+        cap_c = max(16, 4 * b.contour_count)
+        for _ in range(2):
+            pts = np.zeros((cap_p, 2), np.float32)
+            flags = np.zeros((cap_p,), np.uint8)
+            cs = np.zeros((cap_c + 1,), np.uint32)
+            closed = np.zeros((max(1, cap_c),), np.uint8)
+            os_ = np.zeros((b.outline_count + 1,), np.uint32)
+            o = _abi.PFCUDAOutlineOutput()
+            o.points, o.point_flags = pts.ctypes.data, flags.ctypes.data
+            o.contour_starts, o.contour_closed, o.outline_starts = cs.ctypes.data, closed.ctypes.data, os_.ctypes.data
+            o.point_capacity, o.contour_capacity = cap_p, cap_c
+            o.memory = _abi.PF_MEMORY_HOST
+            rc = self._lib.PFCUDADashOutlines(self._h, C.byref(d), C.byref(dd), C.byref(o))
+            if rc == _abi.PF_CUDA_ERR_CAPACITY and (o.point_count > cap_p or o.contour_count > cap_c):
+                cap_p, cap_c = int(o.point_count), int(o.contour_count)
+                continue
+            _abi.check(rc, "PFCUDADashOutlines")
+            n, nc = int(o.point_count), int(o.contour_count)
+            return pts[:n], flags[:n], cs[:nc + 1], closed[:nc], os_
+        raise RuntimeError("PFCUDADashOutlines: capacity did not converge")
+
+    def dash_outlines(self, items):
+        """OutlineDash (content/src/dash.rs:18-152) for many outlines at once on
+        the GPU: [(Outline, dashes, dash_offset)] -> [Outline] (dashed contours
+        open; an outline with an empty pattern unchanged)."""
+        from .stroke import outlines_from_buffers
+        pts, flags, cs, closed, os_ = self.dash_buffers(items)
+        return outlines_from_buffers(pts, flags, cs, os_, closed)
 
     def stroke_to_fill(self, items):
         """OutlineStrokeToFill (content/src/stroke.rs:24-190) for many outlines at

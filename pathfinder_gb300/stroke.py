@@ -1,6 +1,8 @@
 """Stroke to fill: StrokeStyle, LineCap, LineJoin (content/src/stroke.rs:45-86)
 and the batch conversion of outlines to the filled outlines of their strokes
-(OutlineStrokeToFill, :24-190), run on the GPU by PFCUDAStrokeToFill."""
+(OutlineStrokeToFill, :24-190), run on the GPU by PFCUDAStrokeToFill; dashes
+before it (OutlineDash, content/src/dash.rs:18-152) by PFCUDADashOutlines and
+PFCUDAStrokeToFillDashed."""
 from __future__ import annotations
 
 import ctypes as C
@@ -35,12 +37,22 @@ class StrokeStyle:
 
 
 class StrokeBatch:
-    """Outlines with their styles as one host-memory PFCUDAStrokeInput."""
+    """Outlines with their styles as one host-memory PFCUDAStrokeInput, and
+    their dash patterns as a PFCUDADashInput.  An item is ``(outline, style)``
+    or ``(outline, style, dashes, dash_offset)``: ``dashes`` the alternating
+    on/off lengths, used as given (empty: not dashed), ``dash_offset`` the
+    phase.  ``style`` may be None when the batch is only dashed."""
 
     def __init__(self, items):
         pts, flags, cstarts, closed, ostarts, styles = [], [], [0], [], [0], []
+        dashes, dstarts, offsets = [], [0], []
         n = 0
-        for outline, style in items:
+        for item in items:
+            outline, style = item[0], item[1]
+            pattern = list(item[2]) if len(item) > 2 and item[2] is not None else []
+            dashes += [float(x) for x in pattern]
+            dstarts.append(len(dashes))
+            offsets.append(float(item[3]) if len(item) > 3 else 0.0)
             for c in outline.contours:
                 pts.append(np.asarray(c.points, np.float32).reshape(-1, 2))
                 flags.append(np.asarray(c.flags, np.uint8))
@@ -56,10 +68,22 @@ class StrokeBatch:
         self.outline_starts = np.asarray(ostarts, np.uint32)
         self.styles = (_abi.PFCUDAStrokeStyle * max(1, len(styles)))()
         for i, st in enumerate(styles):
+            st = st or StrokeStyle()
             self.styles[i] = _abi.PFCUDAStrokeStyle(float(st.line_width), int(st.line_cap), int(st.line_join),
                                                     float(st.miter_limit))
         self.outline_count = len(styles)
         self.contour_count = len(closed)
+        self.dashes = np.asarray(dashes if dashes else [0.0], np.float32)
+        self.dash_starts = np.asarray(dstarts, np.uint32)
+        self.dash_offsets = np.asarray(offsets if offsets else [0.0], np.float32)
+        self.dashed = bool(dashes)
+
+    def dash_desc(self) -> _abi.PFCUDADashInput:
+        d = _abi.PFCUDADashInput()
+        d.dashes = self.dashes.ctypes.data
+        d.dash_starts = self.dash_starts.ctypes.data
+        d.offsets = self.dash_offsets.ctypes.data
+        return d
 
     def desc(self) -> _abi.PFCUDAStrokeInput:
         d = _abi.PFCUDAStrokeInput()
@@ -76,8 +100,9 @@ class StrokeBatch:
         return d
 
 
-def outlines_from_buffers(points, flags, contour_starts, outline_starts) -> list[Outline]:
-    """Split flat stroke output back into one Outline per input outline."""
+def outlines_from_buffers(points, flags, contour_starts, outline_starts, contour_closed=None) -> list[Outline]:
+    """Split flat stroke (or dash) output back into one Outline per input
+    outline; contours are closed unless ``contour_closed`` says otherwise."""
     out = []
     for o in range(len(outline_starts) - 1):
         ol = Outline()
@@ -86,7 +111,7 @@ def outlines_from_buffers(points, flags, contour_starts, outline_starts) -> list
             ct = Contour()
             ct.points = [(float(x), float(y)) for x, y in points[a:b]]
             ct.flags = [int(f) for f in flags[a:b]]
-            ct.closed = True
+            ct.closed = True if contour_closed is None else bool(contour_closed[c])
             ol.contours.append(ct)  # empty contours are kept: the counts stay aligned
         out.append(ol)
     return out

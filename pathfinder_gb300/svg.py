@@ -9,13 +9,15 @@ command; quadratics, smooth curves and arcs become cubics as usvg makes them),
 repeat, reflect as svg/src/lib.rs:233-261 builds them), one <clipPath> per
 group (clip-path="url(#id)"), and the presentation attributes fill, stroke,
 fill-opacity, stroke-opacity, fill-rule, stroke-width, stroke-linecap,
-stroke-linejoin, stroke-miterlimit, transform, in attributes or in style="".
-Fills become draw paths with the outline transformed; strokes are stroked in
-their local coordinates on the GPU (PFCUDAStrokeToFill, all strokes of the
-document in one batch) and then transformed, as push_draw_path does
-(:264-286).  Stroke widths below 0.0333 use 0.0333 (HAIRLINE_STROKE_WIDTH,
-:38).  Unsupported elements (filters, masks, images, patterns, text, dashes,
-CSS classes) are reported in `unsupported`.
+stroke-linejoin, stroke-miterlimit, stroke-dasharray, stroke-dashoffset,
+transform, in attributes or in style="".
+Fills become draw paths with the outline transformed; strokes are dashed
+(OutlineDash, :159-164) and stroked in their local coordinates on the GPU
+(PFCUDAStrokeToFill or PFCUDAStrokeToFillDashed, all strokes of the document
+in one batch) and then transformed, as push_draw_path does (:264-286).
+Stroke widths below 0.0333 use 0.0333 (HAIRLINE_STROKE_WIDTH, :38).
+Unsupported elements (filters, masks, images, patterns, text, CSS classes) are
+reported in `unsupported`.
 """
 from __future__ import annotations
 
@@ -286,6 +288,18 @@ def _length(v, default=0.0):
     return float(m.group(0)) if m else default
 
 
+def _dasharray(v):
+    """stroke-dasharray as usvg hands it to the reference (svg/src/lib.rs:159):
+    "none", a negative length or a zero sum leave the stroke undashed, and an
+    odd number of lengths is repeated once to make it even (SVG 1.1, 11.4)."""
+    if v is None or v.strip() in ("", "none"):
+        return None
+    vals = [float(x) for x in re.findall(_NUM, v)]
+    if not vals or any(x < 0 for x in vals) or sum(vals) <= 0:
+        return None
+    return vals * 2 if len(vals) % 2 else vals
+
+
 def _style(el):
     """Presentation attributes of an element, style="" winning over attributes."""
     a = dict(el.attrib)
@@ -297,7 +311,7 @@ def _style(el):
 
 
 _INHERITED = ("fill", "stroke", "fill-opacity", "stroke-opacity", "fill-rule", "stroke-width", "stroke-linecap",
-              "stroke-linejoin", "stroke-miterlimit")
+              "stroke-linejoin", "stroke-miterlimit", "stroke-dasharray", "stroke-dashoffset")
 
 
 @dataclass
@@ -524,9 +538,11 @@ def load_svg(text: str, renderer=None) -> SVGScene:
                                     {"round": LineJoin.ROUND, "bevel": LineJoin.BEVEL}.get(
                                         attrs.get("stroke-linejoin"), LineJoin.MITER),
                                     _length(attrs.get("stroke-miterlimit"), 4.0))
-                if "stroke-dasharray" in attrs and attrs["stroke-dasharray"] != "none":
-                    unsupported.add("stroke-dasharray")
-                strokes.append((_outline(contours), style))
+                dashes = _dasharray(attrs.get("stroke-dasharray"))
+                if dashes:
+                    strokes.append((_outline(contours), style, dashes, _length(attrs.get("stroke-dashoffset"), 0.0)))
+                else:
+                    strokes.append((_outline(contours), style))
                 items.append(("stroke", len(strokes) - 1, stroke, sg, clip, m))
             return
         if tag in ("image", "text", "filter", "mask", "pattern", "use", "foreignObject"):

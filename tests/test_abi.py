@@ -41,7 +41,7 @@ def test_library_exports_every_declared_symbol(built):
 STRUCTS = ["PFVector2F", "PFRectF", "PFRectI", "PFColorU", "PFColorF", "PFTransform2F", "PFCUDAPath",
            "PFCUDASceneDesc", "PFCUDABuildOptions", "PFCUDARendererOptions", "PFCUDARenderStats", "PFCUDAFill",
            "PFCUDATile", "PFCUDAClip", "PFCUDASceneParams", "PFCUDAColorStop", "PFCUDAGradient", "PFCUDAPattern", "PFCUDAStrokeStyle",
-           "PFCUDAStrokeInput", "PFCUDAStrokeOutput"]
+           "PFCUDAStrokeInput", "PFCUDAStrokeOutput", "PFCUDADashInput", "PFCUDAOutlineOutput"]
 
 
 def test_struct_layouts_match_ctypes(tmp_path):

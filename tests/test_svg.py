@@ -17,12 +17,18 @@ TIGER = os.path.join(os.environ.get("PATHFINDER_REFERENCE", ""), "resources/svg/
 
 
 class OracleStroker:
-    """The oracle's OutlineStrokeToFill in place of PFCUDAStrokeToFill (CPU tests)."""
+    """The oracle's OutlineDash and OutlineStrokeToFill in place of
+    PFCUDAStrokeToFill(Dashed) (CPU tests)."""
 
     def stroke_to_fill(self, items):
         import oracle
         b = StrokeBatch(items)
-        return outlines_from_buffers(*oracle.stroke(b.desc())[:4])
+        if not b.dashed:
+            return outlines_from_buffers(*oracle.stroke(b.desc())[:4])
+        pts, flags, cs, closed, os_, _ = oracle.dash(b.desc(), b.dash_desc())
+        dashed = outlines_from_buffers(pts, flags, cs, os_, closed)
+        b2 = StrokeBatch([(ol, it[1]) for ol, it in zip(dashed, items)])
+        return outlines_from_buffers(*oracle.stroke(b2.desc())[:4])
 
 
 def test_path_data_commands():
@@ -75,3 +81,29 @@ def test_tiger(built):
     assert (r.fill_count, r.stroke_count) == (130, 52) and not r.unsupported
     img, _ = oracle.OracleFrame(r.scene).render(r.scene.width, r.scene.height)
     assert (img[..., 3] > 0).mean() > 0.6
+
+
+def test_dasharray_attribute():
+    from pathfinder_gb300.svg import _dasharray
+    assert _dasharray(None) is None and _dasharray("none") is None
+    assert _dasharray("4 2") == [4.0, 2.0]
+    assert _dasharray("5,1,2") == [5.0, 1.0, 2.0, 5.0, 1.0, 2.0]  # odd counts repeat
+    assert _dasharray("3 -1") is None and _dasharray("0 0") is None
+
+
+def test_dashed_strokes(built):
+    """A dashed stroke becomes several closed pieces (each dash stroked as an
+    open contour); without a pattern, one ring pair."""
+    doc = ('<svg xmlns="http://www.w3.org/2000/svg" width="64" height="64">'
+           '<g stroke="black" stroke-width="2" fill="none">'
+           '<path d="M4 8 H60" stroke-dasharray="6 4" stroke-dashoffset="1"/>'
+           '<path d="M4 20 H60"/></g></svg>')
+    out = load_svg(doc, OracleStroker())
+    assert out.stroke_count == 2 and "stroke-dasharray" not in out.unsupported
+    sc = out.scene
+    dp = sc.draw_paths
+    assert int(dp[1]["contour_count"]) == 1 and int(dp[0]["contour_count"]) >= 5
+    c0 = int(dp[0]["first_contour"])
+    a, b = int(sc.contour_starts[c0]), int(sc.contour_starts[c0 + int(dp[0]["contour_count"])])
+    ys = sc.points[a:b, 1]
+    assert ys.min() == 7 and ys.max() == 9
