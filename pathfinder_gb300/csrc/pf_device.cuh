@@ -16,6 +16,21 @@
 namespace pf {
 
 // ---------------------------------------------------------------------------
+// Programmatic dependent launch.  A frame kernel may be launched before its
+// predecessor on the stream has finished (pdl_launch), so that its blocks
+// take the multiprocessors as the predecessor's last blocks retire instead of
+// after the grid boundary.  Every such kernel calls pdl_wait() before
+// anything else: it returns once the predecessor grid has completed and its
+// writes are visible (at once when the kernel was launched normally), and as
+// no block of the kernel exits before it, the kernel cannot complete before
+// its predecessor, which keeps the stream's order for whatever follows.
+// pdl_trigger() lets the kernel's own successor be scheduled.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_enter() { pdl_wait(); pdl_trigger(); }
+
+// ---------------------------------------------------------------------------
 // Constants
 // ---------------------------------------------------------------------------
 constexpr uint32_t kInvalid = 0xffffffffu;

@@ -3,6 +3,7 @@
 
 #include "pf_device.cuh"
 
+#include <utility>
 #include <vector>
 
 struct PFCUDAPath;
@@ -190,6 +191,34 @@ int32_t dash_outlines(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in
                       PFCUDAOutlineOutput* out);
 int32_t stroke_dashed(StrokeWork* w, cudaStream_t s, const PFCUDAStrokeInput* in, const PFCUDADashInput* dash,
                       PFCUDAStrokeOutput* out);
+
+// Launch with programmatic stream serialisation while the calling thread's
+// switch is on (frames set it around their launches): the kernel, which must
+// start with pdl_enter(), may be scheduled before its predecessor on the
+// stream has finished.  Launch errors are left for cudaGetLastError, as with
+// the <<< >>> form.
+bool& pdl_switch();
+template <typename... KArgs, typename... Args>
+inline void pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl_switch() ? 1 : 0;
+    (void)cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+// Sets the calling thread's switch for the life of the object.
+struct PdlScope {
+    bool prev;
+    explicit PdlScope(bool on) : prev(pdl_switch()) { pdl_switch() = on; }
+    ~PdlScope() { pdl_switch() = prev; }
+};
 
 // Number of kernels this library has launched (host counter).
 uint64_t launch_counter();

@@ -74,6 +74,7 @@ __device__ __forceinline__ bool frame_screen_tile(const FrameDev& f, const Scene
 // Path sizes are log-normal, so per-path work items would leave a long tail.
 // ---------------------------------------------------------------------------
 __global__ void k_propagate(FrameDev f, int clip_pass) {
+    pdl_enter();
     if (!frame_ok(f) || f.path_count == 0) return;
     const uint32_t T = (uint32_t)f.counters->tiles;
     const uint32_t* offs = f.path.tile_offset + f.path_begin;
@@ -168,13 +169,14 @@ __global__ void k_propagate(FrameDev f, int clip_pass) {
 
 void launch_propagate(const FrameDev& f, bool clip_pass, cudaStream_t s) {
     if (f.path_count == 0) return;
-    { count_launch(); k_propagate<<<f.sms * 16, 256, 0, s>>>(f, clip_pass ? 1 : 0); }
+    { count_launch(); pdl_launch(k_propagate, f.sms * 16, 256, 0, s, f, clip_pass ? 1 : 0); }
 }
 
 // ---------------------------------------------------------------------------
 // visibility: count per screen tile, then scatter global tile indices
 // ---------------------------------------------------------------------------
 __global__ void k_visible(FrameDev f, int scatter) {
+    pdl_enter();
     if (scatter && blockIdx.x == 0 && threadIdx.x == 0 && f.counters->visible > f.vis_cap) {
         atomicOr(&f.counters->status, kStatusVisibleCapacity);  // the visibility scan's total
         f.counters->needed_visible = f.counters->visible;
@@ -229,7 +231,7 @@ __global__ void k_visible(FrameDev f, int scatter) {
 }
 
 void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s) {
-    { count_launch(); k_visible<<<f.sms * 8, 256, 0, s>>>(f, scatter ? 1 : 0); }
+    { count_launch(); pdl_launch(k_visible, f.sms * 8, 256, 0, s, f, scatter ? 1 : 0); }
 }
 
 // ---------------------------------------------------------------------------
@@ -837,6 +839,7 @@ __device__ __forceinline__ bool stage_fills(const FrameDev& f, int4 e, MaskScrat
 }
 
 __global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask(FrameDev f) {
+    pdl_enter();
     __shared__ MaskScratch scratch[kMaskKernelWarps];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     MaskScratch& ws = scratch[wid];
@@ -910,7 +913,7 @@ void launch_mask(const FrameDev& f, cudaStream_t s) {
     if (f.screen_count == 0) return;
     const int blocks = (int)f.sms * resident_blocks(k_mask, kMaskKernelWarps * 32);
     count_launch();
-    k_mask<<<blocks, kMaskKernelWarps * 32, 0, s>>>(f);
+    pdl_launch(k_mask, blocks, kMaskKernelWarps * 32, 0, s, f);
 }
 
 // Composite screen tile st (frame index) into this lane's 8 pixels: n
@@ -1026,6 +1029,7 @@ __device__ __forceinline__ void composite_screen_tile(const FrameDev& f, uint32_
 // against 0.434 at the 111 it takes unbounded, without spills either way).
 template <int MODE, int WARPS, bool PAINT>
 __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_composite(FrameDev f, void* out, float4 bg) {
+    pdl_enter();
     const int lane = threadIdx.x & 31;
     const bool ok = frame_ok(f) && f.counters->fills <= f.fill_cap && f.counters->visible <= f.vis_cap;
     const uint32_t batch = (uint32_t)f.tune.comp_batch;
@@ -1064,7 +1068,7 @@ void launch_composite_instance(const FrameDev& f, void* out, const float4& bg, c
     const uint32_t needed = (f.screen_count + per_block - 1) / per_block;
     const uint32_t resident = f.sms * (uint32_t)resident_blocks(k_composite<MODE, WARPS, PAINT>, threads);
     count_launch();
-    k_composite<MODE, WARPS, PAINT><<<std::max(1u, std::min(needed, resident)), threads, 0, s>>>(f, out, bg);
+    pdl_launch(k_composite<MODE, WARPS, PAINT>, std::max(1u, std::min(needed, resident)), threads, 0, s, f, out, bg);
 }
 
 template <int MODE, int WARPS>
@@ -1146,6 +1150,7 @@ __device__ __forceinline__ void tile_coverage8_diff(const FrameDev& f, int4 rec,
 // composite value below the entry and the coverage derivative codes.
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_composite_diff(FrameDev f, float* out, float4 bg) {
+    pdl_enter();
     __shared__ WarpScratch scratch[WARPS];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t st = blockIdx.x * WARPS + wid;
@@ -1207,7 +1212,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_composite_diff(FrameDev f, float
 void launch_composite_diff(const FrameDev& f, float* out, const float4& bg, cudaStream_t s) {
     if (f.screen_count == 0) return;
     count_launch();
-    k_composite_diff<4><<<(f.screen_count + 3) / 4, 128, 0, s>>>(f, out, bg);
+    pdl_launch(k_composite_diff<4>, (f.screen_count + 3) / 4, 128, 0, s, f, out, bg);
 }
 
 // ---------------------------------------------------------------------------
@@ -1216,6 +1221,7 @@ void launch_composite_diff(const FrameDev& f, float* out, const float4& bg, cuda
 constexpr int kMaskWarps = 4;
 
 __global__ void k_alpha_masks(FrameDev f, float* out) {
+    pdl_enter();
     __shared__ WarpScratch scratch[kMaskWarps];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t a = blockIdx.x * kMaskWarps + wid;
@@ -1230,6 +1236,7 @@ __global__ void k_alpha_masks(FrameDev f, float* out) {
 }
 
 __global__ void k_tile_cov(FrameDev f, float* out) {
+    pdl_enter();
     __shared__ WarpScratch scratch[kMaskWarps];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t g = blockIdx.x * kMaskWarps + wid;
@@ -1248,8 +1255,8 @@ __global__ void k_tile_cov(FrameDev f, float* out) {
 
 void launch_masks(const FrameDev& f, float* alpha_masks, float* tile_cov, cudaStream_t s) {
     uint32_t blocks = (f.tile_cap + kMaskWarps - 1) / kMaskWarps + 1;
-    if (alpha_masks) { count_launch(); k_alpha_masks<<<blocks, kMaskWarps * 32, 0, s>>>(f, alpha_masks); }
-    if (tile_cov) { count_launch(); k_tile_cov<<<blocks, kMaskWarps * 32, 0, s>>>(f, tile_cov); }
+    if (alpha_masks) { count_launch(); pdl_launch(k_alpha_masks, blocks, kMaskWarps * 32, 0, s, f, alpha_masks); }
+    if (tile_cov) { count_launch(); pdl_launch(k_tile_cov, blocks, kMaskWarps * 32, 0, s, f, tile_cov); }
 }
 
 }  // namespace pf

@@ -430,6 +430,8 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     cudaStream_t s = r->stream;
     bool transformed = !is_identity(opts);
     cudaError_t e;
+    // each frame kernel may start while its predecessor on its stream drains
+    PdlScope pdl(true);
     if (transformed) {
         if ((e = r->pts_t.ensure(r->NP))) return e;
         float m6[6] = {opts->transform.m00, opts->transform.m01, opts->transform.m10, opts->transform.m11,

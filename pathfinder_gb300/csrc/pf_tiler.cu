@@ -22,6 +22,7 @@ namespace pf {
 static std::atomic<uint64_t> g_launches{0};
 uint64_t launch_counter() { return g_launches.load(); }
 void count_launch(uint32_t n) { g_launches += n; }
+bool& pdl_switch() { static thread_local bool on = false; return on; }
 
 int resident_blocks_of(const void* kernel, int threads) {
     struct Entry { int dev; const void* kernel; int threads, blocks; };
@@ -166,6 +167,7 @@ __device__ __forceinline__ void store8(uint32_t* out, uint32_t first, uint32_t n
 
 __global__ void k_scan_reduce(const uint32_t* __restrict__ in, const uint64_t* d_n, uint32_t n_host, int mode,
                               uint32_t* __restrict__ partials) {
+    pdl_enter();
     uint32_t n = scan_count(d_n, n_host);
     uint32_t base = blockIdx.x * kScanChunk;
     if (base >= n) return;
@@ -179,6 +181,7 @@ __global__ void k_scan_reduce(const uint32_t* __restrict__ in, const uint64_t* d
 
 __global__ void k_scan_partials(uint32_t* partials, const uint64_t* d_n, uint32_t n_host, uint32_t* out,
                                 uint64_t* total_out) {
+    pdl_enter();
     uint32_t n = scan_count(d_n, n_host);
     uint32_t nb = (n + kScanChunk - 1) / kScanChunk;
     uint32_t carry = 0;
@@ -198,6 +201,7 @@ __global__ void k_scan_partials(uint32_t* partials, const uint64_t* d_n, uint32_
 
 __global__ void k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, const uint64_t* d_n,
                             uint32_t n_host, int mode, const uint32_t* __restrict__ partials) {
+    pdl_enter();
     uint32_t n = scan_count(d_n, n_host);
     uint32_t base = blockIdx.x * kScanChunk;
     if (base >= n) return;
@@ -276,6 +280,7 @@ __device__ __forceinline__ unsigned long long look_back(unsigned long long* word
 template <int NL>
 __global__ void __launch_bounds__(kScanThreads) k_scan_onepass(ScanLanes L, const uint64_t* d_n, uint32_t n_cap,
                                                                unsigned long long* lb, uint32_t nb, uint32_t* status) {
+    pdl_enter();
     __shared__ uint32_t tile_sh;
     __shared__ unsigned long long prefix_sh;
     if (threadIdx.x == 0) tile_sh = atomicAdd(reinterpret_cast<unsigned int*>(lb), 1u);
@@ -331,7 +336,7 @@ static bool launch_scan_onepass(const ScanLanes& lanes, const uint64_t* d_n, uin
     unsigned long long* lb = tmp.lookback + tmp.lookback_used;
     tmp.lookback_used += (uint32_t)words;
     count_launch();
-    k_scan_onepass<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, lb, nb, tmp.status);
+    pdl_launch(k_scan_onepass<NL>, nb, kScanThreads, 0, s, lanes, d_n, n_cap, lb, nb, tmp.status);
     return true;
 }
 
@@ -357,13 +362,13 @@ void launch_scan(const uint32_t* in, uint32_t* out, const uint64_t* d_n, uint32_
         ScanLanes one{};
         one.count = 1;
         one.in[0] = in; one.out[0] = out; one.total[0] = total_out; one.mode[0] = mode;
-        { count_launch(); k_scanm_reduce<1><<<nb, kScanThreads, 0, s>>>(one, d_n, n_host, tmp.partials); }
-        { count_launch(); k_scanm_down_fused<1><<<nb, kScanThreads, 0, s>>>(one, d_n, n_host, tmp.partials); }
+        { count_launch(); pdl_launch(k_scanm_reduce<1>, nb, kScanThreads, 0, s, one, d_n, n_host, tmp.partials); }
+        { count_launch(); pdl_launch(k_scanm_down_fused<1>, nb, kScanThreads, 0, s, one, d_n, n_host, tmp.partials); }
         return;
     }
-    { count_launch(); k_scan_reduce<<<nb, kScanThreads, 0, s>>>(in, d_n, n_host, mode, tmp.partials); }
-    { count_launch(); k_scan_partials<<<1, 1024, 0, s>>>(tmp.partials, d_n, n_host, out, total_out); }
-    { count_launch(); k_scan_down<<<nb, kScanThreads, 0, s>>>(in, out, d_n, n_host, mode, tmp.partials); }
+    { count_launch(); pdl_launch(k_scan_reduce, nb, kScanThreads, 0, s, in, d_n, n_host, mode, tmp.partials); }
+    { count_launch(); pdl_launch(k_scan_partials, 1, 1024, 0, s, tmp.partials, d_n, n_host, out, total_out); }
+    { count_launch(); pdl_launch(k_scan_down, nb, kScanThreads, 0, s, in, out, d_n, n_host, mode, tmp.partials); }
 }
 
 cudaError_t launch_scan_checked(const uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& tmp, cudaStream_t s) {
@@ -392,6 +397,7 @@ cudaError_t launch_scan_checked(const uint32_t* in, uint32_t* out, uint32_t n, S
 // lane table to local memory).
 template <int NL>
 __global__ void k_scanm_reduce(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, uint32_t* __restrict__ partials) {
+    pdl_enter();
     const uint32_t n = scan_count(d_n, n_cap);
     const uint32_t base = blockIdx.x * kScanChunk;
     if (base >= n) return;
@@ -409,6 +415,7 @@ __global__ void k_scanm_reduce(ScanLanes L, const uint64_t* d_n, uint32_t n_cap,
 
 template <int NL>
 __global__ void k_scanm_partials(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, uint32_t* partials) {
+    pdl_enter();
     const uint32_t n = scan_count(d_n, n_cap);
     const uint32_t nb = (n + kScanChunk - 1) / kScanChunk, nbc = (n_cap + kScanChunk - 1) / kScanChunk;
 #pragma unroll
@@ -432,6 +439,7 @@ __global__ void k_scanm_partials(ScanLanes L, const uint64_t* d_n, uint32_t n_ca
 
 template <int NL>
 __global__ void k_scanm_down(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, const uint32_t* __restrict__ partials) {
+    pdl_enter();
     const uint32_t n = scan_count(d_n, n_cap);
     const uint32_t base = blockIdx.x * kScanChunk;
     if (base >= n) return;
@@ -463,6 +471,7 @@ __global__ void k_scanm_down(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, c
 template <int NL>
 __global__ void k_scanm_down_fused(ScanLanes L, const uint64_t* d_n, uint32_t n_cap,
                                    const uint32_t* __restrict__ partials) {
+    pdl_enter();
     const uint32_t n = scan_count(d_n, n_cap);
     const uint32_t base = blockIdx.x * kScanChunk;
     const uint32_t nbc = (n_cap + kScanChunk - 1) / kScanChunk, nb = (n + kScanChunk - 1) / kScanChunk;
@@ -510,13 +519,13 @@ static void launch_scan_lanes(const ScanLanes& lanes, const uint64_t* d_n, uint3
     uint32_t nb = (n_cap + kScanChunk - 1) / kScanChunk;
     if (nb == 0) nb = 1;
     if (nb <= kFusedScanBlocks) {
-        { count_launch(); k_scanm_reduce<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
-        { count_launch(); k_scanm_down_fused<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+        { count_launch(); pdl_launch(k_scanm_reduce<NL>, nb, kScanThreads, 0, s, lanes, d_n, n_cap, tmp.partials); }
+        { count_launch(); pdl_launch(k_scanm_down_fused<NL>, nb, kScanThreads, 0, s, lanes, d_n, n_cap, tmp.partials); }
         return;
     }
-    { count_launch(); k_scanm_reduce<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
-    { count_launch(); k_scanm_partials<NL><<<1, 1024, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
-    { count_launch(); k_scanm_down<NL><<<nb, kScanThreads, 0, s>>>(lanes, d_n, n_cap, tmp.partials); }
+    { count_launch(); pdl_launch(k_scanm_reduce<NL>, nb, kScanThreads, 0, s, lanes, d_n, n_cap, tmp.partials); }
+    { count_launch(); pdl_launch(k_scanm_partials<NL>, 1, 1024, 0, s, lanes, d_n, n_cap, tmp.partials); }
+    { count_launch(); pdl_launch(k_scanm_down<NL>, nb, kScanThreads, 0, s, lanes, d_n, n_cap, tmp.partials); }
 }
 
 void launch_scan_multi(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp, cudaStream_t s) {
@@ -643,6 +652,7 @@ void launch_contour_segemit(const uint32_t* ord_contour, const uint32_t* ord_pat
 // bound: one warp per path
 // ---------------------------------------------------------------------------
 __global__ void k_bound(FrameDev f, const uint32_t* __restrict__ ord_contour, const uint32_t* __restrict__ starts) {
+    pdl_enter();
     const uint32_t wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (wi >= f.path_count) return;
@@ -707,7 +717,7 @@ __global__ void k_bound(FrameDev f, const uint32_t* __restrict__ ord_contour, co
 void launch_bound(const FrameDev& f, const uint32_t* ord_contour, const uint32_t* starts, cudaStream_t s) {
     if (f.path_count == 0) return;
     uint32_t blocks = (f.path_count * 32 + 255) / 256;
-    { count_launch(); k_bound<<<blocks, 256, 0, s>>>(f, ord_contour, starts); }
+    { count_launch(); pdl_launch(k_bound, blocks, 256, 0, s, f, ord_contour, starts); }
 }
 
 // A path's binning context from its tile rect, its scanned offsets and its
@@ -729,6 +739,7 @@ __device__ __forceinline__ PathCtx path_ctx(const FrameDev& f, uint32_t gp) {
 // the path scans' totals against the capacities (one kernel instead of a
 // check kernel and two memsets).
 __global__ void k_zero_tiles(FrameDev f) {
+    pdl_enter();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < f.path_count; i += gridDim.x * blockDim.x)
         f.path_bin[f.path_begin + i] = path_ctx(f, f.path_begin + i);
     uint64_t T = f.counters->tiles, C = f.counters->columns;
@@ -759,7 +770,7 @@ void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     lanes.in[1] = f.path_cols + f.path_begin; lanes.out[1] = f.path.col_offset + f.path_begin;
     lanes.total[1] = &f.counters->columns;
     launch_scan_multi(lanes, nullptr, f.path_count, tmp, s);
-    { count_launch(); k_zero_tiles<<<f.sms * 8, 256, 0, s>>>(f); }
+    { count_launch(); pdl_launch(k_zero_tiles, f.sms * 8, 256, 0, s, f); }
 }
 
 // Launch bounds: the flattening passes run at 32 registers a thread (64 warps
@@ -823,6 +834,7 @@ struct FlattenWarp {
 };
 
 __global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
+    pdl_enter();
     __shared__ FlattenWarp smw[kFlattenMaxWarps];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     FlattenWarp& w = smw[wib];
@@ -890,6 +902,7 @@ __global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
 // adjoint holds these subdivisions fixed.
 template <bool DIFF>
 __global__ void __launch_bounds__(256, 8) k_flatten_emit(FrameDev f) {
+    pdl_enter();
     __shared__ Cubic roots[kFlattenMaxWarps][32];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t s0 = (blockIdx.x * (blockDim.x >> 5) + wib) * 32u;
@@ -971,6 +984,7 @@ __global__ void __launch_bounds__(256, 8) k_flatten_emit(FrameDev f) {
 
 // The D3D11 level's uniform dicing: one thread per input segment.
 __global__ void __launch_bounds__(256, 6) k_dice_count(FrameDev f) {
+    pdl_enter();
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= f.seg_count) return;
     uint32_t n = 0;
@@ -983,6 +997,7 @@ __global__ void __launch_bounds__(256, 6) k_dice_count(FrameDev f) {
 }
 
 __global__ void __launch_bounds__(256, 6) k_dice_emit(FrameDev f) {
+    pdl_enter();
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s == 0 && f.counters->lines > f.line_cap) {  // the dicing scan's total against the capacity
         atomicOr(&f.counters->status, kStatusLineCapacity);
@@ -1012,8 +1027,8 @@ void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     const uint32_t blocks = dice ? (f.seg_count + ft - 1) / ft
                                  : (uint32_t)(((uint64_t)f.seg_count + 31) / 32 * 32 + ft - 1) / ft;
     count_launch();
-    if (dice) k_dice_count<<<blocks, ft, 0, s>>>(f);
-    else k_flatten_count<<<blocks, ft, 0, s>>>(f);
+    if (dice) pdl_launch(k_dice_count, blocks, ft, 0, s, f);
+    else pdl_launch(k_flatten_count, blocks, ft, 0, s, f);
     if (dice) {
         launch_scan(f.seg_line_count, f.seg_line_base, nullptr, f.seg_count, f.seg_count, 0, &f.counters->lines, tmp,
                     s);
@@ -1022,9 +1037,9 @@ void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
         launch_scan(f.seg_warp_lines, f.seg_warp_base, nullptr, warps, warps, 0, &f.counters->lines, tmp, s);
     }
     count_launch();
-    if (dice) k_dice_emit<<<blocks, ft, 0, s>>>(f);
-    else if (f.diff) k_flatten_emit<true><<<blocks, ft, 0, s>>>(f);
-    else k_flatten_emit<false><<<blocks, ft, 0, s>>>(f);
+    if (dice) pdl_launch(k_dice_emit, blocks, ft, 0, s, f);
+    else if (f.diff) pdl_launch(k_flatten_emit<true>, blocks, ft, 0, s, f);
+    else pdl_launch(k_flatten_emit<false>, blocks, ft, 0, s, f);
 }
 
 // ---------------------------------------------------------------------------
@@ -1060,6 +1075,7 @@ struct CountSink {
 
 template <int MODE>
 __global__ void __launch_bounds__(512, 3) k_bin_count(FrameDev f) {
+    pdl_enter();
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     const uint32_t L = line_total(f);
     for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
@@ -1123,6 +1139,7 @@ struct EmitSinkF {
 
 template <int MODE, bool ORDER>
 __global__ void __launch_bounds__(512, 3) k_bin_emit(const __grid_constant__ FrameDev f) {
+    pdl_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) {  // the binning scans' totals against the capacities
         if (f.counters->fills > f.fill_cap) {
             atomicOr(&f.counters->status, kStatusFillCapacity);
@@ -1161,9 +1178,9 @@ void launch_bin_count(const FrameDev& f, cudaStream_t s) {
     count_launch();
     const uint32_t blocks = f.sms * f.tune.bin_blocks_per_sm;
     const int m = fill_mode(f);
-    if (m == kFillF32) k_bin_count<kFillF32><<<blocks, f.tune.bin_threads, 0, s>>>(f);
-    else if (m == kFillD3D11) k_bin_count<kFillD3D11><<<blocks, f.tune.bin_threads, 0, s>>>(f);
-    else k_bin_count<kFillCpu><<<blocks, f.tune.bin_threads, 0, s>>>(f);
+    if (m == kFillF32) pdl_launch(k_bin_count<kFillF32>, blocks, f.tune.bin_threads, 0, s, f);
+    else if (m == kFillD3D11) pdl_launch(k_bin_count<kFillD3D11>, blocks, f.tune.bin_threads, 0, s, f);
+    else pdl_launch(k_bin_count<kFillCpu>, blocks, f.tune.bin_threads, 0, s, f);
 }
 
 // The emit pass runs beside propagation and visibility: two waves of
@@ -1180,13 +1197,13 @@ void launch_bin_emit(const FrameDev& f, cudaStream_t s) {
     const int m = fill_mode(f);
     const int t = f.tune.bin_threads;
     const bool order = f.fill_e != nullptr;
-    if (m == kFillF32) k_bin_emit<kFillF32, false><<<emit_blocks(f, k_bin_emit<kFillF32, false>, t), t, 0, s>>>(f);
+    if (m == kFillF32) pdl_launch(k_bin_emit<kFillF32, false>, emit_blocks(f, k_bin_emit<kFillF32, false>, t), t, 0, s, f);
     else if (m == kFillD3D11 && order)
-        k_bin_emit<kFillD3D11, true><<<emit_blocks(f, k_bin_emit<kFillD3D11, true>, t), t, 0, s>>>(f);
+        pdl_launch(k_bin_emit<kFillD3D11, true>, emit_blocks(f, k_bin_emit<kFillD3D11, true>, t), t, 0, s, f);
     else if (m == kFillD3D11)
-        k_bin_emit<kFillD3D11, false><<<emit_blocks(f, k_bin_emit<kFillD3D11, false>, t), t, 0, s>>>(f);
-    else if (order) k_bin_emit<kFillCpu, true><<<emit_blocks(f, k_bin_emit<kFillCpu, true>, t), t, 0, s>>>(f);
-    else k_bin_emit<kFillCpu, false><<<emit_blocks(f, k_bin_emit<kFillCpu, false>, t), t, 0, s>>>(f);
+        pdl_launch(k_bin_emit<kFillD3D11, false>, emit_blocks(f, k_bin_emit<kFillD3D11, false>, t), t, 0, s, f);
+    else if (order) pdl_launch(k_bin_emit<kFillCpu, true>, emit_blocks(f, k_bin_emit<kFillCpu, true>, t), t, 0, s, f);
+    else pdl_launch(k_bin_emit<kFillCpu, false>, emit_blocks(f, k_bin_emit<kFillCpu, false>, t), t, 0, s, f);
 }
 
 }  // namespace pf
