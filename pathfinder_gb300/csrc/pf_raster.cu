@@ -944,18 +944,21 @@ __device__ __forceinline__ void composite_screen_tile(const FrameDev& f, uint32_
     } else {
         warp_bitonic_sort(f.vis_key + base, n);
     }
-    // entry i of the draw order: slot, paint, meta; its coverage is fetched
-    // one entry ahead
-    // Entry i: its slot, then (read whatever the entry's kind: a solid entry's
-    // slot holds no coverage, and the value is not used) its coverage, then
-    // its record; the coverage read starts before the record is waited for.
+    // Entry i of the draw order: its slot, record and coverage, fetched one
+    // entry ahead.  A short list has every record in the lanes, so a solid
+    // entry (whose slot holds no coverage) skips the coverage read; a long
+    // list reads the coverage whatever the entry's kind, starting it before
+    // the record is waited for (a solid entry's value is not used).
     auto entry = [&](uint32_t i, uint32_t& slot, uint4& mask, uint32_t& paint, uint32_t& meta) {
-        slot = lane_list ? __shfl_sync(0xffffffffu, (uint32_t)lane_key, (int)i) : (uint32_t)f.vis_key[base + i];
-        mask = f.vis_mask[(size_t)slot * 32u + (uint32_t)lane];
         if (lane_list) {
+            slot = __shfl_sync(0xffffffffu, (uint32_t)lane_key, (int)i);
             paint = (uint32_t)__shfl_sync(0xffffffffu, lane_info.x, (int)i);
             meta = (uint32_t)__shfl_sync(0xffffffffu, lane_info.y, (int)i);
+            mask = ((meta >> 9) & 3u) != kVisSolid ? f.vis_mask[(size_t)slot * 32u + (uint32_t)lane]
+                                                   : make_uint4(0u, 0u, 0u, 0u);
         } else {
+            slot = (uint32_t)f.vis_key[base + i];
+            mask = f.vis_mask[(size_t)slot * 32u + (uint32_t)lane];
             const int4 info = f.vis_info[slot];
             paint = (uint32_t)info.z;
             meta = (uint32_t)info.w;
