@@ -408,11 +408,15 @@ typedef struct PFCUDATuning {
                                     resident blocks beside propagation and visibility) */
     int32_t composite_warps;     /* 2, 4 or 8 */
     int32_t composite_batch;     /* screen tiles per work item of the persistent composite: 1, 2, 4 or 8 */
+    int32_t mask_stage_fills;    /* 0: the fill pass reads each mask tile's fills from global memory (the
+                                    default); 1 .. 128: ranges of at least this many fills are copied into
+                                    shared memory by bulk copy (cp.async.bulk + mbarrier), one work item
+                                    ahead of their use */
 } PFCUDATuning;
 int32_t PFCUDASetTuning(PFCUDARendererRef renderer, const PFCUDATuning* tuning);
 int32_t PFCUDAGetTuning(PFCUDARendererRef renderer, PFCUDATuning* out_tuning);
 /* Autotuner: times `repeats` frames of the given range per candidate shape
- * (coordinate descent over the five parameters), keeps the fastest and
+ * (coordinate descent over the six parameters), keeps the fastest and
  * returns it.  Synchronises. */
 int32_t PFCUDAAutotune(PFCUDARendererRef renderer, const PFCUDABuildOptions* options,
                        uint32_t first_scene, uint32_t scene_count, int32_t format, void* out_device,

@@ -193,7 +193,7 @@ class PFCUDASceneTarget(C.Structure):
 
 class PFCUDATuning(C.Structure):
     _fields_ = [("flatten_threads", C.c_int32), ("bin_threads", C.c_int32), ("bin_blocks_per_sm", C.c_int32),
-                ("composite_warps", C.c_int32), ("composite_batch", C.c_int32)]
+                ("composite_warps", C.c_int32), ("composite_batch", C.c_int32), ("mask_stage_fills", C.c_int32)]
 
 
 PF_CUDA_FORMAT_RGBA8 = 0

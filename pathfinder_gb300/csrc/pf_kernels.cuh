@@ -17,6 +17,7 @@ struct TuneParams {
     int bin_blocks_per_sm; // grid of the binning passes = SMs x this
     int comp_warps;        // warps per block of the composite (2, 4 or 8)
     int comp_batch;        // screen tiles per work item of the persistent composite (1, 2, 4 or 8)
+    int mask_stage;        // fill ranges of at least this many fills staged by bulk copy (0: none)
 };
 
 // One frame covers a contiguous range of the uploaded scenes; paths,

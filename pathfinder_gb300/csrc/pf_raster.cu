@@ -810,12 +810,15 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t pari
     return false;
 }
 
-// k_mask: each warp takes every (total warps)-th entry of the mask work list.
-// An entry's fill range is copied into the warp's shared memory by one bulk
-// copy (rounded out to 16-byte boundaries) one entry ahead of its use, and
-// the work list itself is read two entries ahead, so a warp waits on neither.
-// Ranges larger than a staging buffer, and clip-combined or clip-chain tiles
-// (which read tile and clip records), are read from global memory.
+// The fill pass (k_mask): each warp takes every (total warps)-th entry of
+// the mask work list and writes the entry's resolved coverage to its slot.
+// Two forms: by default the fills are read from global memory by the lanes
+// that accumulate them (the work list read two entries ahead); with the
+// tuning knob mask_stage_fills, a fill range of at least that many fills is
+// copied into the warp's shared memory by one bulk copy (rounded out to
+// 16-byte boundaries) one entry ahead of its use.  Ranges larger than a
+// staging buffer, and clip-combined or clip-chain tiles (which read tile and
+// clip records), are read from global memory in both.
 constexpr int kMaskKernelWarps = 4;
 constexpr uint32_t kStageFills = 128;  // per staging buffer (1 KiB)
 struct MaskScratch {
@@ -824,11 +827,62 @@ struct MaskScratch {
     unsigned long long bar[2];
 };
 
+// Coverage of work-list entry e, with a mask entry's fills read from src, to
+// the entry's slot.
+__device__ __forceinline__ void mask_entry(const FrameDev& f, int4 e, const uint2* src, CovBuf& b0, CovBuf& b1) {
+    const uint32_t kind = ((uint32_t)e.z >> 9) & 3u, slot = (uint32_t)e.w;
+    float cov[8];
+    if (kind == kVisMask) {
+        int v[8];
+        warp_accumulate_packed(src, (uint32_t)e.y, b0);
+        warp_column_values(b0, v);
+        __syncwarp();  // the buffer is cleared by the next tile
+        const bool even_odd = ((uint32_t)e.z >> 8) & 1u;
+        const float bd = (float)(int8_t)(e.z & 0xff);
+#pragma unroll
+        for (int q = 0; q < 8; q++) cov[q] = resolve_coverage((float)v[q] * kCovInvScale + bd, even_odd);
+    } else {  // clip-combined or behind a clip chain: from the tile and clip records
+        const uint32_t g = (uint32_t)(f.vis_key[slot] >> 32);
+        tile_coverage8(f, f.tiles[g], g, b0, b1, cov);
+    }
+    f.vis_mask[(size_t)slot * 32u + (uint32_t)(threadIdx.x & 31)] = pack_cov16(cov);
+}
+
+__device__ __forceinline__ bool mask_pass_ok(const FrameDev& f) {
+    return frame_ok(f) && f.counters->fills <= f.fill_cap && f.counters->visible <= f.vis_cap;
+}
+__device__ __forceinline__ uint32_t mask_entry_count(const FrameDev& f) {
+    return (uint32_t)min((unsigned long long)f.counters->mask_items, (unsigned long long)f.vis_cap);
+}
+
+__global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask(FrameDev f) {
+    pdl_enter();
+    __shared__ CovBuf bufs[kMaskKernelWarps][2];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (!mask_pass_ok(f)) return;
+    const uint32_t M = mask_entry_count(f);
+    const uint32_t stride = gridDim.x * kMaskKernelWarps;
+    uint32_t k = blockIdx.x * kMaskKernelWarps + wid;
+    if (k >= M) return;
+    const int4 none = make_int4(0, 0, 0, 0);
+    int4 cur = f.mask_items[k];
+    int4 nxt = k + stride < M ? f.mask_items[k + stride] : none;
+    unsigned long long fills_read = 0;  // the fills of this warp's tiles (frame statistics)
+    for (; k < M; k += stride) {
+        const int4 later = k + 2 * stride < M ? f.mask_items[k + 2 * stride] : none;
+        fills_read += (uint32_t)cur.y;
+        mask_entry(f, cur, f.fills + (uint32_t)cur.x, bufs[wid][0], bufs[wid][1]);
+        cur = nxt;
+        nxt = later;
+    }
+    if (lane == 0) atomicAdd((unsigned long long*)&f.counters->mask_fills, fills_read);
+}
+
 // Issue the bulk copy of entry `e`'s fills into staging buffer `buf` (lane 0;
 // every lane gets the same answer: whether it was issued).
 __device__ __forceinline__ bool stage_fills(const FrameDev& f, int4 e, MaskScratch& ws, int buf) {
     const uint32_t kind = ((uint32_t)e.z >> 9) & 3u;
-    if (kind != kVisMask || e.y == 0) return false;
+    if (kind != kVisMask || e.y == 0 || e.y < f.tune.mask_stage) return false;
     const uint32_t first = (uint32_t)e.x & ~1u, end = ((uint32_t)e.x + (uint32_t)e.y + 1u) & ~1u;
     if (end - first > kStageFills) return false;
     if ((threadIdx.x & 31) == 0) {
@@ -838,13 +892,15 @@ __device__ __forceinline__ bool stage_fills(const FrameDev& f, int4 e, MaskScrat
     return true;
 }
 
-__global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask(FrameDev f) {
+// The staged form: the work list is read two entries ahead and the fills of
+// the next entry are in flight while the current one accumulates.
+__global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask_staged(FrameDev f) {
     pdl_enter();
     __shared__ MaskScratch scratch[kMaskKernelWarps];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     MaskScratch& ws = scratch[wid];
-    if (!frame_ok(f) || f.counters->fills > f.fill_cap || f.counters->visible > f.vis_cap) return;
-    const uint32_t M = (uint32_t)min((unsigned long long)f.counters->mask_items, (unsigned long long)f.vis_cap);
+    if (!mask_pass_ok(f)) return;
+    const uint32_t M = mask_entry_count(f);
     const uint32_t stride = gridDim.x * kMaskKernelWarps;
     uint32_t k = blockIdx.x * kMaskKernelWarps + wid;
     if (k >= M) return;
@@ -854,7 +910,7 @@ __global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask(FrameDev f) {
         fence_mbar_init();
     }
     __syncwarp();
-    const int4 none = make_int4(0, 0, 0, 0);  // a solid entry: no work
+    const int4 none = make_int4(0, 0, 0, 0);  // past the list: no work
     int4 cur = f.mask_items[k];
     int4 nxt = k + stride < M ? f.mask_items[k + stride] : none;
     uint32_t phase = 0;  // bit b: parity of the next completion of buffer b
@@ -863,41 +919,26 @@ __global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask(FrameDev f) {
     bool stalled = false;
     int stall_buf = 0;
     uint32_t stall_parity = 0;
-    unsigned long long fills_read = 0;  // the fills of this warp's tiles (frame statistics)
+    unsigned long long fills_read = 0;
     for (; k < M; k += stride) {
         const int4 later = k + 2 * stride < M ? f.mask_items[k + 2 * stride] : none;
         const bool nxt_staged = !stalled && stage_fills(f, nxt, ws, buf ^ 1);
-        const uint32_t kind = ((uint32_t)cur.z >> 9) & 3u, slot = (uint32_t)cur.w;
         fills_read += (uint32_t)cur.y;
-        float cov[8];
-        if (kind == kVisMask) {
-            const uint2* src = f.fills + (uint32_t)cur.x;
-            if (cur_staged) {
-                const uint32_t parity = (phase >> buf) & 1u;
-                const bool arrived = mbar_wait(&ws.bar[buf], parity);
-                phase ^= 1u << buf;
-                if (arrived) {
-                    src = ws.stage[buf] + ((uint32_t)cur.x & 1u);
-                } else if (!stalled) {
-                    stalled = true;  // no more copies: read global memory from here on
-                    stall_buf = buf;
-                    stall_parity = parity;
-                    if (lane == 0) atomicOr(&f.counters->status, kStatusCopyStall);
-                }
+        const uint2* src = f.fills + (uint32_t)cur.x;
+        if (cur_staged) {
+            const uint32_t parity = (phase >> buf) & 1u;
+            const bool arrived = mbar_wait(&ws.bar[buf], parity);
+            phase ^= 1u << buf;
+            if (arrived) {
+                src = ws.stage[buf] + ((uint32_t)cur.x & 1u);
+            } else if (!stalled) {
+                stalled = true;  // no more copies: read global memory from here on
+                stall_buf = buf;
+                stall_parity = parity;
+                if (lane == 0) atomicOr(&f.counters->status, kStatusCopyStall);
             }
-            int v[8];
-            warp_accumulate_packed(src, (uint32_t)cur.y, ws.b0);
-            warp_column_values(ws.b0, v);
-            __syncwarp();  // the buffer is cleared by the next tile
-            const bool even_odd = ((uint32_t)cur.z >> 8) & 1u;
-            const float bd = (float)(int8_t)(cur.z & 0xff);
-#pragma unroll
-            for (int q = 0; q < 8; q++) cov[q] = resolve_coverage((float)v[q] * kCovInvScale + bd, even_odd);
-        } else {  // clip-combined or behind a clip chain: from the tile and clip records
-            const uint32_t g = (uint32_t)(f.vis_key[slot] >> 32);
-            tile_coverage8(f, f.tiles[g], g, ws.b0, ws.b1, cov);
         }
-        f.vis_mask[(size_t)slot * 32u + (uint32_t)lane] = pack_cov16(cov);
+        mask_entry(f, cur, src, ws.b0, ws.b1);
         cur = nxt;
         nxt = later;
         cur_staged = nxt_staged;
@@ -911,9 +952,14 @@ __global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask(FrameDev f) {
 
 void launch_mask(const FrameDev& f, cudaStream_t s) {
     if (f.screen_count == 0) return;
-    const int blocks = (int)f.sms * resident_blocks(k_mask, kMaskKernelWarps * 32);
     count_launch();
-    pdl_launch(k_mask, blocks, kMaskKernelWarps * 32, 0, s, f);
+    if (f.tune.mask_stage > 0) {
+        const int blocks = (int)f.sms * resident_blocks(k_mask_staged, kMaskKernelWarps * 32);
+        pdl_launch(k_mask_staged, blocks, kMaskKernelWarps * 32, 0, s, f);
+    } else {
+        const int blocks = (int)f.sms * resident_blocks(k_mask, kMaskKernelWarps * 32);
+        pdl_launch(k_mask, blocks, kMaskKernelWarps * 32, 0, s, f);
+    }
 }
 
 // Composite screen tile st (frame index) into this lane's 8 pixels: n

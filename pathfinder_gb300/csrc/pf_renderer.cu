@@ -116,7 +116,7 @@ struct Range {
     uint32_t st0 = 0, st1 = 0;   // screen tiles
 };
 
-const TuneParams kDefaultTune{128, 256, 32, 4, 2};
+const TuneParams kDefaultTune{128, 256, 32, 4, 2, 0};
 
 }  // namespace
 
@@ -1330,10 +1330,10 @@ int32_t PFCUDASetTuning(PFCUDARendererRef r, const PFCUDATuning* t) {
     auto in = [](int v, std::initializer_list<int> ok) { return std::find(ok.begin(), ok.end(), v) != ok.end(); };
     if (!in(t->flatten_threads, {64, 128, 256}) || !in(t->bin_threads, {128, 256, 512}) ||
         t->bin_blocks_per_sm < 4 || t->bin_blocks_per_sm > 64 || !in(t->composite_warps, {2, 4, 8}) ||
-        !in(t->composite_batch, {1, 2, 4, 8}))
+        !in(t->composite_batch, {1, 2, 4, 8}) || t->mask_stage_fills < 0 || t->mask_stage_fills > 128)
         return PF_CUDA_ERR_INVALID;
     r->tune = TuneParams{t->flatten_threads, t->bin_threads, t->bin_blocks_per_sm, t->composite_warps,
-                         t->composite_batch};
+                         t->composite_batch, t->mask_stage_fills};
     release_graph(r);
     return PF_CUDA_OK;
 }
@@ -1341,7 +1341,7 @@ int32_t PFCUDASetTuning(PFCUDARendererRef r, const PFCUDATuning* t) {
 int32_t PFCUDAGetTuning(PFCUDARendererRef r, PFCUDATuning* t) {
     if (!r || !t) return PF_CUDA_ERR_INVALID;
     *t = PFCUDATuning{r->tune.flatten_threads, r->tune.bin_threads, r->tune.bin_blocks_per_sm, r->tune.comp_warps,
-                      r->tune.comp_batch};
+                      r->tune.comp_batch, r->tune.mask_stage};
     return PF_CUDA_OK;
 }
 
@@ -1373,9 +1373,9 @@ int32_t PFCUDAAutotune(PFCUDARendererRef r, const PFCUDABuildOptions* options, u
     float best_ms = 0;
     if ((rc = time_it(best, &best_ms))) return rc;
     const int flat[] = {64, 128, 256}, bin[] = {128, 256, 512}, bps[] = {4, 8, 16, 32}, cw[] = {2, 4, 8},
-              cb[] = {1, 2, 4, 8};
-    for (int dim = 0; dim < 5; dim++) {
-        const int* cand = dim == 0 ? flat : dim == 1 ? bin : dim == 2 ? bps : dim == 3 ? cw : cb;
+              cb[] = {1, 2, 4, 8}, ms[] = {0, 8, 32};
+    for (int dim = 0; dim < 6; dim++) {
+        const int* cand = dim == 0 ? flat : dim == 1 ? bin : dim == 2 ? bps : dim == 3 ? cw : dim == 4 ? cb : ms;
         const int nc = (dim == 2 || dim == 4) ? 4 : 3;
         for (int i = 0; i < nc; i++) {
             TuneParams tp = best;
@@ -1384,6 +1384,7 @@ int32_t PFCUDAAutotune(PFCUDARendererRef r, const PFCUDABuildOptions* options, u
             if (dim == 2) tp.bin_blocks_per_sm = cand[i];
             if (dim == 3) tp.comp_warps = cand[i];
             if (dim == 4) tp.comp_batch = cand[i];
+            if (dim == 5) tp.mask_stage = cand[i];
             float ms = 0;
             if ((rc = time_it(tp, &ms))) return rc;
             if (ms < best_ms) { best_ms = ms; best = tp; }

@@ -76,14 +76,37 @@ def test_autotune_changes_speed_not_pixels(renderer):
     out = torch.zeros_like(ref)
     best = renderer.autotune(batch, out, pf.PF_CUDA_FORMAT_RGBA8, repeats=2)
     assert best["composite_warps"] in (2, 4, 8) and best["bin_threads"] in (128, 256, 512)
-    assert best["composite_batch"] in (1, 2, 4, 8)
-    for warps, per_item in ((2, 1), (8, 8), (4, 2)):
+    assert best["composite_batch"] in (1, 2, 4, 8) and best["mask_stage_fills"] in (0, 8, 32)
+    for warps, per_item, stage in ((2, 1, 0), (8, 8, 1), (4, 2, 16)):
         renderer.set_tuning(composite_warps=warps, composite_batch=per_item, flatten_threads=64, bin_threads=512,
-                            bin_blocks_per_sm=4)
+                            bin_blocks_per_sm=4, mask_stage_fills=stage)
         out.zero_()
         renderer.render_batch(batch, out, pf.PF_CUDA_FORMAT_RGBA8)
         assert torch.equal(out, ref)
     renderer.set_tuning(**best)
+
+
+@pytest.mark.parametrize("stage", [1, 8, 128])
+def test_staged_fill_pass_is_identical(renderer, stage):
+    """The fill pass with its fill ranges staged in shared memory by bulk
+    copies (the mask_stage_fills knob) writes the same coverage as the
+    direct-read default: identical images, paints and clips included."""
+    torch = pytest.importorskip("torch")
+    from tests import paintscenes
+    scenes = [pf.generate_scene(pf.PF_SCENE_SVG_4K, seed=3, scale=0.05), paintscenes.gradient_scene(4),
+              paintscenes.pattern_scene(5)]
+    default = renderer.get_tuning()
+    try:
+        for s in scenes:
+            ref = renderer.render(s)
+            renderer.set_tuning(mask_stage_fills=stage)
+            img = renderer.render(s)
+            renderer.set_tuning(**default)
+            assert np.array_equal(np.asarray(img), np.asarray(ref))
+    finally:
+        renderer.set_tuning(**default)
+    with pytest.raises(pf._abi.PFCUDAError):
+        renderer.set_tuning(mask_stage_fills=129)
 
 
 def test_graph_refused_after_buffers_regrow(built):
