@@ -813,7 +813,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t pari
 // The fill pass (k_mask): each warp takes every (total warps)-th entry of
 // the mask work list and writes the entry's resolved coverage to its slot.
 // Two forms: by default the fills are read from global memory by the lanes
-// that accumulate them (the work list read two entries ahead); with the
+// that accumulate them (the work list read one entry ahead); with the
 // tuning knob mask_stage_fills, a fill range of at least that many fills is
 // copied into the warp's shared memory by one bulk copy (rounded out to
 // 16-byte boundaries) one entry ahead of its use.  Ranges larger than a
@@ -866,14 +866,12 @@ __global__ void __launch_bounds__(kMaskKernelWarps * 32, 8) k_mask(FrameDev f) {
     if (k >= M) return;
     const int4 none = make_int4(0, 0, 0, 0);
     int4 cur = f.mask_items[k];
-    int4 nxt = k + stride < M ? f.mask_items[k + stride] : none;
     unsigned long long fills_read = 0;  // the fills of this warp's tiles (frame statistics)
     for (; k < M; k += stride) {
-        const int4 later = k + 2 * stride < M ? f.mask_items[k + 2 * stride] : none;
+        const int4 nxt = k + stride < M ? f.mask_items[k + stride] : none;
         fills_read += (uint32_t)cur.y;
         mask_entry(f, cur, f.fills + (uint32_t)cur.x, bufs[wid][0], bufs[wid][1]);
         cur = nxt;
-        nxt = later;
     }
     if (lane == 0) atomicAdd((unsigned long long*)&f.counters->mask_fills, fills_read);
 }
