@@ -833,23 +833,49 @@ struct FlattenWarp {
     uint32_t deep;                     // segments deeper than kLeafLevels
 };
 
+// Line k of a leaf mask: the leaf from its start slot to the next leaf's (or
+// the end); its split path and depth.
+__device__ __forceinline__ void leaf_of_mask(unsigned long long m, uint32_t k, uint32_t* addr, int* depth) {
+    const uint32_t start = nth_set_bit64(m, k);
+    const unsigned long long above = start >= 63u ? 0ull : (m >> (start + 1u));
+    const uint32_t next = above ? start + (uint32_t)__ffsll((long long)above) : 64u;
+    const int d = kLeafLevels - (31 - __clz((int)(next - start)));
+    *depth = d;
+    *addr = start >> (kLeafLevels - d);
+}
+
+// Flattening.  ORDERED (frames whose line order is read: record read-back
+// and differentiable frames) is the count pass: leaf masks and line counts
+// for the emit pass, which places each segment's lines in depth-first order
+// after a scan over the warps.  Otherwise (plain frames, whose later stages
+// sum per tile with integer atomics or order by tile, so that no output
+// depends on the order of the lines) the same kernel writes the lines: each
+// block takes its lines' range with one atomic on the frame's line count and
+// places them in depth-first order within it, with no scan and no emit pass.
+template <bool ORDERED>
 __global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
     pdl_enter();
     __shared__ FlattenWarp smw[kFlattenMaxWarps];
+    __shared__ uint32_t warp_base[kFlattenMaxWarps];
+    __shared__ unsigned long long block_base;
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     FlattenWarp& w = smw[wib];
     const uint32_t s0 = (blockIdx.x * (blockDim.x >> 5) + wib) * 32u;
-    if (s0 >= f.seg_count) return;  // whole warps
+    if (ORDERED && s0 >= f.seg_count) return;  // whole warps (the other form's warps meet at barriers)
     const uint32_t s = s0 + lane;
     unsigned long long active = 0;  // nodes of the current level to test
     unsigned long long leaves = 0;
+    uint32_t path = 0;
     if (s < f.seg_count) {
         // level 0 by the segment's own lane: a line, or a curve flat as a
         // whole, is one leaf; otherwise both halves are tested at level 1
         Cubic c;
-        const int kind = segment_root(f.pts, f.segs[f.seg_begin + s], c, &f.counters->status);
+        const SegRec sr = f.segs[f.seg_begin + s];
+        const int kind = segment_root(f.pts, sr, c, &f.counters->status);
+        path = (uint32_t)sr.w;
         if (kind == kRootLine || (kind == kRootCurve && cubic_is_flat(c))) leaves = 1;
-        else if (kind == kRootCurve) { w.root[lane] = c; active = 3; }
+        else if (kind == kRootCurve) active = 3;
+        w.root[lane] = c;
     }
     w.leaves[lane] = leaves;
     w.next[lane] = 0;
@@ -879,22 +905,76 @@ __global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
         __syncwarp();
     }
     uint32_t n = 0;
+    const bool deep = s < f.seg_count && ((w.deep >> lane) & 1u);
     if (s < f.seg_count) {
         leaves = w.leaves[lane];
-        if ((w.deep >> lane) & 1u) {
+        if (deep) {
             flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&, uint32_t, int) { n++; },
                             &f.counters->status);
-            leaves = 0;  // no mask: the emit pass walks the segment
+            leaves = 0;  // no mask: the segment is walked again for its lines
         } else {
             n = (uint32_t)__popcll(leaves);
         }
-        f.seg_line_count[s] = n;
-        f.seg_leaves[s] = leaves;
+        if (ORDERED) {
+            f.seg_line_count[s] = n;
+            f.seg_leaves[s] = leaves;
+        }
     }
-    // the warp's lines: the emit pass places the warp's lines after those of
-    // the warps before it (a scan of one value per warp)
-    const uint32_t warp_lines = __reduce_add_sync(0xffffffffu, n);
-    if (lane == 0) f.seg_warp_lines[s0 / 32u] = warp_lines;
+    const uint32_t incl_n = warp_inclusive_scan(n);
+    const uint32_t warp_lines = __shfl_sync(0xffffffffu, incl_n, 31);
+    if (ORDERED) {
+        // the emit pass places the warp's lines after those of the warps
+        // before it (a scan of one value per warp)
+        if (lane == 0) f.seg_warp_lines[s0 / 32u] = warp_lines;
+        return;
+    }
+    // the block's range of lines, then each warp's part of it
+    if (lane == 0) warp_base[wib] = warp_lines;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (uint32_t k = 0; k < (blockDim.x >> 5); k++) {
+            const uint32_t v = warp_base[k];
+            warp_base[k] = t;
+            t += v;
+        }
+        block_base = t ? atomicAdd((unsigned long long*)&f.counters->lines, (unsigned long long)t) : 0ull;
+    }
+    __syncthreads();
+    if (s0 >= f.seg_count) return;
+    const unsigned long long base = block_base + warp_base[wib] + incl_n - n;
+    auto put = [&](unsigned long long l, const Line& ln, uint32_t pth) {
+        if (l < f.line_cap) {
+            f.lines[l] = make_float4(ln.fx, ln.fy, ln.tx, ln.ty);
+            f.line_path[l] = pth;
+        }
+    };
+    // one leaf at level 0: the root's base line, by its own lane
+    if (n != 0 && leaves == 1ull) put(base, w.root[lane].base, path);
+    // several leaves: the leaves of the warp's segments spread over the lanes
+    const uint32_t nl = leaves > 1ull ? n : 0u;
+    const uint32_t incl = warp_inclusive_scan(nl);
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    for (uint32_t i0 = 0; i0 < total; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const uint32_t j = warp_owner(incl, i);
+        const uint32_t k = i - __shfl_sync(0xffffffffu, incl - nl, j);
+        const unsigned long long lj = __shfl_sync(0xffffffffu, leaves, j);
+        const unsigned long long bj = __shfl_sync(0xffffffffu, base, j);
+        const uint32_t pj = __shfl_sync(0xffffffffu, path, j);
+        if (i < total) {
+            uint32_t addr;
+            int d;
+            leaf_of_mask(lj, k, &addr, &d);
+            put(bj + k, subdivision_node(w.root[j], addr, d).base, pj);
+        }
+    }
+    // deeper segments: walked again by their own lanes
+    if (deep) {
+        unsigned long long l = base;
+        flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line& ln, uint32_t, int) { put(l++, ln, path); },
+                        &f.counters->status);
+    }
 }
 
 // DIFF also records each line's segment and curve-parameter interval: the leaf
@@ -1027,8 +1107,14 @@ void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     const uint32_t blocks = dice ? (f.seg_count + ft - 1) / ft
                                  : (uint32_t)(((uint64_t)f.seg_count + 31) / 32 * 32 + ft - 1) / ft;
     count_launch();
-    if (dice) pdl_launch(k_dice_count, blocks, ft, 0, s, f);
-    else pdl_launch(k_flatten_count, blocks, ft, 0, s, f);
+    if (dice) {
+        pdl_launch(k_dice_count, blocks, ft, 0, s, f);
+    } else if (!f.diff && f.fill_e == nullptr) {  // line order free: one pass
+        pdl_launch(k_flatten_count<false>, blocks, ft, 0, s, f);
+        return;
+    } else {
+        pdl_launch(k_flatten_count<true>, blocks, ft, 0, s, f);
+    }
     if (dice) {
         launch_scan(f.seg_line_count, f.seg_line_base, nullptr, f.seg_count, f.seg_count, 0, &f.counters->lines, tmp,
                     s);
@@ -1076,6 +1162,10 @@ struct CountSink {
 template <int MODE>
 __global__ void __launch_bounds__(512, 3) k_bin_count(FrameDev f) {
     pdl_enter();
+    if (blockIdx.x == 0 && threadIdx.x == 0 && f.counters->lines > f.line_cap) {  // the flattening's total
+        atomicOr(&f.counters->status, kStatusLineCapacity);
+        f.counters->needed_lines = f.counters->lines;
+    }
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     const uint32_t L = line_total(f);
     for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
