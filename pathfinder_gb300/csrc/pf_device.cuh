@@ -155,7 +155,8 @@ struct Counters {
     uint64_t columns;      // sum of tile rect widths
     uint64_t fills;        // F
     uint64_t alpha_tiles;  // A
-    uint64_t lines;        // flattened lines
+    uint64_t lines;        // flattened lines (one-pass flattening: those within one tile)
+    uint64_t lines_back;   // one-pass flattening: lines beyond one tile, at the line array's end
     uint64_t visible;      // composited tiles
     uint64_t needed_fills, needed_tiles, needed_visible, needed_lines;
     uint32_t composite_next;   // work counter of the persistent composite (screen tiles handed out)

@@ -542,7 +542,7 @@ void grow(PFCUDARenderer* r, const Counters& h) {
         r->vis_cap = std::max(r->vis_cap, r->tile_cap);
     }
     if (h.status & kStatusFillCapacity) r->fill_cap = std::max(r->fill_cap, up(h.fills));
-    if (h.status & kStatusLineCapacity) r->line_cap = std::max(r->line_cap, up(h.lines));
+    if (h.status & kStatusLineCapacity) r->line_cap = std::max(r->line_cap, up(h.lines + h.lines_back));
     if (h.status & kStatusVisibleCapacity) r->vis_cap = std::max(r->vis_cap, up(h.visible));
 }
 
@@ -560,7 +560,7 @@ int32_t status_to_code(uint32_t st) {
 void record_stats(PFCUDARenderer* r, const Counters& h, float ms) {
     r->stats.path_count = r->last.p1 - r->last.p0;
     r->stats.segment_count = r->last.g1 - r->last.g0;
-    r->stats.line_count = h.lines;
+    r->stats.line_count = h.lines + h.lines_back;
     r->stats.fill_count = h.fills;
     r->stats.tile_count = h.tiles;
     r->stats.alpha_tile_count = h.alpha_tiles;

@@ -830,8 +830,18 @@ struct FlattenWarp {
     Cubic root[32];                    // each lane's segment as a cubic (a line as its base)
     unsigned long long leaves[32];     // leaf start slots of each segment
     unsigned long long next[32];       // nodes of the next level to test
+    unsigned long long multi[32];      // leaves whose line crosses a tile boundary (one-pass form)
     uint32_t deep;                     // segments deeper than kLeafLevels
 };
+
+// Whether a line reaches beyond the tile of its start (the binning's walk
+// takes more than its one-step path for it).  The one-pass flattening places
+// such lines apart from the others so that each warp of the binning passes
+// mostly walks lines of one kind.
+__device__ __forceinline__ bool line_multi_tile(const Line& l) {
+    const float r = 1.0f / 16.0f;
+    return floorf(l.fx * r) != floorf(l.tx * r) || floorf(l.fy * r) != floorf(l.ty * r);
+}
 
 // Line k of a leaf mask: the leaf from its start slot to the next leaf's (or
 // the end); its split path and depth.
@@ -850,14 +860,16 @@ __device__ __forceinline__ void leaf_of_mask(unsigned long long m, uint32_t k, u
 // after a scan over the warps.  Otherwise (plain frames, whose later stages
 // sum per tile with integer atomics or order by tile, so that no output
 // depends on the order of the lines) the same kernel writes the lines: each
-// block takes its lines' range with one atomic on the frame's line count and
-// places them in depth-first order within it, with no scan and no emit pass.
+// block takes its range of lines within one tile from the front of the line
+// array (counter `lines`) and its range of longer lines from the back
+// (counter `lines_back`), one atomic each, and places them in depth-first
+// order within those ranges, with no scan and no emit pass.
 template <bool ORDERED>
-__global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
+__global__ void __launch_bounds__(256, ORDERED ? 8 : 6) k_flatten_count(FrameDev f) {
     pdl_enter();
     __shared__ FlattenWarp smw[kFlattenMaxWarps];
-    __shared__ uint32_t warp_base[kFlattenMaxWarps];
-    __shared__ unsigned long long block_base;
+    __shared__ uint32_t warp_base[kFlattenMaxWarps][2];
+    __shared__ unsigned long long block_base[2];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     FlattenWarp& w = smw[wib];
     const uint32_t s0 = (blockIdx.x * (blockDim.x >> 5) + wib) * 32u;
@@ -879,6 +891,7 @@ __global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
     }
     w.leaves[lane] = leaves;
     w.next[lane] = 0;
+    if (!ORDERED) w.multi[lane] = (leaves && line_multi_tile(w.root[lane].base)) ? 1ull : 0ull;
     if (lane == 0) w.deep = 0;
     __syncwarp();
     for (int d = 1; d <= kLeafLevels; d++) {
@@ -894,9 +907,15 @@ __global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
             if (i < total) {
                 const uint32_t a = nth_set_bit64(aj, i - first);
                 const Cubic c = subdivision_node(w.root[j], a, d);
-                if (cubic_is_flat(c)) atomicOr(&w.leaves[j], 1ull << (a << (kLeafLevels - d)));
-                else if (d < kLeafLevels) atomicOr(&w.next[j], 3ull << (2u * a));
-                else atomicOr(&w.deep, 1u << j);
+                if (cubic_is_flat(c)) {
+                    const unsigned long long bit = 1ull << (a << (kLeafLevels - d));
+                    atomicOr(&w.leaves[j], bit);
+                    if (!ORDERED && line_multi_tile(c.base)) atomicOr(&w.multi[j], bit);
+                } else if (d < kLeafLevels) {
+                    atomicOr(&w.next[j], 3ull << (2u * a));
+                } else {
+                    atomicOr(&w.deep, 1u << j);
+                }
             }
         }
         __syncwarp();
@@ -904,53 +923,70 @@ __global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
         w.next[lane] = 0;
         __syncwarp();
     }
-    uint32_t n = 0;
+    uint32_t n = 0, n1 = 0;  // lines, and of those the ones beyond one tile (one-pass form)
+    unsigned long long multi = 0;
     const bool deep = s < f.seg_count && ((w.deep >> lane) & 1u);
     if (s < f.seg_count) {
         leaves = w.leaves[lane];
         if (deep) {
-            flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line&, uint32_t, int) { n++; },
-                            &f.counters->status);
+            flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line& ln, uint32_t, int) {
+                n++;
+                if (!ORDERED && line_multi_tile(ln)) n1++;
+            }, &f.counters->status);
             leaves = 0;  // no mask: the segment is walked again for its lines
         } else {
             n = (uint32_t)__popcll(leaves);
+            if (!ORDERED) {
+                multi = w.multi[lane] & leaves;
+                n1 = (uint32_t)__popcll(multi);
+            }
         }
         if (ORDERED) {
             f.seg_line_count[s] = n;
             f.seg_leaves[s] = leaves;
         }
     }
-    const uint32_t incl_n = warp_inclusive_scan(n);
-    const uint32_t warp_lines = __shfl_sync(0xffffffffu, incl_n, 31);
     if (ORDERED) {
         // the emit pass places the warp's lines after those of the warps
         // before it (a scan of one value per warp)
+        const uint32_t warp_lines = __reduce_add_sync(0xffffffffu, n);
         if (lane == 0) f.seg_warp_lines[s0 / 32u] = warp_lines;
         return;
     }
-    // the block's range of lines, then each warp's part of it
-    if (lane == 0) warp_base[wib] = warp_lines;
+    // the block's two ranges of lines, then each warp's part of them
+    const uint32_t n0 = n - n1;
+    const uint32_t incl0 = warp_inclusive_scan(n0), incl1 = warp_inclusive_scan(n1);
+    if (lane == 31) {
+        warp_base[wib][0] = incl0;
+        warp_base[wib][1] = incl1;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint32_t t = 0;
+        uint32_t t0 = 0, t1 = 0;
         for (uint32_t k = 0; k < (blockDim.x >> 5); k++) {
-            const uint32_t v = warp_base[k];
-            warp_base[k] = t;
-            t += v;
+            const uint32_t v0 = warp_base[k][0], v1 = warp_base[k][1];
+            warp_base[k][0] = t0;
+            warp_base[k][1] = t1;
+            t0 += v0;
+            t1 += v1;
         }
-        block_base = t ? atomicAdd((unsigned long long*)&f.counters->lines, (unsigned long long)t) : 0ull;
+        block_base[0] = t0 ? atomicAdd((unsigned long long*)&f.counters->lines, (unsigned long long)t0) : 0ull;
+        block_base[1] = t1 ? atomicAdd((unsigned long long*)&f.counters->lines_back, (unsigned long long)t1) : 0ull;
     }
     __syncthreads();
     if (s0 >= f.seg_count) return;
-    const unsigned long long base = block_base + warp_base[wib] + incl_n - n;
-    auto put = [&](unsigned long long l, const Line& ln, uint32_t pth) {
-        if (l < f.line_cap) {
-            f.lines[l] = make_float4(ln.fx, ln.fy, ln.tx, ln.ty);
-            f.line_path[l] = pth;
-        }
+    // one-tile line r of the segment: front position base0 + r; longer line
+    // r: position base1 + r counted down from the end of the array
+    const unsigned long long base0 = block_base[0] + warp_base[wib][0] + incl0 - n0;
+    const unsigned long long base1 = block_base[1] + warp_base[wib][1] + incl1 - n1;
+    auto put = [&](bool far, unsigned long long r, const Line& ln, uint32_t pth) {
+        if (r >= f.line_cap) return;
+        const unsigned long long l = far ? (unsigned long long)f.line_cap - 1ull - r : r;
+        f.lines[l] = make_float4(ln.fx, ln.fy, ln.tx, ln.ty);
+        f.line_path[l] = pth;
     };
     // one leaf at level 0: the root's base line, by its own lane
-    if (n != 0 && leaves == 1ull) put(base, w.root[lane].base, path);
+    if (n != 0 && leaves == 1ull) put(multi != 0, multi ? base1 : base0, w.root[lane].base, path);
     // several leaves: the leaves of the warp's segments spread over the lanes
     const uint32_t nl = leaves > 1ull ? n : 0u;
     const uint32_t incl = warp_inclusive_scan(nl);
@@ -960,20 +996,29 @@ __global__ void __launch_bounds__(256, 8) k_flatten_count(FrameDev f) {
         const uint32_t j = warp_owner(incl, i);
         const uint32_t k = i - __shfl_sync(0xffffffffu, incl - nl, j);
         const unsigned long long lj = __shfl_sync(0xffffffffu, leaves, j);
-        const unsigned long long bj = __shfl_sync(0xffffffffu, base, j);
+        const unsigned long long mj = __shfl_sync(0xffffffffu, multi, j);
+        const unsigned long long b0j = __shfl_sync(0xffffffffu, base0, j);
+        const unsigned long long b1j = __shfl_sync(0xffffffffu, base1, j);
         const uint32_t pj = __shfl_sync(0xffffffffu, path, j);
         if (i < total) {
             uint32_t addr;
             int d;
             leaf_of_mask(lj, k, &addr, &d);
-            put(bj + k, subdivision_node(w.root[j], addr, d).base, pj);
+            // the leaf's rank among the segment's leaves of its kind
+            const uint32_t start = addr << (kLeafLevels - d);
+            const unsigned long long before = (1ull << start) - 1ull;
+            const uint32_t r1 = (uint32_t)__popcll(mj & before);
+            const bool far = (mj >> start) & 1ull;
+            put(far, far ? b1j + r1 : b0j + (k - r1), subdivision_node(w.root[j], addr, d).base, pj);
         }
     }
     // deeper segments: walked again by their own lanes
     if (deep) {
-        unsigned long long l = base;
-        flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line& ln, uint32_t, int) { put(l++, ln, path); },
-                        &f.counters->status);
+        unsigned long long r0 = base0, r1 = base1;
+        flatten_segment(f.pts, f.segs[f.seg_begin + s], [&](const Line& ln, uint32_t, int) {
+            const bool far = line_multi_tile(ln);
+            put(far, far ? r1++ : r0++, ln, path);
+        }, &f.counters->status);
     }
 }
 
@@ -1133,10 +1178,19 @@ void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
 // adjust_alpha_tile_backdrop: renderer/src/tiler.rs:191-308,
 // renderer/src/builder.rs:509-616)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t line_total(const FrameDev& f) {
-    uint64_t L = f.counters->lines;
-    return L <= f.line_cap ? (uint32_t)L : 0u;
+// The frame's lines: the front range [0, lines) and, from a one-pass
+// flattening, the back range of lines_back lines ending at the array's end.
+// Line i of the frame (i < total) is at i below `front`, else at i + `skip`.
+struct LineRanges {
+    uint32_t total, front, skip;
+    __device__ __forceinline__ uint32_t at(uint32_t i) const { return i < front ? i : i + skip; }
+};
+__device__ __forceinline__ LineRanges line_ranges(const FrameDev& f) {
+    const uint64_t L0 = f.counters->lines, L1 = f.counters->lines_back;
+    if (L0 + L1 > f.line_cap) return LineRanges{0u, 0u, 0u};
+    return LineRanges{(uint32_t)(L0 + L1), (uint32_t)L0, f.line_cap - (uint32_t)(L0 + L1)};
 }
+__device__ __forceinline__ uint32_t line_total(const FrameDev& f) { return line_ranges(f).total; }
 
 struct CountSink {
     const PathCtx* pc;
@@ -1162,13 +1216,17 @@ struct CountSink {
 template <int MODE>
 __global__ void __launch_bounds__(512, 3) k_bin_count(FrameDev f) {
     pdl_enter();
-    if (blockIdx.x == 0 && threadIdx.x == 0 && f.counters->lines > f.line_cap) {  // the flattening's total
-        atomicOr(&f.counters->status, kStatusLineCapacity);
-        f.counters->needed_lines = f.counters->lines;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // the flattening's total against the capacity
+        const uint64_t L = f.counters->lines + f.counters->lines_back;
+        if (L > f.line_cap) {
+            atomicOr(&f.counters->status, kStatusLineCapacity);
+            f.counters->needed_lines = L;
+        }
     }
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
-    const uint32_t L = line_total(f);
-    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
+    const LineRanges lr = line_ranges(f);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < lr.total; i += gridDim.x * blockDim.x) {
+        const uint32_t l = lr.at(i);
         const float4 ln = f.lines[l];
         const PathCtx pc = f.path_bin[f.line_path[l]];
         CountSink sink{&pc, f.tile_fill_count, f.tile_delta, f.col_backdrop, 0};
@@ -1239,11 +1297,12 @@ __global__ void __launch_bounds__(512, 3) k_bin_emit(const __grid_constant__ Fra
     }
     if (f.counters->tiles > f.tile_cap || f.counters->columns > f.col_cap) return;
     if (f.counters->fills > f.fill_cap) return;
-    const uint32_t L = line_total(f);
+    const LineRanges lr = line_ranges(f);
     // one sink for all of the thread's lines: a fill's store waits for the
     // thread's next fill, whichever line it comes from
     EmitSink<ORDER> sink{&f, 0u};
-    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < lr.total; i += gridDim.x * blockDim.x) {
+        const uint32_t l = lr.at(i);
         // the line's reads issued together, its fill count tested after
         const uint32_t nfill = f.line_fill_count[l];
         const float4 ln = f.lines[l];
