@@ -722,7 +722,7 @@ def main():
     ap.add_argument("--clock-soak", type=float, default=1.5,
                     help="seconds of untimed replays sampled for clocks before the timed steps")
     ap.add_argument("--e2e-steps", type=int, default=0)
-    ap.add_argument("--e2e-depth", type=int, default=3, help="frames in flight in the end-to-end leg")
+    ap.add_argument("--e2e-depth", type=int, default=6, help="frames in flight in the end-to-end leg")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="fraction of the 20,000 paths (small cases for profiling only)")
     args = ap.parse_args()
