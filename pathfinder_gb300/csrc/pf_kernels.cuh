@@ -42,8 +42,8 @@ struct FrameDev {
     uint32_t* tile_fill_count;   // [tile_cap+1]
     uint32_t* tile_fill_base;    // [tile_cap+1]
     uint32_t* tile_alpha;        // [tile_cap+1] exclusive scan of has-fill flags
-    int32_t*  tile_delta;        // [tile_cap+1] backdrop deltas, column-major within a path
-    uint32_t* tile_delta_scan;   // [tile_cap+1] exclusive scan of tile_delta
+    int32_t*  tile_delta;        // [tile_cap+1] backdrop deltas, row-major within a path (as the tiles)
+    uint32_t* tile_delta_scan;   // [tile_cap+1] each tile's backdrop before propagation (column sums)
     uint32_t* path_tiles;        // [P+1] tiles per path (scan input)
     uint32_t* path_cols;         // [P+1] tile columns per path (scan input)
     PathCtx*  path_bin;          // [P+1] binning context per global path (written after the path scan)
@@ -322,6 +322,7 @@ struct ScanLanes {
 };
 void launch_scan_multi(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp, cudaStream_t s);
 
+void launch_column_backdrops(const FrameDev& f, cudaStream_t s);
 void launch_propagate(const FrameDev& f, bool clip_pass, cudaStream_t s);
 void launch_visible(const FrameDev& f, bool scatter, cudaStream_t s);
 // mode 0: RGBA8, 1: R8 single channel, 2: FP32 single channel

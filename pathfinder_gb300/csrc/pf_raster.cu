@@ -66,11 +66,53 @@ __device__ __forceinline__ bool frame_screen_tile(const FrameDev& f, const Scene
 }
 
 // ---------------------------------------------------------------------------
+// Column backdrops (Tiler::prepare_tiles's running backdrop down each column,
+// renderer/src/tiler.rs:93-111): the backdrop of tile (ox, oy) is the column's
+// above-rect sum plus the deltas of the tiles above it (wrapping int32 sums).
+// A thread walks one column of one path top to bottom; the lanes of a warp
+// take neighbouring columns, so every read and write of a row is coalesced
+// (the deltas and the tiles are row-major within a path).
+// ---------------------------------------------------------------------------
+__global__ void k_column_backdrops(FrameDev f) {
+    pdl_enter();
+    if (!frame_ok(f) || f.path_count == 0) return;
+    const uint32_t NC = (uint32_t)f.counters->columns;
+    const uint32_t* coffs = f.path.col_offset + f.path_begin;
+    const int32_t* __restrict__ delta = f.tile_delta;
+    uint32_t* __restrict__ out = f.tile_delta_scan;
+    for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < NC; c += gridDim.x * blockDim.x) {
+        const uint32_t gp = f.path_begin + upper_bound_u32(coffs, f.path_count + 1, c) - 1;
+        const int4 r = f.path.tile_rect[gp];
+        const uint32_t w = (uint32_t)(r.z - r.x), h = (uint32_t)(r.w - r.y);
+        uint32_t g = f.path.tile_offset[gp] + (c - f.path.col_offset[gp]);
+        uint32_t acc = (uint32_t)f.col_backdrop[c];
+        uint32_t oy = 0;
+        for (; oy + 4 <= h; oy += 4, g += 4 * w) {  // four rows' reads in flight at once
+            const uint32_t d0 = (uint32_t)delta[g], d1 = (uint32_t)delta[g + w];
+            const uint32_t d2 = (uint32_t)delta[g + 2 * w], d3 = (uint32_t)delta[g + 3 * w];
+            out[g] = acc;
+            out[g + w] = acc + d0;
+            out[g + 2 * w] = acc + d0 + d1;
+            out[g + 3 * w] = acc + d0 + d1 + d2;
+            acc += d0 + d1 + d2 + d3;
+        }
+        for (; oy < h; oy++, g += w) {
+            const uint32_t d = (uint32_t)delta[g];
+            out[g] = acc;
+            acc += d;
+        }
+    }
+}
+
+void launch_column_backdrops(const FrameDev& f, cudaStream_t s) {
+    if (f.path_count == 0) return;
+    count_launch();
+    pdl_launch(k_column_backdrops, f.sms * 16, 256, 0, s, f);
+}
+
+// ---------------------------------------------------------------------------
 // propagate: one thread per tile; clip tiles in the first launch, draw tiles
 // in the second (draw tiles of clipped paths read their clip's final tiles).
-// The backdrop of tile (ox, oy) is the above-rect column sum plus the deltas of
-// the tiles above it in its column: with the deltas stored column-major and
-// scanned, that is above[ox] + S[ox*h + oy] - S[ox*h] (wrapping int32 sums).
 // Path sizes are log-normal, so per-path work items would leave a long tail.
 // ---------------------------------------------------------------------------
 __global__ void k_propagate(FrameDev f, int clip_pass) {
@@ -92,7 +134,7 @@ __global__ void k_propagate(FrameDev f, int clip_pass) {
         if (is_clip != (clip_pass != 0)) continue;
         const int4 r = f.path.tile_rect[gp];
         const int32_t w = r.z - r.x, h = r.w - r.y;
-        const uint32_t tbase = f.path.tile_offset[gp], cbase_col = f.path.col_offset[gp];
+        const uint32_t tbase = f.path.tile_offset[gp];
         const bool even_odd = f.path.rule[gp] == 1;
         const uint8_t ctrl = is_clip ? 0 : (even_odd ? 0x2 : 0x1);
         const uint32_t local = f.path.local_index[gp];
@@ -101,9 +143,7 @@ __global__ void k_propagate(FrameDev f, int clip_pass) {
 
         const uint32_t i = g - tbase;
         const int32_t ox = (int32_t)(i % (uint32_t)w), oy = (int32_t)(i / (uint32_t)w);
-        const uint32_t cm = tbase + (uint32_t)(ox * h);
-        const int32_t acc = f.col_backdrop[cbase_col + (uint32_t)ox] +
-                            (int32_t)(f.tile_delta_scan[cm + (uint32_t)oy] - f.tile_delta_scan[cm]);
+        const int32_t acc = (int32_t)f.tile_delta_scan[g];  // the column backdrop (k_column_backdrops)
         const bool has_fill = f.tile_fill_base[g + 1] > f.tile_fill_base[g];
         const uint32_t own_alpha = has_fill ? f.tile_alpha[g] : kInvalid;
         if (has_fill) f.alpha_owner[own_alpha] = g;

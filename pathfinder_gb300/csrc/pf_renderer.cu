@@ -135,7 +135,8 @@ struct PFCUDARenderer {
     // propagation and visibility.  The second branch of each pair runs on
     // branch_stream, forked from and joined back to the frame's stream.
     cudaStream_t branch_stream = nullptr;
-    cudaEvent_t fork_ev[2] = {}, join_ev[2] = {};
+    cudaStream_t column_stream = nullptr;  // the column backdrops, beside the tile scan
+    cudaEvent_t fork_ev[3] = {}, join_ev[3] = {};
     PFCUDARendererOptions options{};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -464,14 +465,15 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     // Stage-timed frames run every kernel on the frame's stream, in order.
     const bool branches = !r->profiling;
     cudaStream_t b = branches ? r->branch_stream : s;
-    auto fork = [&](int k) -> cudaError_t {
+    cudaStream_t bc = branches ? r->column_stream : s;
+    auto fork = [&](int k, cudaStream_t to) -> cudaError_t {
         if (!branches) return cudaSuccess;
         cudaError_t e1 = cudaEventRecord(r->fork_ev[k], s);
-        return e1 ? e1 : cudaStreamWaitEvent(b, r->fork_ev[k], 0);
+        return e1 ? e1 : cudaStreamWaitEvent(to, r->fork_ev[k], 0);
     };
-    auto join = [&](int k) -> cudaError_t {
+    auto join = [&](int k, cudaStream_t from) -> cudaError_t {
         if (!branches) return cudaSuccess;
-        cudaError_t e1 = cudaEventRecord(r->join_ev[k], b);
+        cudaError_t e1 = cudaEventRecord(r->join_ev[k], from);
         return e1 ? e1 : cudaStreamWaitEvent(s, r->join_ev[k], 0);
     };
     const size_t nst = (size_t)(g.st1 - g.st0) + 1;
@@ -480,38 +482,42 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     if ((e = cudaMemsetAsync(r->scan_lookback.p, 0, r->scan_lookback.cap * sizeof(unsigned long long), s))) return e;
     mark(0);
     // flattening needs no tile rects: it runs beside the bounds and path scans
-    if ((e = fork(0))) return e;
+    if ((e = fork(0, b))) return e;
     launch_bound(f, r->ord_contour.p, r->starts.p, s);
     launch_path_scan(f, tmp, s);
     mark(1);
     launch_flatten(f, branches ? tmp_branch : tmp, b);
-    if ((e = join(0))) return e;
+    if ((e = join(0, b))) return e;
     mark(2);
     launch_bin_count(f, s);
     mark(3);
+    // the column backdrops need only the count pass: they run beside the
+    // scans (in stage-timed frames, in the scans' stage)
+    if ((e = fork(2, bc))) return e;
+    launch_column_backdrops(f, bc);
     // the first fill of each line in emission order: only frames run for
     // record read-back write emission indices
     if (r->fill_order)
         launch_scan(r->line_fill_count.p, r->line_fill_base.p, &c->lines, 0, r->line_cap, 0, &c->fills, tmp, s);
     {
         // per tile: fill offsets (their total is the frame's fill count),
-        // alpha-tile ids, column backdrop prefixes
+        // alpha-tile ids
         ScanLanes lanes{};
-        lanes.count = 3;
+        lanes.count = 2;
         lanes.in[0] = r->tile_fill_count.p; lanes.out[0] = r->tile_fill_base.p; lanes.mode[0] = 0;
         lanes.total[0] = &c->fills;
         lanes.in[1] = r->tile_fill_count.p; lanes.out[1] = r->tile_alpha.p; lanes.mode[1] = 1;
         lanes.total[1] = &c->alpha_tiles;
-        lanes.in[2] = (const uint32_t*)r->tile_delta.p; lanes.out[2] = r->tile_delta_scan.p; lanes.mode[2] = 0;
         launch_scan_multi(lanes, &c->tiles, r->tile_cap, tmp, s);
     }
     mark(4);
     // propagation and visibility read the tile scans, not the fills: the fill
     // emission runs beside them
-    if ((e = fork(1))) return e;
+    if ((e = fork(1, b))) return e;
     launch_bin_emit(f, b);
     mark(5);
     // clip paths first: draw tiles of clipped paths read their clip's finished tiles
+    if ((e = join(2, bc))) return e;
     launch_propagate(f, true, s);
     launch_propagate(f, false, s);
     mark(6);
@@ -519,7 +525,7 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     launch_scan(r->screen_cnt.p, r->screen_base.p, nullptr, (uint32_t)(nst - 1), (uint32_t)(nst - 1), 0, &c->visible,
                 tmp, s);
     launch_visible(f, true, s);
-    if ((e = join(1))) return e;
+    if ((e = join(1, b))) return e;
     mark(7);
     if (mode >= 0 && !diff) launch_mask(f, s);
     mark(8);
@@ -787,10 +793,13 @@ int32_t PFCUDARendererCreate(int32_t device_ordinal, const PFCUDARendererOptions
         (e = cudaEventCreateWithFlags(&r->points_done, cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&r->prior_done, cudaEventDisableTiming)) ||
         (e = cudaStreamCreateWithFlags(&r->branch_stream, cudaStreamNonBlocking)) ||
+        (e = cudaStreamCreateWithFlags(&r->column_stream, cudaStreamNonBlocking)) ||
         (e = cudaEventCreateWithFlags(&r->fork_ev[0], cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&r->fork_ev[1], cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&r->fork_ev[2], cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&r->join_ev[0], cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&r->join_ev[1], cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&r->join_ev[2], cudaEventDisableTiming)) ||
         (e = cudaEventCreate(&r->ev0)) || (e = cudaEventCreate(&r->ev1)) ||
         (e = cudaMallocHost((void**)&r->h_counters, sizeof(Counters))) || (e = r->counters.ensure(1))) {
         PFCUDARendererDestroy(r);
@@ -845,7 +854,11 @@ int32_t PFCUDARendererDestroy(PFCUDARendererRef r) {
         cudaStreamSynchronize(r->branch_stream);
         cudaStreamDestroy(r->branch_stream);
     }
-    for (int k = 0; k < 2; k++) {
+    if (r->column_stream) {
+        cudaStreamSynchronize(r->column_stream);
+        cudaStreamDestroy(r->column_stream);
+    }
+    for (int k = 0; k < 3; k++) {
         if (r->fork_ev[k]) cudaEventDestroy(r->fork_ev[k]);
         if (r->join_ev[k]) cudaEventDestroy(r->join_ev[k]);
     }

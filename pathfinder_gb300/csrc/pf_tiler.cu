@@ -1209,7 +1209,7 @@ struct CountSink {
         int32_t ox = tx - pc->minx, oy = ty - pc->miny;
         if (ox < 0 || ox >= w || oy >= h) return;
         if (oy < 0) atomicAdd(&col_backdrop[pc->col_base + (uint32_t)ox], d);
-        else atomicAdd(&tile_delta[pc->tile_base + (uint32_t)(ox * h + oy)], d);  // column-major
+        else atomicAdd(&tile_delta[pc->tile_base + (uint32_t)(oy * w + ox)], d);  // row-major, as the tiles
     }
 };
 
