@@ -61,7 +61,7 @@ struct FrameDev {
     uint2*    fills;             // [fill_cap] LineSegmentU16
     uint32_t* fill_e;            // [fill_cap] emission index
     int4*     tiles;             // [tile_cap] PFCUDATile records
-    int4*     clips;             // [tile_cap] PFCUDAClip records
+    int4*     clips;             // [tile_cap] PFCUDAClip records of the tiles of clipped draw paths (only)
     uint32_t* alpha_owner;       // [tile_cap] alpha id -> owning global tile
     int32_t*  zbuf;              // [screen_count]
     uint32_t* screen_cnt;        // [screen_count+1]

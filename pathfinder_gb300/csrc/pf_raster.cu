@@ -191,9 +191,7 @@ __global__ void k_propagate(FrameDev f, int clip_pass) {
                 backdrop = 0;
             }
             f.clips[g] = clip_rec;
-        } else if (!is_clip) {
-            f.clips[g] = make_int4((int)kInvalid, 0, (int)kInvalid, 0);
-        }
+        }  // tiles of unclipped paths get no clip record: every reader checks the path's clip first
         f.tiles[g] = pack_tile(tx, ty, alpha, gp, color, tile_ctrl_bits, backdrop);
         // differentiable frames occlude with the FP32 paint alpha being optimised;
         // a tile behind a clip chain may be partly covered, so it never occludes

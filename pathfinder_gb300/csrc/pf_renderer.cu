@@ -1488,11 +1488,15 @@ int32_t PFCUDAReadRecords(PFCUDARendererRef r, PFCUDAFill* fills, uint32_t* fill
         for (uint64_t i = 0; i < T; i++) tiles[i].path_id = path_local_of(r, tiles[i].path_id, nullptr);
     }
     if (clips && T) {
+        std::vector<int32_t> clip_of(NPth + 1);
         PF_TRY(cudaMemcpyAsync(clips, r->clips.p, T * sizeof(PFCUDAClip), cudaMemcpyDeviceToHost, s));
+        PF_TRY(cudaMemcpyAsync(clip_of.data(), r->clip_gpath.p + g.p0, NPth * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               s));
         PF_TRY(cudaStreamSynchronize(s));
-        // tiles of clip paths carry no clip record
+        // tiles of clip paths and of unclipped draw paths carry no clip record
+        // (the frame writes records only for clipped draw paths)
         for (uint64_t q = 0; q < NPth; q++)
-            if (path_is_clip_of(r, g.p0 + q))
+            if (path_is_clip_of(r, g.p0 + q) || clip_of[q] < 0)
                 for (uint32_t t = off[q]; t < off[q + 1]; t++) clips[t] = PFCUDAClip{0xffffffffu, 0, 0xffffffffu, 0};
     }
     if (path_tile_offsets) std::memcpy(path_tile_offsets, off.data(), (NPth + 1) * sizeof(uint32_t));
