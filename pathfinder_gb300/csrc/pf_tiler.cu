@@ -773,14 +773,16 @@ void launch_path_scan(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     { count_launch(); pdl_launch(k_zero_tiles, f.sms * 8, 256, 0, s, f); }
 }
 
-// Launch bounds: the flattening passes run at 32 registers a thread (64 warps
-// an SM, a few spilled values), the binning passes at 40 (48 warps); the
-// extra warps hide their gather and atomic latency (measured: 36 or 32
-// registers spill the binning passes' walk state and slow them).
+// Launch bounds: the ordered flattening passes run at 32 registers a thread
+// (64 warps an SM, a few spilled values), the one-pass flattening and the
+// binning passes at 40 (48 warps); the extra warps hide their gather and
+// atomic latency (measured: 36 or 32 registers spill the binning passes' walk
+// state and slow them, and spill the one-pass flattening's line placement).
 // ---------------------------------------------------------------------------
 // flattening (process_segment's recursion, renderer/src/tiler.rs:166-184).
-// Lines are written in emission order: input segments in path order, each
-// segment's lines depth first.
+// Ordered frames write the lines in emission order (input segments in path
+// order, each segment's lines depth first); plain frames write each
+// segment's lines depth first within its block's ranges (k_flatten_count).
 //
 // A warp takes 32 segments and tests their subdivision level by level: at
 // level d the nodes still to test (children of nodes that were not flat) of
