@@ -897,7 +897,11 @@ __global__ void __launch_bounds__(256, ORDERED ? 8 : 6) k_flatten_count(FrameDev
     if (lane == 0) w.deep = 0;
     __syncwarp();
     for (int d = 1; d <= kLeafLevels; d++) {
-        const uint32_t cnt = (uint32_t)__popcll(active);
+        // the nodes to test come in sibling pairs (both children of a node
+        // that was not flat): an item is a pair, its parent recomputed from
+        // the root and split once, as the recursion splits it
+        const unsigned long long pairs = active & 0x5555555555555555ull;
+        const uint32_t cnt = (uint32_t)__popcll(pairs);
         const uint32_t incl = warp_inclusive_scan(cnt);
         const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
         if (total == 0) break;
@@ -905,18 +909,24 @@ __global__ void __launch_bounds__(256, ORDERED ? 8 : 6) k_flatten_count(FrameDev
             const uint32_t i = i0 + lane;
             const uint32_t j = warp_owner(incl, i);
             const uint32_t first = __shfl_sync(0xffffffffu, incl - cnt, j);
-            const unsigned long long aj = __shfl_sync(0xffffffffu, active, j);
+            const unsigned long long aj = __shfl_sync(0xffffffffu, pairs, j);
             if (i < total) {
-                const uint32_t a = nth_set_bit64(aj, i - first);
-                const Cubic c = subdivision_node(w.root[j], a, d);
-                if (cubic_is_flat(c)) {
-                    const unsigned long long bit = 1ull << (a << (kLeafLevels - d));
-                    atomicOr(&w.leaves[j], bit);
-                    if (!ORDERED && line_multi_tile(c.base)) atomicOr(&w.multi[j], bit);
-                } else if (d < kLeafLevels) {
-                    atomicOr(&w.next[j], 3ull << (2u * a));
-                } else {
-                    atomicOr(&w.deep, 1u << j);
+                const uint32_t a0 = nth_set_bit64(aj, i - first);  // the left child's address
+                Cubic half[2];
+                cubic_split_half(subdivision_node(w.root[j], a0 >> 1, d - 1), half[0], half[1]);
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const uint32_t a = a0 + (uint32_t)h;
+                    const Cubic& c = half[h];
+                    if (cubic_is_flat(c)) {
+                        const unsigned long long bit = 1ull << (a << (kLeafLevels - d));
+                        atomicOr(&w.leaves[j], bit);
+                        if (!ORDERED && line_multi_tile(c.base)) atomicOr(&w.multi[j], bit);
+                    } else if (d < kLeafLevels) {
+                        atomicOr(&w.next[j], 3ull << (2u * a));
+                    } else {
+                        atomicOr(&w.deep, 1u << j);
+                    }
                 }
             }
         }
