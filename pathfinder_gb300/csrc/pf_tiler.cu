@@ -914,20 +914,27 @@ __global__ void __launch_bounds__(256, ORDERED ? 8 : 6) k_flatten_count(FrameDev
                 const uint32_t a0 = nth_set_bit64(aj, i - first);  // the left child's address
                 Cubic half[2];
                 cubic_split_half(subdivision_node(w.root[j], a0 >> 1, d - 1), half[0], half[1]);
+                // both children's bits, then one update of each mask
+                unsigned long long leaf_bits = 0, multi_bits = 0, next_bits = 0;
+                bool deeper = false;
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const uint32_t a = a0 + (uint32_t)h;
                     const Cubic& c = half[h];
                     if (cubic_is_flat(c)) {
                         const unsigned long long bit = 1ull << (a << (kLeafLevels - d));
-                        atomicOr(&w.leaves[j], bit);
-                        if (!ORDERED && line_multi_tile(c.base)) atomicOr(&w.multi[j], bit);
+                        leaf_bits |= bit;
+                        if (!ORDERED && line_multi_tile(c.base)) multi_bits |= bit;
                     } else if (d < kLeafLevels) {
-                        atomicOr(&w.next[j], 3ull << (2u * a));
+                        next_bits |= 3ull << (2u * a);
                     } else {
-                        atomicOr(&w.deep, 1u << j);
+                        deeper = true;
                     }
                 }
+                if (leaf_bits) atomicOr(&w.leaves[j], leaf_bits);
+                if (multi_bits) atomicOr(&w.multi[j], multi_bits);
+                if (next_bits) atomicOr(&w.next[j], next_bits);
+                if (deeper) atomicOr(&w.deep, 1u << j);
             }
         }
         __syncwarp();
