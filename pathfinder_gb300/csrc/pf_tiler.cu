@@ -869,11 +869,13 @@ __device__ __forceinline__ void leaf_of_mask(unsigned long long m, uint32_t k, u
 template <bool ORDERED>
 __global__ void __launch_bounds__(256, ORDERED ? 8 : 6) k_flatten_count(FrameDev f) {
     pdl_enter();
-    __shared__ FlattenWarp smw[kFlattenMaxWarps];
+    // one FlattenWarp per warp of the block, sized at launch (so that blocks
+    // of fewer warps hold less shared memory and more of them fit an SM)
+    extern __shared__ __align__(16) unsigned char flatten_smem[];
     __shared__ uint32_t warp_base[kFlattenMaxWarps][2];
     __shared__ unsigned long long block_base[2];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    FlattenWarp& w = smw[wib];
+    FlattenWarp& w = reinterpret_cast<FlattenWarp*>(flatten_smem)[wib];
     const uint32_t s0 = (blockIdx.x * (blockDim.x >> 5) + wib) * 32u;
     if (ORDERED && s0 >= f.seg_count) return;  // whole warps (the other form's warps meet at barriers)
     const uint32_t s = s0 + lane;
@@ -1163,6 +1165,8 @@ __global__ void __launch_bounds__(256, 6) k_dice_emit(FrameDev f) {
     }
 }
 
+static size_t flatten_smem_bytes(int threads) { return (size_t)(threads / 32) * sizeof(FlattenWarp); }
+
 void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     if (f.seg_count == 0) return;
     const int ft = f.tune.flatten_threads;
@@ -1174,10 +1178,10 @@ void launch_flatten(const FrameDev& f, ScanTemp& tmp, cudaStream_t s) {
     if (dice) {
         pdl_launch(k_dice_count, blocks, ft, 0, s, f);
     } else if (!f.diff && f.fill_e == nullptr) {  // line order free: one pass
-        pdl_launch(k_flatten_count<false>, blocks, ft, 0, s, f);
+        pdl_launch(k_flatten_count<false>, blocks, ft, flatten_smem_bytes(ft), s, f);
         return;
     } else {
-        pdl_launch(k_flatten_count<true>, blocks, ft, 0, s, f);
+        pdl_launch(k_flatten_count<true>, blocks, ft, flatten_smem_bytes(ft), s, f);
     }
     if (dice) {
         launch_scan(f.seg_line_count, f.seg_line_base, nullptr, f.seg_count, f.seg_count, 0, &f.counters->lines, tmp,
