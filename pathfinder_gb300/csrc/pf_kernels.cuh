@@ -318,6 +318,10 @@ struct ScanLanes {
     uint32_t* out[kMaxScanLanes];
     uint64_t* total[kMaxScanLanes];
     int mode[kMaxScanLanes];
+    // optional: the lane's inclusive sums, written after the lane's own reads
+    // (so it may be the lane's input; lanes that read the same input come
+    // before it)
+    uint32_t* incl[kMaxScanLanes];
     int count;
 };
 void launch_scan_multi(const ScanLanes& lanes, const uint64_t* d_n, uint32_t n_cap, ScanTemp& tmp, cudaStream_t s);

@@ -500,14 +500,16 @@ cudaError_t enqueue_frame(PFCUDARenderer* r, const PFCUDABuildOptions* opts, int
     if (r->fill_order)
         launch_scan(r->line_fill_count.p, r->line_fill_base.p, &c->lines, 0, r->line_cap, 0, &c->fills, tmp, s);
     {
-        // per tile: fill offsets (their total is the frame's fill count),
-        // alpha-tile ids
+        // per tile: alpha-tile ids, fill offsets (their total is the frame's
+        // fill count) and, over the counts, each tile's fill end: the emit
+        // pass's cursor, counted down to the tile's offset
         ScanLanes lanes{};
         lanes.count = 2;
-        lanes.in[0] = r->tile_fill_count.p; lanes.out[0] = r->tile_fill_base.p; lanes.mode[0] = 0;
-        lanes.total[0] = &c->fills;
-        lanes.in[1] = r->tile_fill_count.p; lanes.out[1] = r->tile_alpha.p; lanes.mode[1] = 1;
-        lanes.total[1] = &c->alpha_tiles;
+        lanes.in[0] = r->tile_fill_count.p; lanes.out[0] = r->tile_alpha.p; lanes.mode[0] = 1;
+        lanes.total[0] = &c->alpha_tiles;
+        lanes.in[1] = r->tile_fill_count.p; lanes.out[1] = r->tile_fill_base.p; lanes.mode[1] = 0;
+        lanes.total[1] = &c->fills;
+        lanes.incl[1] = r->tile_fill_count.p;
         launch_scan_multi(lanes, &c->tiles, r->tile_cap, tmp, s);
     }
     mark(4);

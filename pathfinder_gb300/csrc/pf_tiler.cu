@@ -312,6 +312,11 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_onepass(ScanLanes L, cons
             ex += v[k];
         }
         store8(L.out[l], first, n, e);
+        if (L.incl[l]) {
+#pragma unroll
+            for (int k = 0; k < kScanItems; k++) e[k] += v[k];
+            store8(L.incl[l], first, n, e);
+        }
         if (threadIdx.x == 0 && t + 1 >= tiles) {  // the last tile: the total
             L.out[l][n] = (uint32_t)(p + total);
             if (L.total[l]) *L.total[l] = p + total;
@@ -461,6 +466,11 @@ __global__ void k_scanm_down(ScanLanes L, const uint64_t* d_n, uint32_t n_cap, c
             ex += v[k];
         }
         store8(L.out[l], first, n, e);
+        if (L.incl[l]) {
+#pragma unroll
+            for (int k = 0; k < kScanItems; k++) e[k] += v[k];
+            store8(L.incl[l], first, n, e);
+        }
     }
 }
 
@@ -506,6 +516,11 @@ __global__ void k_scanm_down_fused(ScanLanes L, const uint64_t* d_n, uint32_t n_
             ex += v[k];
         }
         store8(L.out[l], first, n, e);
+        if (L.incl[l]) {
+#pragma unroll
+            for (int k = 0; k < kScanItems; k++) e[k] += v[k];
+            store8(L.incl[l], first, n, e);
+        }
         if (blockIdx.x == nb - 1 && threadIdx.x == 0) {
             L.out[l][n] = prefix + total;
             if (L.total[l]) *L.total[l] = prefix + total;
@@ -1260,31 +1275,30 @@ __global__ void __launch_bounds__(512, 3) k_bin_count(FrameDev f) {
 
 // ORDER also writes each fill's emission index (only frames run for record
 // read-back do: the order of fills within a tile changes no output).
-// A fill's slot is its tile's fill base plus a decrementing cursor (the
-// tile's count).  The store of each fill waits one fill: the cursor's value
-// comes back from L2 while the DDA computes the next fill (flush() stores the
-// last one).
+// The tile scan leaves each tile's fill end (offset + count) in its count
+// word: a fill's slot is that cursor, decremented, so one atomic gives it.
+// The store of each fill waits one fill: the cursor's value comes back from
+// L2 while the DDA computes the next fill (flush() stores the last one).
 // The sink reads the frame's pointers from the kernel parameter itself.
 template <bool ORDER>
 struct EmitSink {
     const FrameDev* f;
     uint32_t e;
     bool pending = false;
-    uint32_t p_base = 0, p_old = 0, p_e = 0;
+    uint32_t p_end = 0, p_e = 0;
     uint2 p_rec = make_uint2(0u, 0u);
     __device__ __forceinline__ void store_pending() {
-        const uint32_t slot = p_base + p_old - 1u;
+        const uint32_t slot = p_end - 1u;
         if (slot < f->fill_cap) {
             f->fills[slot] = p_rec;
             if (ORDER) f->fill_e[slot] = p_e;
         }
     }
     __device__ __forceinline__ void fill(uint2 rec, uint32_t g) {
-        const uint32_t base = f->tile_fill_base[g];
-        const uint32_t old = atomicSub(&f->tile_fill_count[g], 1u);
+        const uint32_t end = atomicSub(&f->tile_fill_count[g], 1u);
         if (pending) store_pending();
         pending = true;
-        p_base = base; p_old = old; p_rec = rec; p_e = e;
+        p_end = end; p_rec = rec; p_e = e;
         if (ORDER) e++;
     }
     __device__ __forceinline__ void flush() {
@@ -1297,11 +1311,10 @@ struct EmitSink {
 // FP32 fills of differentiable frames (no emission index: nothing reads it).
 struct EmitSinkF {
     float4* fills;
-    const uint32_t* tile_fill_base;
-    uint32_t* cursor;
+    uint32_t* cursor;  // each tile's fill end, counted down
     uint32_t fill_cap;
     __device__ __forceinline__ void fill(float4 rec, uint32_t g) {
-        const uint32_t slot = tile_fill_base[g] + atomicSub(&cursor[g], 1u) - 1u;
+        const uint32_t slot = atomicSub(&cursor[g], 1u) - 1u;
         if (slot < fill_cap) fills[slot] = rec;
     }
     __device__ __forceinline__ void flush() {}
@@ -1333,7 +1346,7 @@ __global__ void __launch_bounds__(512, 3) k_bin_emit(const __grid_constant__ Fra
         if (nfill == 0) continue;
         const PathCtx pc = f.path_bin[gp];
         if constexpr (MODE == kFillF32) {
-            EmitSinkF sinkf{f.fills_f, f.tile_fill_base, f.tile_fill_count, f.fill_cap};
+            EmitSinkF sinkf{f.fills_f, f.tile_fill_count, f.fill_cap};
             dda_line<MODE>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sinkf, f.dda_limit, &f.counters->status);
         } else {
             if (ORDER) sink.e = f.line_fill_base[l];
