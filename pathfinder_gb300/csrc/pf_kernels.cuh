@@ -55,7 +55,7 @@ struct FrameDev {
     unsigned long long* seg_leaves;  // [seg_count] leaf start slots of each segment's subdivision (0: walked)
     float4*   lines;             // [line_cap] flattened lines in emission order
     uint32_t* line_path;         // [line_cap] global path of each line
-    uint32_t* line_fill_count;   // [line_cap+1] kept fills per line
+    uint32_t* line_fill_count;   // [line_cap+1] kept fills per line (frames that write emission indices)
     uint32_t* line_fill_base;    // [line_cap+1] exclusive scan = emission index of the first fill
     uint32_t  line_cap;
     uint2*    fills;             // [fill_cap] LineSegmentU16

@@ -1269,7 +1269,7 @@ __global__ void __launch_bounds__(512, 3) k_bin_count(FrameDev f) {
         const PathCtx pc = f.path_bin[f.line_path[l]];
         CountSink sink{&pc, f.tile_fill_count, f.tile_delta, f.col_backdrop, 0};
         dda_line<MODE, true>(pc, Line{ln.x, ln.y, ln.z, ln.w}, sink, f.dda_limit, &f.counters->status);
-        f.line_fill_count[l] = sink.n;
+        if (f.fill_e != nullptr) f.line_fill_count[l] = sink.n;  // the emission-index scan's input
     }
 }
 
@@ -1339,8 +1339,10 @@ __global__ void __launch_bounds__(512, 3) k_bin_emit(const __grid_constant__ Fra
     EmitSink<ORDER> sink{&f, 0u};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < lr.total; i += gridDim.x * blockDim.x) {
         const uint32_t l = lr.at(i);
-        // the line's reads issued together, its fill count tested after
-        const uint32_t nfill = f.line_fill_count[l];
+        // the line's reads issued together; frames that write emission
+        // indices skip lines without fills by their count (the others walk
+        // them: they emit nothing)
+        const uint32_t nfill = ORDER ? f.line_fill_count[l] : 1u;
         const float4 ln = f.lines[l];
         const uint32_t gp = f.line_path[l];
         if (nfill == 0) continue;
