@@ -104,13 +104,16 @@ STAGE_KERNELS = {"bound": "k_bound", "flatten": "k_flatten_count", "bin_count": 
                  "bin_emit": "k_bin_emit", "fill": "k_mask", "composite": "k_composite"}
 
 
-def measured_traffic(kernel_stage: str, full_size: bool):
+def measured_traffic(kernel_stage: str, full_size: bool, variant: str = "plain"):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
-    capture of the full-size frame (profiles/svg4k_dram_full.md), for the
-    full-size workload only."""
+    capture of the full-size frame of the same workload
+    (profiles/svg4k_dram_full.md, svg4k_paints_dram_full.md,
+    svg4k_d3d11_dram_full.md), for full-size workloads only."""
     if not full_size:
         return None, None
-    rel = os.path.join("profiles", "svg4k_dram_full.md")
+    name = {"plain": "svg4k_dram_full.md", "paints": "svg4k_paints_dram_full.md",
+            "d3d11": "svg4k_d3d11_dram_full.md"}[variant]
+    rel = os.path.join("profiles", name)
     key = f"traffic_bytes_per_launch {kernel_stage}:"
     try:
         with open(os.path.join(ROOT, rel)) as f:
@@ -849,7 +852,8 @@ def main():
     achieved = sb[dom] / (stage_ms[dom] / 1e3) / 1e9
     frame_gbs = sb["frame"] / (ms / 1e3) / 1e9
     # the committed capture is of the plain full-size frame only
-    traffic, traffic_src = measured_traffic(dom, args.scale == 1.0 and not args.paints and not args.d3d11)
+    variant = "paints" if args.paints else ("d3d11" if args.d3d11 else "plain")
+    traffic, traffic_src = measured_traffic(dom, args.scale == 1.0 and not (args.paints and args.d3d11), variant)
 
     # e2e through the public API with host buffers
     e2e_steps = args.e2e_steps or max(3, min(10 * args.steps, 200))
