@@ -856,7 +856,9 @@ def main():
     traffic, traffic_src = measured_traffic(dom, args.scale == 1.0 and not (args.paints and args.d3d11), variant)
 
     # e2e through the public API with host buffers
-    e2e_steps = args.e2e_steps or max(3, min(10 * args.steps, 200))
+    # about 0.4 s of pipelined steps at the default: runs of 200 steps spread
+    # by up to 20% with host-side jitter, runs of 1000 by about 1%
+    e2e_steps = args.e2e_steps or max(3, min(10 * args.steps, 1000))
     depth = max(1, args.e2e_depth)
     pinned = {}
     for name in ("points", "flags", "contour_starts", "clip_paths", "draw_paths"):
